@@ -1,0 +1,213 @@
+"""ORACLE — test infrastructure only.
+
+A CPU restatement of the reference substep (``suna_oracle.cpp``) behind a small
+ctypes wrapper. The test suite, ``__graft_entry__.smoke()`` and the benchmark's
+CPU-baseline leg use it as the checker; the product package never imports it.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+BUILD = HERE / '_build'
+LIB = BUILD / 'libsuna_oracle.so'
+
+
+def build(force: bool = False) -> Path:
+    """Compile the oracle with g++ (OpenMP) into oracle/_build."""
+    src = [HERE / 'suna_oracle.cpp', HERE / 'fixed_ref.h']
+    if LIB.exists() and not force and all(LIB.stat().st_mtime >= s.stat().st_mtime for s in src):
+        return LIB
+    BUILD.mkdir(exist_ok=True)
+    tmp = BUILD / f'libsuna_oracle.{os.getpid()}.so'
+    cmd = ['g++', '-O2', '-std=c++17', '-fopenmp', '-ffp-contract=off', '-shared', '-fPIC',
+           str(HERE / 'suna_oracle.cpp'), '-o', str(tmp)]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        l = ctypes.CDLL(str(build()))
+        P = ctypes.c_void_p
+        i32p = np.ctypeslib.ndpointer(np.int32, flags='C')
+        u32p = np.ctypeslib.ndpointer(np.uint32, flags='C')
+        l.sno_create.restype = P
+        l.sno_create.argtypes = [ctypes.c_uint32, i32p, i32p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int]
+        l.sno_destroy.argtypes = [P]
+        l.sno_load_scene.restype = ctypes.c_int
+        l.sno_load_scene.argtypes = [P, ctypes.c_uint32, ctypes.c_uint32, i32p, i32p, u32p,
+                                     P, P, P, ctypes.c_int32, ctypes.c_int32, ctypes.c_uint32]
+        l.sno_step.restype = ctypes.c_int
+        l.sno_step.argtypes = [P, ctypes.c_uint32]
+        for f in ('sno_digest', 'sno_chain', 'sno_dbg'):
+            getattr(l, f).argtypes = [P, u32p]
+        l.sno_reset_chain.argtypes = [P]
+        for f in ('sno_n', 'sno_nfluid'):
+            getattr(l, f).restype = ctypes.c_uint32
+            getattr(l, f).argtypes = [P]
+        for f in ('sno_substeps', 'sno_formation_clock'):
+            getattr(l, f).restype = ctypes.c_uint64
+            getattr(l, f).argtypes = [P]
+        l.sno_read_state.restype = ctypes.c_int
+        l.sno_read_state.argtypes = [P, i32p, ctypes.c_size_t]
+        l.sno_read_derived.restype = ctypes.c_int
+        l.sno_read_derived.argtypes = [P, i32p, ctypes.c_size_t]
+        l.sno_read_bonds.restype = ctypes.c_int
+        l.sno_read_bonds.argtypes = [P, u32p, ctypes.c_size_t]
+        l.sno_write_state.restype = ctypes.c_int
+        l.sno_write_state.argtypes = [P, i32p, P]
+        l.sno_set_formation_clock.argtypes = [P, ctypes.c_uint64, ctypes.c_int]
+        l.sno_spawn.restype = ctypes.c_int64
+        l.sno_spawn.argtypes = [P, i32p, ctypes.c_uint32, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        l.sno_impulse.restype = ctypes.c_int64
+        l.sno_impulse.argtypes = [P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                  ctypes.c_int32, ctypes.c_uint32]
+        _lib = l
+    return _lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def hex8(words) -> str:
+    return ''.join(f'{int(w) & 0xffffffff:08x}' for w in words)
+
+
+class OracleEngine:
+    """CPU reference engine: ``createEngine`` + ``Engine`` semantics on the host."""
+
+    def __init__(self, max_particles: int = 8192, iters: int = 4, threads: int = 1,
+                 luts=None, mats=None):
+        from sunaengine_gb300 import data
+        l = lib()
+        self._luts = np.ascontiguousarray(data.luts() if luts is None else luts, dtype=np.int32)
+        m = data.mats() if mats is None else mats
+        self._mats = np.ascontiguousarray(m, dtype=np.int32).reshape(-1)
+        self.mat_count = self._mats.size // 48
+        self.h = l.sno_create(max_particles, self._luts, self._mats, self.mat_count, iters, threads)
+        if not self.h:
+            raise ValueError('oracle create failed')
+        self.max_particles = max_particles
+
+    def close(self):
+        if self.h:
+            lib().sno_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def load_scene(self, sc):
+        self._keep = []
+
+        def arr(a, dt):
+            if a is None:
+                return None
+            b = np.ascontiguousarray(a, dtype=dt)
+            self._keep.append(b)
+            return b
+        pos = arr(sc.pos.reshape(-1), np.int32)
+        vel = arr(sc.vel.reshape(-1), np.int32)
+        mat = arr(sc.matId, np.uint32)
+        rc = lib().sno_load_scene(self.h, sc.n, sc.nFluid, pos, vel, mat,
+                                  _ptr(arr(sc.flags, np.uint32)), _ptr(arr(sc.temp, np.int32)),
+                                  _ptr(arr(sc.fuel, np.int32)), int(sc.domW), int(sc.domH), int(sc.cellShift))
+        if rc != 0:
+            raise ValueError(f'oracle loadScene refused the scene (code {rc})')
+        return self
+
+    def step(self, count: int = 1):
+        rc = lib().sno_step(self.h, count)
+        if rc != 0:
+            raise RuntimeError(f'oracle step failed (code {rc})')
+        return self.substep_count
+
+    @property
+    def n(self):
+        return lib().sno_n(self.h)
+
+    @property
+    def n_fluid(self):
+        return lib().sno_nfluid(self.h)
+
+    @property
+    def substep_count(self):
+        return lib().sno_substeps(self.h)
+
+    @property
+    def formation_clock(self):
+        return lib().sno_formation_clock(self.h)
+
+    def digest_words(self):
+        a = np.zeros(8, np.uint32)
+        lib().sno_digest(self.h, a)
+        return a
+
+    def digest(self) -> str:
+        return hex8(self.digest_words())
+
+    def chain_words(self):
+        a = np.zeros(8, np.uint32)
+        lib().sno_chain(self.h, a)
+        return a
+
+    def chain_hex(self) -> str:
+        return hex8(self.chain_words())
+
+    def reset_chain(self):
+        lib().sno_reset_chain(self.h)
+
+    def debug_counters(self):
+        a = np.zeros(16, np.uint32)
+        lib().sno_dbg(self.h, a)
+        return a
+
+    def read_state(self):
+        a = np.zeros(self.n * 8, np.int32)
+        lib().sno_read_state(self.h, a, a.size)
+        return a
+
+    def read_derived(self):
+        a = np.zeros(self.n * 16, np.int32)
+        lib().sno_read_derived(self.h, a, a.size)
+        return a
+
+    def read_bonds(self):
+        a = np.zeros(self.n_fluid * 48, np.uint32)
+        lib().sno_read_bonds(self.h, a, a.size)
+        return a
+
+    def write_state(self, state, derived=None):
+        st = np.ascontiguousarray(state, dtype=np.int32)
+        dv = None if derived is None else np.ascontiguousarray(derived, dtype=np.int32)
+        lib().sno_write_state(self.h, st, _ptr(dv))
+        self._keep2 = dv
+
+    def set_formation_clock(self, clk: int, dirty: bool):
+        lib().sno_set_formation_clock(self.h, clk, 1 if dirty else 0)
+
+    def spawn(self, particles, no_weld: bool = True) -> int:
+        rows = np.zeros((len(particles), 8), np.int32)
+        has_t = any('temp' in p for p in particles)
+        has_f = any('fuel' in p for p in particles)
+        for k, p in enumerate(particles):
+            rows[k] = (p['x'], p['y'], p.get('vx', 0), p.get('vy', 0), p.get('mat', 0),
+                       p.get('flags', 0), p.get('temp', 0), p.get('fuel', 0))
+        r = lib().sno_spawn(self.h, rows.reshape(-1), len(particles), int(has_t), int(has_f), int(no_weld))
+        if r < 0:
+            raise ValueError(f'oracle spawn refused (code {r})')
+        return int(r)
+
+    def impulse(self, cx, cy, r, ix, iy, limit=3000) -> int:
+        return int(lib().sno_impulse(self.h, cx, cy, r, ix, iy, limit))
