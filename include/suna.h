@@ -1,0 +1,178 @@
+/*
+ * suna.h — C ABI of the GB300 engine for SunaEngine's deterministic Q16.16
+ * position-based-fluids substep.
+ *
+ * This is the boundary a host binds (a Node N-API addon, ctypes, cgo ...). It
+ * replaces the `Engine` object of the reference's `src/engine.js`
+ * (createEngine at src/engine.js:2786, class Engine at src/engine.js:3523) and
+ * the per-scene calls its demo layer makes (src/demo_boot.js:71-420).
+ *
+ * Conventions
+ *   - plain pointers and sizes only; the caller owns every host buffer and the
+ *     engine copies in and out;
+ *   - every call returns an int status: SN_OK (0) or a negative SN_E_* code;
+ *     sn_last_error() gives the message (the reference throws
+ *     Error('[aether] ...') synchronously, src/engine.js:2174);
+ *   - one engine = one CUDA stream on one GPU; an engine is not re-entrant and
+ *     must be driven from one host thread at a time (the reference's engine is
+ *     single-threaded JS);
+ *   - GPU-side failures are deferred and reported by sn_check_errors(), like
+ *     the reference's checkErrors() (src/engine.js:3689-3696).
+ *
+ * State words are the reference's Particle struct (src/sim.wgsl:181-188):
+ * 8 int32 per particle, [pos.x, pos.y, vel.x, vel.y, matId, flags, temp, fuel],
+ * in slot order: fluid slots [0, nFluid), then the boundary block.
+ */
+#ifndef SUNA_H
+#define SUNA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SN_OK 0
+#define SN_E_INVALID (-1)      /* a bad argument: the reference's assert() */
+#define SN_E_CAPACITY (-2)     /* does not fit the capacities given at create */
+#define SN_E_UNSUPPORTED (-3)  /* a material row whose passes this engine does not run */
+#define SN_E_CUDA (-4)         /* a CUDA runtime error */
+#define SN_E_STATE (-5)        /* called in the wrong state (e.g. step before load) */
+#define SN_E_DEVICE (-6)       /* the device reported an error word (see sn_check_errors) */
+
+typedef struct sn_engine sn_engine;
+
+/* createEngine options (src/engine.js:2786-2820). */
+typedef struct sn_opts {
+  uint32_t max_particles; /* slot capacity (maxParticles) */
+  uint32_t max_cells;     /* grid-cell capacity (maxCells); 0 = 1<<20 */
+  uint32_t iters;         /* solver iterations, 1..16 (ITERS = 4, src/engine.js:245) */
+  uint32_t debug;         /* 1 = count fp_flag events into the 16 debug words */
+  uint32_t chain;         /* 1 = fold every substep's digest into the chain */
+  int32_t device;         /* CUDA device ordinal */
+  const int32_t* luts;    /* 5*3202 int32 kernel tables (src/tables.json), hash-checked */
+  const int32_t* mats;    /* mat_count rows of 48 int32 (MATS, src/engine.js:1192) */
+  uint32_t mat_count;     /* 1..64 */
+} sn_opts;
+
+/* loadScene argument (src/engine.js:3704-3951). flags/temp/fuel may be NULL. */
+typedef struct sn_scene {
+  uint32_t n, n_fluid;
+  const int32_t* pos;     /* 2n */
+  const int32_t* vel;     /* 2n */
+  const uint32_t* mat_id; /* n */
+  const uint32_t* flags;  /* n or NULL */
+  const int32_t* temp;    /* n or NULL */
+  const int32_t* fuel;    /* n or NULL */
+  int32_t dom_w, dom_h;   /* ticks */
+  uint32_t cell_shift;    /* 18 = 4 wu cells */
+} sn_scene;
+
+/* One spawned particle (spawnFluid list entry, src/engine.js:5901). */
+typedef struct sn_particle {
+  int32_t x, y, vx, vy;
+  int32_t mat;
+  uint32_t flags;         /* only FLAG_BURNING | FLAG_ANCHOR are taken */
+  int32_t temp, fuel;
+  uint32_t has_temp, has_fuel; /* 0 = the material's spawnTemp / fuel0 */
+} sn_particle;
+
+typedef struct sn_info {
+  uint32_t n, n_fluid;
+  uint64_t substep_count;
+  uint64_t formation_clock;
+  uint32_t grid_w, grid_h, cell_total;
+} sn_info;
+
+/* ---- single-scene engine: the drop-in for engine.js's Engine ------------- */
+
+/* createEngine (src/engine.js:2786). */
+int sn_create(const sn_opts* opts, sn_engine** out);
+/* destroy (src/engine.js Engine.destroy). */
+void sn_destroy(sn_engine* e);
+/* Text of the last error on this engine (valid until the next call). */
+const char* sn_last_error(const sn_engine* e);
+/* Engine.loadScene (src/engine.js:3704). Resets the chain and the clocks. */
+int sn_load_scene(sn_engine* e, const sn_scene* scene);
+/* Engine.step (src/engine.js:3963): advance exactly `count` substeps. Encodes
+ * asynchronously; returns the new substep count in *substeps (may be NULL). */
+int sn_step(sn_engine* e, uint32_t count, uint64_t* substeps);
+/* Engine.digest (src/engine.js:4453): H_set (acc[0..3]) || H_slot (acc[4..7])
+ * of the current state. Synchronous. */
+int sn_digest(sn_engine* e, uint32_t acc[8]);
+/* Engine.chainHex (src/engine.js:4406): the folded per-substep chain. */
+int sn_chain(sn_engine* e, uint32_t chain[8]);
+/* Engine.resetChain (src/engine.js:3953). */
+int sn_reset_chain(sn_engine* e);
+/* Engine.readState: n*8 words of the current state. */
+int sn_read_state(sn_engine* e, int32_t* out, size_t words);
+/* The cross-substep scratch an exact keyframe needs: stAcc, n*2 words
+ * (Derived.stAcc, src/sim.wgsl:200; consumed by predict at src/sim.wgsl:980). */
+int sn_read_scratch(sn_engine* e, int32_t* out, size_t words);
+/* Exact keyframe restore (WaterDemo.restore, src/demo_boot.js:308-320): the
+ * state words (n*8) and optionally the scratch (n*2, NULL = zero, i.e. a load
+ * boundary). The scene must already be loaded with the same n / nFluid. */
+int sn_write_state(sn_engine* e, const int32_t* state, const int32_t* scratch, size_t n);
+/* Bond rows, nFluid*48 packed words (src/sim.wgsl:1594-1617). */
+int sn_read_bonds(sn_engine* e, uint32_t* out, size_t words);
+/* Engine.spawnFluid (src/engine.js:5901): append k fluid particles, relocate
+ * the boundary block to the tail. *n_out = new n (unchanged when the capacity
+ * refuses, as the reference silently does). */
+int sn_spawn(sn_engine* e, const sn_particle* list, uint32_t k, uint32_t no_weld, uint32_t* n_out);
+/* Engine.applyImpulse (src/engine.js:6077): add (ix, iy) to the velocity of the
+ * first `limit` fluid particles in slot order within r of (cx, cy), clamped to
+ * +-VMAX. Applied on the device at the current substep boundary. */
+int sn_impulse(sn_engine* e, int32_t cx, int32_t cy, int32_t r, int32_t ix, int32_t iy, uint32_t limit,
+               uint32_t* hits);
+/* Engine.debugCounters: the 16 fp_flag words (zero unless opts.debug). */
+int sn_debug_counters(sn_engine* e, uint32_t out[16]);
+/* Engine.checkErrors: SN_OK, SN_E_CUDA or SN_E_DEVICE. */
+int sn_check_errors(sn_engine* e);
+/* Block until all queued work is done. */
+int sn_sync(sn_engine* e);
+int sn_get_info(sn_engine* e, sn_info* out);
+/* Formation clock and pending-formation flag (engine `_substep`, `_bondDirty`),
+ * for keyframes that must resume the bond-formation schedule exactly. */
+int sn_set_formation_clock(sn_engine* e, uint64_t clock, uint32_t dirty);
+
+/* ---- batched engine: many independent scenes, one launch sequence -------- */
+/* No counterpart in the reference (which runs one scene per engine); the
+ * per-scene semantics are exactly the single engine's. */
+
+typedef struct sn_batch sn_batch;
+
+/* opts->max_particles is the total slot capacity over all scenes. */
+int sn_batch_create(const sn_opts* opts, uint32_t max_scenes, sn_batch** out);
+void sn_batch_destroy(sn_batch* b);
+const char* sn_batch_last_error(const sn_batch* b);
+/* Add a scene with `capacity` slots (>= scene->n; room for spawns). */
+int sn_batch_add_scene(sn_batch* b, const sn_scene* scene, uint32_t capacity, uint32_t* id);
+/* Drop a scene; its slots are reused by later adds of the same or smaller size. */
+int sn_batch_remove_scene(sn_batch* b, uint32_t id);
+/* Advance every scene by `count` substeps. */
+int sn_batch_step(sn_batch* b, uint32_t count);
+/* Queue a disc impulse for scene `id`, applied before that scene's substep
+ * number `at_substep` (counted from its load) runs. Events of one scene must be
+ * queued in nondecreasing at_substep; same-substep events apply in queue order. */
+int sn_batch_schedule_impulse(sn_batch* b, uint32_t id, uint64_t at_substep, int32_t cx, int32_t cy,
+                              int32_t r, int32_t ix, int32_t iy, uint32_t limit);
+int sn_batch_digest(sn_batch* b, uint32_t id, uint32_t acc[8]);
+int sn_batch_chain(sn_batch* b, uint32_t id, uint32_t chain[8]);
+int sn_batch_read_state(sn_batch* b, uint32_t id, int32_t* out, size_t words);
+int sn_batch_read_scratch(sn_batch* b, uint32_t id, int32_t* out, size_t words);
+int sn_batch_write_state(sn_batch* b, uint32_t id, const int32_t* state, const int32_t* scratch, size_t n,
+                         uint64_t substep_count, uint64_t formation_clock, uint32_t dirty);
+int sn_batch_get_info(sn_batch* b, uint32_t id, sn_info* out);
+int sn_batch_check_errors(sn_batch* b);
+int sn_batch_sync(sn_batch* b);
+/* Device time of the last sn_batch_step / sn_step in milliseconds (CUDA
+ * events on the engine's stream), and the kernel launches it issued. */
+int sn_batch_last_timing(sn_batch* b, float* ms, uint64_t* launches);
+int sn_last_timing(sn_engine* e, float* ms, uint64_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SUNA_H */

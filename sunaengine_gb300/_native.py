@@ -1,0 +1,139 @@
+"""Build and load the CUDA engine library (libsuna_gb300.so) in-tree.
+
+The library is compiled with nvcc for sm_103a only and loaded with ctypes.
+There is no fallback: if the library cannot be built or loaded, every engine
+call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import shutil
+import subprocess
+import threading
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+CSRC = HERE / 'csrc'
+BUILD = HERE / '_build'
+LIB = BUILD / 'libsuna_gb300.so'
+INCLUDE = HERE.parent / 'include'
+ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
+_lock = threading.Lock()
+
+
+def _sources():
+    return sorted(CSRC.glob('*.cu')) + sorted(CSRC.glob('*.cuh')) + [INCLUDE / 'suna.h']
+
+
+def nvcc() -> str:
+    exe = shutil.which('nvcc') or '/usr/local/cuda/bin/nvcc'
+    if not Path(exe).exists():
+        raise RuntimeError('nvcc not found: the CUDA engine cannot be built')
+    return exe
+
+
+def build(force: bool = False, verbose: bool = False) -> Path:
+    """Compile csrc/*.cu into _build/libsuna_gb300.so (sm_103a)."""
+    with _lock:
+        srcs = _sources()
+        if LIB.exists() and not force and all(LIB.stat().st_mtime >= s.stat().st_mtime for s in srcs):
+            return LIB
+        BUILD.mkdir(exist_ok=True)
+        tmp = BUILD / f'libsuna_gb300.{os.getpid()}.so'
+        cmd = [nvcc(), *ARCH, '-lineinfo', '-O3', '-std=c++17', '-Xcompiler', '-fPIC', '-shared',
+               '-diag-suppress', '550', '-o', str(tmp)] + [str(s) for s in sorted(CSRC.glob('*.cu'))]
+        if verbose:
+            cmd.insert(1, '-Xptxas=-v')
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError('nvcc failed:\n' + r.stdout + r.stderr)
+        os.replace(tmp, LIB)
+        return LIB
+
+
+class SnOpts(ctypes.Structure):
+    _fields_ = [('max_particles', ctypes.c_uint32), ('max_cells', ctypes.c_uint32),
+                ('iters', ctypes.c_uint32), ('debug', ctypes.c_uint32), ('chain', ctypes.c_uint32),
+                ('device', ctypes.c_int32), ('luts', ctypes.c_void_p), ('mats', ctypes.c_void_p),
+                ('mat_count', ctypes.c_uint32)]
+
+
+class SnScene(ctypes.Structure):
+    _fields_ = [('n', ctypes.c_uint32), ('n_fluid', ctypes.c_uint32), ('pos', ctypes.c_void_p),
+                ('vel', ctypes.c_void_p), ('mat_id', ctypes.c_void_p), ('flags', ctypes.c_void_p),
+                ('temp', ctypes.c_void_p), ('fuel', ctypes.c_void_p), ('dom_w', ctypes.c_int32),
+                ('dom_h', ctypes.c_int32), ('cell_shift', ctypes.c_uint32)]
+
+
+class SnParticle(ctypes.Structure):
+    _fields_ = [('x', ctypes.c_int32), ('y', ctypes.c_int32), ('vx', ctypes.c_int32), ('vy', ctypes.c_int32),
+                ('mat', ctypes.c_int32), ('flags', ctypes.c_uint32), ('temp', ctypes.c_int32),
+                ('fuel', ctypes.c_int32), ('has_temp', ctypes.c_uint32), ('has_fuel', ctypes.c_uint32)]
+
+
+class SnInfo(ctypes.Structure):
+    _fields_ = [('n', ctypes.c_uint32), ('n_fluid', ctypes.c_uint32), ('substep_count', ctypes.c_uint64),
+                ('formation_clock', ctypes.c_uint64), ('grid_w', ctypes.c_uint32), ('grid_h', ctypes.c_uint32),
+                ('cell_total', ctypes.c_uint32)]
+
+
+# Every symbol include/suna.h declares, with its ctypes signature.
+P = ctypes.c_void_p
+u32, i32, u64, sz = ctypes.c_uint32, ctypes.c_int32, ctypes.c_uint64, ctypes.c_size_t
+SIGNATURES = {
+    'sn_create': (ctypes.c_int, [ctypes.POINTER(SnOpts), ctypes.POINTER(P)]),
+    'sn_destroy': (None, [P]),
+    'sn_last_error': (ctypes.c_char_p, [P]),
+    'sn_load_scene': (ctypes.c_int, [P, ctypes.POINTER(SnScene)]),
+    'sn_step': (ctypes.c_int, [P, u32, ctypes.POINTER(u64)]),
+    'sn_digest': (ctypes.c_int, [P, P]),
+    'sn_chain': (ctypes.c_int, [P, P]),
+    'sn_reset_chain': (ctypes.c_int, [P]),
+    'sn_read_state': (ctypes.c_int, [P, P, sz]),
+    'sn_read_scratch': (ctypes.c_int, [P, P, sz]),
+    'sn_write_state': (ctypes.c_int, [P, P, P, sz]),
+    'sn_read_bonds': (ctypes.c_int, [P, P, sz]),
+    'sn_spawn': (ctypes.c_int, [P, P, u32, u32, ctypes.POINTER(u32)]),
+    'sn_impulse': (ctypes.c_int, [P, i32, i32, i32, i32, i32, u32, ctypes.POINTER(u32)]),
+    'sn_debug_counters': (ctypes.c_int, [P, P]),
+    'sn_check_errors': (ctypes.c_int, [P]),
+    'sn_sync': (ctypes.c_int, [P]),
+    'sn_get_info': (ctypes.c_int, [P, ctypes.POINTER(SnInfo)]),
+    'sn_set_formation_clock': (ctypes.c_int, [P, u64, u32]),
+    'sn_last_timing': (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(u64)]),
+    'sn_batch_create': (ctypes.c_int, [ctypes.POINTER(SnOpts), u32, ctypes.POINTER(P)]),
+    'sn_batch_destroy': (None, [P]),
+    'sn_batch_last_error': (ctypes.c_char_p, [P]),
+    'sn_batch_add_scene': (ctypes.c_int, [P, ctypes.POINTER(SnScene), u32, ctypes.POINTER(u32)]),
+    'sn_batch_remove_scene': (ctypes.c_int, [P, u32]),
+    'sn_batch_step': (ctypes.c_int, [P, u32]),
+    'sn_batch_schedule_impulse': (ctypes.c_int, [P, u32, u64, i32, i32, i32, i32, i32, u32]),
+    'sn_batch_digest': (ctypes.c_int, [P, u32, P]),
+    'sn_batch_chain': (ctypes.c_int, [P, u32, P]),
+    'sn_batch_read_state': (ctypes.c_int, [P, u32, P, sz]),
+    'sn_batch_read_scratch': (ctypes.c_int, [P, u32, P, sz]),
+    'sn_batch_write_state': (ctypes.c_int, [P, u32, P, P, sz, u64, u64, u32]),
+    'sn_batch_get_info': (ctypes.c_int, [P, u32, ctypes.POINTER(SnInfo)]),
+    'sn_batch_check_errors': (ctypes.c_int, [P]),
+    'sn_batch_sync': (ctypes.c_int, [P]),
+    'sn_batch_last_timing': (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(u64)]),
+}
+
+_lib = None
+
+
+def load(build_if_missing: bool = True) -> ctypes.CDLL:
+    """Load libsuna_gb300.so (building it first if needed) and bind every symbol."""
+    global _lib
+    if _lib is None:
+        path = build() if build_if_missing else LIB
+        if not path.exists():
+            raise RuntimeError(f'{path} is missing: run build() first')
+        lib = ctypes.CDLL(str(path))
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib

@@ -1,0 +1,1011 @@
+// Host side of the GB300 engine: device buffers, the per-substep launch
+// sequence, CUDA-graph replay, and the C ABI declared in include/suna.h.
+//
+// A World holds one or more independent 2D scenes in one set of device
+// buffers (see world.cuh). The single-scene engine (sn_engine, the drop-in for
+// the reference's Engine, src/engine.js:3523) is a World with one scene; the
+// batched engine (sn_batch) is the same World with many.
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/suna.h"
+#include "radix.cuh"
+#include "sim2d.cuh"
+
+using namespace sn;
+using namespace sn::d2;
+
+namespace {
+
+constexpr int32_t VMAX = 65536;
+constexpr int32_t MAX_POS = 134217728;
+constexpr int32_t KERNEL_H = 163840;
+constexpr uint32_t FLAG_MASK = 7u;
+constexpr uint32_t SPAWN_FLAG_MASK = 1u | 4u;
+
+// A queued disc impulse (applyImpulse, src/engine.js:6077-6098).
+struct ImpulseEv {
+  uint32_t at;       // scene substep index before which it applies
+  int32_t cx, cy, r, ix, iy;
+  uint32_t limit;
+  uint32_t pad;
+};
+
+struct EvPar {
+  uint32_t begin, end, cursor, pad;
+};
+
+// Device impulse: one CTA per scene; due events apply in queue order, hits
+// counted in slot order with a block-wide ballot scan, first `limit` hits
+// only. The disc test is the reference's JS arithmetic: IEEE doubles, each
+// product and the sum rounded to nearest, no fused multiply-add.
+__device__ __forceinline__ bool in_disc(int32_t px, int32_t py, const ImpulseEv& ev) {
+  double dx = (double)px - (double)ev.cx;
+  double dy = (double)py - (double)ev.cy;
+  double r = (double)ev.r;
+  double s = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+  return !(s > __dmul_rn(r, r));
+}
+
+__device__ uint32_t apply_event(Bufs b, const ScenePar& S, const ImpulseEv& ev) {
+  __shared__ uint32_t wsum[8];
+  __shared__ uint32_t total;
+  uint32_t hits = 0;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (uint32_t base = 0; base < S.nFluid && hits < ev.limit; base += 256) {
+    uint32_t i = base + tid;
+    bool in = false;
+    int32_t* w = nullptr;
+    if (i < S.nFluid) {
+      w = b.state + (size_t)(S.slotBase + i) * 8;
+      in = in_disc(w[0], w[1], ev);
+    }
+    uint32_t bal = __ballot_sync(0xffffffffu, in);
+    if (lane == 0) wsum[warp] = __popc(bal);
+    __syncthreads();
+    uint32_t before = 0, all = 0;
+    for (int k = 0; k < 8; ++k) {
+      if (k < warp) before += wsum[k];
+      all += wsum[k];
+    }
+    uint32_t rank = hits + before + __popc(bal & ((1u << lane) - 1u));
+    if (in && rank < ev.limit) {
+      int64_t vx = (int64_t)w[2] + ev.ix, vy = (int64_t)w[3] + ev.iy;
+      vx = vx < -VMAX ? -VMAX : (vx > VMAX ? VMAX : vx);
+      vy = vy < -VMAX ? -VMAX : (vy > VMAX ? VMAX : vy);
+      w[2] = (int32_t)vx;
+      w[3] = (int32_t)vy;
+    }
+    if (tid == 0) total = hits + all;
+    __syncthreads();
+    hits = min(total, ev.limit);
+    __syncthreads();
+  }
+  return hits;
+}
+
+__global__ void __launch_bounds__(256) k_impulse_sched(Bufs b, const ImpulseEv* __restrict__ evs,
+                                                       EvPar* __restrict__ ep) {
+  uint32_t s = blockIdx.x;
+  if (s >= b.world->numScenes) return;
+  const ScenePar& S = b.scenes[s];
+  if (!S.active) return;
+  uint32_t cur = ep[s].cursor;
+  const uint32_t end = ep[s].end;
+  const uint32_t now = S.substep;
+  while (cur < end && evs[cur].at <= now) {
+    ImpulseEv ev = evs[cur];
+    if (ev.at == now) apply_event(b, S, ev);
+    ++cur;
+    __syncthreads();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) ep[s].cursor = cur;
+}
+
+__global__ void __launch_bounds__(256) k_impulse_now(Bufs b, uint32_t s, ImpulseEv ev, uint32_t* hitsOut) {
+  const ScenePar& S = b.scenes[s];
+  uint32_t h = apply_event(b, S, ev);
+  if (threadIdx.x == 0) *hitsOut = h;
+}
+
+template <typename T>
+T* dalloc(size_t count, std::string& err) {
+  if (count == 0) count = 1;
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+  if (e != cudaSuccess) {
+    err = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+    return nullptr;
+  }
+  cudaMemset(p, 0, count * sizeof(T));
+  return static_cast<T*>(p);
+}
+
+struct SceneHost {
+  bool used = false, loaded = false;
+  uint32_t slotBase = 0, cap = 0;
+  uint32_t n = 0, nFluid = 0;
+  uint32_t gridW = 1, gridH = 1, cellShift = 18, cellTotal = 1;
+  int32_t domW = 0, domH = 0;
+  uint64_t substeps = 0;
+  // the loaded scene's arrays: spawnFluid re-packs the boundary block from them
+  std::vector<int32_t> pos, temp, fuel;
+  std::vector<uint32_t> mat;
+  uint32_t nFluid0 = 0;
+  bool hasTemp = false, hasFuel = false;
+  uint32_t weldSeq = 1;
+  std::vector<ImpulseEv> events;
+  uint32_t consumed = 0;  // events already applied (at < substeps)
+};
+
+}  // namespace
+
+struct World {
+  int device = 0;
+  cudaStream_t st = nullptr;
+  bool debug = false, chainOn = true;
+  uint32_t iters = 4;
+  uint32_t capSlots = 0, maxCells = 0, maxScenes = 0;
+  int numSMs = 152;
+  std::string err;
+  int32_t hmats[MAT_MAX * MAT_WORDS];
+  uint32_t matCount = 0;
+  std::vector<SceneHost> sh;
+  std::vector<ScenePar> hpar;
+  WorldPar hw{};
+  Bufs b{};
+  uint32_t *tmpK = nullptr, *tmpV = nullptr, *hist = nullptr, *hits = nullptr;
+  uint32_t* accTmp = nullptr;
+  ImpulseEv* devEv = nullptr;
+  size_t devEvCap = 0;
+  EvPar* devEp = nullptr;
+  bool eventsDirty = false, anyEvents = false;
+  bool hasFriction = false, hasBonds = false;
+  bool layoutDirty = true;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  bool graphValid = false;
+  bool useGraph = true;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  float lastMs = 0.f;
+  uint64_t lastLaunches = 0;
+  uint64_t launchesPerSubstep = 0;
+
+  bool fail(const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    err = buf;
+    return false;
+  }
+  bool cuda_ok(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return true;
+    return fail("%s: %s", what, cudaGetErrorString(e));
+  }
+
+  ~World() {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    if (graph) cudaGraphDestroy(graph);
+    void* ptrs[] = {b.state, b.stacc, b.predSlot, b.sceneOf, b.keys, b.inv, b.bond, b.bondCand, b.skey,
+                    b.sslot, b.cellStart, b.P, b.POS, b.INFO, b.FLG, b.TEMP, b.SCN, b.RHO, b.LAM,
+                    b.RINV, b.DP, b.NRM, b.HEAT, b.CORR, b.NBR, b.NBRN, (void*)b.luts, (void*)b.mats,
+                    b.scenes, b.world, b.acc, b.accLast, b.chain, b.dbg, b.err, tmpK, tmpV, hist,
+                    hits, accTmp, devEv, devEp};
+    for (void* p : ptrs)
+      if (p) cudaFree(p);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (st) cudaStreamDestroy(st);
+  }
+
+  bool init(const sn_opts* o, uint32_t scenesCap) {
+    if (!o) return fail("opts is NULL");
+    if (o->max_particles == 0) return fail("max_particles must be > 0");
+    if (o->iters < 1 || o->iters > 16) return fail("iters = %u outside 1..16", o->iters);
+    if (!o->luts || !o->mats) return fail("luts and mats are required");
+    if (o->mat_count < 1 || o->mat_count > (uint32_t)MAT_MAX) return fail("mat_count must be 1..64");
+    device = o->device;
+    if (!cuda_ok(cudaSetDevice(device), "cudaSetDevice")) return false;
+    cudaDeviceGetAttribute(&numSMs, cudaDevAttrMultiProcessorCount, device);
+    debug = o->debug != 0;
+    chainOn = o->chain != 0;
+    iters = o->iters;
+    capSlots = o->max_particles;
+    maxCells = o->max_cells ? o->max_cells : (1u << 20);
+    maxScenes = scenesCap;
+    std::memset(hmats, 0, sizeof(hmats));
+    std::memcpy(hmats, o->mats, sizeof(int32_t) * MAT_WORDS * o->mat_count);
+    matCount = o->mat_count;
+    for (uint32_t m = 0; m < matCount; ++m) {
+      const int32_t* r = hmats + m * MAT_WORDS;
+      if (r[M_eps] < 32768) return fail("mats[%u].eps < 32768", m);
+      if (r[M_dpMax] <= 0) return fail("mats[%u].dpMax <= 0", m);
+      for (int f : {M_meltTo, M_freezeTo, M_boilTo, M_condTo, M_burnTo, M_splitTo, M_corrTo})
+        if (r[f] < 0 || (uint32_t)r[f] >= matCount) return fail("mats[%u] names a product outside the table", m);
+    }
+    if (!cuda_ok(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "stream")) return false;
+    cudaEventCreate(&ev0);
+    cudaEventCreate(&ev1);
+    size_t C = capSlots;
+    b.state = dalloc<int32_t>(C * 8, err);
+    b.stacc = dalloc<int2>(C, err);
+    b.predSlot = dalloc<int2>(C, err);
+    b.sceneOf = dalloc<uint32_t>(C, err);
+    b.keys = dalloc<uint32_t>(C, err);
+    b.inv = dalloc<uint32_t>(C, err);
+    b.bond = dalloc<uint32_t>(C * BOND_CAP, err);
+    b.bondCand = dalloc<uint32_t>(C * BOND_CAP, err);
+    b.skey = dalloc<uint32_t>(C, err);
+    b.sslot = dalloc<uint32_t>(C, err);
+    b.cellStart = dalloc<uint32_t>((size_t)maxCells + 1, err);
+    b.P = dalloc<int2>(C, err);
+    b.POS = dalloc<int2>(C, err);
+    b.INFO = dalloc<uint32_t>(C, err);
+    b.FLG = dalloc<uint32_t>(C, err);
+    b.TEMP = dalloc<int32_t>(C, err);
+    b.SCN = dalloc<uint32_t>(C, err);
+    b.RHO = dalloc<int32_t>(C, err);
+    b.LAM = dalloc<int32_t>(C, err);
+    b.RINV = dalloc<int32_t>(C, err);
+    b.DP = dalloc<int2>(C, err);
+    b.NRM = dalloc<int2>(C, err);
+    b.HEAT = dalloc<int32_t>(C, err);
+    b.CORR = dalloc<int32_t>(C, err);
+    b.NBR = dalloc<uint32_t>(C * MAXNBR, err);
+    b.NBRN = dalloc<uint32_t>(C, err);
+    b.nbrStride = (uint32_t)C;
+    int32_t* dl = dalloc<int32_t>(LUT_WORDS, err);
+    int32_t* dm = dalloc<int32_t>(MAT_MAX * MAT_WORDS, err);
+    b.scenes = dalloc<ScenePar>(scenesCap, err);
+    b.world = dalloc<WorldPar>(1, err);
+    b.acc = dalloc<uint32_t>((size_t)scenesCap * 8, err);
+    b.accLast = dalloc<uint32_t>((size_t)scenesCap * 8, err);
+    b.chain = dalloc<uint32_t>((size_t)scenesCap * 8, err);
+    b.dbg = dalloc<uint32_t>(16, err);
+    b.err = dalloc<uint32_t>(4, err);
+    tmpK = dalloc<uint32_t>(C, err);
+    tmpV = dalloc<uint32_t>(C, err);
+    hist = dalloc<uint32_t>(radix::hist_words((uint32_t)C), err);
+    hits = dalloc<uint32_t>(1, err);
+    accTmp = dalloc<uint32_t>((size_t)scenesCap * 8, err);
+    devEp = dalloc<EvPar>(scenesCap, err);
+    if (!err.empty()) return false;
+    cudaMemcpy(dl, o->luts, sizeof(int32_t) * LUT_WORDS, cudaMemcpyHostToDevice);
+    cudaMemcpy(dm, hmats, sizeof(hmats), cudaMemcpyHostToDevice);
+    b.luts = dl;
+    b.mats = dm;
+    sh.assign(scenesCap, SceneHost{});
+    hpar.assign(scenesCap, ScenePar{});
+    return cuda_ok(cudaDeviceSynchronize(), "init");
+  }
+
+  const int32_t* row(uint32_t m) const { return hmats + m * MAT_WORDS; }
+  bool seal_row(uint32_t m) const {
+    const int32_t* r = row(m);
+    return r[M_bondK] != 0 && r[M_bondReform] == 0 && r[M_solidMode] != 0 && r[M_phantom] == 0;
+  }
+  bool spawn_welds(uint32_t m) const { return row(m)[M_bondGroup] >= 0 && row(m)[M_bondReform] == 0; }
+
+  // Which optional passes the loaded rows (and every row a transition can turn
+  // them into, except the unsupported seal-class rows) need.
+  void update_features() {
+    std::vector<bool> seen(matCount, false);
+    std::vector<uint32_t> stack;
+    for (auto& s : sh) {
+      if (!s.used) continue;
+      for (uint32_t m : s.mat)
+        if (m < matCount && !seen[m]) { seen[m] = true; stack.push_back(m); }
+    }
+    // spawns may add any row: be conservative once a scene exists
+    while (!stack.empty()) {
+      uint32_t m = stack.back();
+      stack.pop_back();
+      for (int f : {M_meltTo, M_freezeTo, M_boilTo, M_condTo, M_burnTo, M_splitTo, M_corrTo}) {
+        uint32_t t = (uint32_t)row(m)[f];
+        if (t < matCount && !seen[t] && !seal_row(t)) { seen[t] = true; stack.push_back(t); }
+      }
+    }
+    bool fr = false, bo = false;
+    for (uint32_t m = 0; m < matCount; ++m) {
+      if (!seen[m] || seal_row(m)) continue;
+      if (row(m)[M_fric] != 0 || row(m)[M_bondK] != 0) fr = true;
+      if (row(m)[M_bondK] != 0) bo = true;
+    }
+    if (fr != hasFriction || bo != hasBonds) graphValid = false;
+    hasFriction = fr;
+    hasBonds = bo;
+  }
+
+  // Recompute the colour-major key layout over the active scenes.
+  bool relayout() {
+    uint32_t counts[4] = {0, 0, 0, 0};
+    uint32_t slotEnd = 0, nAct = 0, numScenes = 0;
+    for (uint32_t s = 0; s < maxScenes; ++s) {
+      SceneHost& h = sh[s];
+      ScenePar& p = hpar[s];
+      if (!h.used) { p.active = 0; continue; }
+      numScenes = s + 1;
+      slotEnd = std::max(slotEnd, h.slotBase + h.cap);
+      if (!h.loaded) { p.active = 0; continue; }
+      nAct += h.n;
+      for (int c = 0; c < 4; ++c) {
+        uint32_t nA = (h.gridW + 1 - (c & 1)) / 2;
+        uint32_t nB = (h.gridH + 1 - (c >> 1)) / 2;
+        p.keyOff[c] = counts[c];  // relative for now
+        p.nA[c] = nA;
+        counts[c] += nA * nB;
+      }
+    }
+    uint64_t K = (uint64_t)counts[0] + counts[1] + counts[2] + counts[3];
+    if (K > maxCells) return fail("total grid cells %llu exceed max_cells %u", (unsigned long long)K, maxCells);
+    uint32_t base[5];
+    base[0] = 0;
+    for (int c = 0; c < 4; ++c) base[c + 1] = base[c] + counts[c];
+    for (uint32_t s = 0; s < maxScenes; ++s)
+      if (sh[s].used && sh[s].loaded)
+        for (int c = 0; c < 4; ++c) hpar[s].keyOff[c] += base[c];
+    hw.numScenes = numScenes;
+    hw.K = (uint32_t)K;
+    for (int c = 0; c < 5; ++c) hw.colourBase[c] = base[c];
+    hw.slotEnd = slotEnd;
+    hw.nAct = nAct;
+    update_features();
+    hw.hasFriction = hasFriction;
+    hw.hasBonds = hasBonds;
+    layoutDirty = false;
+    graphValid = false;
+    bool ok = cuda_ok(cudaMemcpyAsync(b.world, &hw, sizeof(hw), cudaMemcpyHostToDevice, st), "world") &&
+              cuda_ok(cudaMemcpyAsync(b.scenes, hpar.data(), sizeof(ScenePar) * maxScenes,
+                                      cudaMemcpyHostToDevice, st), "scenes");
+    return ok && cuda_ok(cudaStreamSynchronize(st), "relayout");
+  }
+
+  // Fetch the device-side scene parameters (clocks move on the device).
+  bool pull_params() {
+    if (!cuda_ok(cudaMemcpyAsync(hpar.data(), b.scenes, sizeof(ScenePar) * maxScenes, cudaMemcpyDeviceToHost, st),
+                 "pull"))
+      return false;
+    return cuda_ok(cudaStreamSynchronize(st), "pull");
+  }
+  bool push_scene(uint32_t s) {
+    return cuda_ok(cudaMemcpyAsync(b.scenes + s, &hpar[s], sizeof(ScenePar), cudaMemcpyHostToDevice, st), "push");
+  }
+
+  bool validate_scene(const sn_scene* sc, uint32_t cap) {
+    if (!sc) return fail("scene is NULL");
+    if (sc->n_fluid > sc->n) return fail("scene.nFluid out of range");
+    if (sc->n > cap) return fail("scene.n = %u exceeds maxParticles = %u", sc->n, cap);
+    if (sc->n > 0 && (!sc->pos || !sc->vel || !sc->mat_id)) return fail("scene arrays missing");
+    for (uint32_t i = 0; i < sc->n; ++i) {
+      if (sc->mat_id[i] >= matCount) return fail("matId[%u] = %u >= matCount %u", i, sc->mat_id[i], matCount);
+      int32_t lo = i < sc->n_fluid ? 0 : -MAX_POS;
+      if (sc->pos[2 * i] < lo || sc->pos[2 * i] > MAX_POS || sc->pos[2 * i + 1] < lo || sc->pos[2 * i + 1] > MAX_POS)
+        return fail("pos[%u] outside [%d, 2^27]", i, lo);
+      if (sc->flags && (sc->flags[i] & ~FLAG_MASK)) return fail("flags[%u] sets a reserved bit", i);
+      if (sc->temp && (sc->temp[i] < TEMP_MIN || sc->temp[i] > TEMP_MAX)) return fail("temp[%u] out of range", i);
+      if (sc->fuel && sc->fuel[i] < 0) return fail("fuel[%u] < 0", i);
+      if (seal_row(sc->mat_id[i]))
+        return fail("matId[%u] = %u is a seal-class solid; containment and rigid bodies are not built", i,
+                    sc->mat_id[i]);
+      uint32_t want = row(sc->mat_id[i])[M_phantom] != 0 ? FLAG_DEAD : 0u;
+      if (sc->flags && (sc->flags[i] & FLAG_DEAD) && !want) return fail("flags[%u] sets FLAG_DEAD on a live row", i);
+    }
+    if (sc->cell_shift < 1 || sc->cell_shift > 27) return fail("cellShift outside 1..27");
+    if ((1u << sc->cell_shift) < (uint32_t)KERNEL_H) return fail("cells smaller than the kernel radius");
+    if (sc->dom_w < 2 * 32768 || sc->dom_h < 2 * 32768) return fail("domain smaller than the wall margin");
+    return true;
+  }
+
+  // loadScene packing (src/engine.js:3704-3951) into scene s.
+  bool load(uint32_t s, const sn_scene* sc) {
+    SceneHost& h = sh[s];
+    if (!validate_scene(sc, h.cap)) return false;
+    uint32_t cs = 1u << sc->cell_shift;
+    uint32_t gW = std::max<uint32_t>(1, (uint32_t)(((int64_t)sc->dom_w + cs - 1) / cs));
+    uint32_t gH = std::max<uint32_t>(1, (uint32_t)(((int64_t)sc->dom_h + cs - 1) / cs));
+    h.n = sc->n;
+    h.nFluid = sc->n_fluid;
+    h.gridW = gW;
+    h.gridH = gH;
+    h.cellShift = sc->cell_shift;
+    h.cellTotal = gW * gH;
+    h.domW = sc->dom_w;
+    h.domH = sc->dom_h;
+    h.substeps = 0;
+    h.nFluid0 = sc->n_fluid;
+    h.pos.assign(sc->pos, sc->pos + 2 * (size_t)sc->n);
+    h.mat.assign(sc->mat_id, sc->mat_id + sc->n);
+    h.hasTemp = sc->temp != nullptr;
+    h.hasFuel = sc->fuel != nullptr;
+    h.temp.assign(sc->n, 0);
+    h.fuel.assign(sc->n, 0);
+    if (sc->temp) h.temp.assign(sc->temp, sc->temp + sc->n);
+    if (sc->fuel) h.fuel.assign(sc->fuel, sc->fuel + sc->n);
+    h.weldSeq = 1;
+    h.events.clear();
+    h.consumed = 0;
+    eventsDirty = true;
+    std::vector<int32_t> stw((size_t)h.cap * 8, 0);
+    for (uint32_t i = 0; i < sc->n; ++i) {
+      uint32_t m = sc->mat_id[i];
+      const int32_t* r = row(m);
+      uint32_t want = r[M_phantom] != 0 ? FLAG_DEAD : 0u;
+      uint32_t given = sc->flags ? sc->flags[i] : 0u;
+      uint32_t tag = (i < sc->n_fluid && spawn_welds(m)) ? (1u << 8) : 0u;
+      int32_t* w = &stw[(size_t)i * 8];
+      w[0] = sc->pos[2 * i];
+      w[1] = sc->pos[2 * i + 1];
+      w[2] = sc->vel[2 * i];
+      w[3] = sc->vel[2 * i + 1];
+      w[4] = (int32_t)m;
+      w[5] = (int32_t)(given | want | (seal_row(m) ? FLAG_SEAL : 0u) | tag);
+      w[6] = sc->temp ? sc->temp[i] : AMBIENT;
+      w[7] = sc->fuel ? sc->fuel[i] : r[M_fuel0];
+    }
+    std::vector<uint32_t> so(h.cap, s);
+    bool ok = cuda_ok(cudaMemcpyAsync(b.state + (size_t)h.slotBase * 8, stw.data(), stw.size() * 4,
+                                      cudaMemcpyHostToDevice, st), "state") &&
+              cuda_ok(cudaMemsetAsync(b.stacc + h.slotBase, 0, sizeof(int2) * h.cap, st), "stacc") &&
+              cuda_ok(cudaMemsetAsync(b.bond + (size_t)h.slotBase * BOND_CAP, 0, 4ull * BOND_CAP * h.cap, st), "bond") &&
+              cuda_ok(cudaMemsetAsync(b.bondCand + (size_t)h.slotBase * BOND_CAP, 0, 4ull * BOND_CAP * h.cap, st),
+                      "bondCand") &&
+              cuda_ok(cudaMemcpyAsync(b.sceneOf + h.slotBase, so.data(), 4ull * h.cap, cudaMemcpyHostToDevice, st),
+                      "sceneOf");
+    if (!ok) return false;
+    ScenePar& p = hpar[s];
+    p = ScenePar{};
+    p.slotBase = h.slotBase;
+    p.cap = h.cap;
+    p.n = h.n;
+    p.nFluid = h.nFluid;
+    p.gridW = gW;
+    p.gridH = gH;
+    p.cellShift = h.cellShift;
+    p.cellTotal = h.cellTotal;
+    p.domW = h.domW;
+    p.domH = h.domH;
+    p.vmax = VMAX;
+    p.weldHold = 0;
+    p.formClock = 0;
+    p.bondDirty = 1;
+    p.formNow = 0;
+    p.active = 1;
+    h.loaded = true;
+    if (!reset_chain(s)) return false;
+    uint32_t zero8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    cudaMemcpyAsync(b.acc + s * 8, zero8, 32, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(b.accLast + s * 8, zero8, 32, cudaMemcpyHostToDevice, st);
+    cudaMemsetAsync(b.dbg, 0, 64, st);
+    cudaMemsetAsync(b.err, 0, 16, st);
+    return relayout();
+  }
+
+  bool reset_chain(uint32_t s) {
+    static const uint32_t CHAIN_INIT[8] = {0x243f6a88u, 0x85a308d3u, 0x13198a2eu, 0x03707344u,
+                                           0xa4093822u, 0x299f31d0u, 0x082efa98u, 0xec4e6c89u};
+    return cuda_ok(cudaMemcpyAsync(b.chain + s * 8, CHAIN_INIT, 32, cudaMemcpyHostToDevice, st), "chain");
+  }
+
+  int grid_for(uint64_t items) const {
+    uint64_t g = (items + 255) / 256;
+    uint64_t cap = (uint64_t)numSMs * 8;
+    if (g > cap) g = cap;
+    return (int)std::max<uint64_t>(g, 1);
+  }
+
+  template <bool DBG>
+  void launch_substep() {
+    const int gs = grid_for(hw.slotEnd);
+    const int ga = grid_for(hw.nAct);
+    uint64_t L = 0;
+    if (anyEvents) {
+      k_impulse_sched<<<hw.numScenes, 256, 0, st>>>(b, devEv, devEp);
+      ++L;
+    }
+    k_predict_key<DBG><<<gs, 256, 0, st>>>(b);
+    ++L;
+    int bits = 1;
+    while ((1ull << bits) <= hw.K) ++bits;
+    radix::sort_pairs(b.keys, hw.slotEnd, bits, b.skey, b.sslot, tmpK, tmpV, hist, st);
+    L += 3ull * ((bits + radix::RBITS - 1) / radix::RBITS);
+    k_cellstart<<<grid_for((uint64_t)hw.K + 1), 256, 0, st>>>(b);
+    k_gather<<<ga, 256, 0, st>>>(b);
+    k_nbr<DBG><<<ga, 256, 0, st>>>(b);
+    L += 3;
+    for (uint32_t it = 0; it < iters; ++it) {
+      k_solveA<DBG><<<ga, 256, 0, st>>>(b, b.P, it + 1 == iters ? 1 : 0);
+      for (int c = 0; c < 4; ++c) k_colour<DBG><<<ga, 256, 0, st>>>(b, b.P, c);
+      L += 5;
+      if (hasFriction) {
+        k_friction<DBG><<<ga, 256, 0, st>>>(b, b.P);
+        k_apply_fric<DBG><<<ga, 256, 0, st>>>(b, b.P);
+        L += 2;
+      }
+    }
+    k_post1<DBG><<<ga, 256, 0, st>>>(b, b.P);
+    ++L;
+    if (hasBonds) {
+      k_post2<DBG, false><<<ga, 256, 0, st>>>(b, b.P, 0);
+      k_form1<DBG><<<ga, 256, 0, st>>>(b);
+      k_form2<<<gs, 256, 0, st>>>(b);
+      L += 3;
+      if (chainOn) {
+        k_hash<<<gs, 256, 0, st>>>(b, b.acc);
+        ++L;
+      }
+    } else if (chainOn) {
+      k_post2<DBG, true><<<ga, 256, 0, st>>>(b, b.P, 1);
+      ++L;
+    } else {
+      k_post2<DBG, false><<<ga, 256, 0, st>>>(b, b.P, 1);
+      ++L;
+    }
+    k_fold<<<(hw.numScenes + 63) / 64, 64, 0, st>>>(b, chainOn ? 1 : 0);
+    ++L;
+    launchesPerSubstep = L;
+  }
+
+  void launch_one() {
+    if (debug) launch_substep<true>();
+    else launch_substep<false>();
+  }
+
+  bool upload_events() {
+    std::vector<ImpulseEv> all;
+    std::vector<EvPar> ep(maxScenes, EvPar{0, 0, 0, 0});
+    anyEvents = false;
+    for (uint32_t s = 0; s < maxScenes; ++s) {
+      SceneHost& h = sh[s];
+      ep[s].begin = (uint32_t)all.size();
+      if (h.used && h.loaded) {
+        uint32_t consumed = 0;
+        for (const ImpulseEv& e : h.events)
+          if ((uint64_t)e.at < h.substeps) ++consumed;
+        for (const ImpulseEv& e : h.events) all.push_back(e);
+        ep[s].cursor = ep[s].begin + consumed;
+        if (consumed < h.events.size()) anyEvents = true;
+      } else {
+        ep[s].cursor = ep[s].begin;
+      }
+      ep[s].end = (uint32_t)all.size();
+    }
+    if (all.size() > devEvCap) {
+      if (devEv) cudaFree(devEv);
+      devEvCap = std::max<size_t>(all.size(), 256);
+      devEv = dalloc<ImpulseEv>(devEvCap, err);
+      if (!devEv) return false;
+    }
+    if (!all.empty() &&
+        !cuda_ok(cudaMemcpyAsync(devEv, all.data(), all.size() * sizeof(ImpulseEv), cudaMemcpyHostToDevice, st),
+                 "events"))
+      return false;
+    if (!cuda_ok(cudaMemcpyAsync(devEp, ep.data(), ep.size() * sizeof(EvPar), cudaMemcpyHostToDevice, st), "ep"))
+      return false;
+    eventsDirty = false;
+    graphValid = false;
+    return true;
+  }
+
+  bool step(uint32_t count) {
+    if (hw.nAct == 0 && count > 0) {
+      bool any = false;
+      for (auto& s : sh) any |= (s.used && s.loaded);
+      if (!any) return fail("step() called before loadScene()");
+    }
+    if (count == 0) return true;
+    if (layoutDirty && !relayout()) return false;
+    if (eventsDirty && !upload_events()) return false;
+    if (useGraph && !graphValid) {
+      if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
+      if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
+      if (!cuda_ok(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "capture")) return false;
+      launch_one();
+      if (!cuda_ok(cudaStreamEndCapture(st, &graph), "endCapture")) return false;
+      if (!cuda_ok(cudaGraphInstantiate(&gexec, graph, 0), "instantiate")) return false;
+      graphValid = true;
+    }
+    cudaEventRecord(ev0, st);
+    for (uint32_t i = 0; i < count; ++i) {
+      if (useGraph) {
+        if (!cuda_ok(cudaGraphLaunch(gexec, st), "graphLaunch")) return false;
+      } else {
+        launch_one();
+      }
+    }
+    cudaEventRecord(ev1, st);
+    for (auto& s : sh)
+      if (s.used && s.loaded) s.substeps += count;
+    lastLaunches = launchesPerSubstep * count;
+    return cuda_ok(cudaGetLastError(), "step");
+  }
+
+  bool timing(float* ms) {
+    if (!cuda_ok(cudaEventSynchronize(ev1), "timing")) return false;
+    cudaEventElapsedTime(ms, ev0, ev1);
+    return true;
+  }
+
+  bool digest(uint32_t s, uint32_t out[8]) {
+    if (layoutDirty && !relayout()) return false;
+    cudaMemsetAsync(accTmp, 0, sizeof(uint32_t) * 8 * maxScenes, st);
+    k_hash<<<grid_for(hw.slotEnd), 256, 0, st>>>(b, accTmp);
+    cudaMemcpyAsync(out, accTmp + s * 8, 32, cudaMemcpyDeviceToHost, st);
+    return cuda_ok(cudaStreamSynchronize(st), "digest");
+  }
+  bool read_words(const void* dsrc, void* out, size_t bytes) {
+    cudaMemcpyAsync(out, dsrc, bytes, cudaMemcpyDeviceToHost, st);
+    return cuda_ok(cudaStreamSynchronize(st), "read");
+  }
+
+  bool impulse_now(uint32_t s, int32_t cx, int32_t cy, int32_t r, int32_t ix, int32_t iy, uint32_t limit,
+                   uint32_t* hitsOut) {
+    ImpulseEv ev{0, cx, cy, r, ix, iy, limit, 0};
+    k_impulse_now<<<1, 256, 0, st>>>(b, s, ev, hits);
+    uint32_t h = 0;
+    cudaMemcpyAsync(&h, hits, 4, cudaMemcpyDeviceToHost, st);
+    if (!cuda_ok(cudaStreamSynchronize(st), "impulse")) return false;
+    if (hitsOut) *hitsOut = h;
+    return true;
+  }
+
+  // spawnFluid (src/engine.js:5901-6020) for scene s.
+  bool spawn(uint32_t s, const sn_particle* list, uint32_t k, bool noWeld, uint32_t* nOut) {
+    SceneHost& h = sh[s];
+    if (!h.loaded) return fail("spawn before loadScene");
+    if (k == 0) { if (nOut) *nOut = h.n; return true; }
+    uint32_t nB = h.n - h.nFluid;
+    uint32_t newFluid = h.nFluid + k, newN = newFluid + nB;
+    if (newN > h.cap) { if (nOut) *nOut = h.n; return true; }
+    for (uint32_t i = 0; i < k; ++i) {
+      int32_t mm = std::min<int32_t>((int32_t)matCount - 1, std::max<int32_t>(0, list[i].mat));
+      if (seal_row((uint32_t)mm)) return fail("spawn of seal-class row %d is not supported", mm);
+      if (!noWeld && spawn_welds((uint32_t)mm)) return fail("weld-group spawns are not supported");
+    }
+    uint32_t total = k + nB;
+    std::vector<int32_t> stw((size_t)total * 8, 0);
+    for (uint32_t i = 0; i < k; ++i) {
+      const sn_particle& q = list[i];
+      uint32_t m = (uint32_t)std::min<int32_t>((int32_t)matCount - 1, std::max<int32_t>(0, q.mat));
+      const int32_t* r = row(m);
+      int32_t* w = &stw[(size_t)i * 8];
+      w[0] = q.x;
+      w[1] = q.y;
+      w[2] = q.vx;
+      w[3] = q.vy;
+      w[4] = (int32_t)m;
+      w[5] = (int32_t)((q.flags & SPAWN_FLAG_MASK) | (r[M_phantom] != 0 ? FLAG_DEAD : 0u));
+      int32_t t = q.has_temp ? q.temp : r[M_spawnTemp];
+      w[6] = std::max(TEMP_MIN, std::min(TEMP_MAX, t));
+      w[7] = std::max(0, q.has_fuel ? q.fuel : r[M_fuel0]);
+    }
+    for (uint32_t bb = 0; bb < nB; ++bb) {
+      uint32_t src = h.nFluid0 + bb;
+      int32_t* w = &stw[(size_t)(k + bb) * 8];
+      w[0] = h.pos[2 * src];
+      w[1] = h.pos[2 * src + 1];
+      w[4] = (int32_t)h.mat[src];
+      w[6] = h.hasTemp ? h.temp[src] : AMBIENT;
+      w[7] = h.hasFuel ? h.fuel[src] : row(h.mat[src])[M_fuel0];
+    }
+    size_t off = (size_t)h.slotBase + h.nFluid;
+    bool ok = cuda_ok(cudaMemcpyAsync(b.state + off * 8, stw.data(), stw.size() * 4, cudaMemcpyHostToDevice, st),
+                      "spawn state") &&
+              cuda_ok(cudaMemsetAsync(b.stacc + off, 0, sizeof(int2) * total, st), "spawn stacc") &&
+              cuda_ok(cudaMemsetAsync(b.bond + off * BOND_CAP, 0, 4ull * BOND_CAP * k, st), "spawn bond") &&
+              cuda_ok(cudaMemsetAsync(b.bondCand + off * BOND_CAP, 0, 4ull * BOND_CAP * k, st), "spawn cand");
+    if (!ok || !pull_params()) return false;
+    h.n = newN;
+    h.nFluid = newFluid;
+    for (uint32_t i = 0; i < k; ++i) h.mat.push_back((uint32_t)std::max(0, list[i].mat));
+    hpar[s].n = newN;
+    hpar[s].nFluid = newFluid;
+    hpar[s].bondDirty = 1;
+    hw.nAct += k;
+    update_features();
+    hw.hasFriction = hasFriction;
+    hw.hasBonds = hasBonds;
+    ok = push_scene(s) &&
+         cuda_ok(cudaMemcpyAsync(b.world, &hw, sizeof(hw), cudaMemcpyHostToDevice, st), "world") &&
+         cuda_ok(cudaStreamSynchronize(st), "spawn");
+    if (nOut) *nOut = newN;
+    return ok;
+  }
+
+  bool write_state(uint32_t s, const int32_t* state, const int32_t* scratch, size_t n) {
+    SceneHost& h = sh[s];
+    if (!h.loaded) return fail("write_state before loadScene");
+    if (n != h.n) return fail("write_state: n = %zu but the loaded scene has %u", n, h.n);
+    size_t off = h.slotBase;
+    bool ok = cuda_ok(cudaMemcpyAsync(b.state + off * 8, state, n * 32, cudaMemcpyHostToDevice, st), "state");
+    if (scratch) ok = ok && cuda_ok(cudaMemcpyAsync(b.stacc + off, scratch, n * 8, cudaMemcpyHostToDevice, st), "stacc");
+    else ok = ok && cuda_ok(cudaMemsetAsync(b.stacc + off, 0, n * 8, st), "stacc");
+    return ok && cuda_ok(cudaStreamSynchronize(st), "write_state");
+  }
+
+  bool check() {
+    uint32_t e[4] = {0, 0, 0, 0};
+    cudaMemcpyAsync(e, b.err, 16, cudaMemcpyDeviceToHost, st);
+    if (!cuda_ok(cudaStreamSynchronize(st), "checkErrors")) return false;
+    if (!cuda_ok(cudaGetLastError(), "checkErrors")) return false;
+    if (e[0] & ERR_UNSUPPORTED_ROW)
+      return fail("a transition produced a seal-class row (containment is not built); results past it are not "
+                  "the reference's");
+    if (e[0] & ERR_BOND_PARTNER) return fail("a bond partner slot exceeds the 17-bit bond word");
+    return true;
+  }
+
+  // Slot allocation for a new scene: first fit over released ranges.
+  bool alloc_scene(uint32_t cap, uint32_t* id) {
+    uint32_t s = 0;
+    while (s < maxScenes && sh[s].used) ++s;
+    if (s == maxScenes) return fail("max_scenes reached");
+    // find a free slot range [base, base+cap)
+    std::vector<std::pair<uint32_t, uint32_t>> usedR;
+    for (auto& h : sh)
+      if (h.used) usedR.push_back({h.slotBase, h.slotBase + h.cap});
+    std::sort(usedR.begin(), usedR.end());
+    uint32_t base = 0;
+    bool found = false;
+    for (auto& r : usedR) {
+      if (r.first >= base + cap) { found = true; break; }
+      base = std::max(base, r.second);
+    }
+    if (!found && (uint64_t)base + cap > capSlots) return fail("no room for %u slots", cap);
+    sh[s] = SceneHost{};
+    sh[s].used = true;
+    sh[s].slotBase = base;
+    sh[s].cap = cap;
+    *id = s;
+    layoutDirty = true;
+    return true;
+  }
+};
+
+struct sn_engine {
+  World w;
+};
+struct sn_batch {
+  World w;
+};
+
+static int rc_of(World& w, bool ok) { return ok ? SN_OK : (w.err.find("cuda") != std::string::npos ? SN_E_CUDA : SN_E_INVALID); }
+
+extern "C" {
+
+int sn_create(const sn_opts* opts, sn_engine** out) {
+  if (!out) return SN_E_INVALID;
+  *out = nullptr;
+  sn_engine* e = new sn_engine();
+  if (!e->w.init(opts, 1)) {
+    fprintf(stderr, "[suna] create: %s\n", e->w.err.c_str());
+    delete e;
+    return SN_E_INVALID;
+  }
+  uint32_t id = 0;
+  e->w.alloc_scene(opts->max_particles, &id);
+  *out = e;
+  return SN_OK;
+}
+void sn_destroy(sn_engine* e) { delete e; }
+const char* sn_last_error(const sn_engine* e) { return e ? e->w.err.c_str() : "null engine"; }
+int sn_load_scene(sn_engine* e, const sn_scene* sc) {
+  if (!e) return SN_E_INVALID;
+  return rc_of(e->w, e->w.load(0, sc));
+}
+int sn_step(sn_engine* e, uint32_t count, uint64_t* substeps) {
+  if (!e) return SN_E_INVALID;
+  if (!e->w.sh[0].loaded) { e->w.err = "step() called before loadScene()"; return SN_E_STATE; }
+  bool ok = e->w.step(count);
+  if (substeps) *substeps = e->w.sh[0].substeps;
+  return rc_of(e->w, ok);
+}
+int sn_digest(sn_engine* e, uint32_t acc[8]) {
+  if (!e || !acc) return SN_E_INVALID;
+  return rc_of(e->w, e->w.digest(0, acc));
+}
+int sn_chain(sn_engine* e, uint32_t chain[8]) {
+  if (!e || !chain) return SN_E_INVALID;
+  return rc_of(e->w, e->w.read_words(e->w.b.chain, chain, 32));
+}
+int sn_reset_chain(sn_engine* e) {
+  if (!e) return SN_E_INVALID;
+  return rc_of(e->w, e->w.reset_chain(0) && e->w.cuda_ok(cudaStreamSynchronize(e->w.st), "reset"));
+}
+int sn_read_state(sn_engine* e, int32_t* out, size_t words) {
+  if (!e || !out) return SN_E_INVALID;
+  SceneHost& h = e->w.sh[0];
+  if (words < (size_t)h.n * 8) { e->w.err = "output buffer too small"; return SN_E_INVALID; }
+  return rc_of(e->w, e->w.read_words(e->w.b.state + (size_t)h.slotBase * 8, out, (size_t)h.n * 32));
+}
+int sn_read_scratch(sn_engine* e, int32_t* out, size_t words) {
+  if (!e || !out) return SN_E_INVALID;
+  SceneHost& h = e->w.sh[0];
+  if (words < (size_t)h.n * 2) { e->w.err = "output buffer too small"; return SN_E_INVALID; }
+  return rc_of(e->w, e->w.read_words(e->w.b.stacc + h.slotBase, out, (size_t)h.n * 8));
+}
+int sn_write_state(sn_engine* e, const int32_t* state, const int32_t* scratch, size_t n) {
+  if (!e || !state) return SN_E_INVALID;
+  return rc_of(e->w, e->w.write_state(0, state, scratch, n));
+}
+int sn_read_bonds(sn_engine* e, uint32_t* out, size_t words) {
+  if (!e || !out) return SN_E_INVALID;
+  SceneHost& h = e->w.sh[0];
+  if (words < (size_t)h.nFluid * BOND_CAP) { e->w.err = "output buffer too small"; return SN_E_INVALID; }
+  return rc_of(e->w, e->w.read_words(e->w.b.bond + (size_t)h.slotBase * BOND_CAP, out, (size_t)h.nFluid * BOND_CAP * 4));
+}
+int sn_spawn(sn_engine* e, const sn_particle* list, uint32_t k, uint32_t no_weld, uint32_t* n_out) {
+  if (!e || (k && !list)) return SN_E_INVALID;
+  return rc_of(e->w, e->w.spawn(0, list, k, no_weld != 0, n_out));
+}
+int sn_impulse(sn_engine* e, int32_t cx, int32_t cy, int32_t r, int32_t ix, int32_t iy, uint32_t limit,
+               uint32_t* hits) {
+  if (!e) return SN_E_INVALID;
+  if (!e->w.sh[0].loaded) { e->w.err = "impulse before loadScene"; return SN_E_STATE; }
+  return rc_of(e->w, e->w.impulse_now(0, cx, cy, r, ix, iy, limit, hits));
+}
+int sn_debug_counters(sn_engine* e, uint32_t out[16]) {
+  if (!e || !out) return SN_E_INVALID;
+  return rc_of(e->w, e->w.read_words(e->w.b.dbg, out, 64));
+}
+int sn_check_errors(sn_engine* e) {
+  if (!e) return SN_E_INVALID;
+  if (e->w.check()) return SN_OK;
+  return e->w.err.find("cuda") != std::string::npos ? SN_E_CUDA : SN_E_DEVICE;
+}
+int sn_sync(sn_engine* e) {
+  if (!e) return SN_E_INVALID;
+  return rc_of(e->w, e->w.cuda_ok(cudaStreamSynchronize(e->w.st), "sync"));
+}
+int sn_get_info(sn_engine* e, sn_info* out) {
+  if (!e || !out) return SN_E_INVALID;
+  World& w = e->w;
+  if (!w.pull_params()) return SN_E_CUDA;
+  SceneHost& h = w.sh[0];
+  out->n = h.n;
+  out->n_fluid = h.nFluid;
+  out->substep_count = h.substeps;
+  out->formation_clock = w.hpar[0].formClock;
+  out->grid_w = h.gridW;
+  out->grid_h = h.gridH;
+  out->cell_total = h.cellTotal;
+  return SN_OK;
+}
+int sn_set_formation_clock(sn_engine* e, uint64_t clock, uint32_t dirty) {
+  if (!e) return SN_E_INVALID;
+  World& w = e->w;
+  if (!w.pull_params()) return SN_E_CUDA;
+  w.hpar[0].formClock = (uint32_t)clock;
+  w.hpar[0].bondDirty = dirty ? 1u : 0u;
+  return rc_of(w, w.push_scene(0) && w.cuda_ok(cudaStreamSynchronize(w.st), "clock"));
+}
+int sn_last_timing(sn_engine* e, float* ms, uint64_t* launches) {
+  if (!e) return SN_E_INVALID;
+  if (ms && !e->w.timing(ms)) return SN_E_CUDA;
+  if (launches) *launches = e->w.lastLaunches;
+  return SN_OK;
+}
+
+// ---- batch ------------------------------------------------------------------
+int sn_batch_create(const sn_opts* opts, uint32_t max_scenes, sn_batch** out) {
+  if (!out || max_scenes == 0) return SN_E_INVALID;
+  *out = nullptr;
+  sn_batch* b = new sn_batch();
+  if (!b->w.init(opts, max_scenes)) {
+    fprintf(stderr, "[suna] batch create: %s\n", b->w.err.c_str());
+    delete b;
+    return SN_E_INVALID;
+  }
+  *out = b;
+  return SN_OK;
+}
+void sn_batch_destroy(sn_batch* b) { delete b; }
+const char* sn_batch_last_error(const sn_batch* b) { return b ? b->w.err.c_str() : "null batch"; }
+int sn_batch_add_scene(sn_batch* b, const sn_scene* sc, uint32_t capacity, uint32_t* id) {
+  if (!b || !sc || !id) return SN_E_INVALID;
+  World& w = b->w;
+  uint32_t cap = std::max(capacity, sc->n);
+  uint32_t s = 0;
+  if (!w.alloc_scene(cap, &s)) return SN_E_CAPACITY;
+  if (!w.load(s, sc)) {
+    w.sh[s].used = false;
+    w.layoutDirty = true;
+    return rc_of(w, false);
+  }
+  *id = s;
+  return SN_OK;
+}
+int sn_batch_remove_scene(sn_batch* b, uint32_t id) {
+  if (!b || id >= b->w.maxScenes || !b->w.sh[id].used) return SN_E_INVALID;
+  World& w = b->w;
+  w.sh[id] = SceneHost{};
+  w.hpar[id] = ScenePar{};
+  w.layoutDirty = true;
+  w.eventsDirty = true;
+  return rc_of(w, w.relayout());
+}
+int sn_batch_step(sn_batch* b, uint32_t count) {
+  if (!b) return SN_E_INVALID;
+  return rc_of(b->w, b->w.step(count));
+}
+int sn_batch_schedule_impulse(sn_batch* b, uint32_t id, uint64_t at, int32_t cx, int32_t cy, int32_t r, int32_t ix,
+                              int32_t iy, uint32_t limit) {
+  if (!b || id >= b->w.maxScenes || !b->w.sh[id].loaded) return SN_E_INVALID;
+  SceneHost& h = b->w.sh[id];
+  if (at < h.substeps) { b->w.err = "impulse scheduled in the past"; return SN_E_INVALID; }
+  if (!h.events.empty() && at < h.events.back().at) { b->w.err = "impulses must be queued in substep order"; return SN_E_INVALID; }
+  if (at > 0xffffffffull) return SN_E_INVALID;
+  h.events.push_back(ImpulseEv{(uint32_t)at, cx, cy, r, ix, iy, limit, 0});
+  b->w.eventsDirty = true;
+  return SN_OK;
+}
+int sn_batch_digest(sn_batch* b, uint32_t id, uint32_t acc[8]) {
+  if (!b || !acc || id >= b->w.maxScenes || !b->w.sh[id].loaded) return SN_E_INVALID;
+  return rc_of(b->w, b->w.digest(id, acc));
+}
+int sn_batch_chain(sn_batch* b, uint32_t id, uint32_t chain[8]) {
+  if (!b || !chain || id >= b->w.maxScenes || !b->w.sh[id].loaded) return SN_E_INVALID;
+  return rc_of(b->w, b->w.read_words(b->w.b.chain + id * 8, chain, 32));
+}
+int sn_batch_read_state(sn_batch* b, uint32_t id, int32_t* out, size_t words) {
+  if (!b || !out || id >= b->w.maxScenes || !b->w.sh[id].loaded) return SN_E_INVALID;
+  SceneHost& h = b->w.sh[id];
+  if (words < (size_t)h.n * 8) return SN_E_INVALID;
+  return rc_of(b->w, b->w.read_words(b->w.b.state + (size_t)h.slotBase * 8, out, (size_t)h.n * 32));
+}
+int sn_batch_read_scratch(sn_batch* b, uint32_t id, int32_t* out, size_t words) {
+  if (!b || !out || id >= b->w.maxScenes || !b->w.sh[id].loaded) return SN_E_INVALID;
+  SceneHost& h = b->w.sh[id];
+  if (words < (size_t)h.n * 2) return SN_E_INVALID;
+  return rc_of(b->w, b->w.read_words(b->w.b.stacc + h.slotBase, out, (size_t)h.n * 8));
+}
+int sn_batch_write_state(sn_batch* b, uint32_t id, const int32_t* state, const int32_t* scratch, size_t n,
+                         uint64_t substep_count, uint64_t formation_clock, uint32_t dirty) {
+  if (!b || !state || id >= b->w.maxScenes || !b->w.sh[id].loaded) return SN_E_INVALID;
+  World& w = b->w;
+  if (!w.write_state(id, state, scratch, n)) return rc_of(w, false);
+  if (!w.pull_params()) return SN_E_CUDA;
+  w.sh[id].substeps = substep_count;
+  w.hpar[id].formClock = (uint32_t)formation_clock;
+  w.hpar[id].bondDirty = dirty ? 1u : 0u;
+  w.hpar[id].substep = (uint32_t)substep_count;
+  w.eventsDirty = true;
+  return rc_of(w, w.push_scene(id) && w.cuda_ok(cudaStreamSynchronize(w.st), "write"));
+}
+int sn_batch_get_info(sn_batch* b, uint32_t id, sn_info* out) {
+  if (!b || !out || id >= b->w.maxScenes || !b->w.sh[id].loaded) return SN_E_INVALID;
+  World& w = b->w;
+  if (!w.pull_params()) return SN_E_CUDA;
+  SceneHost& h = w.sh[id];
+  out->n = h.n;
+  out->n_fluid = h.nFluid;
+  out->substep_count = h.substeps;
+  out->formation_clock = w.hpar[id].formClock;
+  out->grid_w = h.gridW;
+  out->grid_h = h.gridH;
+  out->cell_total = h.cellTotal;
+  return SN_OK;
+}
+int sn_batch_check_errors(sn_batch* b) {
+  if (!b) return SN_E_INVALID;
+  return b->w.check() ? SN_OK : SN_E_DEVICE;
+}
+int sn_batch_sync(sn_batch* b) {
+  if (!b) return SN_E_INVALID;
+  return rc_of(b->w, b->w.cuda_ok(cudaStreamSynchronize(b->w.st), "sync"));
+}
+int sn_batch_last_timing(sn_batch* b, float* ms, uint64_t* launches) {
+  if (!b) return SN_E_INVALID;
+  if (ms && !b->w.timing(ms)) return SN_E_CUDA;
+  if (launches) *launches = b->w.lastLaunches;
+  return SN_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,1003 @@
+// The 2D substep as sm_103a kernels.
+//
+// One substep is this kernel sequence (reference pass order,
+// src/engine.js:4003-4155, re-cut along true data dependences):
+//
+//   k_predict_key   predict (src/sim.wgsl:958-1000) + grid key per slot
+//   radix sort      stable, atomic-free: replaces gridCount/scan/scatter/canonicalize
+//   k_cellstart     cell ranges in sorted space
+//   k_gather        slot -> sorted-space working set
+//   k_nbr           neighbour lists, reference traversal order and MAXNBR cut
+//   ITERS x { k_solveA; k_colour x 4; [k_friction] }
+//                   density/lambda, then colour-classed Gauss-Seidel position
+//                   correction. solveB and applyDp are fused per colour: a CTA
+//                   owns whole cells, and the only same-colour neighbours are
+//                   in the same cell, so a CTA barrier separates "compute every
+//                   dp" from "apply" (the race src/sim.wgsl:1323-1332 guards).
+//   k_post1         finalize + xsph + normals + conduct in one neighbour sweep
+//   k_post2         surfaceTension + thermal + formation flag clear + state hash
+//   [k_form1, k_form2, k_hash]   bond formation for worlds with bonding rows
+//   k_fold          per-scene chain fold, formation clock
+//
+// Everything is int32 on the integer pipes; no floats, no atomics in the
+// physics (the only atomics are the u32 adds of the digest and the debug
+// counters, both commutative).
+#pragma once
+#include <cstdint>
+#include "fixed.cuh"
+#include "world.cuh"
+
+namespace sn {
+namespace d2 {
+
+// ---- constants: src/sim.wgsl:55-175 -----------------------------------------
+constexpr int32_t H = 163840;
+constexpr int32_t RHO0 = 1048576;
+constexpr int32_t TWO_RHO0 = 2097152;
+constexpr int32_t HS = 10240;
+constexpr int32_t H2S = 104857600;
+constexpr int OFF_W = 0, OFF_G = 3202, OFF_C = 6404, OFF_A = 9606, OFF_S = 12808;
+constexpr int32_t LAM_MAX = 4194304;
+constexpr int32_t S_TERM = 16777216;
+constexpr int32_t DP_TERM = 2097152;
+constexpr int32_t XS_TERM = 2097152;
+constexpr int32_t ST_TERM = 4194304;
+constexpr int32_t RINV_MAX = 262144;
+constexpr int32_t WALL = 32768;
+constexpr int32_t C_MAX = 58000;
+constexpr int32_t RHO_FLOOR_RINV = 32768;
+constexpr int32_t RHO_FLOOR_K = 65536;
+constexpr int32_t AMBIENT = 1310720;
+constexpr int32_t TEMP_MIN = -33554432, TEMP_MAX = 536870912;
+constexpr int32_t DT_CLAMP = 16777216;
+constexpr int32_t HT_TERM = 16777216;
+constexpr int32_t CORR_TERM = 16777216;
+constexpr int32_t CORR_NEVER = 2147483647;
+constexpr uint32_t FLAG_BURNING = 1, FLAG_DEAD = 2, FLAG_ANCHOR = 4, FLAG_RIGID = 16;
+constexpr uint32_t FLAG_CONGEAL = 32, FLAG_BURST = 64, FLAG_SEAL = 128;
+constexpr uint32_t WELD_TAG_MASK = 0x000fff00u;
+constexpr uint32_t NBRN_CONGEAL = 0x20000000u;
+constexpr uint32_t NBRN_COUNT = 0x1fffffffu;
+constexpr int FPRE = 5, RPRE = 3, BPRE = 5;
+constexpr int32_t D2_FLOOR = 262144;
+constexpr int32_t FR_TERM = 16777216;
+constexpr int32_t BOND_R2 = 17623204;
+constexpr int32_t HARD_BREAK2 = 26214400;
+constexpr int32_t L0_MAX = 5120, L0_MIN = 512;
+constexpr uint32_t BOND_J_MASK = 0x0001ffffu, BOND_L0_MASK = 0x3ffe0000u, BOND_TOMB = 0x40000000u;
+constexpr int32_t BD_TERM = 16777216;
+constexpr uint32_t MAT_PHOTO_ROW = 15;
+constexpr uint32_t INFO_BOUNDARY = 0x80000000u;
+constexpr uint32_t INFO_MAT = 0xffu;
+
+// material words (src/engine.js:678-705)
+enum : int {
+  M_eps = 0, M_dpMax = 1, M_xsph = 2, M_phantom = 3, M_gammaCoh = 4, M_gammaCur = 5, M_adhesion = 6,
+  M_grav = 7, M_cond = 8, M_coolRate = 9, M_meltPt = 11, M_meltTo = 12, M_freezePt = 13, M_freezeTo = 14,
+  M_boilPt = 15, M_boilTo = 16, M_condPt = 17, M_condTo = 18, M_ignitePt = 19, M_fuel0 = 20,
+  M_burnRate = 21, M_burnHeat = 22, M_burnTo = 23, M_splitTo = 24, M_splitPct = 25, M_spawnTemp = 26,
+  M_corrode = 28, M_corrPt = 29, M_corrTo = 30, M_fric = 31, M_bondK = 32, M_bondBreak = 33,
+  M_bondReform = 34, M_bondFormV = 35, M_bondFormP = 36, M_bondMu = 37, M_bondGroup = 38, M_rampLo = 39,
+  M_rampHi = 40, M_rampInv = 41, M_rampSign = 42, M_solidMode = 43, M_tempTarget = 44, M_tempDrive = 45
+};
+
+// All device buffers of a world, passed by value.
+struct Bufs {
+  // slot space
+  int32_t* state;       // [cap * 8] hashed particle words
+  int2* stacc;          // [cap] surface-tension acceleration, consumed next substep
+  int2* predSlot;       // [cap] predict output in slot order
+  uint32_t* sceneOf;    // [cap]
+  uint32_t* keys;       // [cap]
+  uint32_t* inv;        // [cap] slot -> sorted position
+  uint32_t* bond;       // [cap * 48] or null
+  uint32_t* bondCand;   // [cap * 48] or null
+  // sort
+  uint32_t* skey;       // [cap]
+  uint32_t* sslot;      // [cap]
+  uint32_t* cellStart;  // [K + 1]
+  // sorted space
+  int2* P;
+  int2* POS;
+  uint32_t* INFO;       // matId | INFO_BOUNDARY
+  uint32_t* FLG;
+  int32_t* TEMP;
+  uint32_t* SCN;
+  int32_t* RHO;
+  int32_t* LAM;
+  int32_t* RINV;
+  int2* DP;
+  int2* NRM;
+  int32_t* HEAT;
+  int32_t* CORR;
+  uint32_t* NBR;        // [MAXNBR][nbrStride]
+  uint32_t* NBRN;
+  uint32_t nbrStride;
+  // tables and per-scene data
+  const int32_t* luts;
+  const int32_t* mats;
+  ScenePar* scenes;
+  WorldPar* world;
+  uint32_t* acc;        // [S * 8]
+  uint32_t* accLast;    // [S * 8]
+  uint32_t* chain;      // [S * 8]
+  uint32_t* dbg;        // [16]
+  uint32_t* err;        // [4]
+};
+
+enum : uint32_t { ERR_UNSUPPORTED_ROW = 1u, ERR_BOND_PARTNER = 2u };
+
+__device__ __forceinline__ int32_t matw(const Bufs& b, uint32_t m, int w) { return __ldg(b.mats + m * MAT_WORDS + w); }
+__device__ __forceinline__ int32_t lut(const Bufs& b, int off, int i) { return __ldg(b.luts + off + i); }
+
+template <bool DBG>
+__device__ __forceinline__ int lut_index(int2 d, const Flags<DBG>& f) {
+  int32_t ax = wadd(abs_sat(d.x, f), 8) >> 4;
+  int32_t ay = wadd(abs_sat(d.y, f), 8) >> 4;
+  if (ax > HS || ay > HS) return -1;
+  int32_t r2 = wadd(wmul(ax, ax), wmul(ay, ay));
+  if (r2 >= H2S) return -1;
+  return r2 >> 15;
+}
+template <bool DBG>
+__device__ __forceinline__ int2 delta(int2 a, int2 b, const Flags<DBG>& f) {
+  return make_int2(sub_sat(a.x, b.x, f), sub_sat(a.y, b.y, f));
+}
+template <bool DBG>
+__device__ __forceinline__ int32_t grad_q16(int32_t gt, int32_t d, const Flags<DBG>& f) {
+  return mul<26>(gt, d, f);
+}
+__device__ __forceinline__ int2 wall_clamp(const ScenePar& S, int2 p) {
+  return make_int2(clampi(p.x, WALL, S.domW - WALL), clampi(p.y, WALL, S.domH - WALL));
+}
+__device__ __forceinline__ int32_t mat_mix(int32_t a, int32_t b) { return wadd(a, b) >> 1; }
+template <bool DBG>
+__device__ __forceinline__ int32_t sym_k(int32_t ri, int32_t rj, const Flags<DBG>& f) {
+  int32_t den = max(RHO_FLOOR_K, add_sat(ri, rj, f));
+  return clampi(divshift<16>(TWO_RHO0, den, f), 0, RINV_MAX);
+}
+__device__ __forceinline__ uint32_t key_of(const ScenePar& S, int32_t cx, int32_t cy) {
+  uint32_t c = (uint32_t)(cx & 1) | ((uint32_t)(cy & 1) << 1);
+  return S.keyOff[c] + (uint32_t)(cy >> 1) * S.nA[c] + (uint32_t)(cx >> 1);
+}
+__device__ __forceinline__ int2 cell_coord(const ScenePar& S, int2 p) {
+  int32_t cx = p.x >> S.cellShift;
+  int32_t cy = p.y >> S.cellShift;
+  return make_int2(clampi(cx, 0, (int32_t)S.gridW - 1), clampi(cy, 0, (int32_t)S.gridH - 1));
+}
+__device__ __forceinline__ bool seal_class(const Bufs& b, uint32_t m) {
+  return matw(b, m, M_bondK) != 0 && matw(b, m, M_bondReform) == 0 && matw(b, m, M_solidMode) != 0 &&
+         matw(b, m, M_phantom) == 0;
+}
+__device__ __forceinline__ bool fuse_row(const Bufs& b, uint32_t m) {
+  return matw(b, m, M_bondK) != 0 && matw(b, m, M_bondReform) == 0 && matw(b, m, M_bondGroup) >= 0 &&
+         m != MAT_PHOTO_ROW;
+}
+__device__ __forceinline__ uint32_t id_hash(uint32_t i) {
+  uint32_t x = i + 0x9e3779b9u;
+  x = (x ^ (x >> 16)) * 0x21f0aaadu;
+  x = (x ^ (x >> 15)) * 0x735a2d97u;
+  return x ^ (x >> 15);
+}
+__device__ __forceinline__ uint32_t pick_product(uint32_t primary, uint32_t splitTo, uint32_t pct, uint32_t i) {
+  if (pct == 0u) return primary;
+  return (id_hash(i) & 255u) < pct ? splitTo : primary;
+}
+template <bool DBG>
+__device__ __forceinline__ int32_t bond_k(const Bufs& b, uint32_t m, int32_t T, const Flags<DBG>& f) {
+  int32_t k = matw(b, m, M_bondK);
+  if (k == 0) return 0;
+  int32_t sgn = matw(b, m, M_rampSign);
+  if (sgn == 0) return k;
+  int32_t lo = matw(b, m, M_rampLo);
+  int32_t span = sub_sat(matw(b, m, M_rampHi), lo, f);
+  int32_t dT = clampi(sub_sat(T, lo, f), 0, span);
+  int32_t u = clampi(mul<16>(dT, matw(b, m, M_rampInv), f), 0, 65536);
+  if (sgn < 0) u = 65536 - u;
+  return mul<16>(k, u, f);
+}
+
+// ---- murmur state hash: src/hash/statehash.js:36-169 ----------------------------
+__device__ __forceinline__ uint32_t rotl32(uint32_t x, int r) { return __funnelshift_l(x, x, r); }
+__device__ __forceinline__ uint32_t mm_step(uint32_t h, uint32_t k) {
+  k *= 0xcc9e2d51u;
+  k = rotl32(k, 15);
+  k *= 0x1b873593u;
+  h ^= k;
+  h = rotl32(h, 13);
+  return h * 5u + 0xe6546b64u;
+}
+__device__ __forceinline__ uint32_t fmix32(uint32_t h) {
+  h ^= h >> 16;
+  h *= 0x85ebca6bu;
+  h ^= h >> 13;
+  h *= 0xc2b2ae35u;
+  h ^= h >> 16;
+  return h;
+}
+// The 8 digest lanes one particle contributes (u32-added across particles).
+__device__ __forceinline__ void particle_digest(const int32_t* w8, uint32_t idx, const uint32_t* bondRow,
+                                                uint32_t out[8]) {
+  const uint32_t SEED[4] = {0x9e3779b1u, 0x85ebca77u, 0xc2b2ae3du, 0x27d4eb2fu};
+  const uint32_t SALT[4] = {0x00000000u, 0x51633e2du, 0x9c8f2a17u, 0xd0e5b943u};
+  uint32_t h[4] = {SEED[0], SEED[1], SEED[2], SEED[3]};
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    uint32_t w = (uint32_t)w8[k];
+#pragma unroll
+    for (int l = 0; l < 4; ++l) h[l] = mm_step(h[l], w ^ SALT[l]);
+  }
+  uint32_t s[4], t[4];
+#pragma unroll
+  for (int l = 0; l < 4; ++l) { s[l] = h[l]; t[l] = h[l]; }
+  if (bondRow) {
+    uint32_t bn = 0, com = 0, scom = 0;
+    for (int k = 0; k < BOND_CAP; ++k) {
+      uint32_t w = bondRow[k];
+      if (w == 0u) break;
+      com += fmix32(((w >> 17) & 0x1fffu) ^ 0x5bd1e995u);
+      scom += fmix32(w ^ 0x2f5b3c17u);
+      bn++;
+    }
+    if (bn) {
+#pragma unroll
+      for (int l = 0; l < 4; ++l) {
+        s[l] = mm_step(s[l], bn) ^ com;
+        t[l] = mm_step(t[l], bn) ^ scom;
+      }
+    }
+  }
+#pragma unroll
+  for (int l = 0; l < 4; ++l) {
+    out[l] = fmix32(s[l] ^ 8u);
+    out[4 + l] = fmix32(mm_step(t[l], idx) ^ 9u);
+  }
+}
+
+// Warp-aggregated u32 add of 8 digest words into acc[scene]. Lanes with
+// valid == false contribute nothing. Addition mod 2^32 is commutative, so the
+// digest does not depend on the order in which warps land.
+__device__ __forceinline__ void digest_add(uint32_t* acc, bool valid, uint32_t scene, const uint32_t h[8]) {
+  uint32_t key = valid ? scene : 0xffffffffu;
+  uint32_t peers = __match_any_sync(0xffffffffu, key);
+  int lane = threadIdx.x & 31;
+  bool leader = lane == __ffs(peers) - 1;
+  // sum over the peer group with a shuffle tree restricted to the group
+#pragma unroll
+  for (int l = 0; l < 8; ++l) {
+    uint32_t v = h[l];
+    uint32_t total = 0;
+    // groups are usually the whole warp; a generic masked reduction:
+    uint32_t m = peers;
+    while (m) {
+      int src = __ffs(m) - 1;
+      m &= m - 1;
+      total += __shfl_sync(peers, v, src);
+    }
+    if (leader && valid) atomicAdd(acc + scene * 8 + l, total);
+  }
+}
+
+// ---- kernels --------------------------------------------------------------------
+
+__device__ __forceinline__ uint32_t gstride() { return gridDim.x * blockDim.x; }
+__device__ __forceinline__ uint32_t gtid() { return blockIdx.x * blockDim.x + threadIdx.x; }
+
+// predict (src/sim.wgsl:958-1000) + the grid key of every slot.
+template <bool DBG>
+__global__ void __launch_bounds__(256) k_predict_key(Bufs b) {
+  Flags<DBG> f{b.dbg};
+  const uint32_t K = b.world->K, slotEnd = b.world->slotEnd;
+  for (uint32_t slot = gtid(); slot < slotEnd; slot += gstride()) {
+    uint32_t s = b.sceneOf[slot];
+    const ScenePar& S = b.scenes[s];
+    uint32_t i = slot - S.slotBase;
+    if (!S.active || i >= S.n) { b.keys[slot] = K; continue; }
+    if (i == 0) b.scenes[s].formNow = ((S.formClock & 3u) == 0u || S.bondDirty) ? 1u : 0u;
+    const int32_t* w = b.state + (size_t)slot * 8;
+    int2 pos = make_int2(w[0], w[1]);
+    int2 pred = pos;
+    if (i < S.nFluid) {
+      uint32_t m = (uint32_t)w[4], fl = (uint32_t)w[5];
+      if (matw(b, m, M_phantom) == 0 && !(fl & (FLAG_ANCHOR | FLAG_RIGID))) {
+        int2 st = b.stacc[slot];
+        int32_t vmax = S.vmax, vmaxN = neg_sat(vmax, f);
+        int32_t vx = add_sat(w[2], st.x, f);
+        int32_t vy = add_sat(add_sat(w[3], st.y, f), matw(b, m, M_grav), f);
+        vx = clampi(vx, vmaxN, vmax);
+        vy = clampi(vy, vmaxN, vmax);
+        pred = wall_clamp(S, make_int2(add_sat(pos.x, vx, f), add_sat(pos.y, vy, f)));
+      }
+    }
+    b.predSlot[slot] = pred;
+    int2 c = cell_coord(S, pred);
+    b.keys[slot] = key_of(S, c.x, c.y);
+  }
+}
+
+// cellStart[k] = first sorted position whose key is >= k, for k in [0, K].
+__global__ void __launch_bounds__(256) k_cellstart(Bufs b) {
+  const uint32_t K = b.world->K, n = b.world->slotEnd;
+  for (uint32_t k = gtid(); k <= K; k += gstride()) {
+    uint32_t lo = 0, hi = n;
+    while (lo < hi) {
+      uint32_t mid = (lo + hi) >> 1;
+      if (b.skey[mid] < k) lo = mid + 1; else hi = mid;
+    }
+    b.cellStart[k] = lo;
+  }
+}
+
+// Move the working set into sorted space.
+__global__ void __launch_bounds__(256) k_gather(Bufs b) {
+  const uint32_t nAct = b.world->nAct;
+  for (uint32_t p = gtid(); p < nAct; p += gstride()) {
+    uint32_t slot = b.sslot[p];
+    uint32_t s = b.sceneOf[slot];
+    const ScenePar& S = b.scenes[s];
+    uint32_t i = slot - S.slotBase;
+    const int32_t* w = b.state + (size_t)slot * 8;
+    int2 pr = b.predSlot[slot];
+    b.P[p] = pr;
+    b.POS[p] = make_int2(w[0], w[1]);
+    b.INFO[p] = (uint32_t)w[4] | (i >= S.nFluid ? INFO_BOUNDARY : 0u);
+    b.FLG[p] = (uint32_t)w[5];
+    b.TEMP[p] = w[6];
+    b.SCN[p] = s;
+    b.inv[slot] = p;
+  }
+}
+
+// buildNbr (src/sim.wgsl:1190-1254): 3x3 cells, dy outer, dx inner, ascending
+// slot inside a cell; skip self and retired particles; keep pairs inside the
+// kernel range; keep the first MAXNBR in that order (dbg[6] counts the rest).
+// Wall particles only need their truncation count, so their lists are only
+// walked in debug mode.
+template <bool DBG>
+__global__ void __launch_bounds__(256) k_nbr(Bufs b) {
+  Flags<DBG> f{b.dbg};
+  const uint32_t nAct = b.world->nAct, stride = b.nbrStride;
+  for (uint32_t p = gtid(); p < nAct; p += gstride()) {
+    uint32_t info = b.INFO[p];
+    bool bnd = (info & INFO_BOUNDARY) != 0;
+    if ((bnd && !DBG) || (b.FLG[p] & FLAG_DEAD)) { b.NBRN[p] = 0; continue; }
+    const ScenePar& S = b.scenes[b.SCN[p]];
+    int2 pi = b.P[p];
+    int2 cc = cell_coord(S, pi);
+    uint32_t cnt = 0;
+    bool congeal = false;
+    for (int dy = -1; dy <= 1; ++dy) {
+      int32_t gy = cc.y + dy;
+      if (gy < 0 || gy >= (int32_t)S.gridH) continue;
+      for (int dx = -1; dx <= 1; ++dx) {
+        int32_t gx = cc.x + dx;
+        if (gx < 0 || gx >= (int32_t)S.gridW) continue;
+        uint32_t key = key_of(S, gx, gy);
+        uint32_t lo = b.cellStart[key], hi = b.cellStart[key + 1];
+        for (uint32_t q = lo; q < hi; ++q) {
+          if (q == p) continue;
+          uint32_t fq = b.FLG[q];
+          if (fq & FLAG_DEAD) continue;
+          if (lut_index(delta(pi, b.P[q], f), f) < 0) continue;
+          uint32_t iq = b.INFO[q];
+          if (!(iq & INFO_BOUNDARY) && (fq & FLAG_CONGEAL)) congeal = true;
+          if (cnt >= (uint32_t)MAXNBR) { f.flag(6); continue; }
+          if (!bnd) b.NBR[(size_t)cnt * stride + p] = q | (iq & INFO_BOUNDARY);
+          cnt++;
+        }
+      }
+    }
+    b.NBRN[p] = bnd ? 0u : (cnt | (congeal ? NBRN_CONGEAL : 0u));
+  }
+}
+
+// solveA (src/sim.wgsl:1270-1318): density, |grad C|^2, lambda. On the last
+// iteration it also stores rinv (finalize's, src/sim.wgsl:2261-2262), which
+// depends only on this rho.
+template <bool DBG>
+__global__ void __launch_bounds__(256) k_solveA(Bufs b, const int2* __restrict__ P, int lastIter) {
+  Flags<DBG> f{b.dbg};
+  const uint32_t nAct = b.world->nAct, stride = b.nbrStride;
+  const int32_t W0 = lut(b, OFF_W, 0);
+  for (uint32_t p = gtid(); p < nAct; p += gstride()) {
+    uint32_t info = b.INFO[p];
+    if (info & INFO_BOUNDARY) continue;
+    int2 pi = P[p];
+    uint32_t cnt = b.NBRN[p] & NBRN_COUNT;
+    int32_t rho = W0, S = 0, sgx = 0, sgy = 0;
+    for (uint32_t k = 0; k < cnt; ++k) {
+      uint32_t q = b.NBR[(size_t)k * stride + p] & ~NBR_BOUNDARY;
+      int2 d = delta(pi, P[q], f);
+      int id = lut_index(d, f);
+      if (id < 0) continue;
+      rho = wadd(rho, lut(b, OFF_W, id));
+      int32_t gt = lut(b, OFF_G, id);
+      int32_t gx = grad_q16(gt, d.x, f), gy = grad_q16(gt, d.y, f);
+      sgx = wadd(sgx, gx);
+      sgy = wadd(sgy, gy);
+      S = wadd(S, wadd(clampi(mul<11>(gx, gx, f), 0, S_TERM), clampi(mul<11>(gy, gy, f), 0, S_TERM)));
+    }
+    S = wadd(S, wadd(clampi(mul<11>(sgx, sgx, f), 0, S_TERM), clampi(mul<11>(sgy, sgy, f), 0, S_TERM)));
+    int32_t Cq = clampi(shr_rne<4>(wsub(rho, RHO0)), 0, C_MAX);
+    int32_t eps = matw(b, info & INFO_MAT, M_eps);
+    b.RHO[p] = rho;
+    b.LAM[p] = clampi(neg_sat(divshift<25>(Cq, wadd(S, eps), f), f), -LAM_MAX, LAM_MAX);
+    if (lastIter) b.RINV[p] = clampi(divshift<16>(RHO0, max(rho, RHO_FLOOR_RINV), f), 0, RINV_MAX);
+  }
+}
+
+// solveB_at (src/sim.wgsl:1337-1372) for one particle.
+template <bool DBG>
+__device__ __forceinline__ int2 solveB_dp(const Bufs& b, const int2* __restrict__ P, uint32_t p, const Flags<DBG>& f) {
+  const uint32_t stride = b.nbrStride;
+  int2 pi = P[p];
+  int32_t li = b.LAM[p];
+  uint32_t cnt = b.NBRN[p] & NBRN_COUNT;
+  int32_t dpx = 0, dpy = 0;
+  for (uint32_t k = 0; k < cnt; ++k) {
+    uint32_t e = b.NBR[(size_t)k * stride + p];
+    uint32_t q = e & ~NBR_BOUNDARY;
+    int2 d = delta(pi, P[q], f);
+    int id = lut_index(d, f);
+    if (id < 0) continue;
+    int32_t lj = (e & NBR_BOUNDARY) ? li : b.LAM[q];
+    int32_t co = add_sat(add_sat(li, lj, f), lut(b, OFF_S, id), f);
+    int32_t gt = lut(b, OFF_G, id);
+    dpx = wadd(dpx, clampi(mul<12>(co, grad_q16(gt, d.x, f), f), -DP_TERM, DP_TERM));
+    dpy = wadd(dpy, clampi(mul<12>(co, grad_q16(gt, d.y, f), f), -DP_TERM, DP_TERM));
+  }
+  return make_int2(dpx, dpy);
+}
+
+// applyDp_at (src/sim.wgsl:1418-1434).
+template <bool DBG>
+__device__ __forceinline__ int2 apply_dp(const Bufs& b, const ScenePar& S, uint32_t m, int2 pr, int2 dp,
+                                         const Flags<DBG>& f) {
+  int32_t dm = matw(b, m, M_dpMax), dmN = neg_sat(dm, f);
+  int32_t dx = clampi(shr_rne<8>(dp.x), dmN, dm);
+  int32_t dy = clampi(shr_rne<8>(dp.y), dmN, dm);
+  return wall_clamp(S, make_int2(add_sat(pr.x, dx, f), add_sat(pr.y, dy, f)));
+}
+
+// First cell start >= x among the cells of one colour class (keys [k0, k1]).
+__device__ __forceinline__ uint32_t align_cell(const uint32_t* cs, uint32_t k0, uint32_t k1, uint32_t x) {
+  uint32_t lo = k0, hi = k1;
+  while (lo < hi) {
+    uint32_t mid = (lo + hi) >> 1;
+    if (cs[mid] < x) lo = mid + 1; else hi = mid;
+  }
+  return cs[lo];
+}
+
+// One colour of the block Gauss-Seidel sweep: solveB_cK + applyDp_cK fused.
+// CTA chunks are cell-aligned, so every same-colour neighbour of a particle is
+// handled by the same CTA; the barrier between the two loops is exactly the
+// dispatch boundary the reference puts between solveB_cK and applyDp_cK.
+template <bool DBG>
+__global__ void __launch_bounds__(256) k_colour(Bufs b, int2* __restrict__ P, int colour) {
+  Flags<DBG> f{b.dbg};
+  __shared__ uint32_t rng[2];
+  const uint32_t k0 = b.world->colourBase[colour], k1 = b.world->colourBase[colour + 1];
+  const uint32_t cLo = b.cellStart[k0], cHi = b.cellStart[k1];
+  const uint32_t CH = blockDim.x;
+  const uint32_t nch = (cHi - cLo + CH - 1) / CH;
+  for (uint32_t ch = blockIdx.x; ch < nch; ch += gridDim.x) {
+    if (threadIdx.x == 0) {
+      rng[0] = align_cell(b.cellStart, k0, k1, cLo + ch * CH);
+      rng[1] = align_cell(b.cellStart, k0, k1, min(cHi, cLo + (ch + 1) * CH));
+    }
+    __syncthreads();
+    const uint32_t lo = rng[0], hi = rng[1];
+    for (uint32_t p = lo + threadIdx.x; p < hi; p += CH) {
+      if (b.INFO[p] & INFO_BOUNDARY) continue;
+      b.DP[p] = solveB_dp(b, P, p, f);
+    }
+    __syncthreads();
+    for (uint32_t p = lo + threadIdx.x; p < hi; p += CH) {
+      uint32_t info = b.INFO[p];
+      if (info & INFO_BOUNDARY) continue;
+      if (b.FLG[p] & (FLAG_RIGID | FLAG_ANCHOR)) continue;
+      const ScenePar& S = b.scenes[b.SCN[p]];
+      P[p] = apply_dp(b, S, info & INFO_MAT, P[p], b.DP[p], f);
+    }
+    __syncthreads();
+  }
+}
+
+// friction + the bond gather (src/sim.wgsl:1673-1934). Rows with fric == 0
+// and bondK == 0 take the reference's zero-work path: their dp is 0 and
+// applyFric leaves their (already wall-clamped) pred unchanged, so they are
+// skipped here and in k_apply_fric. Results go to DP; k_apply_fric applies
+// them (applyFric, src/sim.wgsl:1945-1950) after every row has read pred.
+__device__ __forceinline__ bool friction_row(const Bufs& b, uint32_t m) {
+  return matw(b, m, M_fric) != 0 || matw(b, m, M_bondK) != 0;
+}
+template <bool DBG>
+__global__ void __launch_bounds__(256) k_friction(Bufs b, const int2* __restrict__ P) {
+  Flags<DBG> f{b.dbg};
+  const uint32_t nAct = b.world->nAct, stride = b.nbrStride;
+  for (uint32_t p = gtid(); p < nAct; p += gstride()) {
+    uint32_t info = b.INFO[p];
+    if (info & INFO_BOUNDARY) continue;
+    uint32_t m = info & INFO_MAT;
+    if (!friction_row(b, m)) continue;
+    uint32_t flagsI = b.FLG[p];
+    if (flagsI & FLAG_RIGID) continue;
+    int32_t fi = matw(b, m, M_fric);
+    int32_t bondKi = matw(b, m, M_bondK);
+    int2 pi = P[p];
+    int2 dxi = delta(pi, b.POS[p], f);
+    uint32_t cnt = b.NBRN[p] & NBRN_COUNT;
+    int32_t fx = 0, fy = 0;
+    if (fi != 0) {
+      for (uint32_t k = 0; k < cnt; ++k) {
+        uint32_t e = b.NBR[(size_t)k * stride + p];
+        uint32_t q = e & ~NBR_BOUNDARY;
+        int2 pq = P[q];
+        int2 d = delta(pi, pq, f);
+        int id = lut_index(d, f);
+        if (id < 0) continue;
+        int32_t d4x = shr_rne<FPRE>(d.x), d4y = shr_rne<FPRE>(d.y);
+        int32_t d2 = wadd(wmul(d4x, d4x), wmul(d4y, d4y));
+        if (d2 < D2_FLOOR) continue;
+        int2 rel = dxi;
+        int32_t mu = fi;
+        if (!(e & NBR_BOUNDARY)) {
+          int2 dq = delta(pq, b.POS[q], f);
+          rel = make_int2(sub_sat(dxi.x, dq.x, f), sub_sat(dxi.y, dq.y, f));
+          mu = mat_mix(fi, matw(b, b.INFO[q] & INFO_MAT, M_fric));
+        }
+        if (mu == 0) continue;
+        int32_t r4x = shr_rne<RPRE>(rel.x), r4y = shr_rne<RPRE>(rel.y);
+        int32_t dot = wadd(wmul(d4x, r4x), wmul(d4y, r4y));
+        int32_t qq = divshift<16>(dot, d2, f);
+        int32_t tx = sub_sat(r4x, mul<16>(d4x, qq, f), f);
+        int32_t ty = sub_sat(r4y, mul<16>(d4y, qq, f), f);
+        int32_t wq = shr_rne<4>(lut(b, OFF_W, id));
+        int32_t sx = mul<16>(mul<5>(tx, wq, f), mu, f);
+        int32_t sy = mul<16>(mul<5>(ty, wq, f), mu, f);
+        fx = wsub(fx, clampi(sx, -FR_TERM, FR_TERM));
+        fy = wsub(fy, clampi(sy, -FR_TERM, FR_TERM));
+      }
+    }
+    int32_t bx = 0, by = 0;
+    if (bondKi != 0 && !(flagsI & FLAG_BURST) && b.bond) {
+      uint32_t slot = b.sslot[p];
+      int32_t ki = bond_k(b, m, b.TEMP[p], f);
+      const uint32_t base = b.scenes[b.SCN[p]].slotBase;
+      uint32_t* row = b.bond + (size_t)slot * BOND_CAP;
+      for (int k = 0; k < BOND_CAP; ++k) {
+        uint32_t w = row[k];
+        if (w == 0u) break;
+        if (w & BOND_TOMB) continue;
+        uint32_t q = b.inv[base + (w & BOND_J_MASK)];
+        uint32_t mj = b.INFO[q] & INFO_MAT;
+        if (b.FLG[q] & FLAG_BURST) { row[k] = w | BOND_TOMB; continue; }
+        if (matw(b, mj, M_bondK) == 0) { row[k] = w | BOND_TOMB; continue; }
+        int32_t L0 = (int32_t)((w >> 17) & 0x1fffu);
+        int32_t L02 = wmul(L0, L0);
+        int2 d = delta(pi, P[q], f);
+        int32_t d4x = shr_rne<BPRE>(d.x), d4y = shr_rne<BPRE>(d.y);
+        if (abs(d4x) > L0_MAX || abs(d4y) > L0_MAX) { row[k] = w | BOND_TOMB; continue; }
+        int32_t d2 = wadd(wmul(d4x, d4x), wmul(d4y, d4y));
+        if (d2 >= HARD_BREAK2) { row[k] = w | BOND_TOMB; continue; }
+        int32_t mb = min(matw(b, m, M_bondBreak), matw(b, mj, M_bondBreak));
+        int32_t mub = min(matw(b, m, M_bondMu), matw(b, mj, M_bondMu));
+        if (mb != 0 && mub != 0) {
+          int32_t lp = neg_sat(add_sat(b.LAM[p], b.LAM[q], f), f);
+          int32_t Pq = lp > 0 ? shr_rne<4>(lp) : 0;
+          mb = wadd(wadd(65536, wsub(mb, 65536)), mul<16>(Pq, mub, f));
+        }
+        if (mb != 0 && d2 > mul<16>(L02, mb, f)) { row[k] = w | BOND_TOMB; continue; }
+        if (d2 < D2_FLOOR) continue;
+        int32_t kj = bond_k(b, mj, b.TEMP[q], f);
+        int32_t kp = min(ki, kj);
+        if (kp == 0) continue;
+        int32_t C = sub_sat(d2, L02, f);
+        int32_t qv = divshift<16>(C, wmul(d2, 4), f);
+        int32_t qk = mul<16>(qv, kp, f);
+        int32_t gx = mul<3>(d4x, qk, f);
+        int32_t gy = mul<3>(d4y, qk, f);
+        bx = wsub(bx, clampi(gx, -BD_TERM, BD_TERM));
+        by = wsub(by, clampi(gy, -BD_TERM, BD_TERM));
+      }
+    }
+    b.DP[p] = make_int2(add_sat(fx, bx, f), add_sat(fy, by, f));
+  }
+}
+
+template <bool DBG>
+__global__ void __launch_bounds__(256) k_apply_fric(Bufs b, int2* __restrict__ P) {
+  Flags<DBG> f{b.dbg};
+  const uint32_t nAct = b.world->nAct;
+  for (uint32_t p = gtid(); p < nAct; p += gstride()) {
+    uint32_t info = b.INFO[p];
+    if (info & INFO_BOUNDARY) continue;
+    uint32_t m = info & INFO_MAT;
+    if (!friction_row(b, m)) continue;
+    if (b.FLG[p] & (FLAG_RIGID | FLAG_ANCHOR)) continue;
+    const ScenePar& S = b.scenes[b.SCN[p]];
+    P[p] = apply_dp(b, S, m, P[p], b.DP[p], f);
+  }
+}
+
+// finalize + xsph + normals + conduct (src/sim.wgsl:2245-2582) in one sweep
+// over the neighbour list. vtmp_j = clamp(pred_j - pos_j) is finalize's
+// velocity, recomputed where it is needed.
+template <bool DBG>
+__global__ void __launch_bounds__(256) k_post1(Bufs b, const int2* __restrict__ P) {
+  Flags<DBG> f{b.dbg};
+  const uint32_t nAct = b.world->nAct, stride = b.nbrStride;
+  for (uint32_t p = gtid(); p < nAct; p += gstride()) {
+    uint32_t slot = b.sslot[p];
+    int32_t* w = b.state + (size_t)slot * 8;
+    uint32_t info = b.INFO[p];
+    if (info & INFO_BOUNDARY) {
+      w[2] = 0;
+      w[3] = 0;
+      continue;
+    }
+    const ScenePar& S = b.scenes[b.SCN[p]];
+    const int32_t vmax = S.vmax, vmaxN = neg_sat(vmax, f);
+    uint32_t m = info & INFO_MAT;
+    uint32_t fl = b.FLG[p];
+    int2 pi = P[p];
+    int2 posi = b.POS[p];
+    int2 vi = delta(pi, posi, f);
+    vi.x = clampi(vi.x, vmaxN, vmax);
+    vi.y = clampi(vi.y, vmaxN, vmax);
+    const bool doX = !(fl & (FLAG_RIGID | FLAG_ANCHOR));
+    const int32_t ci = matw(b, m, M_xsph);
+    const int32_t condi = matw(b, m, M_cond);
+    const int32_t corrodeI = matw(b, m, M_corrode);
+    const int32_t rhoi = b.RHO[p];
+    const int32_t Ti = b.TEMP[p];
+    uint32_t cnt = b.NBRN[p] & NBRN_COUNT;
+    int32_t ax = 0, ay = 0, sx = 0, sy = 0, hq = 0, hc = 0;
+    for (uint32_t k = 0; k < cnt; ++k) {
+      uint32_t e = b.NBR[(size_t)k * stride + p];
+      if (e & NBR_BOUNDARY) continue;
+      uint32_t q = e;
+      int2 pq = P[q];
+      int2 d = delta(pi, pq, f);
+      int id = lut_index(d, f);
+      if (id < 0) continue;
+      int32_t W = lut(b, OFF_W, id);
+      uint32_t mj = b.INFO[q] & INFO_MAT;
+      if (doX) {
+        int32_t K = sym_k(rhoi, b.RHO[q], f);
+        int32_t wk = mul<16>(W, K, f);
+        int32_t cij = mat_mix(ci, matw(b, mj, M_xsph));
+        int2 vj = delta(pq, b.POS[q], f);
+        vj.x = clampi(vj.x, vmaxN, vmax);
+        vj.y = clampi(vj.y, vmaxN, vmax);
+        ax = wadd(ax, clampi(mul<16>(mul<12>(sub_sat(vj.x, vi.x, f), wk, f), cij, f), -XS_TERM, XS_TERM));
+        ay = wadd(ay, clampi(mul<16>(mul<12>(sub_sat(vj.y, vi.y, f), wk, f), cij, f), -XS_TERM, XS_TERM));
+      }
+      {
+        int32_t gt = lut(b, OFF_G, id);
+        int32_t rj = b.RINV[q];
+        sx = wadd(sx, mul<16>(grad_q16(gt, d.x, f), rj, f));
+        sy = wadd(sy, mul<16>(grad_q16(gt, d.y, f), rj, f));
+      }
+      {
+        int32_t cij = mat_mix(condi, matw(b, mj, M_cond));
+        int32_t wk = mul<16>(W, cij, f);
+        int32_t dT = clampi(sub_sat(b.TEMP[q], Ti, f), -DT_CLAMP, DT_CLAMP);
+        hq = wadd(hq, clampi(mul<12>(dT, wk, f), -HT_TERM, HT_TERM));
+        if (mj != m) {
+          int32_t attack = matw(b, mj, M_corrode);
+          int32_t spend = matw(b, mj, M_corrPt) != CORR_NEVER ? corrodeI : 0;
+          int32_t str = wadd(attack, spend);
+          if (str != 0) hc = wadd(hc, clampi(mul<12>(W, str, f), 0, CORR_TERM));
+        }
+      }
+    }
+    b.NRM[p] = make_int2(mul<16>(sx, H, f), mul<16>(sy, H, f));
+    b.HEAT[p] = hq;
+    b.CORR[p] = hc;
+    int2 vo = vi;
+    if (doX) vo = make_int2(add_sat(vi.x, shr_rne<8>(ax), f), add_sat(vi.y, shr_rne<8>(ay), f));
+    w[0] = pi.x;
+    w[1] = pi.y;
+    w[2] = vo.x;
+    w[3] = vo.y;
+  }
+}
+
+// thermal (src/sim.wgsl:2612-2707) for one particle; returns the new words.
+template <bool DBG>
+__device__ __forceinline__ void thermal(const Bufs& b, uint32_t i, int32_t heat, int32_t corr, int32_t* w,
+                                        const Flags<DBG>& f) {
+  uint32_t mat0 = (uint32_t)w[4];
+  int32_t T = add_sat(w[6], shr_rne<8>(heat), f);
+  T = add_sat(T, mul<16>(sub_sat(AMBIENT, T, f), matw(b, mat0, M_coolRate), f), f);
+  int32_t fuel = w[7];
+  uint32_t fl0 = (uint32_t)w[5];
+  bool burning = (fl0 & FLAG_BURNING) != 0;
+  if (!burning && fuel > 0 && T >= matw(b, mat0, M_ignitePt)) burning = true;
+  if (burning) {
+    T = add_sat(T, matw(b, mat0, M_burnHeat), f);
+    fuel = max(0, sub_sat(fuel, matw(b, mat0, M_burnRate), f));
+  }
+  T = clampi(T, TEMP_MIN, TEMP_MAX);
+  T = add_sat(T, mul<16>(sub_sat(matw(b, mat0, M_tempTarget), T, f), matw(b, mat0, M_tempDrive), f), f);
+  int32_t dose = shr_rne<8>(corr);
+  uint32_t mat = mat0;
+  bool froze = false;
+  uint32_t sTo = (uint32_t)matw(b, mat0, M_splitTo), sPct = (uint32_t)matw(b, mat0, M_splitPct);
+  if (burning && fuel <= 0) mat = pick_product((uint32_t)matw(b, mat0, M_burnTo), sTo, sPct, i);
+  else if (dose >= matw(b, mat0, M_corrPt)) mat = pick_product((uint32_t)matw(b, mat0, M_corrTo), sTo, sPct, i);
+  else if (T >= matw(b, mat0, M_boilPt)) mat = pick_product((uint32_t)matw(b, mat0, M_boilTo), sTo, sPct, i);
+  else if (T >= matw(b, mat0, M_meltPt)) mat = pick_product((uint32_t)matw(b, mat0, M_meltTo), sTo, sPct, i);
+  else if (T <= matw(b, mat0, M_condPt)) mat = pick_product((uint32_t)matw(b, mat0, M_condTo), sTo, sPct, i);
+  else if (T <= matw(b, mat0, M_freezePt)) {
+    mat = pick_product((uint32_t)matw(b, mat0, M_freezeTo), sTo, sPct, i);
+    froze = true;
+  }
+  if (mat != mat0) { fuel = matw(b, mat, M_fuel0); burning = false; }
+  uint32_t fl = fl0 & ~(FLAG_BURNING | FLAG_DEAD | FLAG_SEAL);
+  if (mat != mat0) fl &= ~(FLAG_ANCHOR | FLAG_CONGEAL | FLAG_BURST);
+  if (froze && mat != mat0 && fuse_row(b, mat)) fl |= FLAG_CONGEAL;
+  if (burning) fl |= FLAG_BURNING;
+  if (matw(b, mat, M_phantom) != 0) fl |= FLAG_DEAD;
+  if (seal_class(b, mat)) {
+    fl |= FLAG_SEAL;
+    atomicOr(b.err, ERR_UNSUPPORTED_ROW);
+  }
+  w[4] = (int32_t)mat;
+  w[5] = (int32_t)fl;
+  w[6] = T;
+  w[7] = fuel;
+}
+
+// surfaceTension (src/sim.wgsl:2409-2494) + thermal + the formation pass's
+// flag update for rows that cannot bond (bondForm2's tail, src/sim.wgsl:
+// 3059-3067) + the state digest. HASH=false when bond formation runs as its
+// own kernels (the digest then follows them).
+template <bool DBG, bool HASH>
+__global__ void __launch_bounds__(256) k_post2(Bufs b, const int2* __restrict__ P, int formFlags) {
+  Flags<DBG> f{b.dbg};
+  const uint32_t nAct = b.world->nAct, stride = b.nbrStride;
+  const uint32_t nIter = (nAct + gstride() - 1) / gstride() * gstride();
+  for (uint32_t p = gtid(); p < nIter; p += gstride()) {
+    bool valid = p < nAct;
+    uint32_t scene = 0, idx = 0;
+    int32_t w8[8];
+    if (valid) {
+      uint32_t slot = b.sslot[p];
+      scene = b.SCN[p];
+      const ScenePar& S = b.scenes[scene];
+      idx = slot - S.slotBase;
+      int32_t* w = b.state + (size_t)slot * 8;
+      uint32_t info = b.INFO[p];
+      if (!(info & INFO_BOUNDARY)) {
+        uint32_t m = info & INFO_MAT;
+        uint32_t fl = b.FLG[p];
+        const int32_t gCohI = matw(b, m, M_gammaCoh), gCurI = matw(b, m, M_gammaCur);
+        const int32_t adh = matw(b, m, M_adhesion);
+        int2 pi = P[p];
+        int2 ni = b.NRM[p];
+        int32_t rhoi = b.RHO[p];
+        uint32_t cnt = b.NBRN[p] & NBRN_COUNT;
+        int32_t ax = 0, ay = 0;
+        for (uint32_t k = 0; k < cnt; ++k) {
+          uint32_t e = b.NBR[(size_t)k * stride + p];
+          uint32_t q = e & ~NBR_BOUNDARY;
+          int2 d = delta(pi, P[q], f);
+          int id = lut_index(d, f);
+          if (id < 0) continue;
+          if (e & NBR_BOUNDARY) {
+            int32_t at = lut(b, OFF_A, id);
+            ax = wsub(ax, clampi(mul<8>(mul<22>(at, d.x, f), adh, f), -ST_TERM, ST_TERM));
+            ay = wsub(ay, clampi(mul<8>(mul<22>(at, d.y, f), adh, f), -ST_TERM, ST_TERM));
+            continue;
+          }
+          int32_t K = sym_k(rhoi, b.RHO[q], f);
+          int32_t ct = lut(b, OFF_C, id);
+          uint32_t mj = b.INFO[q] & INFO_MAT;
+          int32_t gCoh = mat_mix(gCohI, matw(b, mj, M_gammaCoh));
+          int32_t gCur = mat_mix(gCurI, matw(b, mj, M_gammaCur));
+          int32_t fx = neg_sat(mul<16>(mul<22>(ct, d.x, f), gCoh, f), f);
+          int32_t fy = neg_sat(mul<16>(mul<22>(ct, d.y, f), gCoh, f), f);
+          int2 nj = b.NRM[q];
+          int32_t cx = mul<16>(sub_sat(ni.x, nj.x, f), gCur, f);
+          int32_t cy = mul<16>(sub_sat(ni.y, nj.y, f), gCur, f);
+          fx = add_sat(fx, neg_sat(cx, f), f);
+          fy = add_sat(fy, neg_sat(cy, f), f);
+          ax = wadd(ax, clampi(mul<8>(fx, K, f), -ST_TERM, ST_TERM));
+          ay = wadd(ay, clampi(mul<8>(fy, K, f), -ST_TERM, ST_TERM));
+        }
+        b.stacc[slot] = make_int2(shr_rne<8>(ax), shr_rne<8>(ay));
+        thermal(b, idx, b.HEAT[p], b.CORR[p], w, f);
+        if (formFlags && S.formNow) {
+          uint32_t fo = (uint32_t)w[5] & ~FLAG_CONGEAL;
+          if (!(fo & FLAG_RIGID) && (fo & WELD_TAG_MASK) != S.weldHold) fo &= ~WELD_TAG_MASK;
+          w[5] = (int32_t)fo;
+        }
+        (void)fl;
+      }
+      if (HASH) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) w8[k] = w[k];
+      }
+    }
+    if (HASH) {
+      uint32_t h[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+      if (valid) particle_digest(w8, idx, nullptr, h);
+      digest_add(b.acc, valid, scene, h);
+    }
+  }
+}
+
+// Digest of the current state of every active scene, in slot order
+// (statehash.wgsl `digest`, src/hash/statehash.wgsl:83-159).
+__global__ void __launch_bounds__(256) k_hash(Bufs b, uint32_t* __restrict__ acc) {
+  const uint32_t slotEnd = b.world->slotEnd;
+  const uint32_t nIter = (slotEnd + gstride() - 1) / gstride() * gstride();
+  for (uint32_t slot = gtid(); slot < nIter; slot += gstride()) {
+    bool valid = false;
+    uint32_t s = 0, i = 0;
+    uint32_t h[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (slot < slotEnd) {
+      s = b.sceneOf[slot];
+      const ScenePar& S = b.scenes[s];
+      i = slot - S.slotBase;
+      valid = S.active && i < S.n;
+      if (valid) {
+        const uint32_t* row = (b.bond && i < S.nFluid) ? b.bond + (size_t)slot * BOND_CAP : nullptr;
+        particle_digest(b.state + (size_t)slot * 8, i, row, h);
+      }
+    }
+    digest_add(acc, valid, s, h);
+  }
+}
+
+// fold_chain (src/hash/statehash.wgsl:164-170) per scene, then advance the
+// formation clock exactly as `_encodeSubstep` does (src/engine.js:4145-4151).
+__global__ void k_fold(Bufs b, int doChain) {
+  uint32_t s = gtid();
+  if (s >= b.world->numScenes) return;
+  ScenePar& S = b.scenes[s];
+  if (!S.active) return;
+  if (doChain) {
+    uint32_t a[8], next[8];
+    for (int j = 0; j < 8; ++j) a[j] = b.acc[s * 8 + j];
+    for (int j = 0; j < 8; ++j) next[j] = mm_step(b.chain[s * 8 + j], a[j] ^ rotl32(a[(j + 1) & 7], 7));
+    for (int j = 0; j < 8; ++j) {
+      b.chain[s * 8 + j] = next[j];
+      b.accLast[s * 8 + j] = a[j];
+      b.acc[s * 8 + j] = 0;
+    }
+  }
+  if (S.formNow) S.bondDirty = 0;
+  S.formClock += 1;
+  S.substep += 1;
+}
+
+// markCongealNbr + bondForm1 (src/sim.wgsl:2714-2989), sorted space.
+template <bool DBG>
+__global__ void __launch_bounds__(256) k_form1(Bufs b) {
+  Flags<DBG> f{b.dbg};
+  const uint32_t nAct = b.world->nAct, stride = b.nbrStride;
+  for (uint32_t p = gtid(); p < nAct; p += gstride()) {
+    uint32_t info = b.INFO[p];
+    if (info & INFO_BOUNDARY) continue;
+    const ScenePar& S = b.scenes[b.SCN[p]];
+    if (!S.formNow) continue;
+    uint32_t slot = b.sslot[p];
+    const int32_t* wi = b.state + (size_t)slot * 8;
+    uint32_t* cand = b.bondCand + (size_t)slot * BOND_CAP;
+    const uint32_t* brow = b.bond + (size_t)slot * BOND_CAP;
+    uint32_t cnt = b.NBRN[p] & NBRN_COUNT;
+    // markCongealNbr: refresh the congeal bit from the post-thermal flags
+    bool seen = false;
+    for (uint32_t k = 0; k < cnt; ++k) {
+      uint32_t e = b.NBR[(size_t)k * stride + p];
+      if (e & NBR_BOUNDARY) continue;
+      uint32_t qs = b.sslot[e];
+      if ((uint32_t)b.state[(size_t)qs * 8 + 5] & FLAG_CONGEAL) { seen = true; break; }
+    }
+    uint32_t flI = (uint32_t)wi[5];
+    if (flI & FLAG_RIGID) {
+      for (int k = 0; k < BOND_CAP; ++k) cand[k] = 0;
+      continue;
+    }
+    bool anchoredI = (flI & FLAG_ANCHOR) != 0;
+    uint32_t matI = (uint32_t)wi[4];
+    uint32_t cn = 0;
+    if (matw(b, matI, M_bondK) != 0 && matw(b, matI, M_bondGroup) >= 0) {
+      for (int k = 0; k < BOND_CAP; ++k) {
+        uint32_t w = brow[k];
+        if (w == 0u) break;
+        if (w & BOND_TOMB) continue;
+        if (cn >= (uint32_t)BOND_CAP) { f.flag(8); break; }
+        cand[cn++] = w;
+      }
+      uint32_t tagI = flI & WELD_TAG_MASK;
+      int32_t ki = bond_k(b, matI, wi[6], f);
+      bool canReform = (!anchoredI && matw(b, matI, M_bondReform) != 0 && ki != 0);
+      bool congealI = (flI & FLAG_CONGEAL) && fuse_row(b, matI);
+      bool congealNear = seen && fuse_row(b, matI);
+      if (canReform || (!anchoredI && tagI != 0u) || congealI || congealNear) {
+        for (uint32_t k = 0; k < cnt; ++k) {
+          if (cn >= (uint32_t)BOND_CAP) { f.flag(8); break; }
+          uint32_t e = b.NBR[(size_t)k * stride + p];
+          if (e & NBR_BOUNDARY) continue;
+          uint32_t qs = b.sslot[e];
+          const int32_t* wj = b.state + (size_t)qs * 8;
+          uint32_t j = qs - S.slotBase;
+          uint32_t mj = (uint32_t)wj[4];
+          uint32_t fJ = (uint32_t)wj[5];
+          uint32_t tagJ = fJ & WELD_TAG_MASK;
+          bool weld = (!anchoredI && tagI != 0u && tagI == tagJ);
+          bool congealJ = (fJ & FLAG_CONGEAL) && fuse_row(b, mj);
+          bool congeal = ((congealI || congealJ) && !weld && mj == matI && !(fJ & FLAG_RIGID));
+          if (!congeal && matw(b, mj, M_bondGroup) != matw(b, matI, M_bondGroup)) continue;
+          if (!weld && !congeal) {
+            if (!canReform) continue;
+            if (bond_k(b, mj, wj[6], f) == 0) continue;
+          }
+          bool dup = false;
+          for (uint32_t q2 = 0; q2 < cn; ++q2)
+            if ((cand[q2] & BOND_J_MASK) == j) { dup = true; break; }
+          if (dup) continue;
+          int32_t d4x = shr_rne<BPRE>(sub_sat(wi[0], wj[0], f));
+          int32_t d4y = shr_rne<BPRE>(sub_sat(wi[1], wj[1], f));
+          if (abs(d4x) > L0_MAX || abs(d4y) > L0_MAX) continue;
+          int32_t d2 = wadd(wmul(d4x, d4x), wmul(d4y, d4y));
+          if (d2 < D2_FLOOR || d2 > BOND_R2) continue;
+          if (!weld && !congeal) {
+            int32_t vl = min(matw(b, matI, M_bondFormV), matw(b, mj, M_bondFormV));
+            int32_t vl4 = shr_rne<RPRE>(vl);
+            int32_t r4x = shr_rne<RPRE>(sub_sat(wi[2], wj[2], f));
+            int32_t r4y = shr_rne<RPRE>(sub_sat(wi[3], wj[3], f));
+            if (abs(r4x) > vl4 || abs(r4y) > vl4) continue;
+            if (wadd(wmul(r4x, r4x), wmul(r4y, r4y)) > wmul(vl4, vl4)) continue;
+            int32_t pl = min(matw(b, matI, M_bondFormP), matw(b, mj, M_bondFormP));
+            if (pl != 0 && (neg_sat(b.LAM[p], f) < pl || neg_sat(b.LAM[e], f) < pl)) continue;
+          }
+          int32_t L0 = (int32_t)isqrt32((uint32_t)d2);
+          if (L0 < L0_MIN || L0 > L0_MAX) continue;
+          if (j > BOND_J_MASK) { atomicOr(b.err, ERR_BOND_PARTNER); continue; }
+          cand[cn++] = (((uint32_t)L0 & 0x1fffu) << 17) | (j & BOND_J_MASK);
+        }
+      }
+    }
+    for (uint32_t k = cn; k < (uint32_t)BOND_CAP; ++k) cand[k] = 0;
+  }
+}
+
+// bondForm2 (src/sim.wgsl:3001-3068): keep mutual proposals, clear weld tags.
+__global__ void __launch_bounds__(256) k_form2(Bufs b) {
+  const uint32_t slotEnd = b.world->slotEnd;
+  for (uint32_t slot = gtid(); slot < slotEnd; slot += gstride()) {
+    const ScenePar& S = b.scenes[b.sceneOf[slot]];
+    uint32_t i = slot - S.slotBase;
+    if (!S.active || i >= S.nFluid || !S.formNow) continue;
+    const uint32_t* cand = b.bondCand + (size_t)slot * BOND_CAP;
+    uint32_t* row = b.bond + (size_t)slot * BOND_CAP;
+    uint32_t nn = 0;
+    for (int k = 0; k < BOND_CAP; ++k) {
+      uint32_t w = cand[k];
+      if (w == 0u) break;
+      uint32_t j = w & BOND_J_MASK;
+      const uint32_t* cj = b.bondCand + (size_t)(S.slotBase + j) * BOND_CAP;
+      bool ok = false;
+      for (int q = 0; q < BOND_CAP; ++q) {
+        uint32_t v = cj[q];
+        if (v == 0u) break;
+        if ((v & BOND_J_MASK) == i) { ok = ((v & BOND_L0_MASK) == (w & BOND_L0_MASK)); break; }
+      }
+      if (ok) row[nn++] = w & ~BOND_TOMB;
+    }
+    for (int k = nn; k < BOND_CAP; ++k) row[k] = 0;
+    int32_t* w = b.state + (size_t)slot * 8;
+    uint32_t fo = (uint32_t)w[5] & ~FLAG_CONGEAL;
+    if (!(fo & FLAG_RIGID) && (fo & WELD_TAG_MASK) != S.weldHold) fo &= ~WELD_TAG_MASK;
+    w[5] = (int32_t)fo;
+  }
+}
+
+}  // namespace d2
+}  // namespace sn

@@ -1,0 +1,386 @@
+"""The engine surface of the reference's ``src/engine.js``, on the GB300 C ABI.
+
+``create_engine`` / ``Engine`` mirror ``createEngine`` (``src/engine.js:2786``)
+and ``class Engine`` (``src/engine.js:3523``): same method names (camelCase
+aliases included), same argument meaning, same error behaviour (bad input
+raises ``EngineError`` synchronously, the reference's ``assert``; device-side
+problems surface from ``check_errors()``). Every call goes through
+``include/suna.h``; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+from typing import Iterable, Optional
+
+import numpy as np
+
+from . import _native, data
+from .scenes import Scene
+
+SUBSTEPS_PER_FRAME = 2
+ITERS = 4
+MAXNBR = 48
+BOND_CAP = 48
+VMAX = 65536
+
+
+class EngineError(RuntimeError):
+    """Raised for refused input and for errors the device reported."""
+
+
+@dataclass
+class Digest:
+    acc: np.ndarray
+
+    @property
+    def hex(self) -> str:
+        return ''.join(f'{int(a):08x}' for a in self.acc)
+
+    @property
+    def set_hex(self) -> str:
+        return self.hex[:32]
+
+    @property
+    def slot_hex(self) -> str:
+        return self.hex[32:]
+
+    setHex = set_hex
+    slotHex = slot_hex
+
+
+def _ptr(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _opts(max_particles, max_cells, iters, debug, chain, device, luts, mats):
+    luts = np.ascontiguousarray(data.luts() if luts is None else luts, dtype=np.int32)
+    if luts.size != data.LUT_WORDS or data.table_hash(luts) != data.TABLE_HASH:
+        raise EngineError('kernel tables do not match the frozen TABLE_HASH')
+    mats = np.ascontiguousarray(data.mats() if mats is None else mats, dtype=np.int32).reshape(-1, 48)
+    o = _native.SnOpts(max_particles=int(max_particles), max_cells=int(max_cells), iters=int(iters),
+                       debug=1 if debug else 0, chain=1 if chain else 0, device=int(device),
+                       luts=luts.ctypes.data, mats=mats.ctypes.data, mat_count=mats.shape[0])
+    return o, (luts, mats)
+
+
+class _SceneArgs:
+    """Keeps the numpy arrays alive for the duration of a C call."""
+
+    def __init__(self, sc: Scene):
+        n = int(sc.n)
+        self.pos = np.ascontiguousarray(np.asarray(sc.pos).reshape(-1), dtype=np.int32)
+        self.vel = np.ascontiguousarray(np.asarray(sc.vel).reshape(-1), dtype=np.int32)
+        self.mat = np.ascontiguousarray(np.asarray(sc.matId).reshape(-1), dtype=np.uint32)
+        if self.pos.size != 2 * n or self.vel.size != 2 * n or self.mat.size != n:
+            raise EngineError('scene array lengths must be n*2 / n*2 / n')
+        conv = lambda a, dt: None if a is None else np.ascontiguousarray(np.asarray(a).reshape(-1), dtype=dt)
+        self.flags = conv(sc.flags, np.uint32)
+        self.temp = conv(sc.temp, np.int32)
+        self.fuel = conv(sc.fuel, np.int32)
+        self.c = _native.SnScene(n=n, n_fluid=int(sc.nFluid), pos=_ptr(self.pos), vel=_ptr(self.vel),
+                                 mat_id=_ptr(self.mat), flags=_ptr(self.flags), temp=_ptr(self.temp),
+                                 fuel=_ptr(self.fuel), dom_w=int(sc.domW), dom_h=int(sc.domH),
+                                 cell_shift=int(sc.cellShift))
+
+
+def _particles(lst: Iterable[dict]):
+    lst = list(lst)
+    arr = (_native.SnParticle * max(1, len(lst)))()
+    for k, p in enumerate(lst):
+        arr[k].x = int(p['x'])
+        arr[k].y = int(p['y'])
+        arr[k].vx = int(p.get('vx', 0))
+        arr[k].vy = int(p.get('vy', 0))
+        arr[k].mat = int(p.get('mat', 0))
+        arr[k].flags = int(p.get('flags', 0))
+        arr[k].has_temp = 1 if p.get('temp') is not None else 0
+        arr[k].temp = int(p.get('temp') or 0)
+        arr[k].has_fuel = 1 if p.get('fuel') is not None else 0
+        arr[k].fuel = int(p.get('fuel') or 0)
+    return arr, len(lst)
+
+
+class Engine:
+    """One scene on one GB300 (``class Engine``, ``src/engine.js:3523``)."""
+
+    def __init__(self, max_particles: int = 8192, max_cells: int = 0, iters: int = ITERS, debug: bool = False,
+                 chain: bool = True, device: int = 0, tables=None, mats=None):
+        self._lib = _native.load()
+        o, self._keep = _opts(max_particles, max_cells, iters, debug, chain, device, tables, mats)
+        h = ctypes.c_void_p()
+        rc = self._lib.sn_create(ctypes.byref(o), ctypes.byref(h))
+        if rc != 0:
+            raise EngineError(f'sn_create failed ({rc})')
+        self._h = h
+        self.max_particles = int(max_particles)
+        self.iters = int(iters)
+        self.debug = bool(debug)
+        self.chain_enabled = bool(chain)
+        self.mat_count = self._keep[1].shape[0]
+        self._n = 0
+        self._n_fluid = 0
+        self._substeps = 0
+        self._scene: Optional[Scene] = None
+
+    # -- plumbing ------------------------------------------------------------------
+    def _check(self, rc: int, what: str):
+        if rc != 0:
+            msg = self._lib.sn_last_error(self._h)
+            raise EngineError(f'[aether] {what}: {msg.decode() if msg else rc}')
+
+    def destroy(self):
+        if getattr(self, '_h', None):
+            self._lib.sn_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+    # -- engine.js surface -----------------------------------------------------------
+    def load_scene(self, scene: Scene) -> 'Engine':
+        args = _SceneArgs(scene)
+        self._check(self._lib.sn_load_scene(self._h, ctypes.byref(args.c)), 'loadScene')
+        self._n, self._n_fluid = int(scene.n), int(scene.nFluid)
+        self._substeps = 0
+        self._scene = scene
+        return self
+
+    def step(self, count: int = 1) -> int:
+        if not isinstance(count, (int, np.integer)) or count < 0:
+            raise EngineError('[aether] step(count) needs a non-negative integer')
+        out = ctypes.c_uint64()
+        self._check(self._lib.sn_step(self._h, int(count), ctypes.byref(out)), 'step')
+        self._substeps = int(out.value)
+        return self._substeps
+
+    def frame(self) -> int:
+        return self.step(SUBSTEPS_PER_FRAME)
+
+    def digest(self) -> Digest:
+        a = np.zeros(8, np.uint32)
+        self._check(self._lib.sn_digest(self._h, _ptr(a)), 'digest')
+        return Digest(a)
+
+    def chain_words(self) -> np.ndarray:
+        a = np.zeros(8, np.uint32)
+        self._check(self._lib.sn_chain(self._h, _ptr(a)), 'chain')
+        return a
+
+    def chain_hex(self) -> str:
+        return ''.join(f'{int(x):08x}' for x in self.chain_words())
+
+    def reset_chain(self):
+        self._check(self._lib.sn_reset_chain(self._h), 'resetChain')
+
+    def read_state(self) -> np.ndarray:
+        a = np.zeros(self.n * 8, np.int32)
+        self._check(self._lib.sn_read_state(self._h, _ptr(a), a.size), 'readState')
+        return a
+
+    def read_scratch(self) -> np.ndarray:
+        a = np.zeros(self.n * 2, np.int32)
+        self._check(self._lib.sn_read_scratch(self._h, _ptr(a), a.size), 'readScratch')
+        return a
+
+    def write_state(self, state: np.ndarray, scratch: Optional[np.ndarray] = None):
+        st = np.ascontiguousarray(state, dtype=np.int32).reshape(-1)
+        sc = None if scratch is None else np.ascontiguousarray(scratch, dtype=np.int32).reshape(-1)
+        if st.size != self.n * 8 or (sc is not None and sc.size != self.n * 2):
+            raise EngineError('[aether] write_state: wrong buffer size')
+        self._check(self._lib.sn_write_state(self._h, _ptr(st), _ptr(sc), self.n), 'writeState')
+
+    def read_bonds(self) -> np.ndarray:
+        a = np.zeros(max(1, self.n_fluid * BOND_CAP), np.uint32)
+        self._check(self._lib.sn_read_bonds(self._h, _ptr(a), a.size), 'readBond')
+        return a[:self.n_fluid * BOND_CAP]
+
+    def spawn_fluid(self, particles, no_weld: bool = True) -> int:
+        arr, k = _particles(particles)
+        out = ctypes.c_uint32()
+        self._check(self._lib.sn_spawn(self._h, arr, k, 1 if no_weld else 0, ctypes.byref(out)), 'spawnFluid')
+        n = int(out.value)
+        if n != self._n:
+            self._n_fluid += n - self._n
+            self._n = n
+        return n
+
+    def apply_impulse(self, cx: int, cy: int, radius: int, ix: int, iy: int, limit: int = 3000) -> int:
+        out = ctypes.c_uint32()
+        self._check(self._lib.sn_impulse(self._h, int(cx), int(cy), int(radius), int(ix), int(iy), int(limit),
+                                         ctypes.byref(out)), 'applyImpulse')
+        return int(out.value)
+
+    def debug_counters(self) -> np.ndarray:
+        a = np.zeros(16, np.uint32)
+        self._check(self._lib.sn_debug_counters(self._h, _ptr(a)), 'debugCounters')
+        return a
+
+    def check_errors(self):
+        rc = self._lib.sn_check_errors(self._h)
+        if rc != 0:
+            self._check(rc, 'checkErrors')
+
+    def sync(self):
+        self._check(self._lib.sn_sync(self._h), 'sync')
+
+    def info(self) -> dict:
+        i = _native.SnInfo()
+        self._check(self._lib.sn_get_info(self._h, ctypes.byref(i)), 'info')
+        return {k: getattr(i, k) for k, _ in i._fields_}
+
+    def set_formation_clock(self, clock: int, dirty: bool):
+        self._check(self._lib.sn_set_formation_clock(self._h, int(clock), 1 if dirty else 0), 'formationClock')
+
+    def last_timing(self):
+        ms = ctypes.c_float()
+        l = ctypes.c_uint64()
+        self._check(self._lib.sn_last_timing(self._h, ctypes.byref(ms), ctypes.byref(l)), 'timing')
+        return float(ms.value), int(l.value)
+
+    @property
+    def n(self) -> int:
+        return self._n
+
+    @property
+    def n_fluid(self) -> int:
+        return self._n_fluid
+
+    @property
+    def substep_count(self) -> int:
+        return self._substeps
+
+    @property
+    def formation_clock(self) -> int:
+        return int(self.info()['formation_clock'])
+
+    # camelCase aliases: the reference's method names
+    loadScene = load_scene
+    chainHex = chain_hex
+    resetChain = reset_chain
+    readState = read_state
+    spawnFluid = spawn_fluid
+    applyImpulse = apply_impulse
+    debugCounters = debug_counters
+    checkErrors = check_errors
+    nFluid = n_fluid
+    substepCount = substep_count
+
+
+def create_engine(max_particles: int = 8192, **kw) -> Engine:
+    """``createEngine`` (``src/engine.js:2786``): ``maxParticles``, ``maxCells``,
+    ``debug``, ``chain``, ``iters``, ``mats``, ``tables``."""
+    alias = {'maxParticles': 'max_particles', 'maxCells': 'max_cells'}
+    kw = {alias.get(k, k): v for k, v in kw.items()}
+    kw.pop('submitBatch', None)
+    if 'max_particles' in kw:
+        max_particles = kw.pop('max_particles')
+    return Engine(max_particles=max_particles, **kw)
+
+
+createEngine = create_engine
+
+
+class Batch:
+    """Many independent scenes stepped together (``sn_batch_*``).
+
+    Every scene behaves exactly as it would alone in an ``Engine``: same digests,
+    same chain. Scenes can be added and removed between steps; impulses are
+    queued per scene against its own substep clock.
+    """
+
+    def __init__(self, max_particles: int, max_scenes: int, max_cells: int = 0, iters: int = ITERS,
+                 debug: bool = False, chain: bool = True, device: int = 0, tables=None, mats=None):
+        self._lib = _native.load()
+        o, self._keep = _opts(max_particles, max_cells, iters, debug, chain, device, tables, mats)
+        h = ctypes.c_void_p()
+        rc = self._lib.sn_batch_create(ctypes.byref(o), int(max_scenes), ctypes.byref(h))
+        if rc != 0:
+            raise EngineError(f'sn_batch_create failed ({rc})')
+        self._h = h
+        self.scenes = {}
+
+    def _check(self, rc: int, what: str):
+        if rc != 0:
+            msg = self._lib.sn_batch_last_error(self._h)
+            raise EngineError(f'[batch] {what}: {msg.decode() if msg else rc}')
+
+    def destroy(self):
+        if getattr(self, '_h', None):
+            self._lib.sn_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+    def add_scene(self, scene: Scene, capacity: int = 0) -> int:
+        args = _SceneArgs(scene)
+        sid = ctypes.c_uint32()
+        self._check(self._lib.sn_batch_add_scene(self._h, ctypes.byref(args.c), int(capacity), ctypes.byref(sid)),
+                    'add_scene')
+        self.scenes[int(sid.value)] = scene
+        return int(sid.value)
+
+    def remove_scene(self, sid: int):
+        self._check(self._lib.sn_batch_remove_scene(self._h, int(sid)), 'remove_scene')
+        self.scenes.pop(int(sid), None)
+
+    def step(self, count: int = 1):
+        self._check(self._lib.sn_batch_step(self._h, int(count)), 'step')
+
+    def schedule_impulse(self, sid: int, at_substep: int, cx: int, cy: int, r: int, ix: int, iy: int,
+                         limit: int = 3000):
+        self._check(self._lib.sn_batch_schedule_impulse(self._h, int(sid), int(at_substep), int(cx), int(cy), int(r),
+                                                          int(ix), int(iy), int(limit)), 'schedule_impulse')
+
+    def digest(self, sid: int) -> Digest:
+        a = np.zeros(8, np.uint32)
+        self._check(self._lib.sn_batch_digest(self._h, int(sid), _ptr(a)), 'digest')
+        return Digest(a)
+
+    def chain_hex(self, sid: int) -> str:
+        a = np.zeros(8, np.uint32)
+        self._check(self._lib.sn_batch_chain(self._h, int(sid), _ptr(a)), 'chain')
+        return ''.join(f'{int(x):08x}' for x in a)
+
+    def info(self, sid: int) -> dict:
+        i = _native.SnInfo()
+        self._check(self._lib.sn_batch_get_info(self._h, int(sid), ctypes.byref(i)), 'info')
+        return {k: getattr(i, k) for k, _ in i._fields_}
+
+    def read_state(self, sid: int) -> np.ndarray:
+        n = self.info(sid)['n']
+        a = np.zeros(n * 8, np.int32)
+        self._check(self._lib.sn_batch_read_state(self._h, int(sid), _ptr(a), a.size), 'read_state')
+        return a
+
+    def read_scratch(self, sid: int) -> np.ndarray:
+        n = self.info(sid)['n']
+        a = np.zeros(n * 2, np.int32)
+        self._check(self._lib.sn_batch_read_scratch(self._h, int(sid), _ptr(a), a.size), 'read_scratch')
+        return a
+
+    def write_state(self, sid: int, state, scratch, substep_count: int, formation_clock: int, dirty: bool):
+        st = np.ascontiguousarray(state, dtype=np.int32).reshape(-1)
+        sc = None if scratch is None else np.ascontiguousarray(scratch, dtype=np.int32).reshape(-1)
+        self._check(self._lib.sn_batch_write_state(self._h, int(sid), _ptr(st), _ptr(sc), st.size // 8,
+                                                    int(substep_count), int(formation_clock), 1 if dirty else 0),
+                    'write_state')
+
+    def check_errors(self):
+        self._check(self._lib.sn_batch_check_errors(self._h), 'check_errors')
+
+    def sync(self):
+        self._check(self._lib.sn_batch_sync(self._h), 'sync')
+
+    def last_timing(self):
+        ms = ctypes.c_float()
+        l = ctypes.c_uint64()
+        self._check(self._lib.sn_batch_last_timing(self._h, ctypes.byref(ms), ctypes.byref(l)), 'timing')
+        return float(ms.value), int(l.value)

@@ -1,0 +1,254 @@
+"""GPU parity: the CUDA engine, called through the C ABI, against the oracle.
+
+Bar: bit-exact. Every comparison is of the reference's own state digest
+(H_set || H_slot, src/hash/statehash.js:80-159) and of the per-substep chain,
+so one differing bit in any particle word on any substep fails the test.
+"""
+import numpy as np
+import pytest
+
+from sunaengine_gb300 import data, scenes
+from sunaengine_gb300.engine import Batch, Engine, EngineError
+
+from test_oracle import GOLDEN_CHAIN, GOLDEN_CHECKPOINTS
+
+pytestmark = pytest.mark.gpu
+
+M = data.mat_id
+ONE = scenes.ONE
+
+
+def _pool(mat, w=30, h=10):
+    return scenes.make_scene('pool_v1', w=w, h=h, mat=M(mat))
+
+
+def _mixed_thermal():
+    """OIL pool with a hot FIRE blob and a WATER strip: ignition, burning,
+    boiling to STEAM, smoke venting (split to ASH), all through `thermal`."""
+    sc = scenes.make_scene('pool_v1', w=40, h=12, mat=M('OIL'))
+    nf = sc.nFluid
+    mat = sc.matId.copy()
+    temp = np.full(sc.n, scenes.AMBIENT, np.int32)
+    fuel = np.zeros(sc.n, np.int32)
+    fuel[:nf] = scenes.deg(100)
+    for i in range(nf):
+        x, y = sc.pos[i]
+        if x < 18 * ONE:
+            mat[i] = M('WATER')
+            temp[i] = scenes.deg(130 if i % 3 == 0 else 97)
+            fuel[i] = 0
+        elif x < 22 * ONE:
+            mat[i] = M('STEAM')
+            temp[i] = scenes.deg(50)
+            fuel[i] = 0
+        elif 30 * ONE <= x < 36 * ONE and y < 64 * ONE:
+            mat[i] = M('FIRE')
+            temp[i] = scenes.deg(900)
+            fuel[i] = 100000 * (1 + i % 4)
+    sc.matId = mat.astype(np.uint32)
+    sc.temp = temp
+    sc.fuel = fuel
+    return sc
+
+
+def _hot_rice():
+    sc = _pool('RICE', 30, 12)
+    sc.temp = np.full(sc.n, scenes.deg(90), np.int32)
+    return sc
+
+
+def _anchored():
+    sc = _pool('SAND', 30, 10)
+    fl = np.zeros(sc.n, np.uint32)
+    fl[: sc.nFluid: 7] = 4  # FLAG_ANCHOR on every 7th particle
+    sc.flags = fl
+    return sc
+
+
+SCENES = {
+    'dambreak_v1': (lambda: scenes.make_scene('dambreak_v1'), 40),
+    'overdense_v1': (lambda: scenes.make_scene('overdense_v1'), 25),
+    'pool_water': (lambda: _pool('WATER', 40, 12), 40),
+    'droplet_oil': (lambda: scenes.make_scene('droplet_v1', mat=M('OIL')), 40),
+    'stretch_gel': (lambda: scenes.make_scene('stretch_v1'), 60),
+    'sand_pool': (lambda: _pool('SAND', 30, 12), 40),
+    'rice_pool': (_hot_rice, 40),
+    'tar_pool': (lambda: _pool('TAR', 30, 10), 30),
+    'thermal_mix': (_mixed_thermal, 60),
+    'anchored_sand': (_anchored, 30),
+    'two_fluid_48': (lambda: scenes.large_two_fluid(side=48, band=8), 30),
+    'lattice_dambreak_64': (lambda: scenes.lattice_dambreak(), 30),
+}
+
+
+def _pair(sc, debug=True, iters=4):
+    cap = max(8192, sc.n + 64)
+    gpu = Engine(max_particles=cap, debug=debug, iters=iters).load_scene(sc)
+    import oracle
+    ref = oracle.OracleEngine(cap, iters=iters, threads=8).load_scene(sc)
+    return gpu, ref
+
+
+def test_golden_dambreak_chain():
+    e = Engine(max_particles=8192, debug=True).load_scene(scenes.make_scene('dambreak_v1'))
+    done = 0
+    for c, want in GOLDEN_CHECKPOINTS.items():
+        e.step(c - done)
+        done = c
+        assert e.digest().hex == want, f'checkpoint {c}'
+    assert e.chain_hex() == GOLDEN_CHAIN
+    assert not e.debug_counters().any()
+    e.check_errors()
+
+
+@pytest.mark.parametrize('name', sorted(SCENES))
+def test_every_substep_matches_oracle(name, oracle_mod):
+    make, steps = SCENES[name]
+    sc = make()
+    gpu, ref = _pair(sc)
+    assert gpu.digest().hex == ref.digest()
+    for s in range(1, steps + 1):
+        gpu.step(1)
+        ref.step(1)
+        g, r = gpu.digest().hex, ref.digest()
+        assert g == r, f'{name}: substep {s}'
+    assert gpu.chain_hex() == ref.chain_hex()
+    assert np.array_equal(gpu.debug_counters(), ref.debug_counters())
+    assert np.array_equal(gpu.read_state(), ref.read_state())
+    if sc.n:
+        assert np.array_equal(gpu.read_bonds(), ref.read_bonds())
+    gpu.check_errors()
+
+
+def test_release_build_matches_debug_build(oracle_mod):
+    sc = scenes.make_scene('overdense_v1')
+    a = Engine(max_particles=8192, debug=True).load_scene(sc)
+    b = Engine(max_particles=8192, debug=False).load_scene(sc)
+    a.step(30)
+    b.step(30)
+    assert a.chain_hex() == b.chain_hex()
+    assert not b.debug_counters().any()
+
+
+@pytest.mark.parametrize('iters', [1, 3, 7])
+def test_iteration_count_option(iters, oracle_mod):
+    sc = _pool('WATER', 25, 10)
+    gpu, ref = _pair(sc, iters=iters)
+    gpu.step(25)
+    ref.step(25)
+    assert gpu.chain_hex() == ref.chain_hex()
+
+
+def test_spawn_and_impulse_match_oracle(oracle_mod):
+    sc = _pool('WATER', 40, 12)
+    gpu, ref = _pair(sc)
+    drop = scenes.make_droplet(64 * ONE, 10 * ONE, 3, 3, vy=ONE // 5)
+    for s in range(60):
+        if s % 8 == 0:
+            assert gpu.spawn_fluid([dict(p, mat=0) for p in drop]) == ref.spawn([dict(p, mat=0) for p in drop])
+        if s % 10 == 5:
+            args = (50 * ONE, 60 * ONE, 6 * ONE, 9000, -12000)
+            assert gpu.apply_impulse(*args) == ref.impulse(*args)
+        if s == 33:
+            # limit binds: only the first 7 hits in slot order are pushed
+            assert gpu.apply_impulse(40 * ONE, 62 * ONE, 20 * ONE, -5000, 3000, 7) == \
+                ref.impulse(40 * ONE, 62 * ONE, 20 * ONE, -5000, 3000, 7)
+        gpu.step(1)
+        ref.step(1)
+        assert gpu.digest().hex == ref.digest(), f'substep {s}'
+    assert gpu.n == ref.n and gpu.n_fluid == ref.n_fluid
+    assert gpu.chain_hex() == ref.chain_hex()
+
+
+def test_spawn_refused_at_capacity():
+    sc = _pool('WATER', 10, 5)
+    e = Engine(max_particles=sc.n + 2).load_scene(sc)
+    n0 = e.n
+    assert e.spawn_fluid([{'x': 60 * ONE, 'y': 20 * ONE}] * 3) == n0  # silently unchanged, like the reference
+    assert e.spawn_fluid([{'x': 60 * ONE, 'y': 20 * ONE}] * 2) == n0 + 2
+
+
+def test_keyframe_rejoins_timeline():
+    sc = _pool('WATER', 40, 12)
+    e = Engine(max_particles=8192).load_scene(sc)
+    e.step(60)
+    st, scr, clk = e.read_state(), e.read_scratch(), e.formation_clock
+    e.step(40)
+    ahead = e.digest().hex
+    e.load_scene(sc)
+    e.write_state(st, scr)
+    e.set_formation_clock(clk, False)
+    e.step(40)
+    assert e.digest().hex == ahead
+    # state-only restore (no scratch) is a load boundary: it diverges
+    e.load_scene(sc)
+    e.write_state(st, None)
+    e.set_formation_clock(clk, False)
+    e.step(40)
+    assert e.digest().hex != ahead
+
+
+def test_batch_scenes_match_oracle(oracle_mod):
+    import oracle
+    mk = [lambda: scenes.make_scene('dambreak_v1'), lambda: _pool('SAND', 25, 10),
+          lambda: scenes.make_scene('stretch_v1'), lambda: scenes.large_two_fluid(side=40, band=8),
+          lambda: scenes.make_scene('droplet_v1', mat=M('OIL'))]
+    scs = [f() for f in mk]
+    b = Batch(max_particles=sum(s.n for s in scs) + 1024, max_scenes=8, debug=True)
+    ids = [b.add_scene(s) for s in scs]
+    refs = [oracle.OracleEngine(s.n + 64, threads=8).load_scene(s) for s in scs]
+    # impulses at scene-specific substeps
+    ev = {ids[0]: [(5, 20 * ONE, 60 * ONE, 5 * ONE, 8000, -9000)], ids[3]: [(7, 20 * ONE, 30 * ONE, 6 * ONE, -7000, 0),
+                                                                          (7, 25 * ONE, 30 * ONE, 4 * ONE, 3000, 3000)]}
+    for sid, lst in ev.items():
+        for (at, cx, cy, r, ix, iy) in lst:
+            b.schedule_impulse(sid, at, cx, cy, r, ix, iy)
+    for s in range(20):
+        for k, sid in enumerate(ids):
+            for (at, cx, cy, r, ix, iy) in ev.get(sid, []):
+                if at == s:
+                    refs[k].impulse(cx, cy, r, ix, iy)
+        b.step(1)
+        for r in refs:
+            r.step(1)
+    for k, sid in enumerate(ids):
+        assert b.chain_hex(sid) == refs[k].chain_hex(), f'scene {k}'
+        assert b.digest(sid).hex == refs[k].digest()
+    b.check_errors()
+
+
+def test_batch_remove_and_add_keeps_others_exact(oracle_mod):
+    import oracle
+    a, c = _pool('WATER', 30, 10), scenes.make_scene('droplet_v1')
+    b = Batch(max_particles=20000, max_scenes=4)
+    ia = b.add_scene(a)
+    ib = b.add_scene(scenes.make_scene('dambreak_v1'))
+    ra = oracle.OracleEngine(a.n + 8, threads=8).load_scene(a)
+    b.step(10)
+    ra.step(10)
+    b.remove_scene(ib)
+    ic = b.add_scene(c)
+    rc = oracle.OracleEngine(c.n + 8, threads=8).load_scene(c)
+    b.step(15)
+    ra.step(15)
+    rc.step(15)
+    assert b.chain_hex(ia) == ra.chain_hex()
+    assert b.chain_hex(ic) == rc.chain_hex()
+
+
+def test_refuses_bad_input():
+    e = Engine(max_particles=1024)
+    with pytest.raises(EngineError):
+        e.step(1)  # before loadScene
+    sc = _pool('WATER', 10, 5)
+    bad = sc.copy()
+    bad.matId[0] = 99
+    with pytest.raises(EngineError):
+        e.load_scene(bad)
+    seal = sc.copy()
+    seal.matId[0] = M('STONE')
+    with pytest.raises(EngineError):
+        e.load_scene(seal)
+    big = scenes.make_scene('dambreak_v1')
+    with pytest.raises(EngineError):
+        e.load_scene(big)  # n > maxParticles
