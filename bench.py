@@ -1,0 +1,373 @@
+#!/usr/bin/env python3
+"""Benchmark: particle-substeps/s of the deterministic Q16.16 PBF substep on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Headline workload (one GPU): the 2D large scene — 1,048,576 fluid particles in
+a 1024 x 1024 lattice at 1 wu with seeded +/-0.25 wu jitter, WATER/OIL in
+alternating 64-column bands, per-particle temperatures uniform in
+[10, 90] degrees, 4 density iterations, chain (H_set || H_slot every substep)
+on. One step = one substep of that scene. The working set (~0.5 GB) is far
+larger than the 129 MB L2, so no L2 flush is needed between substeps.
+
+Printed: one JSON line with the device-timed value, the end-to-end value
+through the public API (scene upload from host memory, a digest read back
+after every substep, final state read back), the per-phase roofline of the
+dominant kernel, the CPU baseline, the batched workload (256 scenes of
+1k-64k particles with stir impulses) against the same scenes stepped one at a
+time on the plain path, and GPU clock samples.
+
+--impl reference times the reference's algorithm on the host cores: the
+reference itself is JavaScript + WGSL for WebGPU and cannot run here (no JS
+runtime, no WebGPU), so its CPU restatement (oracle/, pinned bit-exact to the
+reference's golden chain) is timed instead, with all host threads, on a
+65,536-particle sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import numpy as np  # noqa: E402
+
+METRIC = 'particle-substeps/s'
+UNIT = 'particle-substeps/s'
+WORKLOAD = ('2D large scene: 1,048,576 fluid particles (1024x1024 lattice, 1 wu, +/-0.25 wu seeded jitter), '
+            'WATER/OIL 64-column bands, temps U[10,90] deg, ITERS 4, H_slot every substep')
+
+
+def _peaks():
+    p = ROOT / 'MEASURED_PEAKS.json'
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d['hbm_gbs']), 'measured'
+    return 6800.0, 'fallback'
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled every 200 ms."""
+
+    FIELDS = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+              'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+              'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(['nvidia-smi', '-i', str(self.device), f'--query-gpu={self.FIELDS}',
+                                          '--format=csv,noheader,nounits', '-lms', '100'],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(',')]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() in ('active', '1', 'yes'):
+                    reasons.add(nm)
+        if not sm:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['unavailable'], 'samples': 0}
+        return {'sm_mhz': float(np.median(sm)), 'sm_max_mhz': float(max(smax)), 'reasons': sorted(reasons),
+                'samples': len(sm)}
+
+
+def _dist():
+    ws = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        backend = 'nccl' if torch.cuda.is_available() else 'gloo'
+        if backend == 'nccl':
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+        return ws, rank, local, dist
+    return 1, 0, 0, None
+
+
+def _barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def _max_over_ranks(dist, x: float, local: int) -> float:
+    if dist is None:
+        return x
+    import torch
+    dev = f'cuda:{local}' if dist.get_backend() == 'nccl' else 'cpu'
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# --- algorithmic bytes per unit (phase-minimal convention) -------------------------
+# Per fluid particle, per launch of the phase. Each dependent phase reads the
+# fields it needs once and writes its outputs once; neighbour data is served
+# on chip and the neighbour list is not counted.
+PHASE_NAMES_HEAD = ['predict', 'grid sort', 'cell ranges + gather', 'neighbour lists']
+BYTES = {
+    'predict': 48,               # R state 32 + stAcc 8; W pred 8
+    'grid sort': 20,             # R pred 8; W key 4 + sorted id 4; R key 4
+    'cell ranges + gather': 0,
+    'neighbour lists': 16,       # R pred 8 + flags 4; W count 4
+    'solveA': 20,                # R pred 8 + mat 4; W rho 4 + lam 4
+    'colour x4': 88,             # 4 colours: R pred + lam, W dp (56) + apply R dp/pred W pred (32)
+    'friction': 8,
+    'finalize+xsph+normals+conduct': 140,  # finalize 88 + xsph 32 + normals 20
+    'surfaceTension+thermal+digest': 104,  # surfaceTension 32 + conduct/thermal 40 + hash 32
+    'fold': 0,
+}
+
+
+def phase_names(iters: int):
+    names = list(PHASE_NAMES_HEAD)
+    for _ in range(iters):
+        names += ['solveA', 'colour x4', 'friction']
+    names += ['finalize+xsph+normals+conduct', 'surfaceTension+thermal+digest', 'fold']
+    return names
+
+
+def run_cpu_baseline(sample_side: int = 256, seconds: float = 12.0, threads: int = 0):
+    """The oracle (CPU restatement of the reference substep) on a bounded sample."""
+    import oracle
+    from sunaengine_gb300 import scenes
+    threads = threads or os.cpu_count() or 1
+    sc = scenes.large_two_fluid(side=sample_side)
+    e = oracle.OracleEngine(sc.n + 64, threads=threads).load_scene(sc)
+    e.step(1)
+    t0 = time.perf_counter()
+    k = 0
+    while True:
+        e.step(1)
+        k += 1
+        if time.perf_counter() - t0 >= seconds:
+            break
+    dt = time.perf_counter() - t0
+    return {'value': sc.nFluid * k / dt, 'unit': UNIT, 'cores': threads, 'kind': 'port',
+            'sample': f'{sc.nFluid} fluid particles ({sample_side}x{sample_side} slice of the same workload), '
+                      f'{k} substeps, {dt:.1f} s'}
+
+
+def reference_arm(args):
+    ws, rank, local, dist = _dist()
+    if rank != 0:
+        return 0
+    import oracle
+    from sunaengine_gb300 import scenes
+    threads = os.cpu_count() or 1
+    side = 256
+    sc = scenes.large_two_fluid(side=side)
+    e = oracle.OracleEngine(sc.n + 64, threads=threads).load_scene(sc)
+    e.step(args.warmup)
+    t0 = time.perf_counter()
+    e.step(args.steps)
+    dt = time.perf_counter() - t0
+    v = sc.nFluid * args.steps / dt
+    line = {
+        'impl': 'reference', 'metric': METRIC, 'value': v, 'unit': UNIT, 'n_gpus': args.gpus,
+        'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': 1e3 * dt / args.steps,
+        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'int32', 'data': 'synthetic',
+        'config': {'workload': WORKLOAD, 'sample': f'{sc.nFluid}-particle {side}x{side} slice', 'parallelism': 'cpu'},
+        'cpu_baseline': {'value': v, 'unit': UNIT, 'cores': threads, 'kind': 'port',
+                         'sample': f'{sc.nFluid} fluid particles, {args.steps} substeps'},
+        'e2e': {'value': v, 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
+        'note': 'the reference is JS+WGSL for WebGPU (no JS runtime or WebGPU here); its CPU restatement, '
+                'pinned bit-exact to the reference golden chain, is timed',
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def batched_workload(steps: int, warmup: int, device: int, plain_sample: int = 24, seed: int = 0xba7c4):
+    """256 scenes (1k-64k particles, log-uniform) with stir schedules: batched
+    vs the same scenes stepped one at a time on the plain path."""
+    from sunaengine_gb300 import scenes
+    from sunaengine_gb300.engine import Batch, Engine
+    scs, sched = scenes.batch_scenes(count=256, seed=seed, substeps=warmup + steps)
+    total = sum(s.n for s in scs)
+    nf = sum(s.nFluid for s in scs)
+    b = Batch(max_particles=total + 16, max_scenes=len(scs), max_cells=1 << 22, device=device)
+    ids = [b.add_scene(s) for s in scs]
+    for sid, ev in zip(ids, sched):
+        for (at, cx, cy, r, ix, iy) in ev:
+            b.schedule_impulse(sid, at, cx, cy, r, ix, iy)
+    b.step(warmup)
+    b.sync()
+    b.step(steps)
+    ms, launches = b.last_timing()
+    b.check_errors()
+    batched = nf * steps / (ms / 1e3)
+    prof = b.profile_substep(2)
+    b.destroy()
+    # plain path on a sample of the same scenes, one engine per scene, sequentially
+    rng = np.random.Generator(np.random.PCG64(seed ^ 0x5a5a))
+    pick = rng.choice(len(scs), size=min(plain_sample, len(scs)), replace=False)
+    pn, pms = 0, 0.0
+    for k in pick:
+        s = scs[int(k)]
+        e = Engine(max_particles=s.n + 16, max_cells=1 << 20, device=device).load_scene(s)
+        e.step(warmup)
+        e.sync()
+        e.step(steps)
+        t, _ = e.last_timing()
+        pn += s.nFluid * steps
+        pms += t
+        e.destroy()
+    plain = pn / (pms / 1e3)
+    return {'scenes': len(scs), 'particles': int(nf), 'value': batched, 'unit': UNIT,
+            'ms_per_step': ms / steps, 'gpu_launches_per_step': launches // max(1, steps),
+            'plain_same_scenes': plain, 'plain_sample_scenes': int(len(pick)),
+            'batched_vs_plain': batched / plain}
+
+
+def ours(args):
+    ws, rank, local, dist = _dist()
+    from sunaengine_gb300 import scenes
+    from sunaengine_gb300.engine import Engine
+    sc = scenes.large_two_fluid(side=1024)
+    e = Engine(max_particles=sc.n, max_cells=1 << 20, device=local)
+    e.load_scene(sc)
+    e.step(args.warmup)
+    e.sync()
+    _barrier(dist)
+    with ClockSampler(local) as clk:
+        e.sync()
+        _barrier(dist)
+        t0 = time.perf_counter()
+        e.step(args.steps)
+        e.sync()
+        wall = time.perf_counter() - t0
+        _barrier(dist)
+    dev_ms, launches = e.last_timing()
+    e.check_errors()
+    dev_ms = _max_over_ranks(dist, dev_ms, local)
+    ms_step = dev_ms / args.steps
+    value = ws * sc.nFluid * args.steps / (dev_ms / 1e3)
+
+    # per-phase device times (CUDA events on the engine's stream) over real substeps
+    names = phase_names(e.iters)
+    reps = max(3, min(args.steps, 10))
+    ph = e.profile_substep(reps)
+    agg = {}
+    for nm, t in zip(names, ph):
+        agg.setdefault(nm, [0.0, 0])
+        agg[nm][0] += float(t)
+        agg[nm][1] += 1
+    dom = max((k for k in agg if k != 'fold'), key=lambda k: agg[k][0])
+    launches_of = {'colour x4': 4}
+    nl = launches_of.get(dom, 1)
+    per_launch_ms = agg[dom][0] / (agg[dom][1] * nl)
+    units = sc.nFluid // nl
+    bytes_per_launch = BYTES[dom] * sc.nFluid / nl
+    achieved = bytes_per_launch / (per_launch_ms / 1e3) / 1e9
+    peak, peak_kind = _peaks()
+    roof = {'kernel': dom, 'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
+            'frac': achieved / peak, 'peak_source': peak_kind, 'traffic': None,
+            'algorithmic_bytes_per_launch': bytes_per_launch, 'units_per_launch': units,
+            'launch_ms': per_launch_ms,
+            'phases_ms_per_substep': {k: v[0] for k, v in agg.items()}}
+
+    # end to end through the public API: upload from host, H_slot read back every
+    # substep, final state read back
+    e2 = Engine(max_particles=sc.n, max_cells=1 << 20, device=local)
+    e2.load_scene(sc)
+    e2.step(1)
+    e2.sync()
+    _barrier(dist)
+    t0 = time.perf_counter()
+    e2.load_scene(sc)
+    for _ in range(args.steps):
+        e2.step(1)
+        e2.digest()
+    final = e2.read_state()
+    e2wall = time.perf_counter() - t0
+    e2wall = _max_over_ranks(dist, e2wall, local)
+    scene_bytes = sc.n * (8 + 8 + 4 + 4)
+    e2e = {'value': ws * sc.nFluid * args.steps / e2wall, 'unit': UNIT,
+           'h2d_bytes_per_step': scene_bytes / args.steps,
+           'd2h_bytes_per_step': 32 + final.nbytes / args.steps,
+           'how': 'loadScene from host arrays, then per substep step(1) + digest() readback, then readState'}
+    e2.destroy()
+    e.destroy()
+
+    line = {
+        'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': ws, 'steps': args.steps, 'warmup': args.warmup,
+        'ms_per_step': ms_step, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+        'dtype': 'int32', 'data': 'synthetic',
+        'config': {'workload': WORKLOAD, 'particles': sc.n, 'fluid_particles': sc.nFluid,
+                   'parallelism': 'replicas' if ws > 1 else 'single', 'l2': 'working set > L2, no flush'},
+        'wall_ms_per_step': 1e3 * wall / args.steps,
+        'gpu_launches': int(launches),
+        'roofline': roof,
+        'e2e': e2e,
+        'clocks': clk.summary(),
+    }
+    if rank == 0 and not args.no_batched:
+        line['batched'] = batched_workload(args.steps, args.warmup, local)
+    if rank == 0 and not args.no_cpu:
+        line['cpu_baseline'] = run_cpu_baseline(seconds=args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=300)
+    ap.add_argument('--warmup', type=int, default=5)
+    ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    ap.add_argument('--no-batched', action='store_true')
+    ap.add_argument('--no-cpu', action='store_true')
+    ap.add_argument('--cpu-seconds', type=float, default=12.0)
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    if args.impl == 'reference':
+        return reference_arm(args)
+    return ours(args)
+
+
+if __name__ == '__main__':
+    sys.exit(main())

@@ -54,6 +54,9 @@ typedef struct sn_opts {
   const int32_t* luts;    /* 5*3202 int32 kernel tables (src/tables.json), hash-checked */
   const int32_t* mats;    /* mat_count rows of 48 int32 (MATS, src/engine.js:1192) */
   uint32_t mat_count;     /* 1..64 */
+  uint32_t lanes;         /* lanes per particle in the neighbour gathers: 1, 2, 4, 8;
+                             0 = chosen from the active particle count. Results do
+                             not depend on it (the split sums are exact). */
 } sn_opts;
 
 /* loadScene argument (src/engine.js:3704-3951). flags/temp/fuel may be NULL. */
@@ -170,6 +173,15 @@ int sn_batch_sync(sn_batch* b);
  * events on the engine's stream), and the kernel launches it issued. */
 int sn_batch_last_timing(sn_batch* b, float* ms, uint64_t* launches);
 int sn_last_timing(sn_engine* e, float* ms, uint64_t* launches);
+/* profileSubstep (src/engine.js:4221-4267): run `reps` substeps (outside the
+ * CUDA graph) with CUDA events between kernel phases and return the mean
+ * device milliseconds of each phase in ms[0..*n_phases). Phase order:
+ * predict, grid sort, cell ranges + gather, neighbour lists, then per solver
+ * iteration (solveA, the four colour passes, friction), then
+ * finalize/xsph/normals/conduct, surface tension/thermal/formation/digest,
+ * chain fold. The substeps are real: the scene advances by `reps`. */
+int sn_profile_substep(sn_engine* e, uint32_t reps, float* ms, uint32_t max_phases, uint32_t* n_phases);
+int sn_batch_profile_substep(sn_batch* b, uint32_t reps, float* ms, uint32_t max_phases, uint32_t* n_phases);
 
 #ifdef __cplusplus
 }

@@ -56,7 +56,7 @@ class SnOpts(ctypes.Structure):
     _fields_ = [('max_particles', ctypes.c_uint32), ('max_cells', ctypes.c_uint32),
                 ('iters', ctypes.c_uint32), ('debug', ctypes.c_uint32), ('chain', ctypes.c_uint32),
                 ('device', ctypes.c_int32), ('luts', ctypes.c_void_p), ('mats', ctypes.c_void_p),
-                ('mat_count', ctypes.c_uint32)]
+                ('mat_count', ctypes.c_uint32), ('lanes', ctypes.c_uint32)]
 
 
 class SnScene(ctypes.Structure):
@@ -102,6 +102,8 @@ SIGNATURES = {
     'sn_get_info': (ctypes.c_int, [P, ctypes.POINTER(SnInfo)]),
     'sn_set_formation_clock': (ctypes.c_int, [P, u64, u32]),
     'sn_last_timing': (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(u64)]),
+    'sn_profile_substep': (ctypes.c_int, [P, u32, P, u32, ctypes.POINTER(u32)]),
+    'sn_batch_profile_substep': (ctypes.c_int, [P, u32, P, u32, ctypes.POINTER(u32)]),
     'sn_batch_create': (ctypes.c_int, [ctypes.POINTER(SnOpts), u32, ctypes.POINTER(P)]),
     'sn_batch_destroy': (None, [P]),
     'sn_batch_last_error': (ctypes.c_char_p, [P]),

@@ -172,6 +172,7 @@ struct World {
   cudaGraphExec_t gexec = nullptr;
   bool graphValid = false;
   bool useGraph = true;
+  int lanesOverride = 0;  // 0 = choose from the active particle count
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   float lastMs = 0.f;
   uint64_t lastLaunches = 0;
@@ -195,8 +196,8 @@ struct World {
     if (gexec) cudaGraphExecDestroy(gexec);
     if (graph) cudaGraphDestroy(graph);
     void* ptrs[] = {b.state, b.stacc, b.predSlot, b.sceneOf, b.keys, b.inv, b.bond, b.bondCand, b.skey,
-                    b.sslot, b.cellStart, b.P, b.POS, b.INFO, b.FLG, b.TEMP, b.SCN, b.RHO, b.LAM,
-                    b.RINV, b.DP, b.NRM, b.HEAT, b.CORR, b.NBR, b.NBRN, (void*)b.luts, (void*)b.mats,
+                    b.sslot, b.cellStart, b.PL, b.PL2, b.RX, b.NQ, b.POS, b.SCN, b.DP, b.HEAT, b.CORR, b.NBR, b.NBRN,
+                    (void*)b.luts, (void*)b.WG, (void*)b.CA, (void*)b.mats, (void*)b.rcp,
                     b.scenes, b.world, b.acc, b.accLast, b.chain, b.dbg, b.err, tmpK, tmpV, hist,
                     hits, accTmp, devEv, devEp};
     for (void* p : ptrs)
@@ -217,6 +218,9 @@ struct World {
     cudaDeviceGetAttribute(&numSMs, cudaDevAttrMultiProcessorCount, device);
     debug = o->debug != 0;
     chainOn = o->chain != 0;
+    if (o->lanes != 0 && o->lanes != 1 && o->lanes != 2 && o->lanes != 4 && o->lanes != 8)
+      return fail("lanes must be 0, 1, 2, 4 or 8");
+    lanesOverride = (int)o->lanes;
     iters = o->iters;
     capSlots = o->max_particles;
     maxCells = o->max_cells ? o->max_cells : (1u << 20);
@@ -246,23 +250,22 @@ struct World {
     b.skey = dalloc<uint32_t>(C, err);
     b.sslot = dalloc<uint32_t>(C, err);
     b.cellStart = dalloc<uint32_t>((size_t)maxCells + 1, err);
-    b.P = dalloc<int2>(C, err);
+    b.PL = dalloc<int4>(C, err);
+    b.PL2 = dalloc<int4>(C, err);
+    b.RX = dalloc<int4>(C, err);
+    b.NQ = dalloc<int4>(C, err);
     b.POS = dalloc<int2>(C, err);
-    b.INFO = dalloc<uint32_t>(C, err);
-    b.FLG = dalloc<uint32_t>(C, err);
-    b.TEMP = dalloc<int32_t>(C, err);
     b.SCN = dalloc<uint32_t>(C, err);
-    b.RHO = dalloc<int32_t>(C, err);
-    b.LAM = dalloc<int32_t>(C, err);
-    b.RINV = dalloc<int32_t>(C, err);
     b.DP = dalloc<int2>(C, err);
-    b.NRM = dalloc<int2>(C, err);
     b.HEAT = dalloc<int32_t>(C, err);
     b.CORR = dalloc<int32_t>(C, err);
     b.NBR = dalloc<uint32_t>(C * MAXNBR, err);
     b.NBRN = dalloc<uint32_t>(C, err);
     b.nbrStride = (uint32_t)C;
+    uint16_t* drcp = dalloc<uint16_t>(32768, err);
     int32_t* dl = dalloc<int32_t>(LUT_WORDS, err);
+    int2* dwg = dalloc<int2>(TN, err);
+    int2* dca = dalloc<int2>(TN, err);
     int32_t* dm = dalloc<int32_t>(MAT_MAX * MAT_WORDS, err);
     b.scenes = dalloc<ScenePar>(scenesCap, err);
     b.world = dalloc<WorldPar>(1, err);
@@ -278,10 +281,29 @@ struct World {
     accTmp = dalloc<uint32_t>((size_t)scenesCap * 8, err);
     devEp = dalloc<EvPar>(scenesCap, err);
     if (!err.empty()) return false;
+    for (int i = 4 * TN; i < 5 * TN; ++i)
+      if (o->luts[i] != 0) return fail("the s_corr kernel table must be all zero (scorrK = 0 in the frozen tables)");
     cudaMemcpy(dl, o->luts, sizeof(int32_t) * LUT_WORDS, cudaMemcpyHostToDevice);
+    {
+      std::vector<int2> wg(TN), ca(TN);
+      for (int i = 0; i < TN; ++i) {
+        wg[i] = make_int2(o->luts[i], o->luts[TN + i]);
+        ca[i] = make_int2(o->luts[2 * TN + i], o->luts[3 * TN + i]);
+      }
+      cudaMemcpy(dwg, wg.data(), sizeof(int2) * TN, cudaMemcpyHostToDevice);
+      cudaMemcpy(dca, ca.data(), sizeof(int2) * TN, cudaMemcpyHostToDevice);
+    }
+    b.WG = dwg;
+    b.CA = dca;
     cudaMemcpy(dm, hmats, sizeof(hmats), cudaMemcpyHostToDevice);
+    {
+      std::vector<uint16_t> rc(32768);
+      for (uint32_t dn = 32768; dn < 65536; ++dn) rc[dn - 32768] = (uint16_t)((1u << 30) / dn);
+      cudaMemcpy(drcp, rc.data(), 65536, cudaMemcpyHostToDevice);
+    }
     b.luts = dl;
     b.mats = dm;
+    b.rcp = drcp;
     sh.assign(scenesCap, SceneHost{});
     hpar.assign(scenesCap, ScenePar{});
     return cuda_ok(cudaDeviceSynchronize(), "init");
@@ -501,56 +523,99 @@ struct World {
     return (int)std::max<uint64_t>(g, 1);
   }
 
-  template <bool DBG>
-  void launch_substep() {
+  // Optional phase markers (profile_substep): events recorded between phases.
+  cudaEvent_t* pev = nullptr;
+  int npev = 0;
+  void mark() {
+    if (pev) cudaEventRecord(pev[npev++], st);
+  }
+
+  // Lanes per particle for the neighbour gathers: small scenes split each
+  // neighbour list over several lanes so the GPU has enough threads in flight.
+  int lanes() const {
+    uint64_t n = hw.nAct;
+    if (n < 40000) return 8;
+    if (n < 80000) return 4;
+    if (n < 160000) return 2;
+    return 1;
+  }
+
+  template <bool DBG, int L>
+  void launch_substep_l() {
     const int gs = grid_for(hw.slotEnd);
     const int ga = grid_for(hw.nAct);
-    uint64_t L = 0;
+    const int gl = grid_for((uint64_t)hw.nAct * L);
+    uint64_t Lc = 0;
     if (anyEvents) {
       k_impulse_sched<<<hw.numScenes, 256, 0, st>>>(b, devEv, devEp);
-      ++L;
+      ++Lc;
     }
+    mark();
     k_predict_key<DBG><<<gs, 256, 0, st>>>(b);
-    ++L;
+    ++Lc;
+    mark();
     int bits = 1;
     while ((1ull << bits) <= hw.K) ++bits;
     radix::sort_pairs(b.keys, hw.slotEnd, bits, b.skey, b.sslot, tmpK, tmpV, hist, st);
-    L += 3ull * ((bits + radix::RBITS - 1) / radix::RBITS);
+    Lc += 3ull * ((bits + radix::RBITS - 1) / radix::RBITS);
+    mark();
     k_cellstart<<<grid_for((uint64_t)hw.K + 1), 256, 0, st>>>(b);
     k_gather<<<ga, 256, 0, st>>>(b);
+    mark();
     k_nbr<DBG><<<ga, 256, 0, st>>>(b);
-    L += 3;
+    mark();
+    Lc += 3;
     for (uint32_t it = 0; it < iters; ++it) {
-      k_solveA<DBG><<<ga, 256, 0, st>>>(b, b.P, it + 1 == iters ? 1 : 0);
-      for (int c = 0; c < 4; ++c) k_colour<DBG><<<ga, 256, 0, st>>>(b, b.P, c);
-      L += 5;
-      if (hasFriction) {
-        k_friction<DBG><<<ga, 256, 0, st>>>(b, b.P);
-        k_apply_fric<DBG><<<ga, 256, 0, st>>>(b, b.P);
-        L += 2;
+      k_solveA<DBG, L><<<gl, 256, 0, st>>>(b, it + 1 == iters ? 1 : 0);
+      mark();
+      for (int c = 0; c < 4; ++c) {
+        const int4* src = (c & 1) ? b.PL2 : b.PL;
+        int4* dst = (c & 1) ? b.PL : b.PL2;
+        k_colour<DBG, L><<<gl, 256, 0, st>>>(b, c, src, dst);
       }
+      mark();
+      Lc += 5;
+      if (hasFriction) {
+        k_friction<DBG><<<ga, 256, 0, st>>>(b);
+        k_apply_fric<DBG><<<ga, 256, 0, st>>>(b);
+        Lc += 2;
+      }
+      mark();
     }
-    k_post1<DBG><<<ga, 256, 0, st>>>(b, b.P);
-    ++L;
+    k_post1<DBG, L><<<gl, 256, 0, st>>>(b);
+    ++Lc;
+    mark();
     if (hasBonds) {
-      k_post2<DBG, false><<<ga, 256, 0, st>>>(b, b.P, 0);
+      k_post2<DBG, false, L><<<gl, 256, 0, st>>>(b, 0);
       k_form1<DBG><<<ga, 256, 0, st>>>(b);
       k_form2<<<gs, 256, 0, st>>>(b);
-      L += 3;
+      Lc += 3;
       if (chainOn) {
         k_hash<<<gs, 256, 0, st>>>(b, b.acc);
-        ++L;
+        ++Lc;
       }
     } else if (chainOn) {
-      k_post2<DBG, true><<<ga, 256, 0, st>>>(b, b.P, 1);
-      ++L;
+      k_post2<DBG, true, L><<<gl, 256, 0, st>>>(b, 1);
+      ++Lc;
     } else {
-      k_post2<DBG, false><<<ga, 256, 0, st>>>(b, b.P, 1);
-      ++L;
+      k_post2<DBG, false, L><<<gl, 256, 0, st>>>(b, 1);
+      ++Lc;
     }
+    mark();
     k_fold<<<(hw.numScenes + 63) / 64, 64, 0, st>>>(b, chainOn ? 1 : 0);
-    ++L;
-    launchesPerSubstep = L;
+    ++Lc;
+    mark();
+    launchesPerSubstep = Lc;
+  }
+
+  template <bool DBG>
+  void launch_substep() {
+    switch (lanesOverride ? lanesOverride : lanes()) {
+      case 8: launch_substep_l<DBG, 8>(); break;
+      case 4: launch_substep_l<DBG, 4>(); break;
+      case 2: launch_substep_l<DBG, 2>(); break;
+      default: launch_substep_l<DBG, 1>(); break;
+    }
   }
 
   void launch_one() {
@@ -627,6 +692,40 @@ struct World {
     return cuda_ok(cudaGetLastError(), "step");
   }
 
+  // profileSubstep (src/engine.js:4221-4267): run `reps` substeps outside the
+  // graph with events between phases; out[k] = mean device ms of phase k.
+  // Phases: 0 predict, 1 sort, 2 cellstart+gather, 3 nbr, then per
+  // iteration (solveA, colours, friction), then post1, post2(+formation+hash), fold.
+  bool profile(uint32_t reps, float* out, uint32_t maxOut, uint32_t* nOut) {
+    if (layoutDirty && !relayout()) return false;
+    if (eventsDirty && !upload_events()) return false;
+    const int NE = 8 + 3 * (int)iters + 4;
+    std::vector<cudaEvent_t> evs(NE);
+    for (auto& e : evs) cudaEventCreate(&e);
+    std::vector<double> acc(NE, 0.0);
+    int used = 0;
+    for (uint32_t r = 0; r < reps; ++r) {
+      pev = evs.data();
+      npev = 0;
+      launch_one();
+      used = npev;
+      pev = nullptr;
+      if (!cuda_ok(cudaStreamSynchronize(st), "profile")) return false;
+      for (int k = 0; k + 1 < used; ++k) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, evs[k], evs[k + 1]);
+        acc[k] += ms;
+      }
+      for (auto& s2 : sh)
+        if (s2.used && s2.loaded) s2.substeps += 1;
+    }
+    for (auto& e : evs) cudaEventDestroy(e);
+    uint32_t n = (uint32_t)std::max(0, used - 1);
+    for (uint32_t k = 0; k < n && k < maxOut; ++k) out[k] = (float)(acc[k] / std::max(1u, reps));
+    if (nOut) *nOut = n;
+    return true;
+  }
+
   bool timing(float* ms) {
     if (!cuda_ok(cudaEventSynchronize(ev1), "timing")) return false;
     cudaEventElapsedTime(ms, ev0, ev1);
@@ -665,6 +764,10 @@ struct World {
     uint32_t newFluid = h.nFluid + k, newN = newFluid + nB;
     if (newN > h.cap) { if (nOut) *nOut = h.n; return true; }
     for (uint32_t i = 0; i < k; ++i) {
+      // Positions far outside any domain are refused: every pred difference the
+      // solver forms then stays inside i32 (see the range note in sim2d.cuh).
+      if (list[i].x < -(1 << 28) || list[i].x > (1 << 28) || list[i].y < -(1 << 28) || list[i].y > (1 << 28))
+        return fail("spawn position outside [-2^28, 2^28]");
       int32_t mm = std::min<int32_t>((int32_t)matCount - 1, std::max<int32_t>(0, list[i].mat));
       if (seal_row((uint32_t)mm)) return fail("spawn of seal-class row %d is not supported", mm);
       if (!noWeld && spawn_welds((uint32_t)mm)) return fail("weld-group spawns are not supported");
@@ -885,6 +988,15 @@ int sn_set_formation_clock(sn_engine* e, uint64_t clock, uint32_t dirty) {
   w.hpar[0].formClock = (uint32_t)clock;
   w.hpar[0].bondDirty = dirty ? 1u : 0u;
   return rc_of(w, w.push_scene(0) && w.cuda_ok(cudaStreamSynchronize(w.st), "clock"));
+}
+int sn_profile_substep(sn_engine* e, uint32_t reps, float* ms, uint32_t max_phases, uint32_t* n_phases) {
+  if (!e || !ms) return SN_E_INVALID;
+  if (!e->w.sh[0].loaded) { e->w.err = "profile before loadScene"; return SN_E_STATE; }
+  return rc_of(e->w, e->w.profile(reps, ms, max_phases, n_phases));
+}
+int sn_batch_profile_substep(sn_batch* b, uint32_t reps, float* ms, uint32_t max_phases, uint32_t* n_phases) {
+  if (!b || !ms) return SN_E_INVALID;
+  return rc_of(b->w, b->w.profile(reps, ms, max_phases, n_phases));
 }
 int sn_last_timing(sn_engine* e, float* ms, uint64_t* launches) {
   if (!e) return SN_E_INVALID;

@@ -62,6 +62,51 @@ __device__ __forceinline__ int32_t mul(int32_t a, int32_t b, const Flags<DBG>& f
   return lo;
 }
 
+// Release-build helpers for products whose range is known from the operand
+// bounds. The rounding is computed as round-half-up, t = a*b + 2^(S-1) (one
+// IMAD.WIDE with the bias as addend), q = t >> S, then an exact tie (the low S
+// bits of t all zero) clears q's low bit: RNE picks the even neighbour, which
+// is q & ~1 for both signs in two's complement.
+//   mulf : the RNE result provably fits in i32 (no saturation test needed);
+//   mulfc: fits in i32 and is then clamped into [lo, hi];
+//   mulc : may exceed i32, clamped into [lo, hi] inside i32 (clamping the exact
+//          value equals clamping the saturated one).
+// Debug builds use the saturating form so the debug counters see every event.
+template <int S>
+__device__ __forceinline__ int32_t rne_lo(int32_t a, int32_t b) {
+  int64_t t = (int64_t)a * (int64_t)b + (((int64_t)1) << (S - 1));
+  uint32_t lo = (uint32_t)t, hi = (uint32_t)((uint64_t)t >> 32);
+  uint32_t q = __funnelshift_r(lo, hi, S);
+  if ((lo & ((1u << S) - 1u)) == 0u) q &= ~1u;
+  return (int32_t)q;
+}
+template <int S>
+__device__ __forceinline__ int64_t rne64(int64_t p) {
+  int64_t t = p + (((int64_t)1) << (S - 1));
+  int64_t q = t >> S;
+  if (((uint32_t)t & ((1u << S) - 1u)) == 0u) q &= ~(int64_t)1;
+  return q;
+}
+template <int S, bool DBG>
+__device__ __forceinline__ int32_t mulf(int32_t a, int32_t b, const Flags<DBG>& f) {
+  if constexpr (DBG) return mul<S>(a, b, f);
+  else return rne_lo<S>(a, b);
+}
+template <int S, bool DBG>
+__device__ __forceinline__ int32_t mulfc(int32_t a, int32_t b, int32_t lo, int32_t hi, const Flags<DBG>& f) {
+  if constexpr (DBG) return min(max(mul<S>(a, b, f), lo), hi);
+  else return min(max(rne_lo<S>(a, b), lo), hi);
+}
+template <int S, bool DBG>
+__device__ __forceinline__ int32_t mulc(int32_t a, int32_t b, int32_t lo, int32_t hi, const Flags<DBG>& f) {
+  if constexpr (DBG) {
+    return min(max(mul<S>(a, b, f), lo), hi);
+  } else {
+    int64_t q = rne64<S>((int64_t)a * (int64_t)b);
+    return (int32_t)min(max(q, (int64_t)lo), (int64_t)hi);
+  }
+}
+
 template <bool DBG>
 __device__ __forceinline__ int32_t add_sat(int32_t a, int32_t b, const Flags<DBG>& f) {
   int32_t s = wadd(a, b);
@@ -95,8 +140,11 @@ __device__ __forceinline__ int32_t shr_rne(int32_t x) {
 
 // fp_divshift (src/fixed.wgsl:285-309): ~floor(num * 2^k / den) through the
 // clz-normalised 15-bit reciprocal Rn = floor(2^30 / dn), dn in [2^15, 2^16).
+// Rn comes from a 32768-entry table of exact quotients (built on the host by
+// integer division), so the solver's per-pair divides cost one cached load.
 template <int K, bool DBG>
-__device__ __forceinline__ int32_t divshift(int32_t num, int32_t den, const Flags<DBG>& f) {
+__device__ __forceinline__ int32_t divshift(int32_t num, int32_t den, const uint16_t* __restrict__ rcp,
+                                            const Flags<DBG>& f) {
   if (den == 0) {
     f.flag(2);
     return num == 0 ? 0 : (num > 0 ? I32_MAX : I32_MIN);
@@ -105,7 +153,7 @@ __device__ __forceinline__ int32_t divshift(int32_t num, int32_t den, const Flag
   if (d < 0) { f.flag(1); d = abs_sat(d, f); nn = neg_sat(nn, f); }
   int32_t e = 16 - __clz(d);
   int32_t dn = e >= 0 ? (d >> e) : (d << (-e));
-  int32_t Rn = (int32_t)(1073741824u / (uint32_t)dn);
+  int32_t Rn = (int32_t)__ldg(rcp + (dn - 32768));
   int32_t s = 30 + e - K;
   if (s > 31) { f.flag(1); return 0; }
   if (s < 1) {

@@ -17,13 +17,14 @@
 namespace sn {
 namespace radix {
 
-constexpr int RBITS = 8;
+constexpr int RBITS = 9;
 constexpr int RADIX = 1 << RBITS;
-constexpr int TPB = 256;                 // threads per tile
+constexpr int TPB = 512;                 // threads per tile
 constexpr int WARPS = TPB / 32;
 constexpr int ITEMS = 16;                // items per thread
-constexpr int TILE = TPB * ITEMS;        // 4096 items per tile
+constexpr int TILE = TPB * ITEMS;        // 8192 items per tile
 constexpr int WARP_ITEMS = 32 * ITEMS;   // 512 items per warp, in 16 rounds of 32
+static_assert(TPB == RADIX, "one thread per digit in the histogram and scatter prologues");
 
 __device__ __forceinline__ uint32_t digit_of(const uint32_t* keys, uint32_t idx, uint32_t n, int shift) {
   return idx < n ? ((keys[idx] >> shift) & (RADIX - 1)) : (uint32_t)RADIX;
@@ -54,39 +55,55 @@ __global__ void __launch_bounds__(TPB) k_hist(const uint32_t* __restrict__ keys,
   hist[(uint32_t)tid * numTiles + tile] = s;
 }
 
-// Exclusive scan of m words in place, one CTA of 1024 threads.
-__global__ void __launch_bounds__(1024) k_scan(uint32_t* __restrict__ a, uint32_t m) {
+// Exclusive scan of m words in place, one CTA of 1024 threads: tiles of 8192
+// words are staged through shared memory with coalesced loads and stores, each
+// thread scans 8 contiguous words, a warp-shuffle scan joins the threads, and
+// a carry links the tiles.
+constexpr int SCAN_T = 1024, SCAN_I = 8, SCAN_TILE = SCAN_T * SCAN_I;
+__global__ void __launch_bounds__(SCAN_T) k_scan(uint32_t* __restrict__ a, uint32_t m) {
+  __shared__ uint32_t buf[SCAN_TILE + SCAN_TILE / 32];
   __shared__ uint32_t ws[32];
-  int tid = threadIdx.x;
-  uint32_t per = (m + 1023) / 1024;
-  uint32_t lo = min(m, tid * per), hi = min(m, lo + per);
-  uint32_t s = 0;
-  for (uint32_t i = lo; i < hi; ++i) s += a[i];
-  // block exclusive scan of s
-  uint32_t v = s;
-  int lane = tid & 31, warp = tid >> 5;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  auto at = [](int i) { return i + (i >> 5); };  // pad one word per 32 against bank conflicts
+  uint32_t carry = 0;
+  for (uint32_t base = 0; base < m; base += SCAN_TILE) {
+    for (int k = 0; k < SCAN_I; ++k) {
+      uint32_t i = base + k * SCAN_T + tid;
+      buf[at(k * SCAN_T + tid)] = i < m ? a[i] : 0u;
+    }
+    __syncthreads();
+    uint32_t v[SCAN_I], s = 0;
 #pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    uint32_t t = __shfl_up_sync(0xffffffffu, v, o);
-    if (lane >= o) v += t;
-  }
-  if (lane == 31) ws[warp] = v;
-  __syncthreads();
-  if (warp == 0) {
-    uint32_t w = ws[lane];
+    for (int k = 0; k < SCAN_I; ++k) { v[k] = buf[at(tid * SCAN_I + k)]; s += v[k]; }
+    uint32_t x = s;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      uint32_t t = __shfl_up_sync(0xffffffffu, w, o);
-      if (lane >= o) w += t;
+      uint32_t t = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += t;
     }
-    ws[lane] = w;
-  }
-  __syncthreads();
-  uint32_t excl = v - s + (warp > 0 ? ws[warp - 1] : 0u);
-  for (uint32_t i = lo; i < hi; ++i) {
-    uint32_t x = a[i];
-    a[i] = excl;
-    excl += x;
+    if (lane == 31) ws[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      uint32_t w = ws[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        uint32_t t = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += t;
+      }
+      ws[lane] = w;
+    }
+    __syncthreads();
+    uint32_t run = carry + x - s + (warp > 0 ? ws[warp - 1] : 0u);
+#pragma unroll
+    for (int k = 0; k < SCAN_I; ++k) { buf[at(tid * SCAN_I + k)] = run; run += v[k]; }
+    const uint32_t total = ws[31];
+    __syncthreads();
+    for (int k = 0; k < SCAN_I; ++k) {
+      uint32_t i = base + k * SCAN_T + tid;
+      if (i < m) a[i] = buf[at(k * SCAN_T + tid)];
+    }
+    carry += total;
+    __syncthreads();
   }
 }
 
@@ -139,18 +156,16 @@ inline void sort_pairs(uint32_t* keys0, uint32_t n, int keyBits, uint32_t* outKe
   const uint32_t* kin = keys0;
   const uint32_t* vin = nullptr;
   for (int p = 0; p < passes; ++p) {
-    bool last = (p == passes - 1);
     // ping-pong so that the final pass writes (outKeys, outVals)
     bool toOut = ((passes - 1 - p) % 2) == 0;
     uint32_t* ko = toOut ? outKeys : tmpK;
     uint32_t* vo = toOut ? outVals : tmpV;
     int shift = p * RBITS;
     k_hist<<<numTiles, TPB, 0, st>>>(kin, n, shift, hist, numTiles);
-    k_scan<<<1, 1024, 0, st>>>(hist, RADIX * numTiles);
+    k_scan<<<1, SCAN_T, 0, st>>>(hist, RADIX * numTiles);
     k_scatter<<<numTiles, TPB, 0, st>>>(kin, vin, n, shift, hist, numTiles, ko, vo);
     kin = ko;
     vin = vo;
-    (void)last;
   }
 }
 

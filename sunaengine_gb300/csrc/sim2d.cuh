@@ -8,20 +8,32 @@
 //   k_cellstart     cell ranges in sorted space
 //   k_gather        slot -> sorted-space working set
 //   k_nbr           neighbour lists, reference traversal order and MAXNBR cut
-//   ITERS x { k_solveA; k_colour x 4; [k_friction] }
+//   ITERS x { k_solveA; k_colour x 4; [k_friction; k_apply_fric] }
 //                   density/lambda, then colour-classed Gauss-Seidel position
-//                   correction. solveB and applyDp are fused per colour: a CTA
-//                   owns whole cells, and the only same-colour neighbours are
-//                   in the same cell, so a CTA barrier separates "compute every
-//                   dp" from "apply" (the race src/sim.wgsl:1323-1332 guards).
+//                   correction; solveB and applyDp are fused per colour over a
+//                   double-buffered pred (see k_colour).
 //   k_post1         finalize + xsph + normals + conduct in one neighbour sweep
 //   k_post2         surfaceTension + thermal + formation flag clear + state hash
 //   [k_form1, k_form2, k_hash]   bond formation for worlds with bonding rows
 //   k_fold          per-scene chain fold, formation clock
 //
+// Sorted-space records are packed so one neighbour costs one or two wide loads:
+//   PL[p] = {pred.x, pred.y, lam, info}   info = matId | state bits (INFO_*)
+//   RX[p] = {rho, rinv, temp, 0}
+//   NQ[p] = {nrm.x, nrm.y, rho, 0}        (written by k_post1 for k_post2)
+// The kernel tables are interleaved per LUT index: WG = {W, G}, CA = {C, A}.
+//
 // Everything is int32 on the integer pipes; no floats, no atomics in the
 // physics (the only atomics are the u32 adds of the digest and the debug
 // counters, both commutative).
+//
+// Range facts used by the release build (debug builds keep every saturation
+// test so the debug counters stay exact): fluid preds are wall-clamped into
+// [0, 2^27] and wall particles lie in [-2^27, 2^27], so pred differences never
+// overflow; an accepted neighbour has |d| <= 163848 < 2^18; |G| < 2^27, so a
+// gradient term is < 2^19; |lambda| <= 2^22; |vel| <= 2^16; K_ij <= 2^18;
+// |T| <= 2^29. Under these bounds every per-pair product below either fits in
+// i32 after its shift (mulf) or is clamped at once into an i32 range (mulc).
 #pragma once
 #include <cstdint>
 #include "fixed.cuh"
@@ -36,7 +48,6 @@ constexpr int32_t RHO0 = 1048576;
 constexpr int32_t TWO_RHO0 = 2097152;
 constexpr int32_t HS = 10240;
 constexpr int32_t H2S = 104857600;
-constexpr int OFF_W = 0, OFF_G = 3202, OFF_C = 6404, OFF_A = 9606, OFF_S = 12808;
 constexpr int32_t LAM_MAX = 4194304;
 constexpr int32_t S_TERM = 16777216;
 constexpr int32_t DP_TERM = 2097152;
@@ -67,8 +78,14 @@ constexpr int32_t L0_MAX = 5120, L0_MIN = 512;
 constexpr uint32_t BOND_J_MASK = 0x0001ffffu, BOND_L0_MASK = 0x3ffe0000u, BOND_TOMB = 0x40000000u;
 constexpr int32_t BD_TERM = 16777216;
 constexpr uint32_t MAT_PHOTO_ROW = 15;
-constexpr uint32_t INFO_BOUNDARY = 0x80000000u;
+// info word bits (sorted space)
 constexpr uint32_t INFO_MAT = 0xffu;
+constexpr uint32_t INFO_BOUNDARY = 0x80000000u;  // a wall particle (slot >= nFluid)
+constexpr uint32_t INFO_DEAD = 0x40000000u;      // FLAG_DEAD
+constexpr uint32_t INFO_CONGEAL = 0x20000000u;   // FLAG_CONGEAL
+constexpr uint32_t INFO_PINNED = 0x10000000u;    // FLAG_ANCHOR | FLAG_RIGID: never moved by dp
+constexpr uint32_t INFO_BURST = 0x08000000u;     // FLAG_BURST
+constexpr uint32_t INFO_RIGID = 0x04000000u;     // FLAG_RIGID
 
 // material words (src/engine.js:678-705)
 enum : int {
@@ -90,32 +107,31 @@ struct Bufs {
   uint32_t* sceneOf;    // [cap]
   uint32_t* keys;       // [cap]
   uint32_t* inv;        // [cap] slot -> sorted position
-  uint32_t* bond;       // [cap * 48] or null
-  uint32_t* bondCand;   // [cap * 48] or null
+  uint32_t* bond;       // [cap * 48]
+  uint32_t* bondCand;   // [cap * 48]
   // sort
   uint32_t* skey;       // [cap]
   uint32_t* sslot;      // [cap]
   uint32_t* cellStart;  // [K + 1]
   // sorted space
-  int2* P;
+  int4* PL;             // {pred.x, pred.y, lam, info}  (buffer A)
+  int4* PL2;            // buffer B of the colour sweep (same layout)
+  int4* RX;             // {rho, rinv, temp, 0}
+  int4* NQ;             // {nrm.x, nrm.y, rho, 0}
   int2* POS;
-  uint32_t* INFO;       // matId | INFO_BOUNDARY
-  uint32_t* FLG;
-  int32_t* TEMP;
   uint32_t* SCN;
-  int32_t* RHO;
-  int32_t* LAM;
-  int32_t* RINV;
   int2* DP;
-  int2* NRM;
   int32_t* HEAT;
   int32_t* CORR;
   uint32_t* NBR;        // [MAXNBR][nbrStride]
   uint32_t* NBRN;
   uint32_t nbrStride;
   // tables and per-scene data
-  const int32_t* luts;
+  const int32_t* luts;  // 5*TN, reference layout
+  const int2* WG;       // [TN] {W, G}
+  const int2* CA;       // [TN] {C, A}
   const int32_t* mats;
+  const uint16_t* rcp;  // [32768] floor(2^30 / dn), dn in [2^15, 2^16)
   ScenePar* scenes;
   WorldPar* world;
   uint32_t* acc;        // [S * 8]
@@ -128,33 +144,47 @@ struct Bufs {
 enum : uint32_t { ERR_UNSUPPORTED_ROW = 1u, ERR_BOND_PARTNER = 2u };
 
 __device__ __forceinline__ int32_t matw(const Bufs& b, uint32_t m, int w) { return __ldg(b.mats + m * MAT_WORDS + w); }
-__device__ __forceinline__ int32_t lut(const Bufs& b, int off, int i) { return __ldg(b.luts + off + i); }
 
+__device__ __forceinline__ uint32_t gstride() { return gridDim.x * blockDim.x; }
+__device__ __forceinline__ uint32_t gtid() { return blockIdx.x * blockDim.x + threadIdx.x; }
+
+// pred_i - pred_j. Both lie in [-2^27, 2^27], so the reference's fp_sub_sat
+// cannot saturate; debug builds keep the test to count it anyway.
 template <bool DBG>
-__device__ __forceinline__ int lut_index(int2 d, const Flags<DBG>& f) {
-  int32_t ax = wadd(abs_sat(d.x, f), 8) >> 4;
-  int32_t ay = wadd(abs_sat(d.y, f), 8) >> 4;
-  if (ax > HS || ay > HS) return -1;
-  int32_t r2 = wadd(wmul(ax, ax), wmul(ay, ay));
-  if (r2 >= H2S) return -1;
-  return r2 >> 15;
+__device__ __forceinline__ int2 pdelta(int2 a, int2 b, const Flags<DBG>& f) {
+  if constexpr (DBG) return make_int2(sub_sat(a.x, b.x, f), sub_sat(a.y, b.y, f));
+  else return make_int2(a.x - b.x, a.y - b.y);
 }
 template <bool DBG>
 __device__ __forceinline__ int2 delta(int2 a, int2 b, const Flags<DBG>& f) {
   return make_int2(sub_sat(a.x, b.x, f), sub_sat(a.y, b.y, f));
 }
+
+// lut_index (src/sim.wgsl:520-527): symmetric rounding of |d| >> PRE, per-axis
+// reject, r^2 < H2S, index r^2 >> KSH; -1 outside the kernel.
 template <bool DBG>
-__device__ __forceinline__ int32_t grad_q16(int32_t gt, int32_t d, const Flags<DBG>& f) {
-  return mul<26>(gt, d, f);
+__device__ __forceinline__ int lut_index(int2 d, const Flags<DBG>& f) {
+  int32_t ax, ay;
+  if constexpr (DBG) {
+    ax = wadd(abs_sat(d.x, f), 8) >> 4;
+    ay = wadd(abs_sat(d.y, f), 8) >> 4;
+  } else {
+    ax = (abs(d.x) + 8) >> 4;
+    ay = (abs(d.y) + 8) >> 4;
+  }
+  if (max(ax, ay) > HS) return -1;
+  int32_t r2 = wadd(wmul(ax, ax), wmul(ay, ay));
+  if (r2 >= H2S) return -1;
+  return r2 >> 15;
 }
 __device__ __forceinline__ int2 wall_clamp(const ScenePar& S, int2 p) {
   return make_int2(clampi(p.x, WALL, S.domW - WALL), clampi(p.y, WALL, S.domH - WALL));
 }
 __device__ __forceinline__ int32_t mat_mix(int32_t a, int32_t b) { return wadd(a, b) >> 1; }
 template <bool DBG>
-__device__ __forceinline__ int32_t sym_k(int32_t ri, int32_t rj, const Flags<DBG>& f) {
+__device__ __forceinline__ int32_t sym_k(int32_t ri, int32_t rj, const uint16_t* rcp, const Flags<DBG>& f) {
   int32_t den = max(RHO_FLOOR_K, add_sat(ri, rj, f));
-  return clampi(divshift<16>(TWO_RHO0, den, f), 0, RINV_MAX);
+  return clampi(divshift<16>(TWO_RHO0, den, rcp, f), 0, RINV_MAX);
 }
 __device__ __forceinline__ uint32_t key_of(const ScenePar& S, int32_t cx, int32_t cy) {
   uint32_t c = (uint32_t)(cx & 1) | ((uint32_t)(cy & 1) << 1);
@@ -195,6 +225,15 @@ __device__ __forceinline__ int32_t bond_k(const Bufs& b, uint32_t m, int32_t T, 
   int32_t u = clampi(mul<16>(dT, matw(b, m, M_rampInv), f), 0, 65536);
   if (sgn < 0) u = 65536 - u;
   return mul<16>(k, u, f);
+}
+__device__ __forceinline__ uint32_t info_of(uint32_t matId, uint32_t flags, bool boundary) {
+  return (matId & INFO_MAT) | (boundary ? INFO_BOUNDARY : 0u) | ((flags & FLAG_DEAD) ? INFO_DEAD : 0u) |
+         ((flags & FLAG_CONGEAL) ? INFO_CONGEAL : 0u) | ((flags & (FLAG_ANCHOR | FLAG_RIGID)) ? INFO_PINNED : 0u) |
+         ((flags & FLAG_BURST) ? INFO_BURST : 0u) | ((flags & FLAG_RIGID) ? INFO_RIGID : 0u);
+}
+__device__ __forceinline__ int2 xy(int4 v) { return make_int2(v.x, v.y); }
+__device__ __forceinline__ int2 ld_pred(const int4* PL, uint32_t q) {
+  return *reinterpret_cast<const int2*>(PL + q);
 }
 
 // ---- murmur state hash: src/hash/statehash.js:36-169 ----------------------------
@@ -262,13 +301,17 @@ __device__ __forceinline__ void digest_add(uint32_t* acc, bool valid, uint32_t s
   uint32_t peers = __match_any_sync(0xffffffffu, key);
   int lane = threadIdx.x & 31;
   bool leader = lane == __ffs(peers) - 1;
-  // sum over the peer group with a shuffle tree restricted to the group
+  if (peers == 0xffffffffu) {
+#pragma unroll
+    for (int l = 0; l < 8; ++l) {
+      uint32_t t = __reduce_add_sync(0xffffffffu, h[l]);
+      if (leader && valid) atomicAdd(acc + scene * 8 + l, t);
+    }
+    return;
+  }
 #pragma unroll
   for (int l = 0; l < 8; ++l) {
-    uint32_t v = h[l];
-    uint32_t total = 0;
-    // groups are usually the whole warp; a generic masked reduction:
-    uint32_t m = peers;
+    uint32_t v = h[l], total = 0, m = peers;
     while (m) {
       int src = __ffs(m) - 1;
       m &= m - 1;
@@ -278,10 +321,16 @@ __device__ __forceinline__ void digest_add(uint32_t* acc, bool valid, uint32_t s
   }
 }
 
-// ---- kernels --------------------------------------------------------------------
+// Sum over the L lanes that share one particle (L a power of two, groups are
+// aligned within the warp). Wrapping u32 addition, so the split is exact.
+template <int L>
+__device__ __forceinline__ int32_t gsum(int32_t v) {
+#pragma unroll
+  for (int o = L / 2; o > 0; o >>= 1) v = wadd(v, __shfl_xor_sync(0xffffffffu, v, o, L));
+  return v;
+}
 
-__device__ __forceinline__ uint32_t gstride() { return gridDim.x * blockDim.x; }
-__device__ __forceinline__ uint32_t gtid() { return blockIdx.x * blockDim.x + threadIdx.x; }
+// ---- kernels --------------------------------------------------------------------
 
 // predict (src/sim.wgsl:958-1000) + the grid key of every slot.
 template <bool DBG>
@@ -294,24 +343,25 @@ __global__ void __launch_bounds__(256) k_predict_key(Bufs b) {
     uint32_t i = slot - S.slotBase;
     if (!S.active || i >= S.n) { b.keys[slot] = K; continue; }
     if (i == 0) b.scenes[s].formNow = ((S.formClock & 3u) == 0u || S.bondDirty) ? 1u : 0u;
-    const int32_t* w = b.state + (size_t)slot * 8;
-    int2 pos = make_int2(w[0], w[1]);
+    const int4* w4 = reinterpret_cast<const int4*>(b.state + (size_t)slot * 8);
+    int4 a = w4[0], c = w4[1];
+    int2 pos = make_int2(a.x, a.y);
     int2 pred = pos;
     if (i < S.nFluid) {
-      uint32_t m = (uint32_t)w[4], fl = (uint32_t)w[5];
+      uint32_t m = (uint32_t)c.x, fl = (uint32_t)c.y;
       if (matw(b, m, M_phantom) == 0 && !(fl & (FLAG_ANCHOR | FLAG_RIGID))) {
         int2 st = b.stacc[slot];
         int32_t vmax = S.vmax, vmaxN = neg_sat(vmax, f);
-        int32_t vx = add_sat(w[2], st.x, f);
-        int32_t vy = add_sat(add_sat(w[3], st.y, f), matw(b, m, M_grav), f);
+        int32_t vx = add_sat(a.z, st.x, f);
+        int32_t vy = add_sat(add_sat(a.w, st.y, f), matw(b, m, M_grav), f);
         vx = clampi(vx, vmaxN, vmax);
         vy = clampi(vy, vmaxN, vmax);
         pred = wall_clamp(S, make_int2(add_sat(pos.x, vx, f), add_sat(pos.y, vy, f)));
       }
     }
     b.predSlot[slot] = pred;
-    int2 c = cell_coord(S, pred);
-    b.keys[slot] = key_of(S, c.x, c.y);
+    int2 cc = cell_coord(S, pred);
+    b.keys[slot] = key_of(S, cc.x, cc.y);
   }
 }
 
@@ -336,13 +386,14 @@ __global__ void __launch_bounds__(256) k_gather(Bufs b) {
     uint32_t s = b.sceneOf[slot];
     const ScenePar& S = b.scenes[s];
     uint32_t i = slot - S.slotBase;
-    const int32_t* w = b.state + (size_t)slot * 8;
+    const int4* w4 = reinterpret_cast<const int4*>(b.state + (size_t)slot * 8);
+    int4 a = w4[0], c = w4[1];
     int2 pr = b.predSlot[slot];
-    b.P[p] = pr;
-    b.POS[p] = make_int2(w[0], w[1]);
-    b.INFO[p] = (uint32_t)w[4] | (i >= S.nFluid ? INFO_BOUNDARY : 0u);
-    b.FLG[p] = (uint32_t)w[5];
-    b.TEMP[p] = w[6];
+    int4 rec = make_int4(pr.x, pr.y, 0, (int32_t)info_of((uint32_t)c.x, (uint32_t)c.y, i >= S.nFluid));
+    b.PL[p] = rec;
+    b.PL2[p] = rec;
+    b.RX[p] = make_int4(0, 0, c.z, 0);
+    b.POS[p] = make_int2(a.x, a.y);
     b.SCN[p] = s;
     b.inv[slot] = p;
   }
@@ -358,14 +409,16 @@ __global__ void __launch_bounds__(256) k_nbr(Bufs b) {
   Flags<DBG> f{b.dbg};
   const uint32_t nAct = b.world->nAct, stride = b.nbrStride;
   for (uint32_t p = gtid(); p < nAct; p += gstride()) {
-    uint32_t info = b.INFO[p];
+    int4 me = b.PL[p];
+    uint32_t info = (uint32_t)me.w;
     bool bnd = (info & INFO_BOUNDARY) != 0;
-    if ((bnd && !DBG) || (b.FLG[p] & FLAG_DEAD)) { b.NBRN[p] = 0; continue; }
+    if ((bnd && !DBG) || (info & INFO_DEAD)) { b.NBRN[p] = 0; continue; }
     const ScenePar& S = b.scenes[b.SCN[p]];
-    int2 pi = b.P[p];
+    int2 pi = xy(me);
     int2 cc = cell_coord(S, pi);
     uint32_t cnt = 0;
     bool congeal = false;
+    uint32_t* out = b.NBR + p;
     for (int dy = -1; dy <= 1; ++dy) {
       int32_t gy = cc.y + dy;
       if (gy < 0 || gy >= (int32_t)S.gridH) continue;
@@ -376,13 +429,13 @@ __global__ void __launch_bounds__(256) k_nbr(Bufs b) {
         uint32_t lo = b.cellStart[key], hi = b.cellStart[key + 1];
         for (uint32_t q = lo; q < hi; ++q) {
           if (q == p) continue;
-          uint32_t fq = b.FLG[q];
-          if (fq & FLAG_DEAD) continue;
-          if (lut_index(delta(pi, b.P[q], f), f) < 0) continue;
-          uint32_t iq = b.INFO[q];
-          if (!(iq & INFO_BOUNDARY) && (fq & FLAG_CONGEAL)) congeal = true;
+          int4 o = b.PL[q];
+          uint32_t iq = (uint32_t)o.w;
+          if (iq & INFO_DEAD) continue;
+          if (lut_index(pdelta(pi, xy(o), f), f) < 0) continue;
+          if (!(iq & INFO_BOUNDARY) && (iq & INFO_CONGEAL)) congeal = true;
           if (cnt >= (uint32_t)MAXNBR) { f.flag(6); continue; }
-          if (!bnd) b.NBR[(size_t)cnt * stride + p] = q | (iq & INFO_BOUNDARY);
+          if (!bnd) out[(size_t)cnt * stride] = q | (iq & INFO_BOUNDARY);
           cnt++;
         }
       }
@@ -394,57 +447,94 @@ __global__ void __launch_bounds__(256) k_nbr(Bufs b) {
 // solveA (src/sim.wgsl:1270-1318): density, |grad C|^2, lambda. On the last
 // iteration it also stores rinv (finalize's, src/sim.wgsl:2261-2262), which
 // depends only on this rho.
-template <bool DBG>
-__global__ void __launch_bounds__(256) k_solveA(Bufs b, const int2* __restrict__ P, int lastIter) {
+template <bool DBG, int L>
+__global__ void __launch_bounds__(256) k_solveA(Bufs b, int lastIter) {
   Flags<DBG> f{b.dbg};
   const uint32_t nAct = b.world->nAct, stride = b.nbrStride;
-  const int32_t W0 = lut(b, OFF_W, 0);
-  for (uint32_t p = gtid(); p < nAct; p += gstride()) {
-    uint32_t info = b.INFO[p];
-    if (info & INFO_BOUNDARY) continue;
-    int2 pi = P[p];
-    uint32_t cnt = b.NBRN[p] & NBRN_COUNT;
-    int32_t rho = W0, S = 0, sgx = 0, sgy = 0;
-    for (uint32_t k = 0; k < cnt; ++k) {
-      uint32_t q = b.NBR[(size_t)k * stride + p] & ~NBR_BOUNDARY;
-      int2 d = delta(pi, P[q], f);
+  const int32_t W0 = __ldg(b.luts);
+  const uint32_t sub = threadIdx.x & (L - 1), G = gstride() / L;
+  for (uint32_t p = gtid() / L;; p += G) {
+    if (__shfl_sync(0xffffffffu, p, 0) >= nAct) break;  // warp-uniform exit
+    const bool valid = p < nAct;
+    int4 me = valid ? b.PL[p] : make_int4(0, 0, 0, (int32_t)INFO_BOUNDARY);
+    uint32_t info = (uint32_t)me.w;
+    const bool act = !(info & INFO_BOUNDARY);
+    int2 pi = xy(me);
+    uint32_t cnt = act ? (b.NBRN[p] & NBRN_COUNT) : 0u;
+    int32_t rho = 0, S = 0, sgx = 0, sgy = 0;
+    const uint32_t* np = b.NBR + (act ? p : 0u);
+    // one neighbour ahead: its index and position are in flight while the
+    // current pair is computed
+    uint32_t qn = sub < cnt ? (np[(size_t)sub * stride] & ~NBR_BOUNDARY) : 0u;
+    int2 pn = ld_pred(b.PL, qn);
+    for (uint32_t k = sub; k < cnt; k += L) {
+      int2 pj = pn;
+      if (k + L < cnt) {
+        qn = np[(size_t)(k + L) * stride] & ~NBR_BOUNDARY;
+        pn = ld_pred(b.PL, qn);
+      }
+      int2 d = pdelta(pi, pj, f);
       int id = lut_index(d, f);
       if (id < 0) continue;
-      rho = wadd(rho, lut(b, OFF_W, id));
-      int32_t gt = lut(b, OFF_G, id);
-      int32_t gx = grad_q16(gt, d.x, f), gy = grad_q16(gt, d.y, f);
+      int2 wg = __ldg(b.WG + id);
+      rho = wadd(rho, wg.x);
+      int32_t gx = mulf<26>(wg.y, d.x, f), gy = mulf<26>(wg.y, d.y, f);
       sgx = wadd(sgx, gx);
       sgy = wadd(sgy, gy);
-      S = wadd(S, wadd(clampi(mul<11>(gx, gx, f), 0, S_TERM), clampi(mul<11>(gy, gy, f), 0, S_TERM)));
+      S = wadd(S, wadd(mulfc<11>(gx, gx, 0, S_TERM, f), mulfc<11>(gy, gy, 0, S_TERM, f)));
     }
+    if (L > 1) {
+      rho = gsum<L>(rho);
+      S = gsum<L>(S);
+      sgx = gsum<L>(sgx);
+      sgy = gsum<L>(sgy);
+    }
+    if (!act || sub != 0) continue;
+    rho = wadd(rho, W0);
     S = wadd(S, wadd(clampi(mul<11>(sgx, sgx, f), 0, S_TERM), clampi(mul<11>(sgy, sgy, f), 0, S_TERM)));
     int32_t Cq = clampi(shr_rne<4>(wsub(rho, RHO0)), 0, C_MAX);
     int32_t eps = matw(b, info & INFO_MAT, M_eps);
-    b.RHO[p] = rho;
-    b.LAM[p] = clampi(neg_sat(divshift<25>(Cq, wadd(S, eps), f), f), -LAM_MAX, LAM_MAX);
-    if (lastIter) b.RINV[p] = clampi(divshift<16>(RHO0, max(rho, RHO_FLOOR_RINV), f), 0, RINV_MAX);
+    int32_t lam = clampi(neg_sat(divshift<25>(Cq, wadd(S, eps), b.rcp, f), f), -LAM_MAX, LAM_MAX);
+    b.PL[p].z = lam;
+    b.PL2[p].z = lam;
+    int4& rx = b.RX[p];
+    rx.x = rho;
+    if (lastIter) rx.y = clampi(divshift<16>(RHO0, max(rho, RHO_FLOOR_RINV), b.rcp, f), 0, RINV_MAX);
   }
 }
 
-// solveB_at (src/sim.wgsl:1337-1372) for one particle.
-template <bool DBG>
-__device__ __forceinline__ int2 solveB_dp(const Bufs& b, const int2* __restrict__ P, uint32_t p, const Flags<DBG>& f) {
+// solveB_at (src/sim.wgsl:1337-1372) for one particle. The S table is all
+// zeros in the frozen tables (scorrK = 0, checked at load), so the release
+// build drops its term; debug builds still read it.
+template <bool DBG, int L>
+__device__ __forceinline__ int2 solveB_dp(const Bufs& b, const int4* __restrict__ src, uint32_t p, uint32_t cnt,
+                                          uint32_t sub, int2 pi, int32_t li, const Flags<DBG>& f) {
   const uint32_t stride = b.nbrStride;
-  int2 pi = P[p];
-  int32_t li = b.LAM[p];
-  uint32_t cnt = b.NBRN[p] & NBRN_COUNT;
   int32_t dpx = 0, dpy = 0;
-  for (uint32_t k = 0; k < cnt; ++k) {
-    uint32_t e = b.NBR[(size_t)k * stride + p];
-    uint32_t q = e & ~NBR_BOUNDARY;
-    int2 d = delta(pi, P[q], f);
+  const uint32_t* np = b.NBR + p;
+  uint32_t en = sub < cnt ? np[(size_t)sub * stride] : 0u;
+  int4 on = src[en & ~NBR_BOUNDARY];
+  for (uint32_t k = sub; k < cnt; k += L) {
+    uint32_t e = en;
+    int4 o = on;
+    if (k + L < cnt) {
+      en = np[(size_t)(k + L) * stride];
+      on = src[en & ~NBR_BOUNDARY];
+    }
+    int2 d = pdelta(pi, xy(o), f);
     int id = lut_index(d, f);
     if (id < 0) continue;
-    int32_t lj = (e & NBR_BOUNDARY) ? li : b.LAM[q];
-    int32_t co = add_sat(add_sat(li, lj, f), lut(b, OFF_S, id), f);
-    int32_t gt = lut(b, OFF_G, id);
-    dpx = wadd(dpx, clampi(mul<12>(co, grad_q16(gt, d.x, f), f), -DP_TERM, DP_TERM));
-    dpy = wadd(dpy, clampi(mul<12>(co, grad_q16(gt, d.y, f), f), -DP_TERM, DP_TERM));
+    int32_t lj = (e & NBR_BOUNDARY) ? li : o.z;
+    int32_t co;
+    if constexpr (DBG) co = add_sat(add_sat(li, lj, f), __ldg(b.luts + 4 * TN + id), f);
+    else co = li + lj;
+    int32_t gt = __ldg(b.WG + id).y;
+    dpx = wadd(dpx, mulfc<12>(co, mulf<26>(gt, d.x, f), -DP_TERM, DP_TERM, f));
+    dpy = wadd(dpy, mulfc<12>(co, mulf<26>(gt, d.y, f), -DP_TERM, DP_TERM, f));
+  }
+  if (L > 1) {
+    dpx = gsum<L>(dpx);
+    dpy = gsum<L>(dpy);
   }
   return make_int2(dpx, dpy);
 }
@@ -459,48 +549,45 @@ __device__ __forceinline__ int2 apply_dp(const Bufs& b, const ScenePar& S, uint3
   return wall_clamp(S, make_int2(add_sat(pr.x, dx, f), add_sat(pr.y, dy, f)));
 }
 
-// First cell start >= x among the cells of one colour class (keys [k0, k1]).
-__device__ __forceinline__ uint32_t align_cell(const uint32_t* cs, uint32_t k0, uint32_t k1, uint32_t x) {
-  uint32_t lo = k0, hi = k1;
-  while (lo < hi) {
-    uint32_t mid = (lo + hi) >> 1;
-    if (cs[mid] < x) lo = mid + 1; else hi = mid;
-  }
-  return cs[lo];
-}
-
 // One colour of the block Gauss-Seidel sweep: solveB_cK + applyDp_cK fused.
-// CTA chunks are cell-aligned, so every same-colour neighbour of a particle is
-// handled by the same CTA; the barrier between the two loops is exactly the
-// dispatch boundary the reference puts between solveB_cK and applyDp_cK.
-template <bool DBG>
-__global__ void __launch_bounds__(256) k_colour(Bufs b, int2* __restrict__ P, int colour) {
+// The pass reads every pred from `src` and writes its colour's corrected preds
+// to `dst`, so a particle never reads a value written in the same pass: that
+// is the Jacobi-within-a-colour rule the reference gets from its separate
+// solveB/applyDp dispatches (src/sim.wgsl:1323-1332). `dst` must leave the
+// pass complete, so the pass also copies the two colours that are stale in it:
+// the sweep alternates A->B, B->A, A->B, B->A, colour c is written in phase c
+// and read again four phases later, so phase c copies colours c+1 and c-1.
+// After phase 3 buffer A is complete again.
+template <bool DBG, int L>
+__global__ void __launch_bounds__(256) k_colour(Bufs b, int colour, const int4* __restrict__ src,
+                                                int4* __restrict__ dst) {
   Flags<DBG> f{b.dbg};
-  __shared__ uint32_t rng[2];
-  const uint32_t k0 = b.world->colourBase[colour], k1 = b.world->colourBase[colour + 1];
-  const uint32_t cLo = b.cellStart[k0], cHi = b.cellStart[k1];
-  const uint32_t CH = blockDim.x;
-  const uint32_t nch = (cHi - cLo + CH - 1) / CH;
-  for (uint32_t ch = blockIdx.x; ch < nch; ch += gridDim.x) {
-    if (threadIdx.x == 0) {
-      rng[0] = align_cell(b.cellStart, k0, k1, cLo + ch * CH);
-      rng[1] = align_cell(b.cellStart, k0, k1, min(cHi, cLo + (ch + 1) * CH));
+  const uint32_t* cb = b.world->colourBase;
+  const uint32_t lo = b.cellStart[cb[colour]], hi = b.cellStart[cb[colour + 1]];
+  const int c1 = (colour + 1) & 3, c3 = (colour + 3) & 3;
+  const uint32_t lo1 = b.cellStart[cb[c1]], hi1 = b.cellStart[cb[c1 + 1]];
+  const uint32_t lo3 = b.cellStart[cb[c3]], hi3 = b.cellStart[cb[c3 + 1]];
+  const uint32_t nAct = b.world->nAct;
+  const uint32_t sub = threadIdx.x & (L - 1), G = gstride() / L;
+  for (uint32_t p = gtid() / L;; p += G) {
+    if (__shfl_sync(0xffffffffu, p, 0) >= nAct) break;  // warp-uniform exit
+    const bool mine = p < hi && p >= lo;
+    int4 me = mine ? src[p] : make_int4(0, 0, 0, (int32_t)INFO_BOUNDARY);
+    const uint32_t info = (uint32_t)me.w;
+    const bool act = mine && !(info & INFO_BOUNDARY);  // walls are identical in both buffers
+    const uint32_t cnt = act ? (b.NBRN[p] & NBRN_COUNT) : 0u;
+    int2 dp = solveB_dp<DBG, L>(b, src, act ? p : 0u, cnt, sub, xy(me), me.z, f);
+    if (sub != 0) continue;
+    if (act) {
+      int2 pr = xy(me);
+      if (!(info & INFO_PINNED)) {
+        const ScenePar& S = b.scenes[b.SCN[p]];
+        pr = apply_dp(b, S, info & INFO_MAT, pr, dp, f);
+      }
+      *reinterpret_cast<int2*>(dst + p) = pr;
+    } else if ((p >= lo1 && p < hi1) || (p >= lo3 && p < hi3)) {
+      *reinterpret_cast<int2*>(dst + p) = *reinterpret_cast<const int2*>(src + p);
     }
-    __syncthreads();
-    const uint32_t lo = rng[0], hi = rng[1];
-    for (uint32_t p = lo + threadIdx.x; p < hi; p += CH) {
-      if (b.INFO[p] & INFO_BOUNDARY) continue;
-      b.DP[p] = solveB_dp(b, P, p, f);
-    }
-    __syncthreads();
-    for (uint32_t p = lo + threadIdx.x; p < hi; p += CH) {
-      uint32_t info = b.INFO[p];
-      if (info & INFO_BOUNDARY) continue;
-      if (b.FLG[p] & (FLAG_RIGID | FLAG_ANCHOR)) continue;
-      const ScenePar& S = b.scenes[b.SCN[p]];
-      P[p] = apply_dp(b, S, info & INFO_MAT, P[p], b.DP[p], f);
-    }
-    __syncthreads();
   }
 }
 
@@ -513,19 +600,19 @@ __device__ __forceinline__ bool friction_row(const Bufs& b, uint32_t m) {
   return matw(b, m, M_fric) != 0 || matw(b, m, M_bondK) != 0;
 }
 template <bool DBG>
-__global__ void __launch_bounds__(256) k_friction(Bufs b, const int2* __restrict__ P) {
+__global__ void __launch_bounds__(256) k_friction(Bufs b) {
   Flags<DBG> f{b.dbg};
   const uint32_t nAct = b.world->nAct, stride = b.nbrStride;
   for (uint32_t p = gtid(); p < nAct; p += gstride()) {
-    uint32_t info = b.INFO[p];
+    int4 me = b.PL[p];
+    uint32_t info = (uint32_t)me.w;
     if (info & INFO_BOUNDARY) continue;
     uint32_t m = info & INFO_MAT;
     if (!friction_row(b, m)) continue;
-    uint32_t flagsI = b.FLG[p];
-    if (flagsI & FLAG_RIGID) continue;
+    if (info & INFO_RIGID) continue;
     int32_t fi = matw(b, m, M_fric);
     int32_t bondKi = matw(b, m, M_bondK);
-    int2 pi = P[p];
+    int2 pi = xy(me);
     int2 dxi = delta(pi, b.POS[p], f);
     uint32_t cnt = b.NBRN[p] & NBRN_COUNT;
     int32_t fx = 0, fy = 0;
@@ -533,8 +620,9 @@ __global__ void __launch_bounds__(256) k_friction(Bufs b, const int2* __restrict
       for (uint32_t k = 0; k < cnt; ++k) {
         uint32_t e = b.NBR[(size_t)k * stride + p];
         uint32_t q = e & ~NBR_BOUNDARY;
-        int2 pq = P[q];
-        int2 d = delta(pi, pq, f);
+        int4 o = b.PL[q];
+        int2 pq = xy(o);
+        int2 d = pdelta(pi, pq, f);
         int id = lut_index(d, f);
         if (id < 0) continue;
         int32_t d4x = shr_rne<FPRE>(d.x), d4y = shr_rne<FPRE>(d.y);
@@ -545,15 +633,15 @@ __global__ void __launch_bounds__(256) k_friction(Bufs b, const int2* __restrict
         if (!(e & NBR_BOUNDARY)) {
           int2 dq = delta(pq, b.POS[q], f);
           rel = make_int2(sub_sat(dxi.x, dq.x, f), sub_sat(dxi.y, dq.y, f));
-          mu = mat_mix(fi, matw(b, b.INFO[q] & INFO_MAT, M_fric));
+          mu = mat_mix(fi, matw(b, (uint32_t)o.w & INFO_MAT, M_fric));
         }
         if (mu == 0) continue;
         int32_t r4x = shr_rne<RPRE>(rel.x), r4y = shr_rne<RPRE>(rel.y);
         int32_t dot = wadd(wmul(d4x, r4x), wmul(d4y, r4y));
-        int32_t qq = divshift<16>(dot, d2, f);
+        int32_t qq = divshift<16>(dot, d2, b.rcp, f);
         int32_t tx = sub_sat(r4x, mul<16>(d4x, qq, f), f);
         int32_t ty = sub_sat(r4y, mul<16>(d4y, qq, f), f);
-        int32_t wq = shr_rne<4>(lut(b, OFF_W, id));
+        int32_t wq = shr_rne<4>(__ldg(b.WG + id).x);
         int32_t sx = mul<16>(mul<5>(tx, wq, f), mu, f);
         int32_t sy = mul<16>(mul<5>(ty, wq, f), mu, f);
         fx = wsub(fx, clampi(sx, -FR_TERM, FR_TERM));
@@ -561,9 +649,9 @@ __global__ void __launch_bounds__(256) k_friction(Bufs b, const int2* __restrict
       }
     }
     int32_t bx = 0, by = 0;
-    if (bondKi != 0 && !(flagsI & FLAG_BURST) && b.bond) {
+    if (bondKi != 0 && !(info & INFO_BURST)) {
       uint32_t slot = b.sslot[p];
-      int32_t ki = bond_k(b, m, b.TEMP[p], f);
+      int32_t ki = bond_k(b, m, b.RX[p].z, f);
       const uint32_t base = b.scenes[b.SCN[p]].slotBase;
       uint32_t* row = b.bond + (size_t)slot * BOND_CAP;
       for (int k = 0; k < BOND_CAP; ++k) {
@@ -571,12 +659,13 @@ __global__ void __launch_bounds__(256) k_friction(Bufs b, const int2* __restrict
         if (w == 0u) break;
         if (w & BOND_TOMB) continue;
         uint32_t q = b.inv[base + (w & BOND_J_MASK)];
-        uint32_t mj = b.INFO[q] & INFO_MAT;
-        if (b.FLG[q] & FLAG_BURST) { row[k] = w | BOND_TOMB; continue; }
+        int4 o = b.PL[q];
+        uint32_t mj = (uint32_t)o.w & INFO_MAT;
+        if ((uint32_t)o.w & INFO_BURST) { row[k] = w | BOND_TOMB; continue; }
         if (matw(b, mj, M_bondK) == 0) { row[k] = w | BOND_TOMB; continue; }
         int32_t L0 = (int32_t)((w >> 17) & 0x1fffu);
         int32_t L02 = wmul(L0, L0);
-        int2 d = delta(pi, P[q], f);
+        int2 d = delta(pi, xy(o), f);
         int32_t d4x = shr_rne<BPRE>(d.x), d4y = shr_rne<BPRE>(d.y);
         if (abs(d4x) > L0_MAX || abs(d4y) > L0_MAX) { row[k] = w | BOND_TOMB; continue; }
         int32_t d2 = wadd(wmul(d4x, d4x), wmul(d4y, d4y));
@@ -584,17 +673,17 @@ __global__ void __launch_bounds__(256) k_friction(Bufs b, const int2* __restrict
         int32_t mb = min(matw(b, m, M_bondBreak), matw(b, mj, M_bondBreak));
         int32_t mub = min(matw(b, m, M_bondMu), matw(b, mj, M_bondMu));
         if (mb != 0 && mub != 0) {
-          int32_t lp = neg_sat(add_sat(b.LAM[p], b.LAM[q], f), f);
+          int32_t lp = neg_sat(add_sat(me.z, o.z, f), f);
           int32_t Pq = lp > 0 ? shr_rne<4>(lp) : 0;
           mb = wadd(wadd(65536, wsub(mb, 65536)), mul<16>(Pq, mub, f));
         }
         if (mb != 0 && d2 > mul<16>(L02, mb, f)) { row[k] = w | BOND_TOMB; continue; }
         if (d2 < D2_FLOOR) continue;
-        int32_t kj = bond_k(b, mj, b.TEMP[q], f);
+        int32_t kj = bond_k(b, mj, b.RX[q].z, f);
         int32_t kp = min(ki, kj);
         if (kp == 0) continue;
         int32_t C = sub_sat(d2, L02, f);
-        int32_t qv = divshift<16>(C, wmul(d2, 4), f);
+        int32_t qv = divshift<16>(C, wmul(d2, 4), b.rcp, f);
         int32_t qk = mul<16>(qv, kp, f);
         int32_t gx = mul<3>(d4x, qk, f);
         int32_t gy = mul<3>(d4y, qk, f);
@@ -607,105 +696,122 @@ __global__ void __launch_bounds__(256) k_friction(Bufs b, const int2* __restrict
 }
 
 template <bool DBG>
-__global__ void __launch_bounds__(256) k_apply_fric(Bufs b, int2* __restrict__ P) {
+__global__ void __launch_bounds__(256) k_apply_fric(Bufs b) {
   Flags<DBG> f{b.dbg};
   const uint32_t nAct = b.world->nAct;
   for (uint32_t p = gtid(); p < nAct; p += gstride()) {
-    uint32_t info = b.INFO[p];
-    if (info & INFO_BOUNDARY) continue;
+    int4 me = b.PL[p];
+    uint32_t info = (uint32_t)me.w;
+    if (info & (INFO_BOUNDARY | INFO_PINNED)) continue;
     uint32_t m = info & INFO_MAT;
     if (!friction_row(b, m)) continue;
-    if (b.FLG[p] & (FLAG_RIGID | FLAG_ANCHOR)) continue;
     const ScenePar& S = b.scenes[b.SCN[p]];
-    P[p] = apply_dp(b, S, m, P[p], b.DP[p], f);
+    int2 np = apply_dp(b, S, m, xy(me), b.DP[p], f);
+    *reinterpret_cast<int2*>(b.PL + p) = np;
+    *reinterpret_cast<int2*>(b.PL2 + p) = np;
   }
 }
 
 // finalize + xsph + normals + conduct (src/sim.wgsl:2245-2582) in one sweep
 // over the neighbour list. vtmp_j = clamp(pred_j - pos_j) is finalize's
 // velocity, recomputed where it is needed.
-template <bool DBG>
-__global__ void __launch_bounds__(256) k_post1(Bufs b, const int2* __restrict__ P) {
+template <bool DBG, int L>
+__global__ void __launch_bounds__(256) k_post1(Bufs b) {
   Flags<DBG> f{b.dbg};
+  __shared__ int4 smat[MAT_MAX];  // {xsph, cond, corrode, corrPt}
+  for (int m = threadIdx.x; m < MAT_MAX; m += blockDim.x)
+    smat[m] = make_int4(matw(b, m, M_xsph), matw(b, m, M_cond), matw(b, m, M_corrode), matw(b, m, M_corrPt));
+  __syncthreads();
   const uint32_t nAct = b.world->nAct, stride = b.nbrStride;
-  for (uint32_t p = gtid(); p < nAct; p += gstride()) {
-    uint32_t slot = b.sslot[p];
-    int32_t* w = b.state + (size_t)slot * 8;
-    uint32_t info = b.INFO[p];
-    if (info & INFO_BOUNDARY) {
-      w[2] = 0;
-      w[3] = 0;
-      continue;
-    }
-    const ScenePar& S = b.scenes[b.SCN[p]];
+  const uint32_t sub = threadIdx.x & (L - 1), G = gstride() / L;
+  for (uint32_t p = gtid() / L;; p += G) {
+    if (__shfl_sync(0xffffffffu, p, 0) >= nAct) break;  // warp-uniform exit
+    const bool valid = p < nAct;
+    const int4 me = valid ? b.PL[p] : make_int4(0, 0, 0, (int32_t)INFO_BOUNDARY);
+    const uint32_t info = (uint32_t)me.w;
+    const bool act = valid && !(info & INFO_BOUNDARY);
+    const uint32_t pp = act ? p : 0u;
+    const ScenePar& S = b.scenes[b.SCN[pp]];
     const int32_t vmax = S.vmax, vmaxN = neg_sat(vmax, f);
-    uint32_t m = info & INFO_MAT;
-    uint32_t fl = b.FLG[p];
-    int2 pi = P[p];
-    int2 posi = b.POS[p];
-    int2 vi = delta(pi, posi, f);
+    const uint32_t m = info & INFO_MAT;
+    const int2 pi = xy(me);
+    int2 vi = delta(pi, b.POS[pp], f);
     vi.x = clampi(vi.x, vmaxN, vmax);
     vi.y = clampi(vi.y, vmaxN, vmax);
-    const bool doX = !(fl & (FLAG_RIGID | FLAG_ANCHOR));
-    const int32_t ci = matw(b, m, M_xsph);
-    const int32_t condi = matw(b, m, M_cond);
-    const int32_t corrodeI = matw(b, m, M_corrode);
-    const int32_t rhoi = b.RHO[p];
-    const int32_t Ti = b.TEMP[p];
-    uint32_t cnt = b.NBRN[p] & NBRN_COUNT;
+    const bool doX = !(info & INFO_PINNED);
+    const int4 mi = smat[m];
+    const int4 rxi = b.RX[pp];
+    const int32_t rhoi = rxi.x, Ti = rxi.z;
+    const uint32_t cnt = act ? (b.NBRN[p] & NBRN_COUNT) : 0u;
     int32_t ax = 0, ay = 0, sx = 0, sy = 0, hq = 0, hc = 0;
-    for (uint32_t k = 0; k < cnt; ++k) {
-      uint32_t e = b.NBR[(size_t)k * stride + p];
+    const uint32_t* np = b.NBR + pp;
+    uint32_t en = sub < cnt ? np[(size_t)sub * stride] : 0u;
+    int4 on = b.PL[en & ~NBR_BOUNDARY];
+    for (uint32_t k = sub; k < cnt; k += L) {
+      const uint32_t e = en;
+      const int4 o = on;
+      if (k + L < cnt) {
+        en = np[(size_t)(k + L) * stride];
+        on = b.PL[en & ~NBR_BOUNDARY];
+      }
       if (e & NBR_BOUNDARY) continue;
-      uint32_t q = e;
-      int2 pq = P[q];
-      int2 d = delta(pi, pq, f);
-      int id = lut_index(d, f);
+      const uint32_t q = e;
+      const int2 pq = xy(o);
+      const int2 d = pdelta(pi, pq, f);
+      const int id = lut_index(d, f);
       if (id < 0) continue;
-      int32_t W = lut(b, OFF_W, id);
-      uint32_t mj = b.INFO[q] & INFO_MAT;
+      const int2 wg = __ldg(b.WG + id);
+      const int32_t W = wg.x;
+      const int4 rx = b.RX[q];
+      const int4 mj = smat[(uint32_t)o.w & INFO_MAT];
       if (doX) {
-        int32_t K = sym_k(rhoi, b.RHO[q], f);
-        int32_t wk = mul<16>(W, K, f);
-        int32_t cij = mat_mix(ci, matw(b, mj, M_xsph));
+        int32_t K = sym_k(rhoi, rx.x, b.rcp, f);
+        int32_t wk = mulf<16>(W, K, f);
+        int32_t cij = mat_mix(mi.x, mj.x);
         int2 vj = delta(pq, b.POS[q], f);
         vj.x = clampi(vj.x, vmaxN, vmax);
         vj.y = clampi(vj.y, vmaxN, vmax);
-        ax = wadd(ax, clampi(mul<16>(mul<12>(sub_sat(vj.x, vi.x, f), wk, f), cij, f), -XS_TERM, XS_TERM));
-        ay = wadd(ay, clampi(mul<16>(mul<12>(sub_sat(vj.y, vi.y, f), wk, f), cij, f), -XS_TERM, XS_TERM));
+        ax = wadd(ax, mulfc<16>(mulf<12>(sub_sat(vj.x, vi.x, f), wk, f), cij, -XS_TERM, XS_TERM, f));
+        ay = wadd(ay, mulfc<16>(mulf<12>(sub_sat(vj.y, vi.y, f), wk, f), cij, -XS_TERM, XS_TERM, f));
       }
+      sx = wadd(sx, mulf<16>(mulf<26>(wg.y, d.x, f), rx.y, f));
+      sy = wadd(sy, mulf<16>(mulf<26>(wg.y, d.y, f), rx.y, f));
       {
-        int32_t gt = lut(b, OFF_G, id);
-        int32_t rj = b.RINV[q];
-        sx = wadd(sx, mul<16>(grad_q16(gt, d.x, f), rj, f));
-        sy = wadd(sy, mul<16>(grad_q16(gt, d.y, f), rj, f));
-      }
-      {
-        int32_t cij = mat_mix(condi, matw(b, mj, M_cond));
-        int32_t wk = mul<16>(W, cij, f);
-        int32_t dT = clampi(sub_sat(b.TEMP[q], Ti, f), -DT_CLAMP, DT_CLAMP);
-        hq = wadd(hq, clampi(mul<12>(dT, wk, f), -HT_TERM, HT_TERM));
-        if (mj != m) {
-          int32_t attack = matw(b, mj, M_corrode);
-          int32_t spend = matw(b, mj, M_corrPt) != CORR_NEVER ? corrodeI : 0;
-          int32_t str = wadd(attack, spend);
-          if (str != 0) hc = wadd(hc, clampi(mul<12>(W, str, f), 0, CORR_TERM));
+        int32_t cij = mat_mix(mi.y, mj.y);
+        int32_t wk = mulf<16>(W, cij, f);
+        int32_t dT = clampi(sub_sat(rx.z, Ti, f), -DT_CLAMP, DT_CLAMP);
+        hq = wadd(hq, mulfc<12>(dT, wk, -HT_TERM, HT_TERM, f));
+        if (((uint32_t)o.w & INFO_MAT) != m) {
+          int32_t spend = mj.w != CORR_NEVER ? mi.z : 0;
+          int32_t str = wadd(mj.z, spend);
+          if (str != 0) hc = wadd(hc, mulfc<12>(W, str, 0, CORR_TERM, f));
         }
       }
     }
-    b.NRM[p] = make_int2(mul<16>(sx, H, f), mul<16>(sy, H, f));
+    if (L > 1) {
+      ax = gsum<L>(ax);
+      ay = gsum<L>(ay);
+      sx = gsum<L>(sx);
+      sy = gsum<L>(sy);
+      hq = gsum<L>(hq);
+      hc = gsum<L>(hc);
+    }
+    if (!valid || sub != 0) continue;
+    int32_t* w = b.state + (size_t)b.sslot[p] * 8;
+    if (!act) {
+      *reinterpret_cast<int2*>(w + 2) = make_int2(0, 0);  // finalize: walls end with zero velocity
+      continue;
+    }
+    b.NQ[p] = make_int4(mul<16>(sx, H, f), mul<16>(sy, H, f), rhoi, 0);
     b.HEAT[p] = hq;
     b.CORR[p] = hc;
     int2 vo = vi;
     if (doX) vo = make_int2(add_sat(vi.x, shr_rne<8>(ax), f), add_sat(vi.y, shr_rne<8>(ay), f));
-    w[0] = pi.x;
-    w[1] = pi.y;
-    w[2] = vo.x;
-    w[3] = vo.y;
+    *reinterpret_cast<int4*>(w) = make_int4(pi.x, pi.y, vo.x, vo.y);
   }
 }
 
-// thermal (src/sim.wgsl:2612-2707) for one particle; returns the new words.
+// thermal (src/sim.wgsl:2612-2707) for one particle; updates words 4..7.
 template <bool DBG>
 __device__ __forceinline__ void thermal(const Bufs& b, uint32_t i, int32_t heat, int32_t corr, int32_t* w,
                                         const Flags<DBG>& f) {
@@ -755,59 +861,76 @@ __device__ __forceinline__ void thermal(const Bufs& b, uint32_t i, int32_t heat,
 // flag update for rows that cannot bond (bondForm2's tail, src/sim.wgsl:
 // 3059-3067) + the state digest. HASH=false when bond formation runs as its
 // own kernels (the digest then follows them).
-template <bool DBG, bool HASH>
-__global__ void __launch_bounds__(256) k_post2(Bufs b, const int2* __restrict__ P, int formFlags) {
+template <bool DBG, bool HASH, int L>
+__global__ void __launch_bounds__(256) k_post2(Bufs b, int formFlags) {
   Flags<DBG> f{b.dbg};
+  __shared__ int4 smat[MAT_MAX];  // {gammaCoh, gammaCur, adhesion, 0}
+  for (int m = threadIdx.x; m < MAT_MAX; m += blockDim.x)
+    smat[m] = make_int4(matw(b, m, M_gammaCoh), matw(b, m, M_gammaCur), matw(b, m, M_adhesion), 0);
+  __syncthreads();
   const uint32_t nAct = b.world->nAct, stride = b.nbrStride;
-  const uint32_t nIter = (nAct + gstride() - 1) / gstride() * gstride();
-  for (uint32_t p = gtid(); p < nIter; p += gstride()) {
-    bool valid = p < nAct;
+  const uint32_t sub = threadIdx.x & (L - 1), G = gstride() / L;
+  for (uint32_t p = gtid() / L;; p += G) {
+    if (__shfl_sync(0xffffffffu, p, 0) >= nAct) break;  // warp-uniform exit
+    const bool valid = p < nAct;
+    const int4 me = valid ? b.PL[p] : make_int4(0, 0, 0, (int32_t)INFO_BOUNDARY);
+    const uint32_t info = (uint32_t)me.w;
+    const bool act = valid && !(info & INFO_BOUNDARY);
+    const uint32_t pp = act ? p : 0u;
+    const int4 mi = smat[info & INFO_MAT];
+    const int2 pi = xy(me);
+    const int4 nqi = b.NQ[pp];
+    const int32_t rhoi = nqi.z;
+    const uint32_t cnt = act ? (b.NBRN[p] & NBRN_COUNT) : 0u;
+    int32_t ax = 0, ay = 0;
+    const uint32_t* np = b.NBR + pp;
+    uint32_t en = sub < cnt ? np[(size_t)sub * stride] : 0u;
+    int4 on = b.PL[en & ~NBR_BOUNDARY];
+    for (uint32_t k = sub; k < cnt; k += L) {
+      const uint32_t e = en;
+      const int4 o = on;
+      if (k + L < cnt) {
+        en = np[(size_t)(k + L) * stride];
+        on = b.PL[en & ~NBR_BOUNDARY];
+      }
+      const uint32_t q = e & ~NBR_BOUNDARY;
+      const int2 d = pdelta(pi, xy(o), f);
+      const int id = lut_index(d, f);
+      if (id < 0) continue;
+      const int2 ca = __ldg(b.CA + id);
+      if (e & NBR_BOUNDARY) {
+        ax = wsub(ax, mulfc<8>(mulf<22>(ca.y, d.x, f), mi.z, -ST_TERM, ST_TERM, f));
+        ay = wsub(ay, mulfc<8>(mulf<22>(ca.y, d.y, f), mi.z, -ST_TERM, ST_TERM, f));
+        continue;
+      }
+      const int4 nq = b.NQ[q];
+      const int32_t K = sym_k(rhoi, nq.z, b.rcp, f);
+      const int4 mj = smat[(uint32_t)o.w & INFO_MAT];
+      const int32_t gCoh = mat_mix(mi.x, mj.x);
+      const int32_t gCur = mat_mix(mi.y, mj.y);
+      int32_t fx = neg_sat(mulf<16>(mulf<22>(ca.x, d.x, f), gCoh, f), f);
+      int32_t fy = neg_sat(mulf<16>(mulf<22>(ca.x, d.y, f), gCoh, f), f);
+      const int32_t cx = mulf<16>(sub_sat(nqi.x, nq.x, f), gCur, f);
+      const int32_t cy = mulf<16>(sub_sat(nqi.y, nq.y, f), gCur, f);
+      fx = add_sat(fx, neg_sat(cx, f), f);
+      fy = add_sat(fy, neg_sat(cy, f), f);
+      ax = wadd(ax, mulc<8>(fx, K, -ST_TERM, ST_TERM, f));
+      ay = wadd(ay, mulc<8>(fy, K, -ST_TERM, ST_TERM, f));
+    }
+    if (L > 1) {
+      ax = gsum<L>(ax);
+      ay = gsum<L>(ay);
+    }
+    const bool lead = valid && sub == 0;
     uint32_t scene = 0, idx = 0;
     int32_t w8[8];
-    if (valid) {
-      uint32_t slot = b.sslot[p];
+    if (lead) {
+      const uint32_t slot = b.sslot[p];
       scene = b.SCN[p];
       const ScenePar& S = b.scenes[scene];
       idx = slot - S.slotBase;
       int32_t* w = b.state + (size_t)slot * 8;
-      uint32_t info = b.INFO[p];
-      if (!(info & INFO_BOUNDARY)) {
-        uint32_t m = info & INFO_MAT;
-        uint32_t fl = b.FLG[p];
-        const int32_t gCohI = matw(b, m, M_gammaCoh), gCurI = matw(b, m, M_gammaCur);
-        const int32_t adh = matw(b, m, M_adhesion);
-        int2 pi = P[p];
-        int2 ni = b.NRM[p];
-        int32_t rhoi = b.RHO[p];
-        uint32_t cnt = b.NBRN[p] & NBRN_COUNT;
-        int32_t ax = 0, ay = 0;
-        for (uint32_t k = 0; k < cnt; ++k) {
-          uint32_t e = b.NBR[(size_t)k * stride + p];
-          uint32_t q = e & ~NBR_BOUNDARY;
-          int2 d = delta(pi, P[q], f);
-          int id = lut_index(d, f);
-          if (id < 0) continue;
-          if (e & NBR_BOUNDARY) {
-            int32_t at = lut(b, OFF_A, id);
-            ax = wsub(ax, clampi(mul<8>(mul<22>(at, d.x, f), adh, f), -ST_TERM, ST_TERM));
-            ay = wsub(ay, clampi(mul<8>(mul<22>(at, d.y, f), adh, f), -ST_TERM, ST_TERM));
-            continue;
-          }
-          int32_t K = sym_k(rhoi, b.RHO[q], f);
-          int32_t ct = lut(b, OFF_C, id);
-          uint32_t mj = b.INFO[q] & INFO_MAT;
-          int32_t gCoh = mat_mix(gCohI, matw(b, mj, M_gammaCoh));
-          int32_t gCur = mat_mix(gCurI, matw(b, mj, M_gammaCur));
-          int32_t fx = neg_sat(mul<16>(mul<22>(ct, d.x, f), gCoh, f), f);
-          int32_t fy = neg_sat(mul<16>(mul<22>(ct, d.y, f), gCoh, f), f);
-          int2 nj = b.NRM[q];
-          int32_t cx = mul<16>(sub_sat(ni.x, nj.x, f), gCur, f);
-          int32_t cy = mul<16>(sub_sat(ni.y, nj.y, f), gCur, f);
-          fx = add_sat(fx, neg_sat(cx, f), f);
-          fy = add_sat(fy, neg_sat(cy, f), f);
-          ax = wadd(ax, clampi(mul<8>(fx, K, f), -ST_TERM, ST_TERM));
-          ay = wadd(ay, clampi(mul<8>(fy, K, f), -ST_TERM, ST_TERM));
-        }
+      if (act) {
         b.stacc[slot] = make_int2(shr_rne<8>(ax), shr_rne<8>(ay));
         thermal(b, idx, b.HEAT[p], b.CORR[p], w, f);
         if (formFlags && S.formNow) {
@@ -815,17 +938,17 @@ __global__ void __launch_bounds__(256) k_post2(Bufs b, const int2* __restrict__ 
           if (!(fo & FLAG_RIGID) && (fo & WELD_TAG_MASK) != S.weldHold) fo &= ~WELD_TAG_MASK;
           w[5] = (int32_t)fo;
         }
-        (void)fl;
       }
       if (HASH) {
-#pragma unroll
-        for (int k = 0; k < 8; ++k) w8[k] = w[k];
+        int4 a = reinterpret_cast<const int4*>(w)[0], c = reinterpret_cast<const int4*>(w)[1];
+        w8[0] = a.x; w8[1] = a.y; w8[2] = a.z; w8[3] = a.w;
+        w8[4] = c.x; w8[5] = c.y; w8[6] = c.z; w8[7] = c.w;
       }
     }
     if (HASH) {
       uint32_t h[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-      if (valid) particle_digest(w8, idx, nullptr, h);
-      digest_add(b.acc, valid, scene, h);
+      if (lead) particle_digest(w8, idx, nullptr, h);
+      digest_add(b.acc, lead, scene, h);
     }
   }
 }
@@ -881,8 +1004,8 @@ __global__ void __launch_bounds__(256) k_form1(Bufs b) {
   Flags<DBG> f{b.dbg};
   const uint32_t nAct = b.world->nAct, stride = b.nbrStride;
   for (uint32_t p = gtid(); p < nAct; p += gstride()) {
-    uint32_t info = b.INFO[p];
-    if (info & INFO_BOUNDARY) continue;
+    int4 me = b.PL[p];
+    if ((uint32_t)me.w & INFO_BOUNDARY) continue;
     const ScenePar& S = b.scenes[b.SCN[p]];
     if (!S.formNow) continue;
     uint32_t slot = b.sslot[p];
@@ -955,7 +1078,7 @@ __global__ void __launch_bounds__(256) k_form1(Bufs b) {
             if (abs(r4x) > vl4 || abs(r4y) > vl4) continue;
             if (wadd(wmul(r4x, r4x), wmul(r4y, r4y)) > wmul(vl4, vl4)) continue;
             int32_t pl = min(matw(b, matI, M_bondFormP), matw(b, mj, M_bondFormP));
-            if (pl != 0 && (neg_sat(b.LAM[p], f) < pl || neg_sat(b.LAM[e], f) < pl)) continue;
+            if (pl != 0 && (neg_sat(me.z, f) < pl || neg_sat(b.PL[e].z, f) < pl)) continue;
           }
           int32_t L0 = (int32_t)isqrt32((uint32_t)d2);
           if (L0 < L0_MIN || L0 > L0_MAX) continue;

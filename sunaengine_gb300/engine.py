@@ -53,14 +53,15 @@ def _ptr(a: Optional[np.ndarray]):
     return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
 
 
-def _opts(max_particles, max_cells, iters, debug, chain, device, luts, mats):
+def _opts(max_particles, max_cells, iters, debug, chain, device, luts, mats, lanes=0):
     luts = np.ascontiguousarray(data.luts() if luts is None else luts, dtype=np.int32)
     if luts.size != data.LUT_WORDS or data.table_hash(luts) != data.TABLE_HASH:
         raise EngineError('kernel tables do not match the frozen TABLE_HASH')
     mats = np.ascontiguousarray(data.mats() if mats is None else mats, dtype=np.int32).reshape(-1, 48)
     o = _native.SnOpts(max_particles=int(max_particles), max_cells=int(max_cells), iters=int(iters),
                        debug=1 if debug else 0, chain=1 if chain else 0, device=int(device),
-                       luts=luts.ctypes.data, mats=mats.ctypes.data, mat_count=mats.shape[0])
+                       luts=luts.ctypes.data, mats=mats.ctypes.data, mat_count=mats.shape[0],
+                       lanes=int(lanes))
     return o, (luts, mats)
 
 
@@ -105,9 +106,9 @@ class Engine:
     """One scene on one GB300 (``class Engine``, ``src/engine.js:3523``)."""
 
     def __init__(self, max_particles: int = 8192, max_cells: int = 0, iters: int = ITERS, debug: bool = False,
-                 chain: bool = True, device: int = 0, tables=None, mats=None):
+                 chain: bool = True, device: int = 0, tables=None, mats=None, lanes: int = 0):
         self._lib = _native.load()
-        o, self._keep = _opts(max_particles, max_cells, iters, debug, chain, device, tables, mats)
+        o, self._keep = _opts(max_particles, max_cells, iters, debug, chain, device, tables, mats, lanes)
         h = ctypes.c_void_p()
         rc = self._lib.sn_create(ctypes.byref(o), ctypes.byref(h))
         if rc != 0:
@@ -241,6 +242,14 @@ class Engine:
         self._check(self._lib.sn_last_timing(self._h, ctypes.byref(ms), ctypes.byref(l)), 'timing')
         return float(ms.value), int(l.value)
 
+    def profile_substep(self, reps: int = 3) -> np.ndarray:
+        """Mean device ms per kernel phase over `reps` real substeps (profileSubstep)."""
+        out = np.zeros(64, np.float32)
+        n = ctypes.c_uint32()
+        self._check(self._lib.sn_profile_substep(self._h, int(reps), _ptr(out), 64, ctypes.byref(n)), 'profile')
+        self._substeps += int(reps)
+        return out[:n.value].copy()
+
     @property
     def n(self) -> int:
         return self._n
@@ -293,9 +302,9 @@ class Batch:
     """
 
     def __init__(self, max_particles: int, max_scenes: int, max_cells: int = 0, iters: int = ITERS,
-                 debug: bool = False, chain: bool = True, device: int = 0, tables=None, mats=None):
+                 debug: bool = False, chain: bool = True, device: int = 0, tables=None, mats=None, lanes: int = 0):
         self._lib = _native.load()
-        o, self._keep = _opts(max_particles, max_cells, iters, debug, chain, device, tables, mats)
+        o, self._keep = _opts(max_particles, max_cells, iters, debug, chain, device, tables, mats, lanes)
         h = ctypes.c_void_p()
         rc = self._lib.sn_batch_create(ctypes.byref(o), int(max_scenes), ctypes.byref(h))
         if rc != 0:
@@ -378,6 +387,13 @@ class Batch:
 
     def sync(self):
         self._check(self._lib.sn_batch_sync(self._h), 'sync')
+
+    def profile_substep(self, reps: int = 3) -> np.ndarray:
+        out = np.zeros(64, np.float32)
+        n = ctypes.c_uint32()
+        self._check(self._lib.sn_batch_profile_substep(self._h, int(reps), _ptr(out), 64, ctypes.byref(n)),
+                    'profile')
+        return out[:n.value].copy()
 
     def last_timing(self):
         ms = ctypes.c_float()

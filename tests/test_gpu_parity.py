@@ -120,6 +120,21 @@ def test_every_substep_matches_oracle(name, oracle_mod):
     gpu.check_errors()
 
 
+@pytest.mark.parametrize('lanes', [1, 2, 4, 8])
+def test_lane_split_is_exact(lanes, oracle_mod):
+    import oracle
+    sc = scenes.make_scene('stretch_v1')
+    e = Engine(max_particles=sc.n + 64, lanes=lanes).load_scene(sc)
+    r = oracle.OracleEngine(sc.n + 64, threads=8).load_scene(sc)
+    sc2 = scenes.large_two_fluid(side=40, band=8)
+    e2 = Engine(max_particles=sc2.n + 64, lanes=lanes).load_scene(sc2)
+    r2 = oracle.OracleEngine(sc2.n + 64, threads=8).load_scene(sc2)
+    for x in (e, r, e2, r2):
+        x.step(24)
+    assert e.chain_hex() == r.chain_hex()
+    assert e2.chain_hex() == r2.chain_hex()
+
+
 def test_release_build_matches_debug_build(oracle_mod):
     sc = scenes.make_scene('overdense_v1')
     a = Engine(max_particles=8192, debug=True).load_scene(sc)
