@@ -1,0 +1,70 @@
+// The reference's canonical state digest (src/hash/statehash.js:36-169,
+// src/hash/statehash.wgsl:54-170): MurmurHash3_x86_32 body and finalizer run as
+// 4 salted lanes over each particle's 8 state words, giving per particle the 8
+// words that are u32-added across particles (H_set lanes 0..3, H_slot 4..7),
+// with the optional commutative bond fold, plus the per-substep chain fold.
+#pragma once
+#include <cstdint>
+#include "world.cuh"
+
+namespace sn {
+namespace d2 {
+
+__device__ __forceinline__ uint32_t rotl32(uint32_t x, int r) { return __funnelshift_l(x, x, r); }
+__device__ __forceinline__ uint32_t mm_step(uint32_t h, uint32_t k) {
+  k *= 0xcc9e2d51u;
+  k = rotl32(k, 15);
+  k *= 0x1b873593u;
+  h ^= k;
+  h = rotl32(h, 13);
+  return h * 5u + 0xe6546b64u;
+}
+__device__ __forceinline__ uint32_t fmix32(uint32_t h) {
+  h ^= h >> 16;
+  h *= 0x85ebca6bu;
+  h ^= h >> 13;
+  h *= 0xc2b2ae35u;
+  h ^= h >> 16;
+  return h;
+}
+// The 8 digest lanes one particle contributes (u32-added across particles).
+__device__ __forceinline__ void particle_digest(const int32_t* w8, uint32_t idx, const uint32_t* bondRow,
+                                                uint32_t out[8]) {
+  const uint32_t SEED[4] = {0x9e3779b1u, 0x85ebca77u, 0xc2b2ae3du, 0x27d4eb2fu};
+  const uint32_t SALT[4] = {0x00000000u, 0x51633e2du, 0x9c8f2a17u, 0xd0e5b943u};
+  uint32_t h[4] = {SEED[0], SEED[1], SEED[2], SEED[3]};
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    uint32_t w = (uint32_t)w8[k];
+#pragma unroll
+    for (int l = 0; l < 4; ++l) h[l] = mm_step(h[l], w ^ SALT[l]);
+  }
+  uint32_t s[4], t[4];
+#pragma unroll
+  for (int l = 0; l < 4; ++l) { s[l] = h[l]; t[l] = h[l]; }
+  if (bondRow) {
+    uint32_t bn = 0, com = 0, scom = 0;
+    for (int k = 0; k < BOND_CAP; ++k) {
+      uint32_t w = bondRow[k];
+      if (w == 0u) break;
+      com += fmix32(((w >> 17) & 0x1fffu) ^ 0x5bd1e995u);
+      scom += fmix32(w ^ 0x2f5b3c17u);
+      bn++;
+    }
+    if (bn) {
+#pragma unroll
+      for (int l = 0; l < 4; ++l) {
+        s[l] = mm_step(s[l], bn) ^ com;
+        t[l] = mm_step(t[l], bn) ^ scom;
+      }
+    }
+  }
+#pragma unroll
+  for (int l = 0; l < 4; ++l) {
+    out[l] = fmix32(s[l] ^ 8u);
+    out[4 + l] = fmix32(mm_step(t[l], idx) ^ 9u);
+  }
+}
+
+}  // namespace d2
+}  // namespace sn
