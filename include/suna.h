@@ -183,6 +183,26 @@ int sn_last_timing(sn_engine* e, float* ms, uint64_t* launches);
 int sn_profile_substep(sn_engine* e, uint32_t reps, float* ms, uint32_t max_phases, uint32_t* n_phases);
 int sn_batch_profile_substep(sn_batch* b, uint32_t reps, float* ms, uint32_t max_phases, uint32_t* n_phases);
 
+/* ---- digest without device allocation ------------------------------------ */
+/* No counterpart in the reference. For callers that cannot allocate device
+ * memory when they need a digest: code running while a stream is captured
+ * into a CUDA graph (cudaMalloc is not allowed then), latency-bound loops that
+ * cannot absorb cudaMalloc's device synchronisation, and embedding hosts that
+ * own all device memory. The caller passes its own device buffers: d_state
+ * (n*8 words, the Particle layout above), optionally d_bond (n_fluid*48 packed
+ * bond words, or NULL for no bond fold), and d_out (8 words) that receives
+ * H_set (0..3) || H_slot (4..7), exactly as sn_digest computes them. Work is
+ * queued on `stream` (a cudaStream_t; NULL = the legacy default stream).
+ * Scratch is a fixed 64 KiB array in the library's device image, so n is
+ * limited to 16,777,216 particles (SN_E_CAPACITY above that, nothing launched).
+ * The array is shared by all calls on a device: calls that overlap on the GPU
+ * race and must be ordered by the caller. The first call on each device looks
+ * up the array's device address; make that first call before any stream
+ * capture starts. */
+#define SN_NOALLOC_MAX_PARTICLES 16777216u
+int sn_digest_device_noalloc(const int32_t* d_state, uint32_t n, uint32_t n_fluid, const uint32_t* d_bond,
+                             uint32_t* d_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -120,6 +120,7 @@ SIGNATURES = {
     'sn_batch_check_errors': (ctypes.c_int, [P]),
     'sn_batch_sync': (ctypes.c_int, [P]),
     'sn_batch_last_timing': (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(u64)]),
+    'sn_digest_device_noalloc': (ctypes.c_int, [P, u32, u32, P, P, P]),
 }
 
 _lib = None
