@@ -135,6 +135,9 @@ int sn_check_errors(sn_engine* e);
 /* Block until all queued work is done. */
 int sn_sync(sn_engine* e);
 int sn_get_info(sn_engine* e, sn_info* out);
+/* Engine.setWalls (src/engine.js:5262): take the scene's boundary block out
+ * (n = nFluid) or rewrite it from the loaded scene and put it back. */
+int sn_set_walls(sn_engine* e, uint32_t on, uint32_t* walls_on);
 /* Formation clock and pending-formation flag (engine `_substep`, `_bondDirty`),
  * for keyframes that must resume the bond-formation schedule exactly. */
 int sn_set_formation_clock(sn_engine* e, uint64_t clock, uint32_t dirty);

@@ -70,6 +70,8 @@ def lib():
         l.sno_set_formation_clock.argtypes = [P, ctypes.c_uint64, ctypes.c_int]
         l.sno_spawn.restype = ctypes.c_int64
         l.sno_spawn.argtypes = [P, i32p, ctypes.c_uint32, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        l.sno_set_walls.restype = ctypes.c_int
+        l.sno_set_walls.argtypes = [P, ctypes.c_int]
         l.sno_impulse.restype = ctypes.c_int64
         l.sno_impulse.argtypes = [P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                   ctypes.c_int32, ctypes.c_uint32]
@@ -211,3 +213,28 @@ class OracleEngine:
 
     def impulse(self, cx, cy, r, ix, iy, limit=3000) -> int:
         return int(lib().sno_impulse(self.h, cx, cy, r, ix, iy, limit))
+
+    def set_walls(self, on: bool) -> bool:
+        return bool(lib().sno_set_walls(self.h, 1 if on else 0))
+
+    # the Engine method names, so the demo layer can drive either engine
+    def spawn_fluid(self, particles, no_weld: bool = True) -> int:
+        return self.spawn(particles, no_weld)
+
+    def apply_impulse(self, cx, cy, r, ix, iy, limit=3000) -> int:
+        return self.impulse(cx, cy, r, ix, iy, limit)
+
+    def read_scratch(self):
+        d = self.read_derived().reshape(-1, 16)
+        return np.ascontiguousarray(d[:, 8:10]).reshape(-1)
+
+    def write_scratch_state(self, state, scratch):
+        der = np.zeros((self.n, 16), np.int32)
+        st = np.asarray(state, dtype=np.int32).reshape(-1, 8)
+        der[:, 0:2] = st[:, 0:2]
+        if scratch is not None:
+            der[:, 8:10] = np.asarray(scratch, dtype=np.int32).reshape(-1, 2)
+        self.write_state(st.reshape(-1), der.reshape(-1))
+
+    def digest_hex(self) -> str:
+        return self.digest()

@@ -125,6 +125,7 @@ struct SnoEngine {
   uint64_t substepCount = 0;
   uint64_t formationClock = 0;  // engine `_substep`
   bool bondDirty = true;
+  bool wallsOn = true;
   uint32_t unsupported = 0;     // nonzero: a transition produced a row this oracle does not restate
   // the loaded scene's boundary block, for spawnFluid's relocation
   std::vector<int32_t> scenePos, sceneTemp, sceneFuel;
@@ -952,7 +953,7 @@ int sno_load_scene(SnoEngine* e, uint32_t n, uint32_t nFluid, const int32_t* pos
   if (ct > (1u << 24)) return -8;
   e->n = n; e->nFluid = nFluid; e->gridW = gW; e->gridH = gH; e->cellTotal = (uint32_t)ct;
   e->cellShift = cellShift; e->domW = domW; e->domH = domH; e->originX = 0; e->originY = 0;
-  e->vmax = VMAX; e->weldHold = 0; e->fuseTag = 0;
+  e->vmax = VMAX; e->weldHold = 0; e->fuseTag = 0; e->wallsOn = true;
   e->substepCount = 0; e->parity = 0; e->formationClock = 0; e->bondDirty = true;
   e->unsupported = 0;
   uint32_t cap = e->maxParticles;
@@ -1095,6 +1096,33 @@ int64_t sno_spawn(SnoEngine* e, const int32_t* rows, uint32_t k, int hasTemp, in
   e->n = newN; e->nFluid = newFluid;
   e->bondDirty = true;
   return e->n;
+}
+
+// setWalls, src/engine.js:5262-5305: remove the boundary block (n = nFluid)
+// or rewrite it from the loaded scene and put it back. Returns walls-on.
+int sno_set_walls(SnoEngine* e, int on) {
+  uint32_t nB = (uint32_t)e->scenePos.size() / 2 - e->sceneNFluid;
+  bool want = on != 0;
+  if (nB == 0) { e->wallsOn = want; return want; }
+  if (want == e->wallsOn) return e->wallsOn;
+  if (!want) { e->n = e->nFluid; e->wallsOn = false; return 0; }
+  if (e->nFluid + nB > e->maxParticles) return e->wallsOn;
+  std::vector<Particle>& stb = e->st[e->parity];
+  for (uint32_t b = 0; b < nB; ++b) {
+    uint32_t src = e->sceneNFluid + b;
+    Particle p{};
+    p.px = e->scenePos[2 * src]; p.py = e->scenePos[2 * src + 1];
+    p.matId = e->sceneMat[src];
+    p.temp = e->sceneHasTemp ? e->sceneTemp[src] : AMBIENT;
+    p.fuel = e->sceneHasFuel ? e->sceneFuel[src] : e->mats[p.matId][M_fuel0];
+    stb[e->nFluid + b] = p;
+    Derived d{};
+    d.predx = p.px; d.predy = p.py;
+    e->der[e->nFluid + b] = d;
+  }
+  e->n = e->nFluid + nB;
+  e->wallsOn = true;
+  return 1;
 }
 
 // applyImpulse, src/engine.js:6077-6098, on the current state (the mirror the

@@ -101,6 +101,7 @@ SIGNATURES = {
     'sn_sync': (ctypes.c_int, [P]),
     'sn_get_info': (ctypes.c_int, [P, ctypes.POINTER(SnInfo)]),
     'sn_set_formation_clock': (ctypes.c_int, [P, u64, u32]),
+    'sn_set_walls': (ctypes.c_int, [P, u32, ctypes.POINTER(u32)]),
     'sn_last_timing': (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(u64)]),
     'sn_profile_substep': (ctypes.c_int, [P, u32, P, u32, ctypes.POINTER(u32)]),
     'sn_batch_profile_substep': (ctypes.c_int, [P, u32, P, u32, ctypes.POINTER(u32)]),

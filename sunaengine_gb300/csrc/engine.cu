@@ -140,6 +140,7 @@ struct SceneHost {
   uint32_t nFluid0 = 0;
   bool hasTemp = false, hasFuel = false;
   uint32_t weldSeq = 1;
+  bool wallsOn = true;
   std::vector<ImpulseEv> events;
   uint32_t consumed = 0;  // events already applied (at < substeps)
 };
@@ -452,6 +453,7 @@ struct World {
     if (sc->temp) h.temp.assign(sc->temp, sc->temp + sc->n);
     if (sc->fuel) h.fuel.assign(sc->fuel, sc->fuel + sc->n);
     h.weldSeq = 1;
+    h.wallsOn = true;
     h.events.clear();
     h.consumed = 0;
     eventsDirty = true;
@@ -822,6 +824,46 @@ struct World {
     return ok;
   }
 
+  // setWalls (src/engine.js:5262-5305).
+  bool set_walls(uint32_t s, bool want, bool* onOut) {
+    SceneHost& h = sh[s];
+    if (!h.loaded) return fail("setWalls before loadScene");
+    const uint32_t nB = (uint32_t)(h.pos.size() / 2) - h.nFluid0;
+    bool cur = h.wallsOn;
+    if (nB == 0) { h.wallsOn = want; if (onOut) *onOut = want; return true; }
+    if (want == cur) { if (onOut) *onOut = cur; return true; }
+    if (!pull_params()) return false;
+    if (!want) {
+      hw.nAct -= h.n - h.nFluid;
+      h.n = h.nFluid;
+    } else {
+      if (h.nFluid + nB > h.cap) { if (onOut) *onOut = cur; return true; }
+      std::vector<int32_t> stw((size_t)nB * 8, 0);
+      for (uint32_t bb = 0; bb < nB; ++bb) {
+        uint32_t src = h.nFluid0 + bb;
+        int32_t* w = &stw[(size_t)bb * 8];
+        w[0] = h.pos[2 * src];
+        w[1] = h.pos[2 * src + 1];
+        w[4] = (int32_t)h.mat[src];
+        w[6] = h.hasTemp ? h.temp[src] : AMBIENT;
+        w[7] = h.hasFuel ? h.fuel[src] : row(h.mat[src])[M_fuel0];
+      }
+      size_t off = (size_t)h.slotBase + h.nFluid;
+      if (!cuda_ok(cudaMemcpyAsync(b.state + off * 8, stw.data(), stw.size() * 4, cudaMemcpyHostToDevice, st), "walls") ||
+          !cuda_ok(cudaMemsetAsync(b.stacc + off, 0, sizeof(int2) * nB, st), "walls"))
+        return false;
+      h.n = h.nFluid + nB;
+      hw.nAct += nB;
+    }
+    h.wallsOn = want;
+    hpar[s].n = h.n;
+    bool ok = push_scene(s) &&
+              cuda_ok(cudaMemcpyAsync(b.world, &hw, sizeof(hw), cudaMemcpyHostToDevice, st), "world") &&
+              cuda_ok(cudaStreamSynchronize(st), "walls");
+    if (onOut) *onOut = h.wallsOn;
+    return ok;
+  }
+
   bool write_state(uint32_t s, const int32_t* state, const int32_t* scratch, size_t n) {
     SceneHost& h = sh[s];
     if (!h.loaded) return fail("write_state before loadScene");
@@ -997,6 +1039,13 @@ int sn_profile_substep(sn_engine* e, uint32_t reps, float* ms, uint32_t max_phas
 int sn_batch_profile_substep(sn_batch* b, uint32_t reps, float* ms, uint32_t max_phases, uint32_t* n_phases) {
   if (!b || !ms) return SN_E_INVALID;
   return rc_of(b->w, b->w.profile(reps, ms, max_phases, n_phases));
+}
+int sn_set_walls(sn_engine* e, uint32_t on, uint32_t* walls_on) {
+  if (!e) return SN_E_INVALID;
+  bool out = false;
+  bool ok = e->w.set_walls(0, on != 0, &out);
+  if (walls_on) *walls_on = out ? 1u : 0u;
+  return rc_of(e->w, ok);
 }
 int sn_last_timing(sn_engine* e, float* ms, uint64_t* launches) {
   if (!e) return SN_E_INVALID;

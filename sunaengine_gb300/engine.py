@@ -233,6 +233,13 @@ class Engine:
         self._check(self._lib.sn_get_info(self._h, ctypes.byref(i)), 'info')
         return {k: getattr(i, k) for k, _ in i._fields_}
 
+    def set_walls(self, on: bool) -> bool:
+        """setWalls (src/engine.js:5262): remove or restore the boundary container."""
+        out = ctypes.c_uint32()
+        self._check(self._lib.sn_set_walls(self._h, 1 if on else 0, ctypes.byref(out)), 'setWalls')
+        self._n = self.info()['n']
+        return bool(out.value)
+
     def set_formation_clock(self, clock: int, dirty: bool):
         self._check(self._lib.sn_set_formation_clock(self._h, int(clock), 1 if dirty else 0), 'formationClock')
 
@@ -267,6 +274,7 @@ class Engine:
         return int(self.info()['formation_clock'])
 
     # camelCase aliases: the reference's method names
+    setWalls = set_walls
     loadScene = load_scene
     chainHex = chain_hex
     resetChain = reset_chain
