@@ -206,6 +206,84 @@ int sn_batch_profile_substep(sn_batch* b, uint32_t reps, float* ms, uint32_t max
 int sn_digest_device_noalloc(const int32_t* d_state, uint32_t n, uint32_t n_fluid, const uint32_t* d_bond,
                              uint32_t* d_out, void* stream);
 
+/* ---- 3D solver --------------------------------------------------------------
+ * Replaces the simulation half of the reference's 3D page (class App in
+ * 3d/app.js: reset :561-568, runSubsteps :709-714, spawn :575-597,
+ * setBallRadius :599-604, chain :717-744) and its compute shaders
+ * (3d/sim3d.wgsl:188-590). One sn3_engine holds up to max_scenes independent
+ * scenes and advances all of them per sn3_step; sn3_load_scene is the
+ * single-scene reset() and uses scene 0.
+ *
+ * State words per particle (slot order): [p.x, p.y, p.z, mat, v.x, v.y, v.z, 0]
+ * (the reference's p and v vec4s, 3d/sim3d.wgsl:45-50, with mat in p.w).
+ * sn3_fnv returns the reference's own 3D digest (256 FNV-1a stripes folded
+ * into 8 lanes, 3d/app.js:717-744); sn3_digest / sn3_chain apply the 2D
+ * engine's H_set || H_slot hash to the 8 words above, once per substep into
+ * the chain (the reference's 3D page has no per-substep hash; this one has no
+ * counterpart there). */
+typedef struct sn3_engine sn3_engine;
+
+typedef struct sn3_opts {
+  uint32_t max_particles; /* slot capacity over all scenes (the page's NMAX) */
+  uint32_t max_cells;     /* grid cells over all scenes; 0 = 1<<20 */
+  uint32_t max_scenes;    /* 0 = 1 */
+  uint32_t iters;         /* 1..16; the page runs 3 (3d/app.js:21) */
+  uint32_t debug;         /* 1 = count fp_flag events into the 16 debug words */
+  uint32_t chain;         /* 1 = hash every substep into the chain */
+  int32_t device;
+  const int32_t* luts;    /* W[2049] | G[2049] | planeW[513] | planeG[513] (buildLUTs, 3d/app.js:85-160) */
+  const int32_t* mats;    /* mat_count rows of 4: grav, rhoW, damp, f0 (3d/app.js:180-201) */
+  uint32_t mat_count;     /* 1..256; rhoW in -256..3839 */
+} sn3_opts;
+
+typedef struct sn3_scene {
+  uint32_t n;
+  const int32_t* pos;     /* 3n, Q16.16 */
+  const int32_t* vel;     /* 3n or NULL (zero) */
+  const uint32_t* mat;    /* n */
+  uint32_t gx, gy, gz;    /* cells of 2 wu per axis, 1..52 (the page: 28 x 30 x 28) */
+  int32_t stir_amp;       /* CFG.stirAmp (3d/app.js:24); 0 = off */
+} sn3_scene;
+
+typedef struct sn3_info {
+  uint32_t n, cap, gx, gy, gz, iters;
+  uint64_t substep_count;
+} sn3_info;
+
+int sn3_create(const sn3_opts* opts, sn3_engine** out);
+void sn3_destroy(sn3_engine* e);
+const char* sn3_last_error(const sn3_engine* e);
+/* reset(n, scene) (3d/app.js:561-568): scene 0 with every slot as capacity. */
+int sn3_load_scene(sn3_engine* e, const sn3_scene* sc);
+/* Add an independent scene with room for `cap` particles (0 = sc->n). */
+int sn3_add_scene(sn3_engine* e, const sn3_scene* sc, uint32_t cap, uint32_t* scene_out);
+int sn3_remove_scene(sn3_engine* e, uint32_t scene);
+/* runSubsteps(count) (3d/app.js:709-714) for every scene; the stir phase is
+ * (substepCount * 384) & 131071 at the start of the call, as the page writes
+ * its params once per batch. */
+int sn3_step(sn3_engine* e, uint32_t count);
+/* spawn (3d/app.js:575-597): append k particles (positions in Q16.16, velocity
+ * zero); what exceeds the scene's capacity is dropped (*added < k). */
+int sn3_spawn(sn3_engine* e, uint32_t scene, const int32_t* pos, const uint32_t* mat, uint32_t k, uint32_t* added);
+/* The cursor ball (3d/sim3d.wgsl:154-176; tables per buildBallLUT,
+ * 3d/app.js:212-230): centre in Q16.16, radius in world units (0, 64]. */
+int sn3_set_ball(sn3_engine* e, uint32_t scene, uint32_t on, int32_t x, int32_t y, int32_t z, double radius_wu);
+int sn3_fnv(sn3_engine* e, uint32_t scene, uint32_t lanes[8]);
+int sn3_digest(sn3_engine* e, uint32_t scene, uint32_t acc[8]);
+int sn3_chain(sn3_engine* e, uint32_t scene, uint32_t chain[8]);
+int sn3_read_state(sn3_engine* e, uint32_t scene, int32_t* out, size_t words);
+/* Keyframe restore: n particles' state words, the substep count and the chain
+ * (NULL keeps the chain). */
+int sn3_write_state(sn3_engine* e, uint32_t scene, const int32_t* state, uint32_t n, uint64_t substeps,
+                    const uint32_t chain[8]);
+int sn3_debug_counters(sn3_engine* e, uint32_t out[16]);
+int sn3_sync(sn3_engine* e);
+int sn3_get_info(sn3_engine* e, uint32_t scene, sn3_info* out);
+int sn3_last_timing(sn3_engine* e, float* ms, uint64_t* launches);
+/* Phases: predict, sort, cellstart+gather, neighbour lists, then density and
+ * solve per iteration, integrate(+hash), fold. */
+int sn3_profile_substep(sn3_engine* e, uint32_t reps, float* ms, uint32_t max_phases, uint32_t* n_phases);
+
 #ifdef __cplusplus
 }
 #endif

@@ -20,13 +20,13 @@ LIB = BUILD / 'libsuna_oracle.so'
 
 def build(force: bool = False) -> Path:
     """Compile the oracle with g++ (OpenMP) into oracle/_build."""
-    src = [HERE / 'suna_oracle.cpp', HERE / 'fixed_ref.h']
+    src = [HERE / 'suna_oracle.cpp', HERE / 'suna3d_oracle.cpp', HERE / 'fixed_ref.h']
     if LIB.exists() and not force and all(LIB.stat().st_mtime >= s.stat().st_mtime for s in src):
         return LIB
     BUILD.mkdir(exist_ok=True)
     tmp = BUILD / f'libsuna_oracle.{os.getpid()}.so'
     cmd = ['g++', '-O2', '-std=c++17', '-fopenmp', '-ffp-contract=off', '-shared', '-fPIC',
-           str(HERE / 'suna_oracle.cpp'), '-o', str(tmp)]
+           str(HERE / 'suna_oracle.cpp'), str(HERE / 'suna3d_oracle.cpp'), '-o', str(tmp)]
     subprocess.run(cmd, check=True)
     os.replace(tmp, LIB)
     return LIB
@@ -75,6 +75,27 @@ def lib():
         l.sno_impulse.restype = ctypes.c_int64
         l.sno_impulse.argtypes = [P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                   ctypes.c_int32, ctypes.c_uint32]
+        l.sno3_create.restype = P
+        l.sno3_create.argtypes = [ctypes.c_uint32, i32p, ctypes.c_uint32, i32p, ctypes.c_uint32, ctypes.c_uint32,
+                                  ctypes.c_int]
+        l.sno3_destroy.argtypes = [P]
+        l.sno3_load.restype = ctypes.c_int
+        l.sno3_load.argtypes = [P, ctypes.c_uint32, i32p, i32p, u32p, ctypes.c_uint32, ctypes.c_uint32,
+                                ctypes.c_uint32, ctypes.c_int32]
+        l.sno3_step.restype = ctypes.c_int
+        l.sno3_step.argtypes = [P, ctypes.c_uint32]
+        for f in ('sno3_fnv', 'sno3_digest', 'sno3_chain', 'sno3_dbg'):
+            getattr(l, f).argtypes = [P, u32p]
+        l.sno3_read_state.restype = ctypes.c_int
+        l.sno3_read_state.argtypes = [P, i32p, ctypes.c_size_t]
+        l.sno3_spawn.restype = ctypes.c_uint32
+        l.sno3_spawn.argtypes = [P, i32p, u32p, ctypes.c_uint32]
+        l.sno3_set_ball.argtypes = [P, ctypes.c_int, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                    i32p, i32p]
+        l.sno3_n.restype = ctypes.c_uint32
+        l.sno3_n.argtypes = [P]
+        l.sno3_substeps.restype = ctypes.c_uint64
+        l.sno3_substeps.argtypes = [P]
         _lib = l
     return _lib
 
@@ -238,3 +259,78 @@ class OracleEngine:
 
     def digest_hex(self) -> str:
         return self.digest()
+
+
+class Oracle3D:
+    """CPU reference of the 3D solver (3d/sim3d.wgsl driven as 3d/app.js drives it)."""
+
+    def __init__(self, max_particles: int = 65536, iters: int = 3, threads: int = 1):
+        from sunaengine_gb300 import tables3d
+        l = lib()
+        self._luts = np.ascontiguousarray(tables3d.luts3d(), dtype=np.int32)
+        self._mats = np.ascontiguousarray(tables3d.mats3d().reshape(-1), dtype=np.int32)
+        self.h = l.sno3_create(max_particles, self._luts, self._luts.size, self._mats, self._mats.size // 4,
+                               iters, threads)
+        self.max_particles = max_particles
+
+    def close(self):
+        if self.h:
+            lib().sno3_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def load_scene(self, sc, stir_amp: int = 0):
+        pos = np.ascontiguousarray(sc.pos.reshape(-1), dtype=np.int32)
+        vel = np.ascontiguousarray(sc.vel.reshape(-1), dtype=np.int32)
+        mat = np.ascontiguousarray(sc.mat, dtype=np.uint32)
+        rc = lib().sno3_load(self.h, sc.n, pos, vel, mat, sc.gx, sc.gy, sc.gz, stir_amp)
+        if rc != 0:
+            raise ValueError(f'oracle 3D load refused the scene (code {rc})')
+        return self
+
+    def step(self, count: int = 1):
+        lib().sno3_step(self.h, count)
+        return self.substep_count
+
+    @property
+    def n(self):
+        return lib().sno3_n(self.h)
+
+    @property
+    def substep_count(self):
+        return lib().sno3_substeps(self.h)
+
+    def _words(self, f):
+        a = np.zeros(8 if f != 'sno3_dbg' else 16, np.uint32)
+        getattr(lib(), f)(self.h, a)
+        return a
+
+    def fnv_hex(self) -> str:
+        return hex8(self._words('sno3_fnv'))
+
+    def digest(self) -> str:
+        return hex8(self._words('sno3_digest'))
+
+    def chain_hex(self) -> str:
+        return hex8(self._words('sno3_chain'))
+
+    def debug_counters(self):
+        return self._words('sno3_dbg')
+
+    def read_state(self):
+        a = np.zeros(self.n * 8, np.int32)
+        lib().sno3_read_state(self.h, a, a.size)
+        return a
+
+    def spawn(self, pos, mat) -> int:
+        pos = np.ascontiguousarray(np.asarray(pos).reshape(-1), dtype=np.int32)
+        mat = np.ascontiguousarray(mat, dtype=np.uint32)
+        return int(lib().sno3_spawn(self.h, pos, mat, mat.size))
+
+    def set_ball(self, on: bool, x: int = 0, y: int = 0, z: int = 0, radius_wu: float = 3.0):
+        from sunaengine_gb300 import tables3d
+        w, g = tables3d.ball_tables(radius_wu)
+        reach = tables3d.js_round((radius_wu + tables3d.H_WU) * tables3d.ONE)
+        self._ball = (w, g)
+        lib().sno3_set_ball(self.h, int(on), x, y, z, reach, w, g)

@@ -34,20 +34,37 @@ def nvcc() -> str:
 
 
 def build(force: bool = False, verbose: bool = False) -> Path:
-    """Compile csrc/*.cu into _build/libsuna_gb300.so (sm_103a)."""
+    """Compile csrc/*.cu into _build/libsuna_gb300.so (sm_103a): one nvcc per
+    translation unit, run in parallel, then one link."""
     with _lock:
         srcs = _sources()
         if LIB.exists() and not force and all(LIB.stat().st_mtime >= s.stat().st_mtime for s in srcs):
             return LIB
         BUILD.mkdir(exist_ok=True)
-        tmp = BUILD / f'libsuna_gb300.{os.getpid()}.so'
-        cmd = [nvcc(), *ARCH, '-lineinfo', '-O3', '-std=c++17', '-Xcompiler', '-fPIC', '-shared',
-               '-diag-suppress', '550', '-o', str(tmp)] + [str(s) for s in sorted(CSRC.glob('*.cu'))]
+        tag = os.getpid()
+        flags = [*ARCH, '-lineinfo', '-O3', '-std=c++17', '-Xcompiler', '-fPIC', '-diag-suppress', '550']
         if verbose:
-            cmd.insert(1, '-Xptxas=-v')
-        r = subprocess.run(cmd, capture_output=True, text=True)
+            flags.append('-Xptxas=-v')
+        units = sorted(CSRC.glob('*.cu'))
+        objs = [BUILD / f'{u.stem}.{tag}.o' for u in units]
+        procs = [subprocess.Popen([nvcc(), *flags, '-c', str(u), '-o', str(o)], stdout=subprocess.PIPE,
+                                  stderr=subprocess.STDOUT, text=True) for u, o in zip(units, objs)]
+        logs = [p.communicate()[0] for p in procs]
+        bad = [(u, lg) for u, p, lg in zip(units, procs, logs) if p.returncode != 0]
+        if verbose:
+            for u, lg in zip(units, logs):
+                print(f'--- {u.name}\n{lg}')
+        if bad:
+            for o in objs:
+                o.unlink(missing_ok=True)
+            raise RuntimeError('nvcc failed:\n' + '\n'.join(f'{u.name}:\n{lg}' for u, lg in bad))
+        tmp = BUILD / f'libsuna_gb300.{tag}.so'
+        r = subprocess.run([nvcc(), *ARCH, '-shared', '-o', str(tmp)] + [str(o) for o in objs],
+                           capture_output=True, text=True)
+        for o in objs:
+            o.unlink(missing_ok=True)
         if r.returncode != 0:
-            raise RuntimeError('nvcc failed:\n' + r.stdout + r.stderr)
+            raise RuntimeError('nvcc link failed:\n' + r.stdout + r.stderr)
         os.replace(tmp, LIB)
         return LIB
 
@@ -81,6 +98,25 @@ class SnInfo(ctypes.Structure):
 # Every symbol include/suna.h declares, with its ctypes signature.
 P = ctypes.c_void_p
 u32, i32, u64, sz = ctypes.c_uint32, ctypes.c_int32, ctypes.c_uint64, ctypes.c_size_t
+class Sn3Opts(ctypes.Structure):
+    _fields_ = [('max_particles', ctypes.c_uint32), ('max_cells', ctypes.c_uint32),
+                ('max_scenes', ctypes.c_uint32), ('iters', ctypes.c_uint32), ('debug', ctypes.c_uint32),
+                ('chain', ctypes.c_uint32), ('device', ctypes.c_int32), ('luts', ctypes.c_void_p),
+                ('mats', ctypes.c_void_p), ('mat_count', ctypes.c_uint32)]
+
+
+class Sn3Scene(ctypes.Structure):
+    _fields_ = [('n', ctypes.c_uint32), ('pos', ctypes.c_void_p), ('vel', ctypes.c_void_p),
+                ('mat', ctypes.c_void_p), ('gx', ctypes.c_uint32), ('gy', ctypes.c_uint32),
+                ('gz', ctypes.c_uint32), ('stir_amp', ctypes.c_int32)]
+
+
+class Sn3Info(ctypes.Structure):
+    _fields_ = [('n', ctypes.c_uint32), ('cap', ctypes.c_uint32), ('gx', ctypes.c_uint32),
+                ('gy', ctypes.c_uint32), ('gz', ctypes.c_uint32), ('iters', ctypes.c_uint32),
+                ('substep_count', ctypes.c_uint64)]
+
+
 SIGNATURES = {
     'sn_create': (ctypes.c_int, [ctypes.POINTER(SnOpts), ctypes.POINTER(P)]),
     'sn_destroy': (None, [P]),
@@ -122,6 +158,25 @@ SIGNATURES = {
     'sn_batch_sync': (ctypes.c_int, [P]),
     'sn_batch_last_timing': (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(u64)]),
     'sn_digest_device_noalloc': (ctypes.c_int, [P, u32, u32, P, P, P]),
+    'sn3_create': (ctypes.c_int, [ctypes.POINTER(Sn3Opts), ctypes.POINTER(P)]),
+    'sn3_destroy': (None, [P]),
+    'sn3_last_error': (ctypes.c_char_p, [P]),
+    'sn3_load_scene': (ctypes.c_int, [P, ctypes.POINTER(Sn3Scene)]),
+    'sn3_add_scene': (ctypes.c_int, [P, ctypes.POINTER(Sn3Scene), u32, ctypes.POINTER(u32)]),
+    'sn3_remove_scene': (ctypes.c_int, [P, u32]),
+    'sn3_step': (ctypes.c_int, [P, u32]),
+    'sn3_spawn': (ctypes.c_int, [P, u32, P, P, u32, ctypes.POINTER(u32)]),
+    'sn3_set_ball': (ctypes.c_int, [P, u32, u32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_double]),
+    'sn3_fnv': (ctypes.c_int, [P, u32, P]),
+    'sn3_digest': (ctypes.c_int, [P, u32, P]),
+    'sn3_chain': (ctypes.c_int, [P, u32, P]),
+    'sn3_read_state': (ctypes.c_int, [P, u32, P, ctypes.c_size_t]),
+    'sn3_write_state': (ctypes.c_int, [P, u32, P, u32, u64, P]),
+    'sn3_debug_counters': (ctypes.c_int, [P, P]),
+    'sn3_sync': (ctypes.c_int, [P]),
+    'sn3_get_info': (ctypes.c_int, [P, u32, ctypes.POINTER(Sn3Info)]),
+    'sn3_last_timing': (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(u64)]),
+    'sn3_profile_substep': (ctypes.c_int, [P, u32, P, u32, ctypes.POINTER(u32)]),
 }
 
 _lib = None

@@ -16,6 +16,9 @@
 
 namespace sn {
 namespace radix {
+// Internal linkage: every translation unit that sorts gets its own copy of
+// these kernels, so several engines can include this header.
+namespace {
 
 constexpr int RBITS = 9;
 constexpr int RADIX = 1 << RBITS;
@@ -171,5 +174,6 @@ inline void sort_pairs(uint32_t* keys0, uint32_t n, int keyBits, uint32_t* outKe
 
 inline size_t hist_words(uint32_t n) { return (size_t)RADIX * ((n + TILE - 1) / TILE + 1); }
 
+}  // namespace
 }  // namespace radix
 }  // namespace sn

@@ -66,5 +66,33 @@ __device__ __forceinline__ void particle_digest(const int32_t* w8, uint32_t idx,
   }
 }
 
+// Warp-aggregated u32 add of 8 digest words into acc[scene]. Lanes with
+// valid == false contribute nothing. Addition mod 2^32 is commutative, so the
+// digest does not depend on the order in which warps land.
+__device__ __forceinline__ void digest_add(uint32_t* acc, bool valid, uint32_t scene, const uint32_t h[8]) {
+  uint32_t key = valid ? scene : 0xffffffffu;
+  uint32_t peers = __match_any_sync(0xffffffffu, key);
+  int lane = threadIdx.x & 31;
+  bool leader = lane == __ffs(peers) - 1;
+  if (peers == 0xffffffffu) {
+#pragma unroll
+    for (int l = 0; l < 8; ++l) {
+      uint32_t t = __reduce_add_sync(0xffffffffu, h[l]);
+      if (leader && valid) atomicAdd(acc + scene * 8 + l, t);
+    }
+    return;
+  }
+#pragma unroll
+  for (int l = 0; l < 8; ++l) {
+    uint32_t v = h[l], total = 0, m = peers;
+    while (m) {
+      int src = __ffs(m) - 1;
+      m &= m - 1;
+      total += __shfl_sync(peers, v, src);
+    }
+    if (leader && valid) atomicAdd(acc + scene * 8 + l, total);
+  }
+}
+
 }  // namespace d2
 }  // namespace sn
