@@ -159,6 +159,22 @@ BYTES = {
 }
 
 
+# ncu summaries under profiles/ that carry the DRAM traffic of a dominant kernel
+PROFILE_OF = {'colour x4': 'k_colour_2d_large.md'}
+
+
+def profiled_traffic(phase: str):
+    """DRAM bytes (read + write) per launch from the committed ncu summary of
+    this phase's kernel, or None when there is none."""
+    f = PROFILE_OF.get(phase)
+    if not f or not (ROOT / 'profiles' / f).exists():
+        return None
+    for line in (ROOT / 'profiles' / f).read_text().splitlines():
+        if line.startswith('traffic_bytes_per_launch:'):
+            return int(line.split(':', 1)[1].strip())
+    return None
+
+
 def phase_names(iters: int):
     names = list(PHASE_NAMES_HEAD)
     for _ in range(iters):
@@ -302,7 +318,8 @@ def ours(args):
     achieved = bytes_per_launch / (per_launch_ms / 1e3) / 1e9
     peak, peak_kind = _peaks()
     roof = {'kernel': dom, 'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
-            'frac': achieved / peak, 'peak_source': peak_kind, 'traffic': None,
+            'frac': achieved / peak, 'peak_source': peak_kind, 'traffic': profiled_traffic(dom),
+            'traffic_source': f'profiles/{PROFILE_OF[dom]}' if dom in PROFILE_OF else None,
             'algorithmic_bytes_per_launch': bytes_per_launch, 'units_per_launch': units,
             'launch_ms': per_launch_ms,
             'phases_ms_per_substep': {k: v[0] for k, v in agg.items()}}
