@@ -234,6 +234,92 @@ def reference_arm(args):
     return 0
 
 
+# 3D phase bytes per particle (phase-minimal): predict 52, sort 24, neighbour set 16,
+# per iteration density 24 + solveDp/applyDp 64, integrate 48 + hash 28.
+BYTES_3D = {'predict': 52, 'grid sort': 24, 'cell ranges + gather': 0, 'neighbour lists': 16,
+            'density': 24, 'solve+apply': 64, 'integrate+hash': 76, 'fold': 0}
+WORKLOAD_3D = ('3D dam break: 262,144 water particles (64^3 lattice at 1 wu, smix jitter) in the corner of a '
+               '48x40x48-cell (96x80x96 wu) walled box, ITERS 4, H_set||H_slot every substep')
+
+
+def workload_3d(steps: int, warmup: int, device: int, cpu_seconds: float = 6.0, with_cpu: bool = True):
+    """The 3D dam break (262,144 particles, 4 iterations): device-timed
+    particle-substeps/s, end to end through the public API, the per-phase
+    roofline of its dominant kernel, and the oracle on a sample."""
+    from sunaengine_gb300 import tables3d
+    from sunaengine_gb300.engine3d import Engine3D
+    sc = tables3d.dam3d_large()
+    e = Engine3D(max_particles=sc.n, iters=4, device=device).load_scene(sc)
+    e.step(warmup)
+    e.sync()
+    e.step(steps)
+    e.sync()
+    ms, launches = e.last_timing()
+    value = sc.n * steps / (ms / 1e3)
+    names = ['predict', 'grid sort', 'cell ranges + gather', 'neighbour lists']
+    names += ['density', 'solve+apply'] * e.iters + ['integrate+hash', 'fold']
+    ph = e.profile_substep(max(3, min(steps, 10)))
+    agg = {}
+    for nm, t in zip(names, ph):
+        agg.setdefault(nm, [0.0, 0])
+        agg[nm][0] += float(t)
+        agg[nm][1] += 1
+    dom = max((k for k in agg if k != 'fold'), key=lambda k: agg[k][0])
+    per_launch = agg[dom][0] / agg[dom][1]
+    bpl = BYTES_3D[dom] * sc.n
+    peak, kind = _peaks()
+    achieved = bpl / (per_launch / 1e3) / 1e9
+    roof = {'kernel': dom, 'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s', 'frac': achieved / peak,
+            'peak_source': kind, 'traffic': None, 'algorithmic_bytes_per_launch': bpl, 'launch_ms': per_launch,
+            'phases_ms_per_substep': {k: v[0] for k, v in agg.items()}}
+    e.close()
+    # end to end: upload the scene, step(1) + digest() per substep, read the state back
+    e2 = Engine3D(max_particles=sc.n, iters=4, device=device).load_scene(sc)
+    e2.step(1)
+    e2.sync()
+    t0 = time.perf_counter()
+    e2.load_scene(sc)
+    for _ in range(steps):
+        e2.step(1)
+        e2.digest()
+    final = e2.read_state()
+    wall = time.perf_counter() - t0
+    e2.close()
+    out = {'workload': WORKLOAD_3D, 'particles': sc.n, 'steps': steps, 'value': value, 'unit': UNIT,
+           'ms_per_step': ms / steps, 'gpu_launches': int(launches), 'roofline': roof,
+           'e2e': {'value': sc.n * steps / wall, 'unit': UNIT, 'h2d_bytes_per_step': sc.n * 28 / steps,
+                   'd2h_bytes_per_step': 32 + final.nbytes / steps}}
+    if with_cpu:
+        import oracle
+        threads = os.cpu_count() or 1
+        small = tables3d.column_fast(32, 32, 32, 48, 40, 48)
+        o = oracle.Oracle3D(small.n, iters=4, threads=threads).load_scene(small)
+        o.step(1)
+        t0 = time.perf_counter()
+        k = 0
+        while time.perf_counter() - t0 < cpu_seconds:
+            o.step(1)
+            k += 1
+        dt = time.perf_counter() - t0
+        out['cpu_baseline'] = {'value': small.n * k / dt, 'unit': UNIT, 'cores': threads, 'kind': 'port',
+                               'sample': f'{small.n}-particle 32^3 block of the same box, {k} substeps, {dt:.1f} s'}
+    return out
+
+
+def serving_workload(device: int, count: int = 40, rate_hz: float = 4.0, budget_gb: float = 24.0,
+                     seed: int = 0x5e7e):
+    """A seeded Poisson stream of replay and rewind-scrub jobs (2D and 3D, 4k-256k
+    particles, N in [100, 2000]) served with continuous batching in real time."""
+    from sunaengine_gb300 import serving
+    jobs = serving.poisson_jobs(count, rate_hz, seed=seed)
+    s = serving.Server(int(budget_gb * (1 << 30)), device=device)
+    stats = s.run(jobs, realtime=True)
+    s.close()
+    stats.update({'rate_hz': rate_hz, 'hbm_budget_gb': budget_gb, 'quantum_substeps': s.quantum,
+                  'checkpoint_every': s.ckpt_every})
+    return stats
+
+
 def batched_workload(steps: int, warmup: int, device: int, plain_sample: int = 24, seed: int = 0xba7c4):
     """256 scenes (1k-64k particles, log-uniform) with stir schedules: batched
     vs the same scenes stepped one at a time on the plain path."""
@@ -361,6 +447,10 @@ def ours(args):
     }
     if rank == 0 and not args.no_batched:
         line['batched'] = batched_workload(args.steps, args.warmup, local)
+    if rank == 0 and not args.no_3d:
+        line['cfg3_3d'] = workload_3d(args.steps, args.warmup, local, with_cpu=not args.no_cpu)
+    if rank == 0 and not args.no_serving:
+        line['serving'] = serving_workload(local)
     if rank == 0 and not args.no_cpu:
         line['cpu_baseline'] = run_cpu_baseline(seconds=args.cpu_seconds)
     if rank == 0:
@@ -378,6 +468,8 @@ def main():
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--no-batched', action='store_true')
     ap.add_argument('--no-cpu', action='store_true')
+    ap.add_argument('--no-3d', action='store_true')
+    ap.add_argument('--no-serving', action='store_true')
     ap.add_argument('--cpu-seconds', type=float, default=12.0)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)

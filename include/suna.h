@@ -243,6 +243,9 @@ typedef struct sn3_scene {
   const uint32_t* mat;    /* n */
   uint32_t gx, gy, gz;    /* cells of 2 wu per axis, 1..52 (the page: 28 x 30 x 28) */
   int32_t stir_amp;       /* CFG.stirAmp (3d/app.js:24); 0 = off */
+  uint32_t frame;         /* 0: the stir phase is fixed per sn3_step call, as per runSubsteps call in
+                             the page; F > 0: fixed per frame of F substeps counted from the load, the
+                             same as calling sn3_step(F) repeatedly, whatever the call sizes */
 } sn3_scene;
 
 typedef struct sn3_info {
@@ -283,6 +286,32 @@ int sn3_last_timing(sn3_engine* e, float* ms, uint64_t* launches);
 /* Phases: predict, sort, cellstart+gather, neighbour lists, then density and
  * solve per iteration, integrate(+hash), fold. */
 int sn3_profile_substep(sn3_engine* e, uint32_t reps, float* ms, uint32_t max_phases, uint32_t* n_phases);
+
+/* ---- device checkpoints ------------------------------------------------------
+ * No counterpart in the reference (its keyframes are host copies,
+ * src/demo_boot.js:104-125). A pool is one device allocation of `bytes`; a
+ * checkpoint of a scene (2D: state, scratch, chain, bond rows and the
+ * formation/substep clocks; 3D: state, chain and the substep clock) is copied
+ * into it on the engine's stream without a host round trip and restored the
+ * same way. Loading a checkpoint into a scene rewinds (or advances) that
+ * scene exactly: every later substep equals the one after the save. A 2D
+ * checkpoint loads only into a scene with the same n and n_fluid. The pool
+ * orders copies across engines with events, so one pool may serve several
+ * engines on the same device; a pool is not thread-safe. */
+typedef struct sn_ckpt_pool sn_ckpt_pool;
+int sn_ckpt_pool_create(size_t bytes, int32_t device, sn_ckpt_pool** out);
+void sn_ckpt_pool_destroy(sn_ckpt_pool* p);
+const char* sn_ckpt_pool_last_error(const sn_ckpt_pool* p);
+int sn_ckpt_pool_usage(const sn_ckpt_pool* p, size_t* used, size_t* capacity);
+/* Release a checkpoint (waits for copies in flight that touch it). */
+int sn_ckpt_free(sn_ckpt_pool* p, uint64_t handle);
+/* Bytes a checkpoint of this scene takes now (before 256-byte rounding). */
+int sn_batch_ckpt_bytes(sn_batch* b, uint32_t id, size_t* bytes);
+int sn_batch_ckpt_save(sn_batch* b, uint32_t id, sn_ckpt_pool* p, uint64_t* handle);
+int sn_batch_ckpt_load(sn_batch* b, uint32_t id, sn_ckpt_pool* p, uint64_t handle);
+int sn3_ckpt_bytes(sn3_engine* e, uint32_t scene, size_t* bytes);
+int sn3_ckpt_save(sn3_engine* e, uint32_t scene, sn_ckpt_pool* p, uint64_t* handle);
+int sn3_ckpt_load(sn3_engine* e, uint32_t scene, sn_ckpt_pool* p, uint64_t handle);
 
 #ifdef __cplusplus
 }

@@ -81,7 +81,9 @@ def lib():
         l.sno3_destroy.argtypes = [P]
         l.sno3_load.restype = ctypes.c_int
         l.sno3_load.argtypes = [P, ctypes.c_uint32, i32p, i32p, u32p, ctypes.c_uint32, ctypes.c_uint32,
-                                ctypes.c_uint32, ctypes.c_int32]
+                                ctypes.c_uint32, ctypes.c_int32, ctypes.c_uint32]
+        l.sno3_write_state.restype = ctypes.c_int
+        l.sno3_write_state.argtypes = [P, i32p, ctypes.c_uint32, ctypes.c_uint64, P]
         l.sno3_step.restype = ctypes.c_int
         l.sno3_step.argtypes = [P, ctypes.c_uint32]
         for f in ('sno3_fnv', 'sno3_digest', 'sno3_chain', 'sno3_dbg'):
@@ -280,11 +282,11 @@ class Oracle3D:
 
     __del__ = close
 
-    def load_scene(self, sc, stir_amp: int = 0):
+    def load_scene(self, sc, stir_amp: int = 0, frame: int = 0):
         pos = np.ascontiguousarray(sc.pos.reshape(-1), dtype=np.int32)
         vel = np.ascontiguousarray(sc.vel.reshape(-1), dtype=np.int32)
         mat = np.ascontiguousarray(sc.mat, dtype=np.uint32)
-        rc = lib().sno3_load(self.h, sc.n, pos, vel, mat, sc.gx, sc.gy, sc.gz, stir_amp)
+        rc = lib().sno3_load(self.h, sc.n, pos, vel, mat, sc.gx, sc.gy, sc.gz, stir_amp, frame)
         if rc != 0:
             raise ValueError(f'oracle 3D load refused the scene (code {rc})')
         return self
@@ -322,6 +324,16 @@ class Oracle3D:
         a = np.zeros(self.n * 8, np.int32)
         lib().sno3_read_state(self.h, a, a.size)
         return a
+
+    def write_state(self, state, substeps: int, chain_words=None):
+        st = np.ascontiguousarray(np.asarray(state).reshape(-1), dtype=np.int32)
+        ch = None if chain_words is None else np.ascontiguousarray(chain_words, dtype=np.uint32)
+        self._ch = ch
+        if lib().sno3_write_state(self.h, st, st.size // 8, int(substeps), _ptr(ch)) != 0:
+            raise ValueError('oracle 3D write_state refused')
+
+    def chain_words(self):
+        return self._words('sno3_chain')
 
     def spawn(self, pos, mat) -> int:
         pos = np.ascontiguousarray(np.asarray(pos).reshape(-1), dtype=np.int32)

@@ -49,6 +49,7 @@ struct Sno3 {
   uint32_t n = 0, gx = 1, gy = 1, gz = 1, cellTotal = 1;
   int32_t stirAmp = 0;
   int32_t stirPhase = 0;  // fixed for one step() call, as the reference writes params once per batch
+  uint32_t frame = 0;     // > 0: the phase is fixed per frame of `frame` substeps instead
   bool ballOn = false;
   V3 ballPos{0, 0, 0};
   int32_t ballReach = 0;
@@ -355,10 +356,11 @@ Sno3* sno3_create(uint32_t maxN, const int32_t* luts, uint32_t lutWords, const i
 void sno3_destroy(Sno3* e) { delete e; }
 
 int sno3_load(Sno3* e, uint32_t n, const int32_t* pos, const int32_t* vel, const uint32_t* mat, uint32_t gx,
-              uint32_t gy, uint32_t gz, int32_t stirAmp) {
+              uint32_t gy, uint32_t gz, int32_t stirAmp, uint32_t frame) {
   if (n > e->maxN || gx == 0 || gy == 0 || gz == 0) return -1;
   e->n = n; e->gx = gx; e->gy = gy; e->gz = gz; e->cellTotal = gx * gy * gz;
   e->stirAmp = stirAmp;
+  e->frame = frame;
   e->ps.assign(n, P3{});
   for (uint32_t i = 0; i < n; ++i) {
     if (mat[i] >= e->matCount) return -2;
@@ -383,6 +385,7 @@ int sno3_load(Sno3* e, uint32_t n, const int32_t* pos, const int32_t* vel, const
 int sno3_step(Sno3* e, uint32_t count) {
   e->stirPhase = (int32_t)((e->substeps * 384) & 131071);
   for (uint32_t s = 0; s < count; ++s) {
+    if (e->frame) e->stirPhase = (int32_t)(((e->substeps - e->substeps % e->frame) * 384) & 131071);
     predict3(*e);
     grid3(*e);
     nbr3(*e);
@@ -454,6 +457,26 @@ void sno3_set_ball(Sno3* e, int on, int32_t x, int32_t y, int32_t z, int32_t rea
   e->ballG.assign(g1024, g1024 + 1024);
 }
 uint32_t sno3_n(Sno3* e) { return e->n; }
+int sno3_write_state(Sno3* e, const int32_t* words, uint32_t n, uint64_t substeps, const uint32_t* chain) {
+  if (n > e->maxN) return -1;
+  e->ps.assign(n, P3{});
+  for (uint32_t i = 0; i < n; ++i) {
+    const int32_t* w = words + 8 * (size_t)i;
+    P3& q = e->ps[i];
+    q.p = V3{w[0], w[1], w[2]};
+    q.mat = (uint32_t)w[3];
+    q.v = V3{w[4], w[5], w[6]};
+    q.pr = q.p;
+  }
+  e->n = n;
+  e->cellOf.assign(n, 0);
+  e->sorted.assign(n, 0);
+  e->nbr.assign((size_t)n * MAXNBR, 0);
+  e->nbrN.assign(n, 0);
+  e->substeps = substeps;
+  if (chain) std::memcpy(e->chain, chain, 32);
+  return 0;
+}
 uint64_t sno3_substeps(Sno3* e) { return e->substeps; }
 void sno3_digest(Sno3* e, uint32_t acc[8]) { murmur3(*e, acc); }
 void sno3_chain(Sno3* e, uint32_t c[8]) { std::memcpy(c, e->chain, 32); }

@@ -108,7 +108,7 @@ class Sn3Opts(ctypes.Structure):
 class Sn3Scene(ctypes.Structure):
     _fields_ = [('n', ctypes.c_uint32), ('pos', ctypes.c_void_p), ('vel', ctypes.c_void_p),
                 ('mat', ctypes.c_void_p), ('gx', ctypes.c_uint32), ('gy', ctypes.c_uint32),
-                ('gz', ctypes.c_uint32), ('stir_amp', ctypes.c_int32)]
+                ('gz', ctypes.c_uint32), ('stir_amp', ctypes.c_int32), ('frame', ctypes.c_uint32)]
 
 
 class Sn3Info(ctypes.Structure):
@@ -177,6 +177,17 @@ SIGNATURES = {
     'sn3_get_info': (ctypes.c_int, [P, u32, ctypes.POINTER(Sn3Info)]),
     'sn3_last_timing': (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(u64)]),
     'sn3_profile_substep': (ctypes.c_int, [P, u32, P, u32, ctypes.POINTER(u32)]),
+    'sn_ckpt_pool_create': (ctypes.c_int, [ctypes.c_size_t, ctypes.c_int32, ctypes.POINTER(P)]),
+    'sn_ckpt_pool_destroy': (None, [P]),
+    'sn_ckpt_pool_last_error': (ctypes.c_char_p, [P]),
+    'sn_ckpt_pool_usage': (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)]),
+    'sn_ckpt_free': (ctypes.c_int, [P, u64]),
+    'sn_batch_ckpt_bytes': (ctypes.c_int, [P, u32, ctypes.POINTER(ctypes.c_size_t)]),
+    'sn_batch_ckpt_save': (ctypes.c_int, [P, u32, P, ctypes.POINTER(u64)]),
+    'sn_batch_ckpt_load': (ctypes.c_int, [P, u32, P, u64]),
+    'sn3_ckpt_bytes': (ctypes.c_int, [P, u32, ctypes.POINTER(ctypes.c_size_t)]),
+    'sn3_ckpt_save': (ctypes.c_int, [P, u32, P, ctypes.POINTER(u64)]),
+    'sn3_ckpt_load': (ctypes.c_int, [P, u32, P, u64]),
 }
 
 _lib = None

@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "../../include/suna.h"
+#include "ckptpool.h"
 #include "radix.cuh"
 #include "sim2d.cuh"
 
@@ -123,7 +124,10 @@ T* dalloc(size_t count, std::string& err) {
     err = std::string("cudaMalloc: ") + cudaGetErrorString(e);
     return nullptr;
   }
+  // The zeroing runs on the legacy default stream, which does not order with
+  // the engine's non-blocking stream: finish it before anything is queued there.
   cudaMemset(p, 0, count * sizeof(T));
+  cudaDeviceSynchronize();
   return static_cast<T*>(p);
 }
 
@@ -348,7 +352,32 @@ struct World {
   }
 
   // Recompute the colour-major key layout over the active scenes.
+  // The clocks in ScenePar (formClock, bondDirty, formNow, substep) advance on
+  // the device; before the host pushes the whole parameter array again (scene
+  // added or removed) it takes them back, except for a scene whose parameters
+  // the host has just written (freshScene).
+  uint32_t freshScene = 0xffffffffu;
+  bool paramsStale = false;
+  bool merge_device_clocks() {
+    if (!paramsStale) return true;
+    std::vector<ScenePar> dev(maxScenes);
+    if (!cuda_ok(cudaMemcpyAsync(dev.data(), b.scenes, sizeof(ScenePar) * maxScenes, cudaMemcpyDeviceToHost, st),
+                 "clocks") ||
+        !cuda_ok(cudaStreamSynchronize(st), "clocks"))
+      return false;
+    for (uint32_t s = 0; s < maxScenes; ++s) {
+      if (s == freshScene || !sh[s].used || !sh[s].loaded) continue;
+      hpar[s].formClock = dev[s].formClock;
+      hpar[s].bondDirty = dev[s].bondDirty;
+      hpar[s].formNow = dev[s].formNow;
+      hpar[s].substep = dev[s].substep;
+    }
+    paramsStale = false;
+    return true;
+  }
+
   bool relayout() {
+    if (!merge_device_clocks()) return false;
     uint32_t counts[4] = {0, 0, 0, 0};
     uint32_t slotEnd = 0, nAct = 0, numScenes = 0;
     for (uint32_t s = 0; s < maxScenes; ++s) {
@@ -396,7 +425,9 @@ struct World {
     if (!cuda_ok(cudaMemcpyAsync(hpar.data(), b.scenes, sizeof(ScenePar) * maxScenes, cudaMemcpyDeviceToHost, st),
                  "pull"))
       return false;
-    return cuda_ok(cudaStreamSynchronize(st), "pull");
+    if (!cuda_ok(cudaStreamSynchronize(st), "pull")) return false;
+    paramsStale = false;
+    return true;
   }
   bool push_scene(uint32_t s) {
     return cuda_ok(cudaMemcpyAsync(b.scenes + s, &hpar[s], sizeof(ScenePar), cudaMemcpyHostToDevice, st), "push");
@@ -509,7 +540,10 @@ struct World {
     cudaMemcpyAsync(b.accLast + s * 8, zero8, 32, cudaMemcpyHostToDevice, st);
     cudaMemsetAsync(b.dbg, 0, 64, st);
     cudaMemsetAsync(b.err, 0, 16, st);
-    return relayout();
+    freshScene = s;
+    bool ok2 = relayout();
+    freshScene = 0xffffffffu;
+    return ok2;
   }
 
   bool reset_chain(uint32_t s) {
@@ -691,6 +725,7 @@ struct World {
     for (auto& s : sh)
       if (s.used && s.loaded) s.substeps += count;
     lastLaunches = launchesPerSubstep * count;
+    paramsStale = true;
     return cuda_ok(cudaGetLastError(), "step");
   }
 
@@ -720,6 +755,7 @@ struct World {
       }
       for (auto& s2 : sh)
         if (s2.used && s2.loaded) s2.substeps += 1;
+      paramsStale = true;
     }
     for (auto& e : evs) cudaEventDestroy(e);
     uint32_t n = (uint32_t)std::max(0, used - 1);
@@ -885,6 +921,73 @@ struct World {
                   "the reference's");
     if (e[0] & ERR_BOND_PARTNER) return fail("a bond partner slot exceeds the 17-bit bond word");
     return true;
+  }
+
+  // Device checkpoint of scene s: [state n*8][stAcc n*2][chain 8][bond rows nFluid*48 when the
+  // world has bonding rows], copied on the engine stream.
+  size_t ckpt_bytes(uint32_t s) const {
+    const SceneHost& h = sh[s];
+    return (size_t)h.n * 40 + 32 + (hasBonds ? (size_t)h.nFluid * BOND_CAP * 4 : 0);
+  }
+  bool ckpt_save(uint32_t s, sn_ckpt_pool* pool, uint64_t* handle) {
+    SceneHost& h = sh[s];
+    if (!h.loaded) return fail("checkpoint of a scene that is not loaded");
+    if (pool->device != device) return fail("checkpoint pool is on device %d, the engine on %d", pool->device, device);
+    if (layoutDirty && !relayout()) return false;
+    if (!pull_params()) return false;
+    sn_ckpt_pool::Rec* r = nullptr;
+    if (!pool->reserve(ckpt_bytes(s), 2, handle, &r)) return fail("%s", pool->err.c_str());
+    char* d = pool->base + r->off;
+    const size_t n = h.n;
+    bool ok = cuda_ok(cudaMemcpyAsync(d, b.state + (size_t)h.slotBase * 8, n * 32, cudaMemcpyDeviceToDevice, st), "ckpt") &&
+              cuda_ok(cudaMemcpyAsync(d + n * 32, b.stacc + h.slotBase, n * 8, cudaMemcpyDeviceToDevice, st), "ckpt") &&
+              cuda_ok(cudaMemcpyAsync(d + n * 40, b.chain + (size_t)s * 8, 32, cudaMemcpyDeviceToDevice, st), "ckpt");
+    if (ok && hasBonds)
+      ok = cuda_ok(cudaMemcpyAsync(d + n * 40 + 32, b.bond + (size_t)h.slotBase * BOND_CAP,
+                                   (size_t)h.nFluid * BOND_CAP * 4, cudaMemcpyDeviceToDevice, st), "ckpt");
+    r->n = h.n;
+    r->nFluid = h.nFluid;
+    r->hasBonds = hasBonds ? 1u : 0u;
+    r->substeps = h.substeps;
+    r->formClock = hpar[s].formClock;
+    r->dirty = hpar[s].bondDirty;
+    cudaEventRecord(r->done, st);
+    if (!ok) {
+      pool->free_rec(*handle);
+      return false;
+    }
+    return true;
+  }
+  bool ckpt_load(uint32_t s, sn_ckpt_pool* pool, uint64_t handle) {
+    SceneHost& h = sh[s];
+    if (!h.loaded) return fail("checkpoint load into a scene that is not loaded");
+    sn_ckpt_pool::Rec* r = pool->find(handle);
+    if (!r || r->kind != 2) return fail("no 2D checkpoint %llu in the pool", (unsigned long long)handle);
+    if (r->n != h.n || r->nFluid != h.nFluid)
+      return fail("checkpoint holds n = %u, n_fluid = %u; the scene has n = %u, n_fluid = %u", r->n, r->nFluid, h.n,
+                  h.nFluid);
+    if (layoutDirty && !relayout()) return false;
+    if (!pull_params()) return false;
+    cudaStreamWaitEvent(st, r->done, 0);
+    const char* d = pool->base + r->off;
+    const size_t n = h.n;
+    bool ok = cuda_ok(cudaMemcpyAsync(b.state + (size_t)h.slotBase * 8, d, n * 32, cudaMemcpyDeviceToDevice, st), "load") &&
+              cuda_ok(cudaMemcpyAsync(b.stacc + h.slotBase, d + n * 32, n * 8, cudaMemcpyDeviceToDevice, st), "load") &&
+              cuda_ok(cudaMemcpyAsync(b.chain + (size_t)s * 8, d + n * 40, 32, cudaMemcpyDeviceToDevice, st), "load");
+    uint32_t* bondRows = b.bond + (size_t)h.slotBase * BOND_CAP;
+    if (ok && r->hasBonds)
+      ok = cuda_ok(cudaMemcpyAsync(bondRows, d + n * 40 + 32, (size_t)h.nFluid * BOND_CAP * 4,
+                                   cudaMemcpyDeviceToDevice, st), "load");
+    else if (ok)
+      ok = cuda_ok(cudaMemsetAsync(bondRows, 0, (size_t)h.nFluid * BOND_CAP * 4, st), "load");
+    cudaEventRecord(r->done, st);
+    if (!ok) return false;
+    h.substeps = r->substeps;
+    hpar[s].formClock = (uint32_t)r->formClock;
+    hpar[s].bondDirty = r->dirty;
+    hpar[s].substep = (uint32_t)r->substeps;
+    eventsDirty = true;
+    return push_scene(s) && cuda_ok(cudaStreamSynchronize(st), "load");
   }
 
   // Slot allocation for a new scene: first fit over released ranges.
@@ -1139,6 +1242,49 @@ int sn_batch_write_state(sn_batch* b, uint32_t id, const int32_t* state, const i
   w.hpar[id].substep = (uint32_t)substep_count;
   w.eventsDirty = true;
   return rc_of(w, w.push_scene(id) && w.cuda_ok(cudaStreamSynchronize(w.st), "write"));
+}
+int sn_ckpt_pool_create(size_t bytes, int32_t device, sn_ckpt_pool** out) {
+  if (!out || bytes == 0) return SN_E_INVALID;
+  *out = nullptr;
+  if (cudaSetDevice(device) != cudaSuccess) return SN_E_CUDA;
+  sn_ckpt_pool* p = new sn_ckpt_pool();
+  p->device = device;
+  p->cap = sn_ckpt_pool::round_up(bytes);
+  if (cudaMalloc(&p->base, p->cap) != cudaSuccess) {
+    fprintf(stderr, "[suna] checkpoint pool: cudaMalloc of %zu bytes failed\n", p->cap);
+    p->base = nullptr;
+    delete p;
+    return SN_E_CAPACITY;
+  }
+  p->freeList[0] = p->cap;
+  *out = p;
+  return SN_OK;
+}
+void sn_ckpt_pool_destroy(sn_ckpt_pool* p) { delete p; }
+const char* sn_ckpt_pool_last_error(const sn_ckpt_pool* p) { return p ? p->err.c_str() : "null pool"; }
+int sn_ckpt_pool_usage(const sn_ckpt_pool* p, size_t* used, size_t* capacity) {
+  if (!p) return SN_E_INVALID;
+  if (used) *used = p->used;
+  if (capacity) *capacity = p->cap;
+  return SN_OK;
+}
+int sn_ckpt_free(sn_ckpt_pool* p, uint64_t handle) {
+  if (!p) return SN_E_INVALID;
+  return p->free_rec(handle) ? SN_OK : SN_E_INVALID;
+}
+int sn_batch_ckpt_bytes(sn_batch* b, uint32_t id, size_t* bytes) {
+  if (!b || !bytes || id >= b->w.maxScenes || !b->w.sh[id].loaded) return SN_E_INVALID;
+  *bytes = b->w.ckpt_bytes(id);
+  return SN_OK;
+}
+int sn_batch_ckpt_save(sn_batch* b, uint32_t id, sn_ckpt_pool* p, uint64_t* handle) {
+  if (!b || !p || !handle || id >= b->w.maxScenes) return SN_E_INVALID;
+  if (b->w.ckpt_save(id, p, handle)) return SN_OK;
+  return b->w.err.rfind("checkpoint pool full", 0) == 0 ? SN_E_CAPACITY : rc_of(b->w, false);
+}
+int sn_batch_ckpt_load(sn_batch* b, uint32_t id, sn_ckpt_pool* p, uint64_t handle) {
+  if (!b || !p || id >= b->w.maxScenes) return SN_E_INVALID;
+  return rc_of(b->w, b->w.ckpt_load(id, p, handle));
 }
 int sn_batch_get_info(sn_batch* b, uint32_t id, sn_info* out) {
   if (!b || !out || id >= b->w.maxScenes || !b->w.sh[id].loaded) return SN_E_INVALID;

@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "../../include/suna.h"
+#include "ckptpool.h"
 #include "radix.cuh"
 #include "sim3d.cuh"
 
@@ -32,7 +33,10 @@ T* dalloc3(size_t count, std::string& err) {
     if (err.empty()) err = std::string("cudaMalloc: ") + cudaGetErrorString(e);
     return nullptr;
   }
+  // The zeroing runs on the legacy default stream, which does not order with
+  // the engine's non-blocking stream: finish it before anything is queued there.
   cudaMemset(p, 0, count * sizeof(T));
+  cudaDeviceSynchronize();
   return static_cast<T*>(p);
 }
 
@@ -50,6 +54,7 @@ struct Scene3Host {
   uint32_t slotBase = 0, cap = 0, n = 0;
   uint32_t gx = 1, gy = 1, gz = 1;
   int32_t stirAmp = 0;
+  uint32_t frame = 0;
   uint64_t substeps = 0;
   bool ballOn = false;
   int32_t ball[3] = {0, 0, 0};
@@ -232,6 +237,8 @@ struct Engine3 {
         p.wmax[2] = (int32_t)h.gz * H;
         p.stirPhase = (int32_t)((h.substeps * 384ull) & 131071ull);
         p.stirAmp = h.stirAmp;
+        p.substep = (uint32_t)h.substeps;
+        p.frame = h.frame;
         p.ballOn = h.ballOn ? 1u : 0u;
         p.ball[0] = h.ball[0];
         p.ball[1] = h.ball[1];
@@ -293,15 +300,11 @@ struct Engine3 {
       std::swap(cur, nxt);
       launches += 2;
     }
-    if (chainOn) {
-      k3_integrate<DBG, true><<<gA, 256, 0, st>>>(b, cur);
-      mark(nullptr);
-      k3_fold<<<(hw.numScenes + 63) / 64, 64, 0, st>>>(b);
-      launches += 2;
-    } else {
-      k3_integrate<DBG, false><<<gA, 256, 0, st>>>(b, cur);
-      ++launches;
-    }
+    if (chainOn) k3_integrate<DBG, true><<<gA, 256, 0, st>>>(b, cur);
+    else k3_integrate<DBG, false><<<gA, 256, 0, st>>>(b, cur);
+    mark(nullptr);
+    k3_fold<<<(hw.numScenes + 63) / 64, 64, 0, st>>>(b, chainOn ? 1 : 0);
+    launches += 2;
     mark(nullptr);
     launchesPerSubstep = (uint64_t)launches;
   }
@@ -318,7 +321,10 @@ struct Engine3 {
   // runSubsteps (3d/app.js:709-714): the stir phase is written once per call.
   bool upload_phase() {
     for (uint32_t s = 0; s < maxScenes; ++s)
-      if (sh[s].used && sh[s].loaded) hpar[s].stirPhase = (int32_t)((sh[s].substeps * 384ull) & 131071ull);
+      if (sh[s].used && sh[s].loaded) {
+        hpar[s].stirPhase = (int32_t)((sh[s].substeps * 384ull) & 131071ull);
+        hpar[s].substep = (uint32_t)sh[s].substeps;
+      }
     return cuda_ok(cudaMemcpyAsync(b.scenes, hpar.data(), sizeof(Scene3) * hw.numScenes, cudaMemcpyHostToDevice, st),
                    "params");
   }
@@ -450,6 +456,7 @@ struct Engine3 {
     h.gy = sc->gy;
     h.gz = sc->gz;
     h.stirAmp = sc->stir_amp;
+    h.frame = sc->frame;
     h.substeps = 0;
     h.loaded = true;
     layoutDirty = true;
@@ -570,6 +577,54 @@ struct Engine3 {
     h.substeps = substeps;
     layoutDirty = true;
     return true;
+  }
+
+  // Device checkpoint of scene s: [state n*8][chain 8] and the substep clock.
+  size_t ckpt_bytes(uint32_t s) const { return (size_t)sh[s].n * 32 + 32; }
+  bool ckpt_save(uint32_t s, sn_ckpt_pool* pool, uint64_t* handle) {
+    if (!check_scene(s)) return false;
+    if (pool->device != device) return fail("checkpoint pool is on device %d, the engine on %d", pool->device, device);
+    const Scene3Host& h = sh[s];
+    sn_ckpt_pool::Rec* r = nullptr;
+    if (!pool->reserve(ckpt_bytes(s), 3, handle, &r)) return fail("%s", pool->err.c_str());
+    char* d = pool->base + r->off;
+    bool ok = cuda_ok(cudaMemcpyAsync(d, b.state + (size_t)h.slotBase * 8, (size_t)h.n * 32, cudaMemcpyDeviceToDevice,
+                                      st), "ckpt") &&
+              cuda_ok(cudaMemcpyAsync(d + (size_t)h.n * 32, b.chain + (size_t)s * 8, 32, cudaMemcpyDeviceToDevice, st),
+                      "ckpt");
+    r->n = h.n;
+    r->substeps = h.substeps;
+    cudaEventRecord(r->done, st);
+    if (!ok) {
+      pool->free_rec(*handle);
+      return false;
+    }
+    return true;
+  }
+  bool ckpt_load(uint32_t s, sn_ckpt_pool* pool, uint64_t handle) {
+    if (!check_scene(s)) return false;
+    sn_ckpt_pool::Rec* r = pool->find(handle);
+    if (!r || r->kind != 3) return fail("no 3D checkpoint %llu in the pool", (unsigned long long)handle);
+    Scene3Host& h = sh[s];
+    if (r->n > h.cap) return fail("checkpoint holds %u particles, above this scene's capacity %u", r->n, h.cap);
+    cudaStreamWaitEvent(st, r->done, 0);
+    const char* d = pool->base + r->off;
+    bool ok = cuda_ok(cudaMemcpyAsync(b.state + (size_t)h.slotBase * 8, d, (size_t)r->n * 32, cudaMemcpyDeviceToDevice,
+                                      st), "load") &&
+              cuda_ok(cudaMemcpyAsync(b.chain + (size_t)s * 8, d + (size_t)r->n * 32, 32, cudaMemcpyDeviceToDevice, st),
+                      "load");
+    cudaEventRecord(r->done, st);
+    if (!ok) return false;
+    if (h.n != r->n) layoutDirty = true;
+    h.n = r->n;
+    h.substeps = r->substeps;
+    // the device copy of the substep clock follows the host one
+    hpar[s].substep = (uint32_t)h.substeps;
+    hpar[s].stirPhase = (int32_t)((h.substeps * 384ull) & 131071ull);
+    if (!layoutDirty &&
+        !cuda_ok(cudaMemcpyAsync(b.scenes + s, &hpar[s], sizeof(Scene3), cudaMemcpyHostToDevice, st), "load"))
+      return false;
+    return cuda_ok(cudaStreamSynchronize(st), "load");
   }
 
   bool timing(float* ms) {
@@ -704,6 +759,22 @@ int sn3_last_timing(sn3_engine* e, float* ms, uint64_t* launches) {
 int sn3_profile_substep(sn3_engine* e, uint32_t reps, float* ms, uint32_t max_phases, uint32_t* n_phases) {
   if (!e || !ms) return SN_E_INVALID;
   return rc3(e->w, e->w.profile(reps, ms, max_phases, n_phases));
+}
+
+int sn3_ckpt_bytes(sn3_engine* e, uint32_t scene, size_t* bytes) {
+  if (!e || !bytes) return SN_E_INVALID;
+  if (!e->w.check_scene(scene)) return SN_E_INVALID;
+  *bytes = e->w.ckpt_bytes(scene);
+  return SN_OK;
+}
+int sn3_ckpt_save(sn3_engine* e, uint32_t scene, sn_ckpt_pool* p, uint64_t* handle) {
+  if (!e || !p || !handle) return SN_E_INVALID;
+  if (e->w.ckpt_save(scene, p, handle)) return SN_OK;
+  return e->w.err.rfind("checkpoint pool full", 0) == 0 ? SN_E_CAPACITY : rc3(e->w, false);
+}
+int sn3_ckpt_load(sn3_engine* e, uint32_t scene, sn_ckpt_pool* p, uint64_t handle) {
+  if (!e || !p) return SN_E_INVALID;
+  return rc3(e->w, e->w.ckpt_load(scene, p, handle));
 }
 
 }  // extern "C"

@@ -51,7 +51,10 @@ struct Scene3 {
   uint32_t ballOn;
   int32_t ball[3];
   int32_t reach;
-  uint32_t active, pad[3];
+  uint32_t active;
+  uint32_t substep;  // this scene's substep counter (low 32 bits), advanced by k3_fold
+  uint32_t frame;    // 0: stir phase fixed per step call; F > 0: fixed per frame of F substeps
+  uint32_t pad;
 };
 
 struct World3 {
@@ -130,7 +133,9 @@ __global__ void __launch_bounds__(256) k3_predict(Bufs3 b) {
     const int32_t grav = __ldg(b.mats + m * 4 + 0), rhoW = __ldg(b.mats + m * 4 + 1), damp = __ldg(b.mats + m * 4 + 2);
     int32_t vx = v4.x, vy = sub_sat(v4.y, grav, f), vz = v4.z;
     if (S.stirAmp != 0) {
-      int32_t t0 = ((S.stirPhase + 32768) & 131071) - 65536;
+      const int32_t phase =
+          S.frame ? (int32_t)(((S.substep - S.substep % S.frame) * 384u) & 131071u) : S.stirPhase;
+      int32_t t0 = ((phase + 32768) & 131071) - 65536;
       int32_t tri = (t0 < 0 ? -t0 : t0) - 32768;
       vx = add_sat(vx, mul<16>(tri, S.stirAmp, f), f);
     }
@@ -367,10 +372,13 @@ __global__ void __launch_bounds__(256) k3_hash(Bufs3 b, uint32_t* __restrict__ a
   }
 }
 
-// Per-scene chain fold of this substep's digest (src/engine.js:4154 semantics).
-__global__ void k3_fold(Bufs3 b) {
+// Per-scene chain fold of this substep's digest (src/engine.js:4154 semantics)
+// and the scene's substep counter.
+__global__ void k3_fold(Bufs3 b, int doChain) {
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= b.world->numScenes || !b.scenes[s].active) return;
+  b.scenes[s].substep += 1u;
+  if (!doChain) return;
   uint32_t a[8], nx[8];
 #pragma unroll
   for (int j = 0; j < 8; ++j) a[j] = b.acc[s * 8 + j];

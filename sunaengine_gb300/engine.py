@@ -396,6 +396,20 @@ class Batch:
     def sync(self):
         self._check(self._lib.sn_batch_sync(self._h), 'sync')
 
+    # device keyframes (sn_batch_ckpt_*): see checkpoints.CheckpointPool
+    def ckpt_bytes(self, sid: int) -> int:
+        out = ctypes.c_size_t()
+        self._check(self._lib.sn_batch_ckpt_bytes(self._h, int(sid), ctypes.byref(out)), 'ckpt_bytes')
+        return int(out.value)
+
+    def ckpt_save(self, sid: int, pool) -> int:
+        out = ctypes.c_uint64()
+        self._check(self._lib.sn_batch_ckpt_save(self._h, int(sid), pool.h, ctypes.byref(out)), 'ckpt_save')
+        return int(out.value)
+
+    def ckpt_load(self, sid: int, pool, handle: int):
+        self._check(self._lib.sn_batch_ckpt_load(self._h, int(sid), pool.h, int(handle)), 'ckpt_load')
+
     def profile_substep(self, reps: int = 3) -> np.ndarray:
         out = np.zeros(64, np.float32)
         n = ctypes.c_uint32()

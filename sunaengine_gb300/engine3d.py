@@ -30,7 +30,7 @@ def _ptr(a: Optional[np.ndarray]):
 
 
 class _Scene3Args:
-    def __init__(self, sc: tables3d.Scene3D, stir_amp: int = 0):
+    def __init__(self, sc: tables3d.Scene3D, stir_amp: int = 0, frame: int = 0):
         n = int(sc.n)
         self.pos = np.ascontiguousarray(np.asarray(sc.pos).reshape(-1), dtype=np.int32)
         self.vel = np.ascontiguousarray(np.asarray(sc.vel).reshape(-1), dtype=np.int32)
@@ -39,7 +39,7 @@ class _Scene3Args:
             raise EngineError('3D scene array lengths must be n*3 / n*3 / n')
         self.c = _native.Sn3Scene(n=n, pos=self.pos.ctypes.data, vel=self.vel.ctypes.data,
                                   mat=self.mat.ctypes.data, gx=int(sc.gx), gy=int(sc.gy), gz=int(sc.gz),
-                                  stir_amp=int(stir_amp))
+                                  stir_amp=int(stir_amp), frame=int(frame))
 
 
 class Engine3D:
@@ -77,8 +77,8 @@ class Engine3D:
             raise EngineError(f'[aether-3d] {what}: {msg.decode() if msg else rc}')
 
     # ---- scenes -------------------------------------------------------------
-    def load_scene(self, sc: tables3d.Scene3D, stir_amp: int = 0) -> 'Engine3D':
-        a = _Scene3Args(sc, stir_amp)
+    def load_scene(self, sc: tables3d.Scene3D, stir_amp: int = 0, frame: int = 0) -> 'Engine3D':
+        a = _Scene3Args(sc, stir_amp, frame)
         self._check(self._lib.sn3_load_scene(self.h, ctypes.byref(a.c)), 'load_scene')
         self._seed = tables3d.SpawnSeed()
         return self
@@ -87,8 +87,8 @@ class Engine3D:
         """reset(n, scene) (3d/app.js:561-568): the page's starting column."""
         return self.load_scene(tables3d.initial_state(min(n, self.max_particles), scene, *grid), stir_amp)
 
-    def add_scene(self, sc: tables3d.Scene3D, cap: int = 0, stir_amp: int = 0) -> int:
-        a = _Scene3Args(sc, stir_amp)
+    def add_scene(self, sc: tables3d.Scene3D, cap: int = 0, stir_amp: int = 0, frame: int = 0) -> int:
+        a = _Scene3Args(sc, stir_amp, frame)
         out = ctypes.c_uint32()
         self._check(self._lib.sn3_add_scene(self.h, ctypes.byref(a.c), int(cap), ctypes.byref(out)), 'add_scene')
         return int(out.value)
@@ -180,6 +180,20 @@ class Engine3D:
 
     def chain_words(self, scene: int = 0) -> np.ndarray:
         return self._words(self._lib.sn3_chain, scene)
+
+    # device keyframes (sn3_ckpt_*): see checkpoints.CheckpointPool
+    def ckpt_bytes(self, scene: int = 0) -> int:
+        out = ctypes.c_size_t()
+        self._check(self._lib.sn3_ckpt_bytes(self.h, int(scene), ctypes.byref(out)), 'ckpt_bytes')
+        return int(out.value)
+
+    def ckpt_save(self, scene: int, pool) -> int:
+        out = ctypes.c_uint64()
+        self._check(self._lib.sn3_ckpt_save(self.h, int(scene), pool.h, ctypes.byref(out)), 'ckpt_save')
+        return int(out.value)
+
+    def ckpt_load(self, scene: int, pool, handle: int):
+        self._check(self._lib.sn3_ckpt_load(self.h, int(scene), pool.h, int(handle)), 'ckpt_load')
 
     def debug_counters(self) -> np.ndarray:
         a = np.zeros(16, np.uint32)
