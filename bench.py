@@ -334,12 +334,13 @@ def batched_workload(steps: int, warmup: int, device: int, plain_sample: int = 2
         for (at, cx, cy, r, ix, iy) in ev:
             b.schedule_impulse(sid, at, cx, cy, r, ix, iy)
     b.step(warmup)
+    tuned = b.autotune(1)
     b.sync()
     b.step(steps)
     ms, launches = b.last_timing()
     b.check_errors()
     batched = nf * steps / (ms / 1e3)
-    prof = b.profile_substep(2)
+    lanes_b = b.lanes()
     b.destroy()
     # plain path on a sample of the same scenes, one engine per scene, sequentially
     rng = np.random.Generator(np.random.PCG64(seed ^ 0x5a5a))
@@ -349,6 +350,7 @@ def batched_workload(steps: int, warmup: int, device: int, plain_sample: int = 2
         s = scs[int(k)]
         e = Engine(max_particles=s.n + 16, max_cells=1 << 20, device=device).load_scene(s)
         e.step(warmup)
+        e.autotune(1)
         e.sync()
         e.step(steps)
         t, _ = e.last_timing()
@@ -358,7 +360,7 @@ def batched_workload(steps: int, warmup: int, device: int, plain_sample: int = 2
     plain = pn / (pms / 1e3)
     return {'scenes': len(scs), 'particles': int(nf), 'value': batched, 'unit': UNIT,
             'ms_per_step': ms / steps, 'gpu_launches_per_step': launches // max(1, steps),
-            'plain_same_scenes': plain, 'plain_sample_scenes': int(len(pick)),
+            'plain_same_scenes': plain, 'plain_sample_scenes': int(len(pick)), 'lanes': lanes_b,
             'batched_vs_plain': batched / plain}
 
 
@@ -370,6 +372,7 @@ def ours(args):
     e = Engine(max_particles=sc.n, max_cells=1 << 20, device=local)
     e.load_scene(sc)
     e.step(args.warmup)
+    e.autotune(1)   # lane split per gather class, tuned on real (untimed) substeps
     e.sync()
     _barrier(dist)
     with ClockSampler(local) as clk:
@@ -381,6 +384,7 @@ def ours(args):
         wall = time.perf_counter() - t0
         _barrier(dist)
     dev_ms, launches = e.last_timing()
+    lanes_used = e.lanes()
     e.check_errors()
     dev_ms = _max_over_ranks(dist, dev_ms, local)
     ms_step = dev_ms / args.steps
@@ -438,7 +442,8 @@ def ours(args):
         'ms_per_step': ms_step, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
         'dtype': 'int32', 'data': 'synthetic',
         'config': {'workload': WORKLOAD, 'particles': sc.n, 'fluid_particles': sc.nFluid,
-                   'parallelism': 'replicas' if ws > 1 else 'single', 'l2': 'working set > L2, no flush'},
+                   'parallelism': 'replicas' if ws > 1 else 'single', 'l2': 'working set > L2, no flush',
+                   'lanes': lanes_used},
         'wall_ms_per_step': 1e3 * wall / args.steps,
         'gpu_launches': int(launches),
         'roofline': roof,

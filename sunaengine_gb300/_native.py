@@ -177,6 +177,10 @@ SIGNATURES = {
     'sn3_get_info': (ctypes.c_int, [P, u32, ctypes.POINTER(Sn3Info)]),
     'sn3_last_timing': (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(u64)]),
     'sn3_profile_substep': (ctypes.c_int, [P, u32, P, u32, ctypes.POINTER(u32)]),
+    'sn_autotune': (ctypes.c_int, [P, u32, ctypes.POINTER(u32)]),
+    'sn_batch_autotune': (ctypes.c_int, [P, u32, ctypes.POINTER(u32)]),
+    'sn_lanes': (ctypes.c_int, [P, P]),
+    'sn_batch_lanes': (ctypes.c_int, [P, P]),
     'sn_ckpt_pool_create': (ctypes.c_int, [ctypes.c_size_t, ctypes.c_int32, ctypes.POINTER(P)]),
     'sn_ckpt_pool_destroy': (None, [P]),
     'sn_ckpt_pool_last_error': (ctypes.c_char_p, [P]),

@@ -226,6 +226,7 @@ struct World {
     if (o->lanes != 0 && o->lanes != 1 && o->lanes != 2 && o->lanes != 4 && o->lanes != 8)
       return fail("lanes must be 0, 1, 2, 4 or 8");
     lanesOverride = (int)o->lanes;
+    autoLanes = o->lanes == 0;
     iters = o->iters;
     capSlots = o->max_particles;
     maxCells = o->max_cells ? o->max_cells : (1u << 20);
@@ -410,6 +411,7 @@ struct World {
     hw.slotEnd = slotEnd;
     hw.nAct = nAct;
     update_features();
+    default_lanes();
     hw.hasFriction = hasFriction;
     hw.hasBonds = hasBonds;
     layoutDirty = false;
@@ -552,6 +554,23 @@ struct World {
     return cuda_ok(cudaMemcpyAsync(b.chain + s * 8, CHAIN_INIT, 32, cudaMemcpyHostToDevice, st), "chain");
   }
 
+  // Resident CTAs per SM of a kernel at 256 threads (cached per kernel); a
+  // grid of numSMs x that runs in one wave and grid-strides over its items.
+  std::vector<std::pair<const void*, int>> occCache;
+  int occ_blocks(const void* k) {
+    for (auto& kv : occCache)
+      if (kv.first == k) return kv.second;
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, 256, 0) != cudaSuccess || nb < 1) nb = 1;
+    occCache.push_back({k, nb});
+    return nb;
+  }
+  int grid_occ(const void* k, uint64_t items) {
+    uint64_t g = (items + 255) / 256;
+    uint64_t cap = (uint64_t)numSMs * occ_blocks(k);
+    return (int)std::max<uint64_t>(1, std::min(g, cap));
+  }
+
   int grid_for(uint64_t items) const {
     uint64_t g = (items + 255) / 256;
     uint64_t cap = (uint64_t)numSMs * 8;
@@ -568,19 +587,51 @@ struct World {
 
   // Lanes per particle for the neighbour gathers: small scenes split each
   // neighbour list over several lanes so the GPU has enough threads in flight.
-  int lanes() const {
-    uint64_t n = hw.nAct;
-    if (n < 40000) return 8;
-    if (n < 80000) return 4;
-    if (n < 160000) return 2;
-    return 1;
-  }
+  // Lanes per particle for each gather class (solveA, the colour passes,
+  // post1, post2). Results do not depend on them (split sums are exact); only
+  // speed does, so the autotuner may try them on real substeps.
+  struct LaneCfg {
+    int a = 1, c = 1, p1 = 1, p2 = 1;
+  };
+  LaneCfg lanesCfg;
+  bool autoLanes = true, lanesTuned = false;
+  uint32_t tunedAtN = 0;
 
   template <bool DBG, int L>
-  void launch_substep_l() {
+  void launch_solveA(int lastIter) {
+    k_solveA<DBG, L><<<grid_occ((const void*)k_solveA<DBG, L>, (uint64_t)hw.nAct * L), 256, 0, st>>>(b, lastIter);
+  }
+  template <bool DBG, int L>
+  void launch_colours() {
+    const int g = grid_occ((const void*)k_colour<DBG, L>, (uint64_t)hw.nAct * L / 4 + 256);
+    for (int c = 0; c < 4; ++c) {
+      const int4* src = (c & 1) ? b.PL2 : b.PL;
+      int4* dst = (c & 1) ? b.PL : b.PL2;
+      k_colour<DBG, L><<<g, 256, 0, st>>>(b, c, src, dst);
+    }
+  }
+  template <bool DBG, int L>
+  void launch_post1() {
+    k_post1<DBG, L><<<grid_occ((const void*)k_post1<DBG, L>, (uint64_t)hw.nAct * L), 256, 0, st>>>(b);
+  }
+  template <bool DBG, bool HASH, int L>
+  void launch_post2(int formFlags) {
+    k_post2<DBG, HASH, L><<<grid_occ((const void*)k_post2<DBG, HASH, L>, (uint64_t)hw.nAct * L), 256, 0, st>>>(
+        b, formFlags);
+  }
+#define SN_LANES(LV, CALL)      \
+  switch (LV) {                 \
+    case 8: { constexpr int L_ = 8; CALL; } break; \
+    case 4: { constexpr int L_ = 4; CALL; } break; \
+    case 2: { constexpr int L_ = 2; CALL; } break; \
+    default: { constexpr int L_ = 1; CALL; } break; \
+  }
+
+  template <bool DBG>
+  void launch_substep() {
+    const LaneCfg lc = lanesCfg;
     const int gs = grid_for(hw.slotEnd);
     const int ga = grid_for(hw.nAct);
-    const int gl = grid_for((uint64_t)hw.nAct * L);
     uint64_t Lc = 0;
     if (anyEvents) {
       k_impulse_sched<<<hw.numScenes, 256, 0, st>>>(b, devEv, devEp);
@@ -598,17 +649,14 @@ struct World {
     k_cellstart<<<grid_for((uint64_t)hw.K + 1), 256, 0, st>>>(b);
     k_gather<<<ga, 256, 0, st>>>(b);
     mark();
-    k_nbr<DBG><<<ga, 256, 0, st>>>(b);
+    k_nbr<DBG><<<grid_occ((const void*)k_nbr<DBG>, hw.nAct), 256, 0, st>>>(b);
     mark();
     Lc += 3;
     for (uint32_t it = 0; it < iters; ++it) {
-      k_solveA<DBG, L><<<gl, 256, 0, st>>>(b, it + 1 == iters ? 1 : 0);
+      const int last = it + 1 == iters ? 1 : 0;
+      SN_LANES(lc.a, (launch_solveA<DBG, L_>(last)));
       mark();
-      for (int c = 0; c < 4; ++c) {
-        const int4* src = (c & 1) ? b.PL2 : b.PL;
-        int4* dst = (c & 1) ? b.PL : b.PL2;
-        k_colour<DBG, L><<<gl, 256, 0, st>>>(b, c, src, dst);
-      }
+      SN_LANES(lc.c, (launch_colours<DBG, L_>()));
       mark();
       Lc += 5;
       if (hasFriction) {
@@ -618,11 +666,11 @@ struct World {
       }
       mark();
     }
-    k_post1<DBG, L><<<gl, 256, 0, st>>>(b);
+    SN_LANES(lc.p1, (launch_post1<DBG, L_>()));
     ++Lc;
     mark();
     if (hasBonds) {
-      k_post2<DBG, false, L><<<gl, 256, 0, st>>>(b, 0);
+      SN_LANES(lc.p2, (launch_post2<DBG, false, L_>(0)));
       k_form1<DBG><<<ga, 256, 0, st>>>(b);
       k_form2<<<gs, 256, 0, st>>>(b);
       Lc += 3;
@@ -631,10 +679,10 @@ struct World {
         ++Lc;
       }
     } else if (chainOn) {
-      k_post2<DBG, true, L><<<gl, 256, 0, st>>>(b, 1);
+      SN_LANES(lc.p2, (launch_post2<DBG, true, L_>(1)));
       ++Lc;
     } else {
-      k_post2<DBG, false, L><<<gl, 256, 0, st>>>(b, 1);
+      SN_LANES(lc.p2, (launch_post2<DBG, false, L_>(1)));
       ++Lc;
     }
     mark();
@@ -643,15 +691,94 @@ struct World {
     mark();
     launchesPerSubstep = Lc;
   }
+#undef SN_LANES
 
-  template <bool DBG>
-  void launch_substep() {
-    switch (lanesOverride ? lanesOverride : lanes()) {
-      case 8: launch_substep_l<DBG, 8>(); break;
-      case 4: launch_substep_l<DBG, 4>(); break;
-      case 2: launch_substep_l<DBG, 2>(); break;
-      default: launch_substep_l<DBG, 1>(); break;
+  // Lanes before (or without) tuning, from the active particle count: each
+  // class is sized by the particles one launch works on and how heavy its
+  // per-particle epilogue is (measured on the 1 M-particle scene: solveA 1,
+  // colours 4, post1 2, post2 1).
+  static int lanes_for(uint64_t n) {
+    if (n < 40000) return 8;
+    if (n < 80000) return 4;
+    if (n < 160000) return 2;
+    return 1;
+  }
+  void default_lanes() {
+    if (!autoLanes) {
+      lanesCfg = LaneCfg{lanesOverride, lanesOverride, lanesOverride, lanesOverride};
+      return;
     }
+    if (lanesTuned && hw.nAct * 2 >= tunedAtN && hw.nAct <= tunedAtN * 2ull) return;
+    lanesTuned = false;
+    const uint64_t n = hw.nAct;
+    lanesCfg = LaneCfg{lanes_for(n), lanes_for(n / 16), lanes_for(n / 8), lanes_for(n)};
+  }
+
+  // The autotuner: run `per` real substeps under each uniform lane count with
+  // phase events, then keep the fastest count per gather class. Every lane
+  // count gives the same results, so the tuning substeps are ordinary
+  // substeps of the scenes (they count toward the caller's request).
+  bool autotune(uint32_t per, uint32_t* used) {
+    if (used) *used = 0;
+    if (!autoLanes) return true;  // lanes were pinned at create
+    bool any = false;
+    for (auto& s2 : sh) any |= (s2.used && s2.loaded);
+    if (!any) return fail("autotune before loadScene()");
+    if (layoutDirty && !relayout()) return false;
+    if (eventsDirty && !upload_events()) return false;
+    return tune_lanes(std::max(1u, per), used);
+  }
+
+  bool tune_lanes(uint32_t per, uint32_t* used) {
+    static const int cand[4] = {1, 2, 4, 8};
+    const int NE = 8 + 3 * (int)iters + 4;
+    std::vector<cudaEvent_t> evs(NE);
+    for (auto& e : evs) cudaEventCreate(&e);
+    double best[4] = {1e30, 1e30, 1e30, 1e30};
+    int pick[4] = {1, 1, 1, 1};
+    uint32_t n = 0;
+    bool ok = true;
+    for (int ci = 0; ci < 4 && ok; ++ci) {
+      lanesCfg = LaneCfg{cand[ci], cand[ci], cand[ci], cand[ci]};
+      double t[4] = {0, 0, 0, 0};
+      for (uint32_t r = 0; r < per && ok; ++r) {
+        pev = evs.data();
+        npev = 0;
+        launch_one();
+        int used2 = npev;
+        pev = nullptr;
+        ok = cuda_ok(cudaStreamSynchronize(st), "tune");
+        for (auto& s2 : sh)
+          if (s2.used && s2.loaded) s2.substeps += 1;
+        paramsStale = true;
+        ++n;
+        auto span = [&](int k) {
+          float ms = 0.f;
+          if (k + 1 < used2) cudaEventElapsedTime(&ms, evs[k], evs[k + 1]);
+          return (double)ms;
+        };
+        // phases: 0 predict, 1 sort, 2 ranges+gather, 3 nbr, then per
+        // iteration (solveA, colours, friction), then post1, post2, fold
+        for (uint32_t it = 0; it < iters; ++it) {
+          t[0] += span(4 + 3 * (int)it);
+          t[1] += span(5 + 3 * (int)it);
+        }
+        t[2] += span(4 + 3 * (int)iters);
+        t[3] += span(5 + 3 * (int)iters);
+      }
+      for (int k = 0; k < 4; ++k)
+        if (t[k] < best[k]) {
+          best[k] = t[k];
+          pick[k] = cand[ci];
+        }
+    }
+    for (auto& e : evs) cudaEventDestroy(e);
+    lanesCfg = LaneCfg{pick[0], pick[1], pick[2], pick[3]};
+    lanesTuned = true;
+    tunedAtN = hw.nAct;
+    graphValid = false;
+    if (used) *used = n;
+    return ok;
   }
 
   void launch_one() {
@@ -1242,6 +1369,26 @@ int sn_batch_write_state(sn_batch* b, uint32_t id, const int32_t* state, const i
   w.hpar[id].substep = (uint32_t)substep_count;
   w.eventsDirty = true;
   return rc_of(w, w.push_scene(id) && w.cuda_ok(cudaStreamSynchronize(w.st), "write"));
+}
+int sn_autotune(sn_engine* e, uint32_t reps, uint32_t* substeps_run) {
+  if (!e) return SN_E_INVALID;
+  return rc_of(e->w, e->w.autotune(reps, substeps_run));
+}
+int sn_batch_autotune(sn_batch* b, uint32_t reps, uint32_t* substeps_run) {
+  if (!b) return SN_E_INVALID;
+  return rc_of(b->w, b->w.autotune(reps, substeps_run));
+}
+int sn_lanes(sn_engine* e, uint32_t out[4]) {
+  if (!e || !out) return SN_E_INVALID;
+  const auto& c = e->w.lanesCfg;
+  out[0] = c.a; out[1] = c.c; out[2] = c.p1; out[3] = c.p2;
+  return SN_OK;
+}
+int sn_batch_lanes(sn_batch* b, uint32_t out[4]) {
+  if (!b || !out) return SN_E_INVALID;
+  const auto& c = b->w.lanesCfg;
+  out[0] = c.a; out[1] = c.c; out[2] = c.p1; out[3] = c.p2;
+  return SN_OK;
 }
 int sn_ckpt_pool_create(size_t bytes, int32_t device, sn_ckpt_pool** out) {
   if (!out || bytes == 0) return SN_E_INVALID;

@@ -483,27 +483,31 @@ __global__ void __launch_bounds__(256) k_colour(Bufs b, int colour, const int4* 
   const int c1 = (colour + 1) & 3, c3 = (colour + 3) & 3;
   const uint32_t lo1 = b.cellStart[cb[c1]], hi1 = b.cellStart[cb[c1 + 1]];
   const uint32_t lo3 = b.cellStart[cb[c3]], hi3 = b.cellStart[cb[c3 + 1]];
-  const uint32_t nAct = b.world->nAct;
+  // The grid covers this colour's range only (the launch is sized to the
+  // resident capacity); the copies of the neighbouring colours follow.
+  const uint32_t nC = hi - lo;
   const uint32_t sub = threadIdx.x & (L - 1), G = gstride() / L;
-  for (uint32_t p = gtid() / L;; p += G) {
-    if (__shfl_sync(0xffffffffu, p, 0) >= nAct) break;  // warp-uniform exit
-    const bool mine = p < hi && p >= lo;
+  for (uint32_t i = gtid() / L;; i += G) {
+    if (__shfl_sync(0xffffffffu, i, 0) >= nC) break;  // warp-uniform exit
+    const uint32_t p = lo + i;
+    const bool mine = i < nC;
     int4 me = mine ? src[p] : make_int4(0, 0, 0, (int32_t)INFO_BOUNDARY);
     const uint32_t info = (uint32_t)me.w;
     const bool act = mine && !(info & INFO_BOUNDARY);  // walls are identical in both buffers
     const uint32_t cnt = act ? (b.NBRN[p] & NBRN_COUNT) : 0u;
     int2 dp = solveB_dp<DBG, L>(b, src, act ? p : 0u, cnt, sub, xy(me), me.z, f);
-    if (sub != 0) continue;
-    if (act) {
-      int2 pr = xy(me);
-      if (!(info & INFO_PINNED)) {
-        const ScenePar& S = b.scenes[b.SCN[p]];
-        pr = apply_dp(b, S, info & INFO_MAT, pr, dp, f);
-      }
-      *reinterpret_cast<int2*>(dst + p) = pr;
-    } else if ((p >= lo1 && p < hi1) || (p >= lo3 && p < hi3)) {
-      *reinterpret_cast<int2*>(dst + p) = *reinterpret_cast<const int2*>(src + p);
+    if (sub != 0 || !act) continue;
+    int2 pr = xy(me);
+    if (!(info & INFO_PINNED)) {
+      const ScenePar& S = b.scenes[b.SCN[p]];
+      pr = apply_dp(b, S, info & INFO_MAT, pr, dp, f);
     }
+    *reinterpret_cast<int2*>(dst + p) = pr;
+  }
+  const uint32_t n1 = hi1 - lo1, n13 = n1 + (hi3 - lo3);
+  for (uint32_t i = gtid(); i < n13; i += gstride()) {
+    const uint32_t p = i < n1 ? lo1 + i : lo3 + (i - n1);
+    *reinterpret_cast<int2*>(dst + p) = *reinterpret_cast<const int2*>(src + p);
   }
 }
 

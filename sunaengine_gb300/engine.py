@@ -249,6 +249,18 @@ class Engine:
         self._check(self._lib.sn_last_timing(self._h, ctypes.byref(ms), ctypes.byref(l)), 'timing')
         return float(ms.value), int(l.value)
 
+    def autotune(self, reps: int = 1) -> int:
+        """Pick the gather lanes per kernel class on real substeps (the scene
+        advances by the returned count, exactly as step() would)."""
+        n = ctypes.c_uint32()
+        self._check(self._lib.sn_autotune(self._h, int(reps), ctypes.byref(n)), 'autotune')
+        return int(n.value)
+
+    def lanes(self):
+        a = np.zeros(4, np.uint32)
+        self._check(self._lib.sn_lanes(self._h, _ptr(a)), 'lanes')
+        return dict(zip(('solveA', 'colours', 'post1', 'post2'), (int(x) for x in a)))
+
     def profile_substep(self, reps: int = 3) -> np.ndarray:
         """Mean device ms per kernel phase over `reps` real substeps (profileSubstep)."""
         out = np.zeros(64, np.float32)
@@ -395,6 +407,16 @@ class Batch:
 
     def sync(self):
         self._check(self._lib.sn_batch_sync(self._h), 'sync')
+
+    def autotune(self, reps: int = 1) -> int:
+        n = ctypes.c_uint32()
+        self._check(self._lib.sn_batch_autotune(self._h, int(reps), ctypes.byref(n)), 'autotune')
+        return int(n.value)
+
+    def lanes(self):
+        a = np.zeros(4, np.uint32)
+        self._check(self._lib.sn_batch_lanes(self._h, _ptr(a)), 'lanes')
+        return dict(zip(('solveA', 'colours', 'post1', 'post2'), (int(x) for x in a)))
 
     # device keyframes (sn_batch_ckpt_*): see checkpoints.CheckpointPool
     def ckpt_bytes(self, sid: int) -> int:
