@@ -475,7 +475,7 @@ __device__ __forceinline__ int2 apply_dp(const Bufs& b, const ScenePar& S, uint3
 // and read again four phases later, so phase c copies colours c+1 and c-1.
 // After phase 3 buffer A is complete again.
 template <bool DBG, int L>
-__global__ void __launch_bounds__(256) k_colour(Bufs b, int colour, const int4* __restrict__ src,
+__global__ void __launch_bounds__(256, 8) k_colour(Bufs b, int colour, const int4* __restrict__ src,
                                                 int4* __restrict__ dst) {
   Flags<DBG> f{b.dbg};
   const uint32_t* cb = b.world->colourBase;
@@ -636,7 +636,7 @@ __global__ void __launch_bounds__(256) k_apply_fric(Bufs b) {
 // over the neighbour list. vtmp_j = clamp(pred_j - pos_j) is finalize's
 // velocity, recomputed where it is needed.
 template <bool DBG, int L>
-__global__ void __launch_bounds__(256) k_post1(Bufs b) {
+__global__ void __launch_bounds__(256, 5) k_post1(Bufs b) {
   Flags<DBG> f{b.dbg};
   __shared__ int4 smat[MAT_MAX];  // {xsph, cond, corrode, corrPt}
   for (int m = threadIdx.x; m < MAT_MAX; m += blockDim.x)
@@ -782,7 +782,7 @@ __device__ __forceinline__ void thermal(const Bufs& b, uint32_t i, int32_t heat,
 // 3059-3067) + the state digest. HASH=false when bond formation runs as its
 // own kernels (the digest then follows them).
 template <bool DBG, bool HASH, int L>
-__global__ void __launch_bounds__(256) k_post2(Bufs b, int formFlags) {
+__global__ void __launch_bounds__(256, 6) k_post2(Bufs b, int formFlags) {
   Flags<DBG> f{b.dbg};
   __shared__ int4 smat[MAT_MAX];  // {gammaCoh, gammaCur, adhesion, 0}
   for (int m = threadIdx.x; m < MAT_MAX; m += blockDim.x)
