@@ -188,7 +188,7 @@ int sn_batch_profile_substep(sn_batch* b, uint32_t reps, float* ms, uint32_t max
 
 /* ---- lane autotuner ----------------------------------------------------------
  * No counterpart in the reference. The neighbour gathers of solveA, the colour
- * passes, post1 and post2 can split each particle's list over 1, 2, 4 or 8
+ * passes, post1, post2 and the neighbour-list build can split each particle's list over 1, 2, 4 or 8
  * lanes; results are identical for every choice, speed is not. With
  * opts.lanes == 0 each class starts from a rule on the active particle count
  * (re-applied when the scene set changes by more than 2x); sn_autotune runs
@@ -196,11 +196,11 @@ int sn_batch_profile_substep(sn_batch* b, uint32_t reps, float* ms, uint32_t max
  * their chains exactly like sn_step) under each lane count with phase timers
  * and keeps the fastest count per class. *substeps_run receives how many
  * substeps it ran. With opts.lanes != 0 the lanes are pinned and it runs none.
- * sn_lanes reports {solveA, colours, post1, post2}. */
+ * sn_lanes reports {solveA, colours, post1, post2, neighbour lists}. */
 int sn_autotune(sn_engine* e, uint32_t reps, uint32_t* substeps_run);
 int sn_batch_autotune(sn_batch* b, uint32_t reps, uint32_t* substeps_run);
-int sn_lanes(sn_engine* e, uint32_t out[4]);
-int sn_batch_lanes(sn_batch* b, uint32_t out[4]);
+int sn_lanes(sn_engine* e, uint32_t out[5]);
+int sn_batch_lanes(sn_batch* b, uint32_t out[5]);
 
 /* ---- digest without device allocation ------------------------------------ */
 /* No counterpart in the reference. For callers that cannot allocate device

@@ -203,7 +203,7 @@ struct World {
     void* ptrs[] = {b.state, b.stacc, b.predSlot, b.sceneOf, b.keys, b.inv, b.bond, b.bondCand, b.skey,
                     b.sslot, b.cellStart, b.PL, b.PL2, b.RX, b.NQ, b.POS, b.SCN, b.DP, b.HEAT, b.CORR, b.NBR, b.NBRN,
                     (void*)b.luts, (void*)b.WG, (void*)b.CA, (void*)b.mats, (void*)b.rcp,
-                    b.scenes, b.world, b.acc, b.accLast, b.chain, b.dbg, b.err, tmpK, tmpV, hist,
+                    b.scenes, b.world, b.acc, b.accLast, b.chain, b.dbg, b.err, b.work, tmpK, tmpV, hist,
                     hits, accTmp, devEv, devEp};
     for (void* p : ptrs)
       if (p) cudaFree(p);
@@ -280,6 +280,7 @@ struct World {
     b.chain = dalloc<uint32_t>((size_t)scenesCap * 8, err);
     b.dbg = dalloc<uint32_t>(16, err);
     b.err = dalloc<uint32_t>(4, err);
+    b.work = dalloc<uint32_t>(4, err);
     tmpK = dalloc<uint32_t>(C, err);
     tmpV = dalloc<uint32_t>(C, err);
     hist = dalloc<uint32_t>(radix::hist_words((uint32_t)C), err);
@@ -462,6 +463,7 @@ struct World {
 
   // loadScene packing (src/engine.js:3704-3951) into scene s.
   bool load(uint32_t s, const sn_scene* sc) {
+    accFresh = false;
     SceneHost& h = sh[s];
     if (!validate_scene(sc, h.cap)) return false;
     uint32_t cs = 1u << sc->cell_shift;
@@ -591,7 +593,7 @@ struct World {
   // post1, post2). Results do not depend on them (split sums are exact); only
   // speed does, so the autotuner may try them on real substeps.
   struct LaneCfg {
-    int a = 1, c = 1, p1 = 1, p2 = 1;
+    int a = 1, c = 1, p1 = 1, p2 = 1, n = 1;
   };
   LaneCfg lanesCfg;
   bool autoLanes = true, lanesTuned = false;
@@ -609,6 +611,10 @@ struct World {
       int4* dst = (c & 1) ? b.PL : b.PL2;
       k_colour<DBG, L><<<g, 256, 0, st>>>(b, c, src, dst);
     }
+  }
+  template <bool DBG, int L>
+  void launch_nbr() {
+    k_nbr<DBG, L><<<grid_occ((const void*)k_nbr<DBG, L>, (uint64_t)hw.nAct * L), 256, 0, st>>>(b);
   }
   template <bool DBG, int L>
   void launch_post1() {
@@ -649,7 +655,7 @@ struct World {
     k_cellstart<<<grid_for((uint64_t)hw.K + 1), 256, 0, st>>>(b);
     k_gather<<<ga, 256, 0, st>>>(b);
     mark();
-    k_nbr<DBG><<<grid_occ((const void*)k_nbr<DBG>, hw.nAct), 256, 0, st>>>(b);
+    SN_LANES(lc.n, (launch_nbr<DBG, L_>()));
     mark();
     Lc += 3;
     for (uint32_t it = 0; it < iters; ++it) {
@@ -705,13 +711,13 @@ struct World {
   }
   void default_lanes() {
     if (!autoLanes) {
-      lanesCfg = LaneCfg{lanesOverride, lanesOverride, lanesOverride, lanesOverride};
+      lanesCfg = LaneCfg{lanesOverride, lanesOverride, lanesOverride, lanesOverride, lanesOverride};
       return;
     }
     if (lanesTuned && hw.nAct * 2 >= tunedAtN && hw.nAct <= tunedAtN * 2ull) return;
     lanesTuned = false;
     const uint64_t n = hw.nAct;
-    lanesCfg = LaneCfg{lanes_for(n), lanes_for(n / 16), lanes_for(n / 8), lanes_for(n)};
+    lanesCfg = LaneCfg{lanes_for(n), lanes_for(n / 16), lanes_for(n / 8), lanes_for(n), lanes_for(n / 8)};
   }
 
   // The autotuner: run `per` real substeps under each uniform lane count with
@@ -734,13 +740,13 @@ struct World {
     const int NE = 8 + 3 * (int)iters + 4;
     std::vector<cudaEvent_t> evs(NE);
     for (auto& e : evs) cudaEventCreate(&e);
-    double best[4] = {1e30, 1e30, 1e30, 1e30};
-    int pick[4] = {1, 1, 1, 1};
+    double best[5] = {1e30, 1e30, 1e30, 1e30, 1e30};
+    int pick[5] = {1, 1, 1, 1, 1};
     uint32_t n = 0;
     bool ok = true;
     for (int ci = 0; ci < 4 && ok; ++ci) {
-      lanesCfg = LaneCfg{cand[ci], cand[ci], cand[ci], cand[ci]};
-      double t[4] = {0, 0, 0, 0};
+      lanesCfg = LaneCfg{cand[ci], cand[ci], cand[ci], cand[ci], cand[ci]};
+      double t[5] = {0, 0, 0, 0, 0};
       for (uint32_t r = 0; r < per && ok; ++r) {
         pev = evs.data();
         npev = 0;
@@ -751,6 +757,7 @@ struct World {
         for (auto& s2 : sh)
           if (s2.used && s2.loaded) s2.substeps += 1;
         paramsStale = true;
+        accFresh = chainOn;
         ++n;
         auto span = [&](int k) {
           float ms = 0.f;
@@ -765,15 +772,16 @@ struct World {
         }
         t[2] += span(4 + 3 * (int)iters);
         t[3] += span(5 + 3 * (int)iters);
+        t[4] += span(3);
       }
-      for (int k = 0; k < 4; ++k)
+      for (int k = 0; k < 5; ++k)
         if (t[k] < best[k]) {
           best[k] = t[k];
           pick[k] = cand[ci];
         }
     }
     for (auto& e : evs) cudaEventDestroy(e);
-    lanesCfg = LaneCfg{pick[0], pick[1], pick[2], pick[3]};
+    lanesCfg = LaneCfg{pick[0], pick[1], pick[2], pick[3], pick[4]};
     lanesTuned = true;
     tunedAtN = hw.nAct;
     graphValid = false;
@@ -853,6 +861,7 @@ struct World {
       if (s.used && s.loaded) s.substeps += count;
     lastLaunches = launchesPerSubstep * count;
     paramsStale = true;
+    accFresh = chainOn;
     return cuda_ok(cudaGetLastError(), "step");
   }
 
@@ -883,6 +892,7 @@ struct World {
       for (auto& s2 : sh)
         if (s2.used && s2.loaded) s2.substeps += 1;
       paramsStale = true;
+      accFresh = chainOn;
     }
     for (auto& e : evs) cudaEventDestroy(e);
     uint32_t n = (uint32_t)std::max(0, used - 1);
@@ -897,7 +907,15 @@ struct World {
     return true;
   }
 
+  // accFresh: the last substep's digest (kept by the fold in accLast) is the
+  // digest of the current state, so digest() needs no hashing pass. Any call
+  // that changes a scene's state outside a substep clears it.
+  bool accFresh = false;
   bool digest(uint32_t s, uint32_t out[8]) {
+    if (accFresh && !layoutDirty) {
+      cudaMemcpyAsync(out, b.accLast + s * 8, 32, cudaMemcpyDeviceToHost, st);
+      return cuda_ok(cudaStreamSynchronize(st), "digest");
+    }
     if (layoutDirty && !relayout()) return false;
     cudaMemsetAsync(accTmp, 0, sizeof(uint32_t) * 8 * maxScenes, st);
     k_hash<<<grid_for(hw.slotEnd), 256, 0, st>>>(b, accTmp);
@@ -911,6 +929,7 @@ struct World {
 
   bool impulse_now(uint32_t s, int32_t cx, int32_t cy, int32_t r, int32_t ix, int32_t iy, uint32_t limit,
                    uint32_t* hitsOut) {
+    accFresh = false;
     ImpulseEv ev{0, cx, cy, r, ix, iy, limit, 0};
     k_impulse_now<<<1, 256, 0, st>>>(b, s, ev, hits);
     uint32_t h = 0;
@@ -922,6 +941,7 @@ struct World {
 
   // spawnFluid (src/engine.js:5901-6020) for scene s.
   bool spawn(uint32_t s, const sn_particle* list, uint32_t k, bool noWeld, uint32_t* nOut) {
+    accFresh = false;
     SceneHost& h = sh[s];
     if (!h.loaded) return fail("spawn before loadScene");
     if (k == 0) { if (nOut) *nOut = h.n; return true; }
@@ -989,6 +1009,7 @@ struct World {
 
   // setWalls (src/engine.js:5262-5305).
   bool set_walls(uint32_t s, bool want, bool* onOut) {
+    accFresh = false;
     SceneHost& h = sh[s];
     if (!h.loaded) return fail("setWalls before loadScene");
     const uint32_t nB = (uint32_t)(h.pos.size() / 2) - h.nFluid0;
@@ -1028,6 +1049,7 @@ struct World {
   }
 
   bool write_state(uint32_t s, const int32_t* state, const int32_t* scratch, size_t n) {
+    accFresh = false;
     SceneHost& h = sh[s];
     if (!h.loaded) return fail("write_state before loadScene");
     if (n != h.n) return fail("write_state: n = %zu but the loaded scene has %u", n, h.n);
@@ -1086,6 +1108,7 @@ struct World {
     return true;
   }
   bool ckpt_load(uint32_t s, sn_ckpt_pool* pool, uint64_t handle) {
+    accFresh = false;
     SceneHost& h = sh[s];
     if (!h.loaded) return fail("checkpoint load into a scene that is not loaded");
     sn_ckpt_pool::Rec* r = pool->find(handle);
@@ -1378,16 +1401,16 @@ int sn_batch_autotune(sn_batch* b, uint32_t reps, uint32_t* substeps_run) {
   if (!b) return SN_E_INVALID;
   return rc_of(b->w, b->w.autotune(reps, substeps_run));
 }
-int sn_lanes(sn_engine* e, uint32_t out[4]) {
+int sn_lanes(sn_engine* e, uint32_t out[5]) {
   if (!e || !out) return SN_E_INVALID;
   const auto& c = e->w.lanesCfg;
-  out[0] = c.a; out[1] = c.c; out[2] = c.p1; out[3] = c.p2;
+  out[0] = c.a; out[1] = c.c; out[2] = c.p1; out[3] = c.p2; out[4] = c.n;
   return SN_OK;
 }
-int sn_batch_lanes(sn_batch* b, uint32_t out[4]) {
+int sn_batch_lanes(sn_batch* b, uint32_t out[5]) {
   if (!b || !out) return SN_E_INVALID;
   const auto& c = b->w.lanesCfg;
-  out[0] = c.a; out[1] = c.c; out[2] = c.p1; out[3] = c.p2;
+  out[0] = c.a; out[1] = c.c; out[2] = c.p1; out[3] = c.p2; out[4] = c.n;
   return SN_OK;
 }
 int sn_ckpt_pool_create(size_t bytes, int32_t device, sn_ckpt_pool** out) {

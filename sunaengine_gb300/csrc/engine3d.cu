@@ -103,7 +103,7 @@ struct Engine3 {
     if (graph) cudaGraphDestroy(graph);
     void* ptrs[] = {b.state, b.sceneOf, b.PRS, b.keys, b.skey, b.sslot, b.cellStart, b.PW, b.PW2, b.PL, b.NBR,
                     b.NBRN, (void*)b.WG, (void*)b.PG, (void*)b.mats, (void*)b.rcp, b.scenes, b.world, b.acc,
-                    b.chain, b.dbg, tmpK, tmpV, hist, accTmp, fnvBuf, ballDev};
+                    b.accLast, b.chain, b.dbg, tmpK, tmpV, hist, accTmp, fnvBuf, ballDev};
     for (void* p : ptrs)
       if (p) cudaFree(p);
     if (ev0) cudaEventDestroy(ev0);
@@ -160,6 +160,7 @@ struct Engine3 {
     b.scenes = dalloc3<Scene3>(maxScenes, err);
     b.world = dalloc3<World3>(1, err);
     b.acc = dalloc3<uint32_t>((size_t)maxScenes * 8, err);
+    b.accLast = dalloc3<uint32_t>((size_t)maxScenes * 8, err);
     b.chain = dalloc3<uint32_t>((size_t)maxScenes * 8, err);
     b.dbg = dalloc3<uint32_t>(16, err);
     tmpK = dalloc3<uint32_t>(C, err);
@@ -355,6 +356,7 @@ struct Engine3 {
     for (auto& s : sh)
       if (s.used && s.loaded) s.substeps += count;
     lastLaunches = launchesPerSubstep * count;
+    accFresh = chainOn;
     return cuda_ok(cudaGetLastError(), "step");
   }
 
@@ -383,6 +385,7 @@ struct Engine3 {
       }
       for (auto& s2 : sh)
         if (s2.used && s2.loaded) s2.substeps += 1;
+      accFresh = chainOn;
     }
     for (auto& e : evs) cudaEventDestroy(e);
     uint32_t n = (uint32_t)std::max(0, used - 1);
@@ -423,6 +426,7 @@ struct Engine3 {
   }
 
   bool load(uint32_t s, const sn3_scene* sc) {
+    accFresh = false;
     if (!check_scene(s, false)) return false;
     if (!sc) return fail("scene is NULL");
     Scene3Host& h = sh[s];
@@ -473,6 +477,7 @@ struct Engine3 {
   // spawn (3d/app.js:575-597): append up to k particles (velocity zero) past
   // the scene's live count; what does not fit the capacity is dropped.
   bool spawn(uint32_t s, const int32_t* pos, const uint32_t* mat, uint32_t k, uint32_t* added) {
+    accFresh = false;
     if (!check_scene(s)) return false;
     if (k > 0 && (!pos || !mat)) return fail("pos and mat are required");
     Scene3Host& h = sh[s];
@@ -519,8 +524,15 @@ struct Engine3 {
     return true;
   }
 
+  // accFresh: the fold's last digest is the digest of the current state (set
+  // by stepping with the chain on, cleared by any change made outside a substep).
+  bool accFresh = false;
   bool digest(uint32_t s, uint32_t out[8]) {
     if (!check_scene(s)) return false;
+    if (accFresh && !layoutDirty) {
+      cudaMemcpyAsync(out, b.accLast + (size_t)s * 8, 32, cudaMemcpyDeviceToHost, st);
+      return cuda_ok(cudaStreamSynchronize(st), "digest");
+    }
     if (layoutDirty && !relayout()) return false;
     cudaMemsetAsync(accTmp, 0, sizeof(uint32_t) * 8 * maxScenes, st);
     k3_hash<<<grid_for(hw.slotEnd), 256, 0, st>>>(b, accTmp);
@@ -563,6 +575,7 @@ struct Engine3 {
   // solver's other fields are rewritten before they are read), plus the
   // substep count (for the stir phase) and the chain.
   bool write_state(uint32_t s, const int32_t* state, uint32_t n, uint64_t substeps, const uint32_t* chainIn) {
+    accFresh = false;
     if (!check_scene(s)) return false;
     Scene3Host& h = sh[s];
     if (n > h.cap) return fail("state has %u particles, above capacity %u", n, h.cap);
@@ -602,6 +615,7 @@ struct Engine3 {
     return true;
   }
   bool ckpt_load(uint32_t s, sn_ckpt_pool* pool, uint64_t handle) {
+    accFresh = false;
     if (!check_scene(s)) return false;
     sn_ckpt_pool::Rec* r = pool->find(handle);
     if (!r || r->kind != 3) return fail("no 3D checkpoint %llu in the pool", (unsigned long long)handle);

@@ -140,6 +140,7 @@ struct Bufs {
   uint32_t* chain;      // [S * 8]
   uint32_t* dbg;        // [16]
   uint32_t* err;        // [4]
+  uint32_t* work;       // [4] per-substep flags: [0] = some particle has a friction/bond row
 };
 
 enum : uint32_t { ERR_UNSUPPORTED_ROW = 1u, ERR_BOND_PARTNER = 2u };
@@ -253,6 +254,7 @@ template <bool DBG>
 __global__ void __launch_bounds__(256) k_predict_key(Bufs b) {
   Flags<DBG> f{b.dbg};
   const uint32_t K = b.world->K, slotEnd = b.world->slotEnd;
+  if (gtid() == 0) b.work[0] = 0u;  // set again by k_gather
   for (uint32_t slot = gtid(); slot < slotEnd; slot += gstride()) {
     uint32_t s = b.sceneOf[slot];
     const ScenePar& S = b.scenes[s];
@@ -312,6 +314,12 @@ __global__ void __launch_bounds__(256) k_gather(Bufs b) {
     b.POS[p] = make_int2(a.x, a.y);
     b.SCN[p] = s;
     b.inv[slot] = p;
+    const uint32_t m = (uint32_t)rec.w & INFO_MAT;
+    // the particles k_friction or k_apply_fric would touch (a superset of each)
+    const bool fr = !((uint32_t)rec.w & INFO_BOUNDARY) && (matw(b, m, M_fric) != 0 || matw(b, m, M_bondK) != 0);
+    const unsigned bal = __ballot_sync(__activemask(), fr);
+    if (fr && (threadIdx.x & 31u) == (unsigned)(__ffs(bal) - 1) && *(volatile uint32_t*)b.work == 0u)
+      atomicOr(b.work, 1u);
   }
 }
 
@@ -320,43 +328,106 @@ __global__ void __launch_bounds__(256) k_gather(Bufs b) {
 // kernel range; keep the first MAXNBR in that order (dbg[6] counts the rest).
 // Wall particles only need their truncation count, so their lists are only
 // walked in debug mode.
-template <bool DBG>
+//
+// L lanes share one particle: they test L consecutive candidates of a cell at
+// once and place the hits with a ballot prefix, so the list keeps exactly the
+// sequential order (and the same MAXNBR cut) whatever L is.
+template <bool DBG, int L>
 __global__ void __launch_bounds__(256) k_nbr(Bufs b) {
+  if constexpr (L == 1) {
+    Flags<DBG> f{b.dbg};
+    const uint32_t nAct = b.world->nAct, stride = b.nbrStride;
+    for (uint32_t p = gtid(); p < nAct; p += gstride()) {
+      int4 me = b.PL[p];
+      uint32_t info = (uint32_t)me.w;
+      bool bnd = (info & INFO_BOUNDARY) != 0;
+      if ((bnd && !DBG) || (info & INFO_DEAD)) { b.NBRN[p] = 0; continue; }
+      const ScenePar& S = b.scenes[b.SCN[p]];
+      int2 pi = xy(me);
+      int2 cc = cell_coord(S, pi);
+      uint32_t cnt = 0;
+      bool congeal = false;
+      uint32_t* out = b.NBR + p;
+      for (int dy = -1; dy <= 1; ++dy) {
+        int32_t gy = cc.y + dy;
+        if (gy < 0 || gy >= (int32_t)S.gridH) continue;
+        for (int dx = -1; dx <= 1; ++dx) {
+          int32_t gx = cc.x + dx;
+          if (gx < 0 || gx >= (int32_t)S.gridW) continue;
+          uint32_t key = key_of(S, gx, gy);
+          uint32_t lo = b.cellStart[key], hi = b.cellStart[key + 1];
+          for (uint32_t q = lo; q < hi; ++q) {
+            if (q == p) continue;
+            int4 o = b.PL[q];
+            uint32_t iq = (uint32_t)o.w;
+            if (iq & INFO_DEAD) continue;
+            if (lut_index(pdelta(pi, xy(o), f), f) < 0) continue;
+            if (!(iq & INFO_BOUNDARY) && (iq & INFO_CONGEAL)) congeal = true;
+            if (cnt >= (uint32_t)MAXNBR) { f.flag(6); continue; }
+            if (!bnd) out[(size_t)cnt * stride] = q | (iq & INFO_BOUNDARY);
+            cnt++;
+          }
+        }
+      }
+      b.NBRN[p] = bnd ? 0u : (cnt | (congeal ? NBRN_CONGEAL : 0u));
+    }
+    return;
+  }
   Flags<DBG> f{b.dbg};
   const uint32_t nAct = b.world->nAct, stride = b.nbrStride;
-  for (uint32_t p = gtid(); p < nAct; p += gstride()) {
-    int4 me = b.PL[p];
-    uint32_t info = (uint32_t)me.w;
-    bool bnd = (info & INFO_BOUNDARY) != 0;
-    if ((bnd && !DBG) || (info & INFO_DEAD)) { b.NBRN[p] = 0; continue; }
-    const ScenePar& S = b.scenes[b.SCN[p]];
-    int2 pi = xy(me);
-    int2 cc = cell_coord(S, pi);
+  const uint32_t lane = threadIdx.x & 31u, sub = lane & (L - 1);
+  const uint32_t gmask = (L == 32 ? 0xffffffffu : ((1u << L) - 1u)) << (lane & ~(uint32_t)(L - 1));
+  const uint32_t below = (1u << lane) - 1u;
+  const uint32_t G = gstride() / L;
+  for (uint32_t p = gtid() / L;; p += G) {
+    if (__shfl_sync(0xffffffffu, p, 0) >= nAct) break;  // warp-uniform exit
+    const bool valid = p < nAct;
+    const int4 me = valid ? b.PL[p] : make_int4(0, 0, 0, (int32_t)INFO_DEAD);
+    const uint32_t info = (uint32_t)me.w;
+    const bool bnd = (info & INFO_BOUNDARY) != 0;
+    const bool work = valid && !((bnd && !DBG) || (info & INFO_DEAD));
+    const ScenePar& S = b.scenes[work ? b.SCN[p] : 0u];
+    const int2 pi = xy(me);
+    const int2 cc = work ? cell_coord(S, pi) : make_int2(0, 0);
     uint32_t cnt = 0;
     bool congeal = false;
     uint32_t* out = b.NBR + p;
     for (int dy = -1; dy <= 1; ++dy) {
-      int32_t gy = cc.y + dy;
-      if (gy < 0 || gy >= (int32_t)S.gridH) continue;
       for (int dx = -1; dx <= 1; ++dx) {
-        int32_t gx = cc.x + dx;
-        if (gx < 0 || gx >= (int32_t)S.gridW) continue;
-        uint32_t key = key_of(S, gx, gy);
-        uint32_t lo = b.cellStart[key], hi = b.cellStart[key + 1];
-        for (uint32_t q = lo; q < hi; ++q) {
-          if (q == p) continue;
-          int4 o = b.PL[q];
-          uint32_t iq = (uint32_t)o.w;
-          if (iq & INFO_DEAD) continue;
-          if (lut_index(pdelta(pi, xy(o), f), f) < 0) continue;
-          if (!(iq & INFO_BOUNDARY) && (iq & INFO_CONGEAL)) congeal = true;
-          if (cnt >= (uint32_t)MAXNBR) { f.flag(6); continue; }
-          if (!bnd) out[(size_t)cnt * stride] = q | (iq & INFO_BOUNDARY);
-          cnt++;
+        const int32_t gy = cc.y + dy, gx = cc.x + dx;
+        uint32_t lo = 0, len = 0;
+        if (work && gy >= 0 && gy < (int32_t)S.gridH && gx >= 0 && gx < (int32_t)S.gridW) {
+          const uint32_t key = key_of(S, gx, gy);
+          lo = b.cellStart[key];
+          len = b.cellStart[key + 1] - lo;
+        }
+        const uint32_t maxLen = L == 1 ? len : __reduce_max_sync(0xffffffffu, len);
+        for (uint32_t t = sub; t - sub < maxLen; t += L) {
+          const uint32_t q = lo + t;
+          bool hit = false;
+          uint32_t iq = 0;
+          if (t < len && q != p) {
+            const int4 o = b.PL[q];
+            iq = (uint32_t)o.w;
+            hit = !(iq & INFO_DEAD) && lut_index(pdelta(pi, xy(o), f), f) >= 0;
+          }
+          uint32_t pos = cnt, nhit = hit ? 1u : 0u;
+          if (L > 1) {
+            const uint32_t bal = __ballot_sync(0xffffffffu, hit) & gmask;
+            pos = cnt + __popc(bal & below);
+            nhit = __popc(bal);
+          }
+          if (hit) {
+            if (!(iq & INFO_BOUNDARY) && (iq & INFO_CONGEAL)) congeal = true;
+            if (pos >= (uint32_t)MAXNBR) f.flag(6);
+            else if (!bnd) out[(size_t)pos * stride] = q | (iq & INFO_BOUNDARY);
+          }
+          cnt += nhit;
         }
       }
     }
-    b.NBRN[p] = bnd ? 0u : (cnt | (congeal ? NBRN_CONGEAL : 0u));
+    if (L > 1) congeal = (__ballot_sync(0xffffffffu, congeal) & gmask) != 0u;
+    if (valid && sub == 0) b.NBRN[p] = (bnd || !work) ? 0u : (min(cnt, (uint32_t)MAXNBR) | (congeal ? NBRN_CONGEAL : 0u));
   }
 }
 
@@ -521,6 +592,7 @@ __device__ __forceinline__ bool friction_row(const Bufs& b, uint32_t m) {
 }
 template <bool DBG>
 __global__ void __launch_bounds__(256) k_friction(Bufs b) {
+  if (*b.work == 0u) return;  // no particle has a friction or bond row this substep
   Flags<DBG> f{b.dbg};
   const uint32_t nAct = b.world->nAct, stride = b.nbrStride;
   for (uint32_t p = gtid(); p < nAct; p += gstride()) {
@@ -617,6 +689,7 @@ __global__ void __launch_bounds__(256) k_friction(Bufs b) {
 
 template <bool DBG>
 __global__ void __launch_bounds__(256) k_apply_fric(Bufs b) {
+  if (*b.work == 0u) return;
   Flags<DBG> f{b.dbg};
   const uint32_t nAct = b.world->nAct;
   for (uint32_t p = gtid(); p < nAct; p += gstride()) {

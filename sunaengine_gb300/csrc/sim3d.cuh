@@ -76,7 +76,7 @@ struct Bufs3 {
   const uint16_t* rcp;
   Scene3* scenes;
   World3* world;
-  uint32_t *acc, *chain, *dbg;
+  uint32_t *acc, *accLast, *chain, *dbg;
 };
 
 __device__ __forceinline__ uint32_t gstride3() { return gridDim.x * blockDim.x; }
@@ -387,6 +387,7 @@ __global__ void k3_fold(Bufs3 b, int doChain) {
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
     b.chain[s * 8 + j] = nx[j];
+    b.accLast[s * 8 + j] = a[j];
     b.acc[s * 8 + j] = 0u;
   }
 }

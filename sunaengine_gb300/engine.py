@@ -257,9 +257,9 @@ class Engine:
         return int(n.value)
 
     def lanes(self):
-        a = np.zeros(4, np.uint32)
+        a = np.zeros(5, np.uint32)
         self._check(self._lib.sn_lanes(self._h, _ptr(a)), 'lanes')
-        return dict(zip(('solveA', 'colours', 'post1', 'post2'), (int(x) for x in a)))
+        return dict(zip(('solveA', 'colours', 'post1', 'post2', 'nbr'), (int(x) for x in a)))
 
     def profile_substep(self, reps: int = 3) -> np.ndarray:
         """Mean device ms per kernel phase over `reps` real substeps (profileSubstep)."""
@@ -414,9 +414,9 @@ class Batch:
         return int(n.value)
 
     def lanes(self):
-        a = np.zeros(4, np.uint32)
+        a = np.zeros(5, np.uint32)
         self._check(self._lib.sn_batch_lanes(self._h, _ptr(a)), 'lanes')
-        return dict(zip(('solveA', 'colours', 'post1', 'post2'), (int(x) for x in a)))
+        return dict(zip(('solveA', 'colours', 'post1', 'post2', 'nbr'), (int(x) for x in a)))
 
     # device keyframes (sn_batch_ckpt_*): see checkpoints.CheckpointPool
     def ckpt_bytes(self, sid: int) -> int:

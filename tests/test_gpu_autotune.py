@@ -13,7 +13,7 @@ def test_autotune_keeps_the_chain():
     ran = a.autotune(1)
     assert ran == 4
     lanes = a.lanes()
-    assert set(lanes) == {'solveA', 'colours', 'post1', 'post2'}
+    assert set(lanes) == {'solveA', 'colours', 'post1', 'post2', 'nbr'}
     assert all(v in (1, 2, 4, 8) for v in lanes.values())
     a.step(6)
     b = Engine(max_particles=sc.n, lanes=1).load_scene(sc)
