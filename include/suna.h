@@ -250,6 +250,9 @@ typedef struct sn3_opts {
   const int32_t* luts;    /* W[2049] | G[2049] | planeW[513] | planeG[513] (buildLUTs, 3d/app.js:85-160) */
   const int32_t* mats;    /* mat_count rows of 4: grav, rhoW, damp, f0 (3d/app.js:180-201) */
   uint32_t mat_count;     /* 1..256; rhoW in -256..3839 */
+  uint32_t lanes;         /* lanes per particle in the density and solve gathers: 1, 2 or 4;
+                             0 = chosen from the active particle count. Results do not depend
+                             on it. */
 } sn3_opts;
 
 typedef struct sn3_scene {

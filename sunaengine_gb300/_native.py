@@ -102,7 +102,7 @@ class Sn3Opts(ctypes.Structure):
     _fields_ = [('max_particles', ctypes.c_uint32), ('max_cells', ctypes.c_uint32),
                 ('max_scenes', ctypes.c_uint32), ('iters', ctypes.c_uint32), ('debug', ctypes.c_uint32),
                 ('chain', ctypes.c_uint32), ('device', ctypes.c_int32), ('luts', ctypes.c_void_p),
-                ('mats', ctypes.c_void_p), ('mat_count', ctypes.c_uint32)]
+                ('mats', ctypes.c_void_p), ('mat_count', ctypes.c_uint32), ('lanes', ctypes.c_uint32)]
 
 
 class Sn3Scene(ctypes.Structure):

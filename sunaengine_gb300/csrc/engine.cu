@@ -650,7 +650,7 @@ struct World {
     int bits = 1;
     while ((1ull << bits) <= hw.K) ++bits;
     radix::sort_pairs(b.keys, hw.slotEnd, bits, b.skey, b.sslot, tmpK, tmpV, hist, st);
-    Lc += 3ull * ((bits + radix::RBITS - 1) / radix::RBITS);
+    Lc += (uint64_t)radix::LAUNCHES_PER_PASS * ((bits + radix::RBITS - 1) / radix::RBITS);
     mark();
     k_cellstart<<<grid_for((uint64_t)hw.K + 1), 256, 0, st>>>(b);
     k_gather<<<ga, 256, 0, st>>>(b);

@@ -119,6 +119,8 @@ struct Engine3 {
     if (!o->luts || !o->mats) return fail("luts and mats are required");
     if (o->mat_count < 1 || o->mat_count > MAT3_MAX) return fail("mat_count must be 1..%u", MAT3_MAX);
     maxScenes = o->max_scenes ? o->max_scenes : 1;
+    if (o->lanes != 0 && o->lanes != 1 && o->lanes != 2 && o->lanes != 4) return fail("lanes must be 0, 1, 2 or 4");
+    lanesPin = (int)o->lanes;
     if (maxScenes > (1u << 19)) return fail("max_scenes above 2^19");
     for (uint32_t m = 0; m < o->mat_count; ++m) {
       int32_t rhoW = o->mats[m * 4 + 1];
@@ -209,6 +211,33 @@ struct Engine3 {
     }
   }
 
+  // Lanes per particle in the density and solve gathers (results do not
+  // depend on them), and resident CTAs per SM per kernel for one-wave grids.
+  int lanesD = 1, lanesS = 1, lanesN = 1, lanesPin = 0;
+  bool lanesTuned = false;
+  std::vector<std::pair<const void*, int>> occCache;
+  int grid_occ(const void* k, uint64_t items) {
+    int nb = 0;
+    for (auto& kv : occCache)
+      if (kv.first == k) nb = kv.second;
+    if (!nb) {
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, 256, 0) != cudaSuccess || nb < 1) nb = 1;
+      occCache.push_back({k, nb});
+    }
+    uint64_t g = (items + 255) / 256;
+    return (int)std::max<uint64_t>(1, std::min<uint64_t>(g, (uint64_t)numSMs * nb));
+  }
+  void default_lanes() {
+    if (lanesPin) {
+      lanesD = lanesS = lanesN = lanesPin;
+      return;
+    }
+    if (lanesTuned) return;
+    const uint32_t n = hw.nAct;
+    lanesD = lanesS = n < 65536 ? 4 : (n < 131072 ? 2 : 1);
+    lanesN = 1;  // measured: the split list build only pays off at L = 1 on a full GPU
+  }
+
   uint32_t grid_for(uint32_t n) const {
     uint32_t g = (n + 255) / 256;
     return std::max(1u, std::min(g, (uint32_t)numSMs * 64u));
@@ -254,6 +283,7 @@ struct Engine3 {
     }
     if (K > maxCells) return fail("the scenes need %u grid cells, above max_cells = %u", K, maxCells);
     hw = World3{numScenes, K, slotEnd, nAct};
+    default_lanes();
     std::vector<uint32_t> sceneOf(std::max(slotEnd, 1u), NO_SCENE);
     for (uint32_t s = 0; s < maxScenes; ++s)
       if (sh[s].used && sh[s].loaded)
@@ -282,21 +312,33 @@ struct Engine3 {
     mark(nullptr);
     int keyBits = 32 - __builtin_clz(std::max(hw.K, 1u));
     radix::sort_pairs(b.keys, hw.slotEnd, keyBits, b.skey, b.sslot, tmpK, tmpV, hist, st);
-    launches += 3 * std::max(1, (keyBits + radix::RBITS - 1) / radix::RBITS);
+    launches += radix::LAUNCHES_PER_PASS * std::max(1, (keyBits + radix::RBITS - 1) / radix::RBITS);
     mark(nullptr);
     k3_cellstart<<<gK, 256, 0, st>>>(b);
     k3_gather<<<gA, 256, 0, st>>>(b);
     launches += 2;
     mark(nullptr);
-    k3_nbr<DBG><<<gA, 256, 0, st>>>(b);
+    switch (lanesN) {
+      case 4: k3_nbr<DBG, 4><<<grid_occ((const void*)k3_nbr<DBG, 4>, (uint64_t)hw.nAct * 4), 256, 0, st>>>(b); break;
+      case 2: k3_nbr<DBG, 2><<<grid_occ((const void*)k3_nbr<DBG, 2>, (uint64_t)hw.nAct * 2), 256, 0, st>>>(b); break;
+      default: k3_nbr<DBG, 1><<<grid_occ((const void*)k3_nbr<DBG, 1>, hw.nAct), 256, 0, st>>>(b); break;
+    }
     ++launches;
     mark(nullptr);
     int4* cur = b.PW;
     int4* nxt = b.PW2;
     for (uint32_t it = 0; it < iters; ++it) {
-      k3_density<DBG><<<gA, 256, 0, st>>>(b, cur);
+      switch (lanesD) {
+        case 4: k3_density<DBG, 4><<<grid_occ((const void*)k3_density<DBG, 4>, (uint64_t)hw.nAct * 4), 256, 0, st>>>(b, cur); break;
+        case 2: k3_density<DBG, 2><<<grid_occ((const void*)k3_density<DBG, 2>, (uint64_t)hw.nAct * 2), 256, 0, st>>>(b, cur); break;
+        default: k3_density<DBG, 1><<<grid_occ((const void*)k3_density<DBG, 1>, hw.nAct), 256, 0, st>>>(b, cur); break;
+      }
       mark(nullptr);
-      k3_solve<DBG><<<gA, 256, 0, st>>>(b, cur, nxt);
+      switch (lanesS) {
+        case 4: k3_solve<DBG, 4><<<grid_occ((const void*)k3_solve<DBG, 4>, (uint64_t)hw.nAct * 4), 256, 0, st>>>(b, cur, nxt); break;
+        case 2: k3_solve<DBG, 2><<<grid_occ((const void*)k3_solve<DBG, 2>, (uint64_t)hw.nAct * 2), 256, 0, st>>>(b, cur, nxt); break;
+        default: k3_solve<DBG, 1><<<grid_occ((const void*)k3_solve<DBG, 1>, hw.nAct), 256, 0, st>>>(b, cur, nxt); break;
+      }
       mark(nullptr);
       std::swap(cur, nxt);
       launches += 2;

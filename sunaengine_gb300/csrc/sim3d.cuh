@@ -168,39 +168,93 @@ __global__ void __launch_bounds__(256) k3_gather(Bufs3 b) {
 }
 
 // buildNbr (3d/sim3d.wgsl:341-390): dz, dy, dx, ascending id; MAXNBR cut
-// drops the tail of that order and raises dbg[6].
-template <bool DBG>
+// drops the tail of that order and raises dbg[6]. With L > 1 the L lanes of
+// a particle test L consecutive candidates of a row at once and place the
+// hits with a ballot prefix, so the list is the same for every L.
+template <bool DBG, int L>
 __global__ void __launch_bounds__(256) k3_nbr(Bufs3 b) {
+  if constexpr (L == 1) {
+    const uint32_t nAct = b.world->nAct, stride = b.nbrStride;
+    Flags<DBG> f{b.dbg};
+    for (uint32_t s = gtid3(); s < nAct; s += gstride3()) {
+      const int4 me = b.PW[s];
+      const uint32_t sc = (uint32_t)me.w >> TAG_SHIFT;
+      const Scene3& S = b.scenes[sc];
+      const int32_t cx = me.x >> HSHIFT, cy = me.y >> HSHIFT, cz = me.z >> HSHIFT;
+      const int32_t x0 = max(cx - 1, 0), x1 = min(cx + 1, (int32_t)S.gx - 1);
+      uint32_t cnt = 0;
+      for (int dz = -1; dz <= 1; ++dz) {
+        int32_t z = cz + dz;
+        if (z < 0 || z >= (int32_t)S.gz) continue;
+        for (int dy = -1; dy <= 1; ++dy) {
+          int32_t y = cy + dy;
+          if (y < 0 || y >= (int32_t)S.gy) continue;
+          uint32_t row = S.keyOff + ((uint32_t)z * S.gy + (uint32_t)y) * S.gx;
+          uint32_t lo = b.cellStart[row + x0], hi = b.cellStart[row + x1 + 1];
+          for (uint32_t t = lo; t < hi; ++t) {
+            if (t == s) continue;
+            int4 o = b.PW[t];
+            int32_t dx = wsub(o.x, me.x), dy2 = wsub(o.y, me.y), dz2 = wsub(o.z, me.z);
+            if (abs_sat(dx, f) >= H || abs_sat(dy2, f) >= H || abs_sat(dz2, f) >= H) continue;
+            if (r2q_of(dx, dy2, dz2) >= H2Q) continue;
+            if (cnt >= MAXNBR) { f.flag(6); continue; }
+            b.NBR[(size_t)cnt * stride + s] = t;
+            ++cnt;
+          }
+        }
+      }
+      b.NBRN[s] = cnt;
+    }
+    return;
+  }
   const uint32_t nAct = b.world->nAct, stride = b.nbrStride;
   Flags<DBG> f{b.dbg};
-  for (uint32_t s = gtid3(); s < nAct; s += gstride3()) {
-    const int4 me = b.PW[s];
+  const uint32_t lane = threadIdx.x & 31u, sub = lane & (L - 1);
+  const uint32_t gmask = ((L == 32) ? 0xffffffffu : ((1u << L) - 1u)) << (lane & ~(uint32_t)(L - 1));
+  const uint32_t below = (1u << lane) - 1u;
+  const uint32_t G = gstride3() / L;
+  for (uint32_t s = gtid3() / L;; s += G) {
+    if (__shfl_sync(0xffffffffu, s, 0) >= nAct) break;  // warp-uniform exit
+    const bool valid = s < nAct;
+    const int4 me = valid ? b.PW[s] : make_int4(0, 0, 0, 0);
     const uint32_t sc = (uint32_t)me.w >> TAG_SHIFT;
     const Scene3& S = b.scenes[sc];
     const int32_t cx = me.x >> HSHIFT, cy = me.y >> HSHIFT, cz = me.z >> HSHIFT;
     const int32_t x0 = max(cx - 1, 0), x1 = min(cx + 1, (int32_t)S.gx - 1);
     uint32_t cnt = 0;
     for (int dz = -1; dz <= 1; ++dz) {
-      int32_t z = cz + dz;
-      if (z < 0 || z >= (int32_t)S.gz) continue;
       for (int dy = -1; dy <= 1; ++dy) {
-        int32_t y = cy + dy;
-        if (y < 0 || y >= (int32_t)S.gy) continue;
-        uint32_t row = S.keyOff + ((uint32_t)z * S.gy + (uint32_t)y) * S.gx;
-        uint32_t lo = b.cellStart[row + x0], hi = b.cellStart[row + x1 + 1];
-        for (uint32_t t = lo; t < hi; ++t) {
-          if (t == s) continue;
-          int4 o = b.PW[t];
-          int32_t dx = wsub(o.x, me.x), dy2 = wsub(o.y, me.y), dz2 = wsub(o.z, me.z);
-          if (abs_sat(dx, f) >= H || abs_sat(dy2, f) >= H || abs_sat(dz2, f) >= H) continue;
-          if (r2q_of(dx, dy2, dz2) >= H2Q) continue;
-          if (cnt >= MAXNBR) { f.flag(6); continue; }
-          b.NBR[(size_t)cnt * stride + s] = t;
-          ++cnt;
+        const int32_t z = cz + dz, y = cy + dy;
+        uint32_t lo = 0, len = 0;
+        if (valid && z >= 0 && z < (int32_t)S.gz && y >= 0 && y < (int32_t)S.gy) {
+          const uint32_t row = S.keyOff + ((uint32_t)z * S.gy + (uint32_t)y) * S.gx;
+          lo = b.cellStart[row + x0];
+          len = b.cellStart[row + x1 + 1] - lo;
+        }
+        const uint32_t maxLen = L == 1 ? len : __reduce_max_sync(0xffffffffu, len);
+        for (uint32_t k = sub; k - sub < maxLen; k += L) {
+          const uint32_t t = lo + k;
+          bool hit = false;
+          if (k < len && t != s) {
+            const int4 o = b.PW[t];
+            const int32_t dx = wsub(o.x, me.x), dy2 = wsub(o.y, me.y), dz2 = wsub(o.z, me.z);
+            hit = abs_sat(dx, f) < H && abs_sat(dy2, f) < H && abs_sat(dz2, f) < H && r2q_of(dx, dy2, dz2) < H2Q;
+          }
+          uint32_t pos = cnt, nhit = hit ? 1u : 0u;
+          if (L > 1) {
+            const uint32_t bal = __ballot_sync(0xffffffffu, hit) & gmask;
+            pos = cnt + __popc(bal & below);
+            nhit = __popc(bal);
+          }
+          if (hit) {
+            if (pos >= MAXNBR) f.flag(6);
+            else b.NBR[(size_t)pos * stride + s] = t;
+          }
+          cnt += nhit;
         }
       }
     }
-    b.NBRN[s] = cnt;
+    if (valid && sub == 0) b.NBRN[s] = min(cnt, MAXNBR);
   }
 }
 
@@ -213,19 +267,37 @@ __device__ __forceinline__ int32_t wall_dist(const Scene3& S, int32_t x, int32_t
   return (w & 1) ? wsub(S.wmax[axis], pos) : pos;
 }
 
-// density (3d/sim3d.wgsl:397-468)
-template <bool DBG>
+// Sum over the L lanes that share one particle (wrapping u32 addition, so
+// the split is exact); OR-reduction for magnitude bounds.
+template <int L>
+__device__ __forceinline__ int32_t gsum3(int32_t v) {
+#pragma unroll
+  for (int o = L / 2; o > 0; o >>= 1) v = wadd(v, __shfl_xor_sync(0xffffffffu, v, o, L));
+  return v;
+}
+template <int L>
+__device__ __forceinline__ uint32_t gor3(uint32_t v) {
+#pragma unroll
+  for (int o = L / 2; o > 0; o >>= 1) v |= __shfl_xor_sync(0xffffffffu, v, o, L);
+  return v;
+}
+
+// density (3d/sim3d.wgsl:397-468). L lanes share a particle's neighbour list;
+// every sum here is a wrapping i32 sum (per-term clamps only), so any split is
+// exact.
+template <bool DBG, int L>
 __global__ void __launch_bounds__(256) k3_density(Bufs3 b, const int4* __restrict__ PW) {
   const uint32_t nAct = b.world->nAct, stride = b.nbrStride;
   Flags<DBG> f{b.dbg};
-  for (uint32_t s = gtid3(); s < nAct; s += gstride3()) {
-    const int4 me = PW[s];
-    const uint32_t sc = (uint32_t)me.w >> TAG_SHIFT;
-    const Scene3& S = b.scenes[sc];
-    int32_t rho = wmul(__ldg(&b.WG[0].x), (int32_t)((uint32_t)me.w & TAG_W)) >> 8;
-    int32_t St = 0, sgx = 0, sgy = 0, sgz = 0;
-    const uint32_t cnt = b.NBRN[s];
-    for (uint32_t k = 0; k < cnt; ++k) {
+  const uint32_t sub = threadIdx.x & (L - 1), G = gstride3() / L;
+  const int32_t W0 = __ldg(&b.WG[0].x);
+  for (uint32_t s = gtid3() / L;; s += G) {
+    if (__shfl_sync(0xffffffffu, s, 0) >= nAct) break;  // warp-uniform exit
+    const bool valid = s < nAct;
+    const int4 me = valid ? PW[s] : make_int4(0, 0, 0, 0);
+    int32_t rho = 0, St = 0, sgx = 0, sgy = 0, sgz = 0;
+    const uint32_t cnt = valid ? b.NBRN[s] : 0u;
+    for (uint32_t k = sub; k < cnt; k += L) {
       uint32_t t = b.NBR[(size_t)k * stride + s];
       int4 o = PW[t];
       int32_t dx = wsub(o.x, me.x), dy = wsub(o.y, me.y), dz = wsub(o.z, me.z);
@@ -239,6 +311,17 @@ __global__ void __launch_bounds__(256) k3_density(Bufs3 b, const int4* __restric
       sgz = wadd(sgz, gz);
       St = wadd(St, wadd(wadd(s_term(gx, f), s_term(gy, f)), s_term(gz, f)));
     }
+    if (L > 1) {
+      rho = gsum3<L>(rho);
+      St = gsum3<L>(St);
+      sgx = gsum3<L>(sgx);
+      sgy = gsum3<L>(sgy);
+      sgz = gsum3<L>(sgz);
+    }
+    if (!valid || sub != 0) continue;
+    const uint32_t sc = (uint32_t)me.w >> TAG_SHIFT;
+    const Scene3& S = b.scenes[sc];
+    rho = wadd(rho, wmul(W0, (int32_t)((uint32_t)me.w & TAG_W)) >> 8);
 #pragma unroll
     for (int w = 0; w < 6; ++w) {
       int32_t dist = wall_dist(S, me.x, me.y, me.z, w);
@@ -267,34 +350,87 @@ __global__ void __launch_bounds__(256) k3_density(Bufs3 b, const int4* __restric
   }
 }
 
+// One solveDp pair term (3d/sim3d.wgsl:493-509); false when the pair is out
+// of range (it adds nothing).
+template <bool DBG>
+__device__ __forceinline__ bool dp_term(const Bufs3& b, const int4& me, const int4& o, int32_t& tx, int32_t& ty,
+                                        int32_t& tz, const Flags<DBG>& f) {
+  int32_t dx = wsub(o.x, me.x), dy = wsub(o.y, me.y), dz = wsub(o.z, me.z);
+  int32_t r2q = r2q_of(dx, dy, dz);
+  if (r2q >= H2Q) return false;
+  int32_t gt = __ldg(&b.WG[(uint32_t)r2q >> 7].y);
+  int32_t lsum = add_sat(me.w, o.w, f);
+  tx = mul<20>(lsum, mul<16>(gt, dx, f), f);
+  ty = mul<20>(lsum, mul<16>(gt, dy, f), f);
+  tz = mul<20>(lsum, mul<16>(gt, dz, f), f);
+  return true;
+}
+
 // solveDp + applyDp (3d/sim3d.wgsl:476-537), fused over a double buffer:
 // every read is of the PL / PW written by the previous kernel, the new
 // position goes to PWout.
-template <bool DBG>
+//
+// solveDp's running sum saturates, which makes it order-dependent in general.
+// The lanes keep wrapping partial sums and an OR of the terms' magnitudes:
+// when cnt x max|term| <= INT_MAX no prefix of the sequential sum can leave
+// i32, every saturating add is an exact add, and the wrapping total IS the
+// sequential result. Otherwise (never seen in practice) lane 0 redoes the sum
+// sequentially with saturation in the canonical order.
+template <bool DBG, int L>
 __global__ void __launch_bounds__(256) k3_solve(Bufs3 b, const int4* __restrict__ PWin, int4* __restrict__ PWout) {
   const uint32_t nAct = b.world->nAct, stride = b.nbrStride;
   Flags<DBG> f{b.dbg};
-  for (uint32_t s = gtid3(); s < nAct; s += gstride3()) {
-    const int4 me = b.PL[s];
+  const uint32_t sub = threadIdx.x & (L - 1), G = gstride3() / L;
+  for (uint32_t s = gtid3() / L;; s += G) {
+    if (__shfl_sync(0xffffffffu, s, 0) >= nAct) break;  // warp-uniform exit
+    const bool valid = s < nAct;
+    const int4 me = valid ? b.PL[s] : make_int4(0, 0, 0, 0);
+    const uint32_t cnt = valid ? b.NBRN[s] : 0u;
+    int32_t ax = 0, ay = 0, az = 0;
+    uint32_t mag = 0;
+    for (uint32_t k = sub; k < cnt; k += L) {
+      uint32_t t = b.NBR[(size_t)k * stride + s];
+      int4 o = b.PL[t];
+      int32_t tx, ty, tz;
+      if (!dp_term(b, me, o, tx, ty, tz, f)) continue;
+      if constexpr (DBG) {
+        if (L == 1) {
+          ax = add_sat(ax, tx, f);
+          ay = add_sat(ay, ty, f);
+          az = add_sat(az, tz, f);
+          continue;
+        }
+      }
+      ax = wadd(ax, tx);
+      ay = wadd(ay, ty);
+      az = wadd(az, tz);
+      mag |= (uint32_t)abs(tx) | (uint32_t)abs(ty) | (uint32_t)abs(tz);
+    }
+    if (L > 1) {
+      ax = gsum3<L>(ax);
+      ay = gsum3<L>(ay);
+      az = gsum3<L>(az);
+      mag = gor3<L>(mag);
+    }
+    if (!valid || sub != 0) continue;
+    const bool exact = (DBG && L == 1) || (uint64_t)mag * cnt <= 0x7fffffffull;
+    if (!exact) {
+      // the terms' own events were counted in the lane pass; recount only the sum's
+      const Flags<false> quiet{nullptr};
+      ax = ay = az = 0;
+      for (uint32_t k = 0; k < cnt; ++k) {
+        int4 o = b.PL[b.NBR[(size_t)k * stride + s]];
+        int32_t tx, ty, tz;
+        if (!dp_term(b, me, o, tx, ty, tz, quiet)) continue;
+        ax = add_sat(ax, tx, f);
+        ay = add_sat(ay, ty, f);
+        az = add_sat(az, tz, f);
+      }
+    }
     const int32_t tag = PWin[s].w;
     const uint32_t sc = (uint32_t)tag >> TAG_SHIFT;
     const Scene3& S = b.scenes[sc];
     const int32_t lami = me.w;
-    int32_t ax = 0, ay = 0, az = 0;
-    const uint32_t cnt = b.NBRN[s];
-    for (uint32_t k = 0; k < cnt; ++k) {
-      uint32_t t = b.NBR[(size_t)k * stride + s];
-      int4 o = b.PL[t];
-      int32_t dx = wsub(o.x, me.x), dy = wsub(o.y, me.y), dz = wsub(o.z, me.z);
-      int32_t r2q = r2q_of(dx, dy, dz);
-      if (r2q >= H2Q) continue;
-      int32_t gt = __ldg(&b.WG[(uint32_t)r2q >> 7].y);
-      int32_t gx = mul<16>(gt, dx, f), gy = mul<16>(gt, dy, f), gz = mul<16>(gt, dz, f);
-      int32_t lsum = add_sat(lami, o.w, f);
-      ax = add_sat(ax, mul<20>(lsum, gx, f), f);
-      ay = add_sat(ay, mul<20>(lsum, gy, f), f);
-      az = add_sat(az, mul<20>(lsum, gz, f), f);
-    }
 #pragma unroll
     for (int w = 0; w < 6; ++w) {
       int32_t dist = wall_dist(S, me.x, me.y, me.z, w);

@@ -46,14 +46,14 @@ class Engine3D:
     """Device-resident 3D scenes advanced by one launch sequence per substep."""
 
     def __init__(self, max_particles: int = NMAX, max_cells: int = 0, max_scenes: int = 1,
-                 iters: int = ITERS, debug: bool = False, chain: bool = True, device: int = 0):
+                 iters: int = ITERS, debug: bool = False, chain: bool = True, device: int = 0, lanes: int = 0):
         self._lib = _native.load()
         self._luts = np.ascontiguousarray(tables3d.luts3d(), dtype=np.int32)
         self._mats = np.ascontiguousarray(tables3d.mats3d().reshape(-1), dtype=np.int32)
         o = _native.Sn3Opts(max_particles=int(max_particles), max_cells=int(max_cells),
                             max_scenes=int(max_scenes), iters=int(iters), debug=1 if debug else 0,
                             chain=1 if chain else 0, device=int(device), luts=self._luts.ctypes.data,
-                            mats=self._mats.ctypes.data, mat_count=self._mats.size // 4)
+                            mats=self._mats.ctypes.data, mat_count=self._mats.size // 4, lanes=int(lanes))
         h = ctypes.c_void_p()
         rc = self._lib.sn3_create(ctypes.byref(o), ctypes.byref(h))
         if rc != 0 or not h.value:

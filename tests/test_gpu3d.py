@@ -148,3 +148,17 @@ def test_bad_input_is_refused():
     sc.mat[3] = 99
     with pytest.raises(EngineError):
         e.load_scene(sc)
+
+
+@pytest.mark.parametrize('lanes', [1, 2, 4])
+@pytest.mark.parametrize('name,n', [('pool', 16000), ('overdense', 24000)])
+def test_lane_split_gathers_are_exact(lanes, name, n):
+    sc = tables3d.initial_state(n, name)
+    g = Engine3D(max_particles=sc.n, iters=4, lanes=lanes, debug=(lanes == 2)).load_scene(sc, stir_amp=500)
+    r = oracle3(sc.n, 4).load_scene(sc, stir_amp=500)
+    for k in (1, 4, 10):
+        g.step(k)
+        r.step(k)
+    same(g, r)
+    if lanes == 2:
+        assert np.array_equal(g.debug_counters(), r.debug_counters())
