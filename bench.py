@@ -364,7 +364,28 @@ def batched_workload(steps: int, warmup: int, device: int, plain_sample: int = 2
             'batched_vs_plain': batched / plain}
 
 
+def sections_only(args):
+    """--no-2d: the 3D / batched / serving sections alone (a profiling aid; the
+    line carries no headline value)."""
+    ws, rank, local, dist = _dist()
+    line = {'metric': METRIC, 'value': None, 'unit': UNIT, 'n_gpus': ws, 'steps': args.steps,
+            'warmup': args.warmup, 'note': 'headline section skipped (--no-2d)'}
+    if rank == 0 and not args.no_batched:
+        line['batched'] = batched_workload(args.steps, args.warmup, local)
+    if rank == 0 and not args.no_3d:
+        line['cfg3_3d'] = workload_3d(args.steps, args.warmup, local, with_cpu=not args.no_cpu)
+    if rank == 0 and not args.no_serving:
+        line['serving'] = serving_workload(local)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
 def ours(args):
+    if args.no_2d:
+        return sections_only(args)
     ws, rank, local, dist = _dist()
     from sunaengine_gb300 import scenes
     from sunaengine_gb300.engine import Engine
@@ -372,7 +393,8 @@ def ours(args):
     e = Engine(max_particles=sc.n, max_cells=1 << 20, device=local)
     e.load_scene(sc)
     e.step(args.warmup)
-    e.autotune(1)   # lane split per gather class, tuned on real (untimed) substeps
+    if not args.no_autotune:
+        e.autotune(1)   # lane split per gather class, tuned on real (untimed) substeps
     e.sync()
     _barrier(dist)
     with ClockSampler(local) as clk:
@@ -474,6 +496,9 @@ def main():
     ap.add_argument('--no-batched', action='store_true')
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-3d', action='store_true')
+    ap.add_argument('--no-2d', action='store_true', help='skip the headline 2D section (profiling runs)')
+    ap.add_argument('--no-autotune', action='store_true',
+                    help='keep the rule-based lanes (profiling runs: a tuner under ncu sees serialised timings)')
     ap.add_argument('--no-serving', action='store_true')
     ap.add_argument('--cpu-seconds', type=float, default=12.0)
     args = ap.parse_args()

@@ -717,7 +717,7 @@ struct World {
     if (lanesTuned && hw.nAct * 2 >= tunedAtN && hw.nAct <= tunedAtN * 2ull) return;
     lanesTuned = false;
     const uint64_t n = hw.nAct;
-    lanesCfg = LaneCfg{lanes_for(n), lanes_for(n / 16), lanes_for(n / 8), lanes_for(n), lanes_for(n / 8)};
+    lanesCfg = LaneCfg{lanes_for(n), lanes_for(n / 16), lanes_for(n / 8), lanes_for(n), lanes_for(n)};
   }
 
   // The autotuner: run `per` real substeps under each uniform lane count with

@@ -235,7 +235,7 @@ struct Engine3 {
     if (lanesTuned) return;
     const uint32_t n = hw.nAct;
     lanesD = lanesS = n < 65536 ? 4 : (n < 131072 ? 2 : 1);
-    lanesN = 1;  // measured: the split list build only pays off at L = 1 on a full GPU
+    lanesN = 1;  // the ballot-split list build measured slower than one lane per particle
   }
 
   uint32_t grid_for(uint32_t n) const {

@@ -861,6 +861,8 @@ __global__ void __launch_bounds__(256, 6) k_post2(Bufs b, int formFlags) {
   for (int m = threadIdx.x; m < MAT_MAX; m += blockDim.x)
     smat[m] = make_int4(matw(b, m, M_gammaCoh), matw(b, m, M_gammaCur), matw(b, m, M_adhesion), 0);
   __syncthreads();
+  __shared__ uint32_t dsacc[8], dsscene;
+  if (HASH) digest_block_begin(dsacc, &dsscene);
   const uint32_t nAct = b.world->nAct, stride = b.nbrStride;
   const uint32_t sub = threadIdx.x & (L - 1), G = gstride() / L;
   for (uint32_t p = gtid() / L;; p += G) {
@@ -941,14 +943,17 @@ __global__ void __launch_bounds__(256, 6) k_post2(Bufs b, int formFlags) {
     if (HASH) {
       uint32_t h[8] = {0, 0, 0, 0, 0, 0, 0, 0};
       if (lead) particle_digest(w8, idx, nullptr, h);
-      digest_add(b.acc, lead, scene, h);
+      digest_add_block(b.acc, dsacc, &dsscene, lead, scene, h);
     }
   }
+  if (HASH) digest_block_end(b.acc, dsacc, &dsscene);
 }
 
 // Digest of the current state of every active scene, in slot order
 // (statehash.wgsl `digest`, src/hash/statehash.wgsl:83-159).
 __global__ void __launch_bounds__(256) k_hash(Bufs b, uint32_t* __restrict__ acc) {
+  __shared__ uint32_t dsacc[8], dsscene;
+  digest_block_begin(dsacc, &dsscene);
   const uint32_t slotEnd = b.world->slotEnd;
   const uint32_t nIter = (slotEnd + gstride() - 1) / gstride() * gstride();
   for (uint32_t slot = gtid(); slot < nIter; slot += gstride()) {
@@ -965,8 +970,9 @@ __global__ void __launch_bounds__(256) k_hash(Bufs b, uint32_t* __restrict__ acc
         particle_digest(b.state + (size_t)slot * 8, i, row, h);
       }
     }
-    digest_add(acc, valid, s, h);
+    digest_add_block(acc, dsacc, &dsscene, valid, s, h);
   }
+  digest_block_end(acc, dsacc, &dsscene);
 }
 
 // fold_chain (src/hash/statehash.wgsl:164-170) per scene, then advance the

@@ -459,6 +459,8 @@ __global__ void __launch_bounds__(256) k3_solve(Bufs3 b, const int4* __restrict_
 // state hash of the new state when HASH is set.
 template <bool DBG, bool HASH>
 __global__ void __launch_bounds__(256) k3_integrate(Bufs3 b, const int4* __restrict__ PW) {
+  __shared__ uint32_t dsacc[8], dsscene;
+  if (HASH) d2::digest_block_begin(dsacc, &dsscene);
   const uint32_t nAct = b.world->nAct;
   Flags<DBG> f{b.dbg};
   const uint32_t nIter = (nAct + gstride3() - 1) / gstride3() * gstride3();
@@ -483,13 +485,16 @@ __global__ void __launch_bounds__(256) k3_integrate(Bufs3 b, const int4* __restr
     if constexpr (HASH) {
       uint32_t h[8] = {0, 0, 0, 0, 0, 0, 0, 0};
       if (valid) d2::particle_digest(w8, local, nullptr, h);
-      d2::digest_add(b.acc, valid, sc, h);
+      d2::digest_add_block(b.acc, dsacc, &dsscene, valid, sc, h);
     }
   }
+  if (HASH) d2::digest_block_end(b.acc, dsacc, &dsscene);
 }
 
 // State hash of every active scene's slots, on demand.
 __global__ void __launch_bounds__(256) k3_hash(Bufs3 b, uint32_t* __restrict__ acc) {
+  __shared__ uint32_t dsacc[8], dsscene;
+  d2::digest_block_begin(dsacc, &dsscene);
   const uint32_t slotEnd = b.world->slotEnd;
   const uint32_t nIter = (slotEnd + gstride3() - 1) / gstride3() * gstride3();
   for (uint32_t slot = gtid3(); slot < nIter; slot += gstride3()) {
@@ -504,8 +509,9 @@ __global__ void __launch_bounds__(256) k3_hash(Bufs3 b, uint32_t* __restrict__ a
     }
     uint32_t h[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     if (valid) d2::particle_digest(b.state + (size_t)slot * 8, local, nullptr, h);
-    d2::digest_add(acc, valid, valid ? sc : 0u, h);
+    d2::digest_add_block(acc, dsacc, &dsscene, valid, valid ? sc : 0u, h);
   }
+  d2::digest_block_end(acc, dsacc, &dsscene);
 }
 
 // Per-scene chain fold of this substep's digest (src/engine.js:4154 semantics)

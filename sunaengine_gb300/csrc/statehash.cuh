@@ -94,5 +94,60 @@ __device__ __forceinline__ void digest_add(uint32_t* acc, bool valid, uint32_t s
   }
 }
 
+// Block-level digest accumulation. Almost every warp of a block hashes
+// particles of one scene; their warp sums go to 8 shared-memory words (the
+// first scene a warp leader claims for the block) and reach global memory with
+// 8 atomics per block at the end, instead of 8 same-address global atomics per
+// warp. Warps of any other scene add to global memory directly. u32 addition
+// is commutative and associative, so the totals are exact in any order.
+// digest_block_begin/end must be reached by every thread of the block.
+constexpr uint32_t DIGEST_NO_SCENE = 0xffffffffu;
+__device__ __forceinline__ void digest_block_begin(uint32_t* sacc, uint32_t* sscene) {
+  if (threadIdx.x < 8) sacc[threadIdx.x] = 0u;
+  if (threadIdx.x == 0) *sscene = DIGEST_NO_SCENE;
+  __syncthreads();
+}
+__device__ __forceinline__ void digest_add_block(uint32_t* acc, uint32_t* sacc, uint32_t* sscene, bool valid,
+                                                 uint32_t scene, const uint32_t h[8]) {
+  uint32_t key = valid ? scene : DIGEST_NO_SCENE;
+  uint32_t peers = __match_any_sync(0xffffffffu, key);
+  int lane = threadIdx.x & 31;
+  bool leader = lane == __ffs(peers) - 1;
+  uint32_t t[8];
+  if (peers == 0xffffffffu) {
+#pragma unroll
+    for (int l = 0; l < 8; ++l) t[l] = __reduce_add_sync(0xffffffffu, h[l]);
+  } else {
+#pragma unroll
+    for (int l = 0; l < 8; ++l) {
+      uint32_t v = h[l], total = 0, m = peers;
+      while (m) {
+        int src = __ffs(m) - 1;
+        m &= m - 1;
+        total += __shfl_sync(peers, v, src);
+      }
+      t[l] = total;
+    }
+  }
+  if (!(leader && valid)) return;
+  uint32_t owner = *(volatile uint32_t*)sscene;
+  if (owner == DIGEST_NO_SCENE) {
+    const uint32_t prev = atomicCAS(sscene, DIGEST_NO_SCENE, scene);
+    owner = prev == DIGEST_NO_SCENE ? scene : prev;
+  }
+  if (owner == scene) {
+#pragma unroll
+    for (int l = 0; l < 8; ++l) atomicAdd(sacc + l, t[l]);
+  } else {
+#pragma unroll
+    for (int l = 0; l < 8; ++l) atomicAdd(acc + scene * 8 + l, t[l]);
+  }
+}
+__device__ __forceinline__ void digest_block_end(uint32_t* acc, uint32_t* sacc, uint32_t* sscene) {
+  __syncthreads();
+  const uint32_t owner = *sscene;
+  if (threadIdx.x < 8 && owner != DIGEST_NO_SCENE) atomicAdd(acc + owner * 8 + threadIdx.x, sacc[threadIdx.x]);
+}
+
 }  // namespace d2
 }  // namespace sn
