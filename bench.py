@@ -160,7 +160,7 @@ BYTES = {
 
 
 # ncu summaries under profiles/ that carry the DRAM traffic of a dominant kernel
-PROFILE_OF = {'colour x4': 'k_colour_2d_large.md'}
+PROFILE_OF = {'colour x4': 'k_colour_2d_large.md', 'solve+apply': 'k3_solve_3d_dam.md'}
 
 
 def profiled_traffic(phase: str):
@@ -270,7 +270,9 @@ def workload_3d(steps: int, warmup: int, device: int, cpu_seconds: float = 6.0, 
     peak, kind = _peaks()
     achieved = bpl / (per_launch / 1e3) / 1e9
     roof = {'kernel': dom, 'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s', 'frac': achieved / peak,
-            'peak_source': kind, 'traffic': None, 'algorithmic_bytes_per_launch': bpl, 'launch_ms': per_launch,
+            'peak_source': kind, 'traffic': profiled_traffic(dom),
+            'traffic_source': f'profiles/{PROFILE_OF[dom]}' if dom in PROFILE_OF else None,
+            'algorithmic_bytes_per_launch': bpl, 'launch_ms': per_launch,
             'phases_ms_per_substep': {k: v[0] for k, v in agg.items()}}
     e.close()
     # end to end: upload the scene, step(1) + digest() per substep, read the state back
