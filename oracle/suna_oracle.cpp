@@ -145,6 +145,12 @@ inline bool seal_class_row(const int32_t* m) {
   return m[M_bondK] != 0 && m[M_bondReform] == 0 && m[M_solidMode] != 0 && m[M_phantom] == 0;
 }
 inline bool spawn_welds(const int32_t* m) { return m[M_bondGroup] >= 0 && m[M_bondReform] == 0; }
+// Rows whose passes this oracle does not restate: rigid bodies (§20).
+constexpr int32_t SOLID_RIGID = 2;
+inline bool rigid_row(const int32_t* m) { return m[M_solidMode] == SOLID_RIGID; }
+inline bool seal_liquid_row(const int32_t* m) {
+  return m[M_bondK] == 0 && m[M_fric] == 0 && m[M_grav] > 0 && m[M_phantom] == 0;
+}
 inline bool fuse_row(const int32_t* m, uint32_t id) {
   return m[M_bondK] != 0 && m[M_bondReform] == 0 && m[M_bondGroup] >= 0 && id != MAT_PHOTO_ROW;
 }
@@ -688,8 +694,8 @@ void pass_thermal(E& e, std::vector<Particle>& out) {
     if (froze && mat != mat0 && fuse_row(e.M(mat), mat)) fl |= FLAG_CONGEAL;
     if (burning) fl |= FLAG_BURNING;
     if (e.M(mat)[M_phantom] != 0) fl |= FLAG_DEAD;
-    if (seal_class_row(e.M(mat))) {
-      fl |= FLAG_SEAL;
+    if (seal_class_row(e.M(mat))) fl |= FLAG_SEAL;
+    if (rigid_row(e.M(mat))) {
 #ifdef _OPENMP
 #pragma omp atomic
 #endif
@@ -868,6 +874,179 @@ void fold_chain(uint32_t chain[8], const uint32_t acc[8]) {
   for (int j = 0; j < 8; ++j) chain[j] = next[j];
 }
 
+// fp_div_s (src/fixed.wgsl:219-261): (|a| << s) / |b| exactly, rounded half
+// to even on the exact remainder, signed and saturated.
+inline int32_t fp_div_s(int32_t a, int32_t b, uint32_t s, const Dbg& d) {
+  if (b == 0) {
+    d.flag(2);
+    return a == 0 ? 0 : (a > 0 ? I32_MAX : I32_MIN);
+  }
+  const bool neg = (a < 0) != (b < 0);
+  const uint64_t ua = a < 0 ? (uint64_t)(-(int64_t)a) : (uint64_t)a;
+  const uint64_t ub = b < 0 ? (uint64_t)(-(int64_t)b) : (uint64_t)b;
+  const uint64_t n = ua << s;
+  const uint64_t q = n / ub, rem = n % ub;
+  bool ovf = q > 0xffffffffull;
+  uint32_t q32 = (uint32_t)q;
+  const uint64_t other = ub - rem;
+  if (rem > other || (rem == other && (q32 & 1u))) {
+    if (q32 == 0xffffffffu) { ovf = true; q32 = 0; } else { ++q32; }
+  }
+  if (ovf) { d.flag(1); return neg ? I32_MIN : I32_MAX; }
+  if (neg) {
+    if (q32 > 2147483648u) { d.flag(1); return I32_MIN; }
+    if (q32 == 2147483648u) return I32_MIN;
+    return -(int32_t)q32;
+  }
+  if (q32 > 2147483647u) { d.flag(1); return I32_MAX; }
+  return (int32_t)q32;
+}
+
+// §29 containment (src/sim.wgsl:1953-2235, 2733-2771).
+constexpr int32_t SEAL_SEG_MAX2 = 8820900, SEAL_SEG_MIN2 = 670761, SEAL_KEEP4 = 717, SEAL_REACH = 95027;
+constexpr int32_t SEAL_STRESS4 = 2560;
+
+// seal_cross_sign: the sign of ax*by - ay*bx, exact in 64 bits.
+inline int seal_cross_sign(int32_t ax, int32_t ay, int32_t bx, int32_t by) {
+  const int64_t d = (int64_t)ax * by - (int64_t)ay * bx;
+  return d == 0 ? 0 : (d < 0 ? -1 : 1);
+}
+
+// The geometry shared by contain and containOverflow: the keep-out push from
+// each seal endpoint, then the swept-segment test against every pair of seal
+// endpoints (a crossing reverts the motion). `filter` = the list still holds
+// non-seal entries to skip (contain's neighbour list).
+V2 contain_core(const E& e, const std::vector<Particle>& in, const uint32_t* list, uint32_t n, bool filter, V2 pos,
+                V2 pr, bool liquidI, const Dbg& g) {
+  auto sealj = [&](uint32_t j) { return !is_boundary(e, j) && seal_class_row(e.M(in[j].matId)); };
+  bool touched = false;
+  for (uint32_t k = 0; k < n; ++k) {
+    const uint32_t j = list[k];
+    if (filter && !sealj(j)) continue;
+    touched = true;
+    const V2 pj = pred_of(e, j);
+    const int32_t dx4 = fp_shr_rne(fp_sub_sat(pr.x, pj.x, g), BPRE);
+    const int32_t dy4 = fp_shr_rne(fp_sub_sat(pr.y, pj.y, g), BPRE);
+    const int32_t d2 = wadd(wmul(dx4, dx4), wmul(dy4, dy4));
+    if (d2 > 0 && d2 < SEAL_KEEP4 * SEAL_KEEP4) {
+      const int32_t d4 = (int32_t)isqrt64((uint64_t)(uint32_t)d2);
+      if (d4 > 0) {
+        const int32_t ux = fp_div_s(dx4, d4, 16, g), uy = fp_div_s(dy4, d4, 16, g);
+        const int32_t amt = (int32_t)((uint32_t)(SEAL_KEEP4 - d4) << BPRE);
+        pr.x = fp_add_sat(pr.x, fp_mul_s(ux, amt, 16, g), g);
+        pr.y = fp_add_sat(pr.y, fp_mul_s(uy, amt, 16, g), g);
+      }
+    }
+  }
+  if (!touched) return pr;
+  for (uint32_t k = 0; k < n; ++k) {
+    const uint32_t j = list[k];
+    if (filter && !sealj(j)) continue;
+    const int32_t* Mj = e.M(in[j].matId);
+    const V2 pj = pred_of(e, j);
+    for (uint32_t q = k + 1; q < n; ++q) {
+      const uint32_t k2 = list[q];
+      if (filter && !sealj(k2)) continue;
+      const int32_t* Mk = e.M(in[k2].matId);
+      if (liquidI && Mj[M_sealMode] != 0 && Mk[M_sealMode] != 0) continue;
+      const V2 pk = pred_of(e, k2);
+      const int32_t ex4 = fp_shr_rne(fp_sub_sat(pk.x, pj.x, g), BPRE);
+      const int32_t ey4 = fp_shr_rne(fp_sub_sat(pk.y, pj.y, g), BPRE);
+      const int32_t e2 = wadd(wmul(ex4, ex4), wmul(ey4, ey4));
+      if (e2 > SEAL_SEG_MAX2 || e2 < SEAL_SEG_MIN2) continue;
+      if (std::min(pj.x, pk.x) > std::max(pos.x, pr.x) || std::max(pj.x, pk.x) < std::min(pos.x, pr.x) ||
+          std::min(pj.y, pk.y) > std::max(pos.y, pr.y) || std::max(pj.y, pk.y) < std::min(pos.y, pr.y))
+        continue;
+      const int32_t ex = fp_sub_sat(pk.x, pj.x, g), ey = fp_sub_sat(pk.y, pj.y, g);
+      const int s0 = seal_cross_sign(ex, ey, fp_sub_sat(pos.x, pj.x, g), fp_sub_sat(pos.y, pj.y, g));
+      const int s1 = seal_cross_sign(ex, ey, fp_sub_sat(pr.x, pj.x, g), fp_sub_sat(pr.y, pj.y, g));
+      if (s0 == 0 || s0 == s1) continue;
+      const int32_t mx = fp_sub_sat(pr.x, pos.x, g), my = fp_sub_sat(pr.y, pos.y, g);
+      const int t0 = seal_cross_sign(mx, my, fp_sub_sat(pj.x, pos.x, g), fp_sub_sat(pj.y, pos.y, g));
+      const int t1 = seal_cross_sign(mx, my, fp_sub_sat(pk.x, pos.x, g), fp_sub_sat(pk.y, pos.y, g));
+      if (t0 == t1 && t0 != 0) continue;
+      pr = pos;
+    }
+  }
+  return pr;
+}
+
+// contain (src/sim.wgsl:2058-2140) and containOverflow (:2144-2235). Each
+// writes only an intruder's pred and reads only seal endpoints' preds, which
+// neither pass moves, so one in-place sweep equals the two dispatches.
+void pass_contain(E& e, const std::vector<Particle>& in) {
+  PFOR for (int64_t ii = 0; ii < (int64_t)e.nFluid; ++ii) {
+    const uint32_t i = (uint32_t)ii;
+    Dbg g = e.D();
+    if (!(e.nbrN[i] & NBR_SEAL_BIT)) continue;
+    const int32_t* Mi = e.M(in[i].matId);
+    if (seal_class_row(Mi) || Mi[M_phantom] != 0) continue;
+    if (in[i].flags & (FLAG_ANCHOR | FLAG_RIGID)) continue;
+    const V2 pos{in[i].px, in[i].py};
+    V2 pr = pred_of(e, i);
+    const bool liquidI = seal_liquid_row(Mi);
+    const uint32_t cnt = nbr_count(e, i);
+    if (cnt < MAXNBR) {
+      pr = contain_core(e, in, &e.nbr[(size_t)i * MAXNBR], cnt, true, pos, pr, liquidI, g);
+    } else {
+      uint32_t seals[MAXNBR];
+      uint32_t sealN = 0;
+      const int32_t loX = fp_sub_sat(std::min(pos.x, pr.x), SEAL_REACH, g);
+      const int32_t hiX = fp_add_sat(std::max(pos.x, pr.x), SEAL_REACH, g);
+      const int32_t loY = fp_sub_sat(std::min(pos.y, pr.y), SEAL_REACH, g);
+      const int32_t hiY = fp_add_sat(std::max(pos.y, pr.y), SEAL_REACH, g);
+      const V2 cc = cell_coord(e, pr);
+      for (int32_t gy = cc.y - 1; gy <= cc.y + 1; ++gy) {
+        if (gy < 0 || gy >= (int32_t)e.gridH) continue;
+        for (int32_t gx = cc.x - 1; gx <= cc.x + 1; ++gx) {
+          if (gx < 0 || gx >= (int32_t)e.gridW) continue;
+          const uint32_t c = (uint32_t)gy * e.gridW + (uint32_t)gx;
+          for (uint32_t t = e.cellStart[c]; t < e.cellStart[c + 1]; ++t) {
+            const uint32_t j = e.sortedIds[t];
+            if (is_boundary(e, j) || !seal_class_row(e.M(in[j].matId))) continue;
+            const V2 pj = pred_of(e, j);
+            if (pj.x < loX || pj.x > hiX || pj.y < loY || pj.y > hiY) continue;
+            if (sealN < MAXNBR) seals[sealN++] = j;
+          }
+        }
+      }
+      pr = contain_core(e, in, seals, sealN, false, pos, pr, liquidI, g);
+    }
+    e.der[i].predx = pr.x;
+    e.der[i].predy = pr.y;
+  }
+}
+
+// containStress (src/sim.wgsl:2742-2771): a held seal particle sums nearby
+// intrusion and, past its row's burstP, lets go (FLAG_BURST).
+void pass_containStress(E& e, std::vector<Particle>& out) {
+  PFOR for (int64_t ii = 0; ii < (int64_t)e.nFluid; ++ii) {
+    const uint32_t i = (uint32_t)ii;
+    Dbg g = e.D();
+    const int32_t* Mi = e.M(out[i].matId);
+    if (!seal_class_row(Mi) || Mi[M_burstP] <= 0) continue;
+    const uint32_t fl = out[i].flags;
+    if (!(fl & (FLAG_ANCHOR | FLAG_RIGID))) continue;
+    const V2 pi{out[i].px, out[i].py};
+    const uint32_t cnt = nbr_count(e, i), base = i * MAXNBR;
+    int32_t stress = 0;
+    for (uint32_t k = 0; k < cnt; ++k) {
+      const uint32_t j = e.nbr[base + k];
+      if (is_boundary(e, j)) continue;
+      const int32_t* Mj = e.M(out[j].matId);
+      if (seal_class_row(Mj) || Mj[M_phantom] != 0) continue;
+      const int32_t dx4 = fp_shr_rne(fp_sub_sat(pi.x, out[j].px, g), BPRE);
+      const int32_t dy4 = fp_shr_rne(fp_sub_sat(pi.y, out[j].py, g), BPRE);
+      const int32_t d2 = wadd(wmul(dx4, dx4), wmul(dy4, dy4));
+      if (d2 >= SEAL_STRESS4 * SEAL_STRESS4) continue;
+      const int32_t d4 = (int32_t)isqrt64((uint64_t)(uint32_t)d2);
+      stress = wadd(stress, SEAL_STRESS4 - d4);
+    }
+    if ((int32_t)((uint32_t)stress << BPRE) > Mi[M_burstP])
+      out[i].flags = (fl & ~(FLAG_ANCHOR | FLAG_RIGID | WELD_TAG_MASK)) | FLAG_BURST;
+  }
+}
+
 // One substep, in _encodeSubstep's order (src/engine.js:4003-4155).
 void substep(E& e) {
   std::vector<Particle>& in = e.st[e.parity];
@@ -884,14 +1063,15 @@ void substep(E& e) {
     pass_friction(e, in);
     pass_applyDp(e, in, -1);
   }
-  // contain/containOverflow: inert (no seal-class rows are admitted)
+  pass_contain(e, in);
   pass_finalize(e, in, out);
   pass_xsph(e, out);
   pass_normals(e);
   pass_surfaceTension(e, out);
   pass_conduct(e, out);
   pass_thermal(e, out);
-  // containStress, rigidMember: inert (no seal-class rows, no bodies)
+  pass_containStress(e, out);
+  // rigidMember: inert (no rigid-body rows are admitted)
   if ((e.formationClock % BOND_PERIOD) == 0 || e.bondDirty) {
     pass_markCongealNbr(e, out);
     pass_bondForm1(e, out);
@@ -930,7 +1110,7 @@ void sno_destroy(SnoEngine* e) { delete e; }
 // loadScene, src/engine.js:3704-3951. Returns 0 or a negative error code:
 // -1 bad sizes, -2 matId out of range, -3 position out of range, -4 flags,
 // -5 temp, -6 fuel, -7 cellShift, -8 too many cells, -9 a row this oracle
-// does not restate (seal-class or rigid).
+// does not restate (a rigid-body row, solidMode 2).
 int sno_load_scene(SnoEngine* e, uint32_t n, uint32_t nFluid, const int32_t* pos, const int32_t* vel,
                    const uint32_t* matId, const uint32_t* flags, const int32_t* temp, const int32_t* fuel,
                    int32_t domW, int32_t domH, uint32_t cellShift) {
@@ -943,7 +1123,7 @@ int sno_load_scene(SnoEngine* e, uint32_t n, uint32_t nFluid, const int32_t* pos
     if (flags && (flags[i] & ~7u)) return -4;
     if (temp && (temp[i] < TEMP_MIN || temp[i] > TEMP_MAX)) return -5;
     if (fuel && fuel[i] < 0) return -6;
-    if (seal_class_row(e->mats[matId[i]])) return -9;
+    if (rigid_row(e->mats[matId[i]])) return -9;
   }
   if (cellShift < 1 || cellShift > 27 || (1u << cellShift) < (uint32_t)H) return -7;
   uint32_t cs = 1u << cellShift;
@@ -1059,7 +1239,7 @@ int64_t sno_spawn(SnoEngine* e, const int32_t* rows, uint32_t k, int hasTemp, in
     const int32_t* r = rows + 8 * i;
     int32_t mm = r[4] < 0 ? 0 : r[4];
     uint32_t m = (uint32_t)std::min<int32_t>((int32_t)e->matCount - 1, mm);
-    if (seal_class_row(e->mats[m])) return -9;
+    if (rigid_row(e->mats[m])) return -9;
   }
   for (uint32_t i = 0; i < k; ++i) {
     const int32_t* r = rows + 8 * i;

@@ -171,7 +171,7 @@ struct World {
   size_t devEvCap = 0;
   EvPar* devEp = nullptr;
   bool eventsDirty = false, anyEvents = false;
-  bool hasFriction = false, hasBonds = false;
+  bool hasFriction = false, hasBonds = false, hasSeal = false;
   bool layoutDirty = true;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
@@ -240,6 +240,12 @@ struct World {
       if (r[M_dpMax] <= 0) return fail("mats[%u].dpMax <= 0", m);
       for (int f : {M_meltTo, M_freezeTo, M_boilTo, M_condTo, M_burnTo, M_splitTo, M_corrTo})
         if (r[f] < 0 || (uint32_t)r[f] >= matCount) return fail("mats[%u] names a product outside the table", m);
+      // §29 words (src/engine.js:3247-3256): only seal-class rows carry them
+      const bool sealRow = r[M_bondK] != 0 && r[M_bondReform] == 0 && r[M_solidMode] != 0 && r[M_phantom] == 0;
+      if (r[M_burstP] < 0) return fail("mats[%u].burstP < 0", m);
+      if (r[M_sealMode] != 0 && r[M_sealMode] != 1) return fail("mats[%u].sealMode must be 0 or 1", m);
+      if (!sealRow && (r[M_burstP] != 0 || r[M_sealMode] != 0))
+        return fail("mats[%u] is not seal-class but carries burstP/sealMode", m);
     }
     if (!cuda_ok(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "stream")) return false;
     cudaEventCreate(&ev0);
@@ -322,9 +328,12 @@ struct World {
     return r[M_bondK] != 0 && r[M_bondReform] == 0 && r[M_solidMode] != 0 && r[M_phantom] == 0;
   }
   bool spawn_welds(uint32_t m) const { return row(m)[M_bondGroup] >= 0 && row(m)[M_bondReform] == 0; }
+  // Rigid-body rows (solidMode 2: ICE, WOOD, STONE, METAL, BEDROCK in MATS)
+  // need §20's body solve, which this engine does not run.
+  bool rigid_row(uint32_t m) const { return row(m)[M_solidMode] == SOLID_RIGID; }
 
   // Which optional passes the loaded rows (and every row a transition can turn
-  // them into, except the unsupported seal-class rows) need.
+  // them into, except the unsupported rigid-body rows) need.
   void update_features() {
     std::vector<bool> seen(matCount, false);
     std::vector<uint32_t> stack;
@@ -339,18 +348,20 @@ struct World {
       stack.pop_back();
       for (int f : {M_meltTo, M_freezeTo, M_boilTo, M_condTo, M_burnTo, M_splitTo, M_corrTo}) {
         uint32_t t = (uint32_t)row(m)[f];
-        if (t < matCount && !seen[t] && !seal_row(t)) { seen[t] = true; stack.push_back(t); }
+        if (t < matCount && !seen[t] && !rigid_row(t)) { seen[t] = true; stack.push_back(t); }
       }
     }
-    bool fr = false, bo = false;
+    bool fr = false, bo = false, se = false;
     for (uint32_t m = 0; m < matCount; ++m) {
-      if (!seen[m] || seal_row(m)) continue;
+      if (!seen[m] || rigid_row(m)) continue;
       if (row(m)[M_fric] != 0 || row(m)[M_bondK] != 0) fr = true;
       if (row(m)[M_bondK] != 0) bo = true;
+      if (seal_row(m)) se = true;
     }
-    if (fr != hasFriction || bo != hasBonds) graphValid = false;
+    if (fr != hasFriction || bo != hasBonds || se != hasSeal) graphValid = false;
     hasFriction = fr;
     hasBonds = bo;
+    hasSeal = se;
   }
 
   // Recompute the colour-major key layout over the active scenes.
@@ -449,8 +460,8 @@ struct World {
       if (sc->flags && (sc->flags[i] & ~FLAG_MASK)) return fail("flags[%u] sets a reserved bit", i);
       if (sc->temp && (sc->temp[i] < TEMP_MIN || sc->temp[i] > TEMP_MAX)) return fail("temp[%u] out of range", i);
       if (sc->fuel && sc->fuel[i] < 0) return fail("fuel[%u] < 0", i);
-      if (seal_row(sc->mat_id[i]))
-        return fail("matId[%u] = %u is a seal-class solid; containment and rigid bodies are not built", i,
+      if (rigid_row(sc->mat_id[i]))
+        return fail("matId[%u] = %u is a rigid-body row (solidMode 2); rigid bodies are not built", i,
                     sc->mat_id[i]);
       uint32_t want = row(sc->mat_id[i])[M_phantom] != 0 ? FLAG_DEAD : 0u;
       if (sc->flags && (sc->flags[i] & FLAG_DEAD) && !want) return fail("flags[%u] sets FLAG_DEAD on a live row", i);
@@ -672,11 +683,19 @@ struct World {
       }
       mark();
     }
+    if (hasSeal) {
+      k_contain<DBG><<<grid_for(hw.nAct), 256, 0, st>>>(b);
+      ++Lc;
+    }
     SN_LANES(lc.p1, (launch_post1<DBG, L_>()));
     ++Lc;
     mark();
     if (hasBonds) {
       SN_LANES(lc.p2, (launch_post2<DBG, false, L_>(0)));
+      if (hasSeal) {
+        k_contain_stress<DBG><<<ga, 256, 0, st>>>(b);
+        ++Lc;
+      }
       k_form1<DBG><<<ga, 256, 0, st>>>(b);
       k_form2<<<gs, 256, 0, st>>>(b);
       Lc += 3;
@@ -954,7 +973,7 @@ struct World {
       if (list[i].x < -(1 << 28) || list[i].x > (1 << 28) || list[i].y < -(1 << 28) || list[i].y > (1 << 28))
         return fail("spawn position outside [-2^28, 2^28]");
       int32_t mm = std::min<int32_t>((int32_t)matCount - 1, std::max<int32_t>(0, list[i].mat));
-      if (seal_row((uint32_t)mm)) return fail("spawn of seal-class row %d is not supported", mm);
+      if (rigid_row((uint32_t)mm)) return fail("spawn of rigid-body row %d (solidMode 2) is not supported", mm);
       if (!noWeld && spawn_welds((uint32_t)mm)) return fail("weld-group spawns are not supported");
     }
     uint32_t total = k + nB;
@@ -969,7 +988,8 @@ struct World {
       w[2] = q.vx;
       w[3] = q.vy;
       w[4] = (int32_t)m;
-      w[5] = (int32_t)((q.flags & SPAWN_FLAG_MASK) | (r[M_phantom] != 0 ? FLAG_DEAD : 0u));
+      w[5] = (int32_t)((q.flags & SPAWN_FLAG_MASK) | (r[M_phantom] != 0 ? FLAG_DEAD : 0u) |
+                       (seal_row(m) ? FLAG_SEAL : 0u));
       int32_t t = q.has_temp ? q.temp : r[M_spawnTemp];
       w[6] = std::max(TEMP_MIN, std::min(TEMP_MAX, t));
       w[7] = std::max(0, q.has_fuel ? q.fuel : r[M_fuel0]);

@@ -69,6 +69,7 @@ constexpr uint32_t FLAG_BURNING = 1, FLAG_DEAD = 2, FLAG_ANCHOR = 4, FLAG_RIGID 
 constexpr uint32_t FLAG_CONGEAL = 32, FLAG_BURST = 64, FLAG_SEAL = 128;
 constexpr uint32_t WELD_TAG_MASK = 0x000fff00u;
 constexpr uint32_t NBRN_CONGEAL = 0x20000000u;
+constexpr uint32_t NBRN_SEAL = 0x40000000u;      // a non-wall neighbour carries FLAG_SEAL (nbr_has_seal)
 constexpr uint32_t NBRN_COUNT = 0x1fffffffu;
 constexpr int FPRE = 5, RPRE = 3, BPRE = 5;
 constexpr int32_t D2_FLOOR = 262144;
@@ -87,6 +88,7 @@ constexpr uint32_t INFO_CONGEAL = 0x20000000u;   // FLAG_CONGEAL
 constexpr uint32_t INFO_PINNED = 0x10000000u;    // FLAG_ANCHOR | FLAG_RIGID: never moved by dp
 constexpr uint32_t INFO_BURST = 0x08000000u;     // FLAG_BURST
 constexpr uint32_t INFO_RIGID = 0x04000000u;     // FLAG_RIGID
+constexpr uint32_t INFO_SEAL = 0x02000000u;      // FLAG_SEAL
 
 // material words (src/engine.js:678-705)
 enum : int {
@@ -96,8 +98,10 @@ enum : int {
   M_burnRate = 21, M_burnHeat = 22, M_burnTo = 23, M_splitTo = 24, M_splitPct = 25, M_spawnTemp = 26,
   M_corrode = 28, M_corrPt = 29, M_corrTo = 30, M_fric = 31, M_bondK = 32, M_bondBreak = 33,
   M_bondReform = 34, M_bondFormV = 35, M_bondFormP = 36, M_bondMu = 37, M_bondGroup = 38, M_rampLo = 39,
-  M_rampHi = 40, M_rampInv = 41, M_rampSign = 42, M_solidMode = 43, M_tempTarget = 44, M_tempDrive = 45
+  M_rampHi = 40, M_rampInv = 41, M_rampSign = 42, M_solidMode = 43, M_tempTarget = 44, M_tempDrive = 45,
+  M_burstP = 46, M_sealMode = 47
 };
+constexpr int32_t SOLID_RIGID = 2;
 
 // All device buffers of a world, passed by value.
 struct Bufs {
@@ -197,6 +201,24 @@ __device__ __forceinline__ int2 cell_coord(const ScenePar& S, int2 p) {
   int32_t cy = p.y >> S.cellShift;
   return make_int2(clampi(cx, 0, (int32_t)S.gridW - 1), clampi(cy, 0, (int32_t)S.gridH - 1));
 }
+// A neighbouring cell column (row) whose nearest edge is at least REJECT_D
+// ticks from the particle holds no particle the kernel can accept: lut_index
+// rejects |d| >= REJECT_D on either axis. Every particle assigned to column
+// c >= 1 has x >= c * cell (clamping only moves x < 0 into column 0), and every
+// particle of column c <= gridW - 2 has x < (c + 1) * cell, so the test below
+// is exact and skipping such a column changes neither the list nor its order.
+constexpr int32_t REJECT_D = (HS + 1) * 16 - 8;  // smallest |d| with (|d| + 8) >> 4 > HS
+constexpr uint32_t SKIP_LEFT = 1u, SKIP_RIGHT = 2u, SKIP_DOWN = 4u, SKIP_UP = 8u;
+__device__ __forceinline__ uint32_t far_sides(const ScenePar& S, int2 p, int2 cc) {
+  const int64_t x0 = (int64_t)cc.x << S.cellShift, y0 = (int64_t)cc.y << S.cellShift;
+  const int64_t cs = (int64_t)1 << S.cellShift;
+  uint32_t m = 0;
+  if ((int64_t)p.x - x0 >= REJECT_D) m |= SKIP_LEFT;
+  if (x0 + cs - (int64_t)p.x >= REJECT_D) m |= SKIP_RIGHT;
+  if ((int64_t)p.y - y0 >= REJECT_D) m |= SKIP_DOWN;
+  if (y0 + cs - (int64_t)p.y >= REJECT_D) m |= SKIP_UP;
+  return m;
+}
 __device__ __forceinline__ bool seal_class(const Bufs& b, uint32_t m) {
   return matw(b, m, M_bondK) != 0 && matw(b, m, M_bondReform) == 0 && matw(b, m, M_solidMode) != 0 &&
          matw(b, m, M_phantom) == 0;
@@ -231,7 +253,8 @@ __device__ __forceinline__ int32_t bond_k(const Bufs& b, uint32_t m, int32_t T, 
 __device__ __forceinline__ uint32_t info_of(uint32_t matId, uint32_t flags, bool boundary) {
   return (matId & INFO_MAT) | (boundary ? INFO_BOUNDARY : 0u) | ((flags & FLAG_DEAD) ? INFO_DEAD : 0u) |
          ((flags & FLAG_CONGEAL) ? INFO_CONGEAL : 0u) | ((flags & (FLAG_ANCHOR | FLAG_RIGID)) ? INFO_PINNED : 0u) |
-         ((flags & FLAG_BURST) ? INFO_BURST : 0u) | ((flags & FLAG_RIGID) ? INFO_RIGID : 0u);
+         ((flags & FLAG_BURST) ? INFO_BURST : 0u) | ((flags & FLAG_RIGID) ? INFO_RIGID : 0u) |
+         ((flags & FLAG_SEAL) ? INFO_SEAL : 0u);
 }
 __device__ __forceinline__ int2 xy(int4 v) { return make_int2(v.x, v.y); }
 __device__ __forceinline__ int2 ld_pred(const int4* PL, uint32_t q) {
@@ -345,15 +368,18 @@ __global__ void __launch_bounds__(256) k_nbr(Bufs b) {
       const ScenePar& S = b.scenes[b.SCN[p]];
       int2 pi = xy(me);
       int2 cc = cell_coord(S, pi);
+      const uint32_t skip = far_sides(S, pi, cc);
       uint32_t cnt = 0;
-      bool congeal = false;
+      bool congeal = false, sealSeen = false;
       uint32_t* out = b.NBR + p;
       for (int dy = -1; dy <= 1; ++dy) {
         int32_t gy = cc.y + dy;
         if (gy < 0 || gy >= (int32_t)S.gridH) continue;
+        if ((dy < 0 && (skip & SKIP_DOWN)) || (dy > 0 && (skip & SKIP_UP))) continue;
         for (int dx = -1; dx <= 1; ++dx) {
           int32_t gx = cc.x + dx;
           if (gx < 0 || gx >= (int32_t)S.gridW) continue;
+          if ((dx < 0 && (skip & SKIP_LEFT)) || (dx > 0 && (skip & SKIP_RIGHT))) continue;
           uint32_t key = key_of(S, gx, gy);
           uint32_t lo = b.cellStart[key], hi = b.cellStart[key + 1];
           for (uint32_t q = lo; q < hi; ++q) {
@@ -363,13 +389,14 @@ __global__ void __launch_bounds__(256) k_nbr(Bufs b) {
             if (iq & INFO_DEAD) continue;
             if (lut_index(pdelta(pi, xy(o), f), f) < 0) continue;
             if (!(iq & INFO_BOUNDARY) && (iq & INFO_CONGEAL)) congeal = true;
+            if (!(iq & INFO_BOUNDARY) && (iq & INFO_SEAL)) sealSeen = true;
             if (cnt >= (uint32_t)MAXNBR) { f.flag(6); continue; }
             if (!bnd) out[(size_t)cnt * stride] = q | (iq & INFO_BOUNDARY);
             cnt++;
           }
         }
       }
-      b.NBRN[p] = bnd ? 0u : (cnt | (congeal ? NBRN_CONGEAL : 0u));
+      b.NBRN[p] = bnd ? 0u : (cnt | (congeal ? NBRN_CONGEAL : 0u) | (sealSeen ? NBRN_SEAL : 0u));
     }
     return;
   }
@@ -389,14 +416,17 @@ __global__ void __launch_bounds__(256) k_nbr(Bufs b) {
     const ScenePar& S = b.scenes[work ? b.SCN[p] : 0u];
     const int2 pi = xy(me);
     const int2 cc = work ? cell_coord(S, pi) : make_int2(0, 0);
+    const uint32_t skip = work ? far_sides(S, pi, cc) : 0u;
     uint32_t cnt = 0;
-    bool congeal = false;
+    bool congeal = false, sealSeen = false;
     uint32_t* out = b.NBR + p;
     for (int dy = -1; dy <= 1; ++dy) {
       for (int dx = -1; dx <= 1; ++dx) {
         const int32_t gy = cc.y + dy, gx = cc.x + dx;
         uint32_t lo = 0, len = 0;
-        if (work && gy >= 0 && gy < (int32_t)S.gridH && gx >= 0 && gx < (int32_t)S.gridW) {
+        const bool far = (dy < 0 && (skip & SKIP_DOWN)) || (dy > 0 && (skip & SKIP_UP)) ||
+                         (dx < 0 && (skip & SKIP_LEFT)) || (dx > 0 && (skip & SKIP_RIGHT));
+        if (work && !far && gy >= 0 && gy < (int32_t)S.gridH && gx >= 0 && gx < (int32_t)S.gridW) {
           const uint32_t key = key_of(S, gx, gy);
           lo = b.cellStart[key];
           len = b.cellStart[key + 1] - lo;
@@ -419,6 +449,7 @@ __global__ void __launch_bounds__(256) k_nbr(Bufs b) {
           }
           if (hit) {
             if (!(iq & INFO_BOUNDARY) && (iq & INFO_CONGEAL)) congeal = true;
+            if (!(iq & INFO_BOUNDARY) && (iq & INFO_SEAL)) sealSeen = true;
             if (pos >= (uint32_t)MAXNBR) f.flag(6);
             else if (!bnd) out[(size_t)pos * stride] = q | (iq & INFO_BOUNDARY);
           }
@@ -426,8 +457,14 @@ __global__ void __launch_bounds__(256) k_nbr(Bufs b) {
         }
       }
     }
-    if (L > 1) congeal = (__ballot_sync(0xffffffffu, congeal) & gmask) != 0u;
-    if (valid && sub == 0) b.NBRN[p] = (bnd || !work) ? 0u : (min(cnt, (uint32_t)MAXNBR) | (congeal ? NBRN_CONGEAL : 0u));
+    if (L > 1) {
+      congeal = (__ballot_sync(0xffffffffu, congeal) & gmask) != 0u;
+      sealSeen = (__ballot_sync(0xffffffffu, sealSeen) & gmask) != 0u;
+    }
+    if (valid && sub == 0)
+      b.NBRN[p] = (bnd || !work) ? 0u
+                                 : (min(cnt, (uint32_t)MAXNBR) | (congeal ? NBRN_CONGEAL : 0u) |
+                                    (sealSeen ? NBRN_SEAL : 0u));
   }
 }
 
@@ -804,6 +841,198 @@ __global__ void __launch_bounds__(256, 5) k_post1(Bufs b) {
   }
 }
 
+// ---- §29 containment (src/sim.wgsl:1953-2235, 2733-2771) ---------------------
+constexpr int32_t SEAL_SEG_MAX2 = 8820900, SEAL_SEG_MIN2 = 670761, SEAL_KEEP4 = 717, SEAL_REACH = 95027;
+constexpr int32_t SEAL_STRESS4 = 2560;
+
+__device__ __forceinline__ bool seal_liquid(const Bufs& b, uint32_t m) {
+  return matw(b, m, M_bondK) == 0 && matw(b, m, M_fric) == 0 && matw(b, m, M_grav) > 0 && matw(b, m, M_phantom) == 0;
+}
+
+// fp_div_s with s = 16 (src/fixed.wgsl:219-261): (|a| << 16) / |b| exactly,
+// rounded half to even on the exact remainder, signed and saturated. Only
+// the rare close-contact case of the keep-out push divides.
+template <bool DBG>
+__device__ int32_t div_s16(int32_t a, int32_t b, const Flags<DBG>& f) {
+  if (b == 0) {
+    f.flag(2);
+    return a == 0 ? 0 : (a > 0 ? I32_MAX : I32_MIN);
+  }
+  const bool neg = (a < 0) != (b < 0);
+  const uint64_t ua = a < 0 ? (uint64_t)(-(int64_t)a) : (uint64_t)a;
+  const uint64_t ub = b < 0 ? (uint64_t)(-(int64_t)b) : (uint64_t)b;
+  const uint64_t n = ua << 16;
+  const uint64_t q = n / ub, rem = n - q * ub;
+  bool ovf = q > 0xffffffffull;
+  uint32_t q32 = (uint32_t)q;
+  const uint64_t other = ub - rem;
+  if (rem > other || (rem == other && (q32 & 1u))) {
+    if (q32 == 0xffffffffu) { ovf = true; q32 = 0; } else { ++q32; }
+  }
+  if (ovf) { f.flag(1); return neg ? I32_MIN : I32_MAX; }
+  if (neg) {
+    if (q32 > 2147483648u) { f.flag(1); return I32_MIN; }
+    if (q32 == 2147483648u) return I32_MIN;
+    return -(int32_t)q32;
+  }
+  if (q32 > 2147483647u) { f.flag(1); return I32_MAX; }
+  return (int32_t)q32;
+}
+
+// seal_cross_sign: the sign of ax*by - ay*bx, exact in 64 bits.
+__device__ __forceinline__ int seal_cross_sign(int32_t ax, int32_t ay, int32_t bx, int32_t by) {
+  const int64_t d = (int64_t)ax * by - (int64_t)ay * bx;
+  return d == 0 ? 0 : (d < 0 ? -1 : 1);
+}
+
+// The geometry contain and containOverflow share: a keep-out push from each
+// seal endpoint, then the swept-segment test against every pair of seal
+// endpoints, where a crossing reverts this substep's motion. `entry(k)` gives
+// the k-th candidate's sorted index with NBR_BOUNDARY set for wall particles;
+// `filter` means the list still holds entries that are not seal endpoints.
+template <bool DBG, typename Entry>
+__device__ int2 contain_core(const Bufs& b, Entry entry, uint32_t n, bool filter, int2 pos, int2 pr, bool liquidI,
+                             const Flags<DBG>& f) {
+  auto seal_at = [&](uint32_t e) {
+    return !(e & NBR_BOUNDARY) && seal_class(b, (uint32_t)b.PL[e & ~NBR_BOUNDARY].w & INFO_MAT);
+  };
+  bool touched = false;
+  for (uint32_t k = 0; k < n; ++k) {
+    const uint32_t e = entry(k);
+    if (filter && !seal_at(e)) continue;
+    touched = true;
+    const int2 pj = ld_pred(b.PL, e & ~NBR_BOUNDARY);
+    const int32_t dx4 = shr_rne<BPRE>(sub_sat(pr.x, pj.x, f)), dy4 = shr_rne<BPRE>(sub_sat(pr.y, pj.y, f));
+    const int32_t d2 = wadd(wmul(dx4, dx4), wmul(dy4, dy4));
+    if (d2 > 0 && d2 < SEAL_KEEP4 * SEAL_KEEP4) {
+      const int32_t d4 = (int32_t)isqrt32((uint32_t)d2);
+      if (d4 > 0) {
+        const int32_t ux = div_s16(dx4, d4, f), uy = div_s16(dy4, d4, f);
+        const int32_t amt = (int32_t)((uint32_t)(SEAL_KEEP4 - d4) << BPRE);
+        pr.x = add_sat(pr.x, mul<16>(ux, amt, f), f);
+        pr.y = add_sat(pr.y, mul<16>(uy, amt, f), f);
+      }
+    }
+  }
+  if (!touched) return pr;
+  for (uint32_t k = 0; k < n; ++k) {
+    const uint32_t e = entry(k);
+    if (filter && !seal_at(e)) continue;
+    const uint32_t j = e & ~NBR_BOUNDARY;
+    const int4 oj = b.PL[j];
+    const int32_t sealModeJ = matw(b, (uint32_t)oj.w & INFO_MAT, M_sealMode);
+    const int2 pj = xy(oj);
+    for (uint32_t q = k + 1; q < n; ++q) {
+      const uint32_t e2 = entry(q);
+      if (filter && !seal_at(e2)) continue;
+      const int4 ok = b.PL[e2 & ~NBR_BOUNDARY];
+      if (liquidI && sealModeJ != 0 && matw(b, (uint32_t)ok.w & INFO_MAT, M_sealMode) != 0) continue;
+      const int2 pk = xy(ok);
+      const int32_t ex4 = shr_rne<BPRE>(sub_sat(pk.x, pj.x, f)), ey4 = shr_rne<BPRE>(sub_sat(pk.y, pj.y, f));
+      const int32_t el2 = wadd(wmul(ex4, ex4), wmul(ey4, ey4));
+      if (el2 > SEAL_SEG_MAX2 || el2 < SEAL_SEG_MIN2) continue;
+      if (min(pj.x, pk.x) > max(pos.x, pr.x) || max(pj.x, pk.x) < min(pos.x, pr.x) ||
+          min(pj.y, pk.y) > max(pos.y, pr.y) || max(pj.y, pk.y) < min(pos.y, pr.y))
+        continue;
+      const int32_t ex = sub_sat(pk.x, pj.x, f), ey = sub_sat(pk.y, pj.y, f);
+      const int s0 = seal_cross_sign(ex, ey, sub_sat(pos.x, pj.x, f), sub_sat(pos.y, pj.y, f));
+      const int s1 = seal_cross_sign(ex, ey, sub_sat(pr.x, pj.x, f), sub_sat(pr.y, pj.y, f));
+      if (s0 == 0 || s0 == s1) continue;
+      const int32_t mx = sub_sat(pr.x, pos.x, f), my = sub_sat(pr.y, pos.y, f);
+      const int t0 = seal_cross_sign(mx, my, sub_sat(pj.x, pos.x, f), sub_sat(pj.y, pos.y, f));
+      const int t1 = seal_cross_sign(mx, my, sub_sat(pk.x, pos.x, f), sub_sat(pk.y, pos.y, f));
+      if (t0 == t1 && t0 != 0) continue;
+      pr = pos;
+    }
+  }
+  return pr;
+}
+
+// contain (src/sim.wgsl:2058-2140) + containOverflow (:2144-2235) in one
+// launch: each writes only an intruder's pred and reads only seal endpoints'
+// preds, which neither moves, so fusing them changes nothing. Runs after the
+// last solver iteration, on the final preds in PL.
+template <bool DBG>
+__global__ void __launch_bounds__(256) k_contain(Bufs b) {
+  Flags<DBG> f{b.dbg};
+  const uint32_t nAct = b.world->nAct, stride = b.nbrStride;
+  for (uint32_t p = gtid(); p < nAct; p += gstride()) {
+    const uint32_t nn = b.NBRN[p];
+    if (!(nn & NBRN_SEAL)) continue;
+    const int4 me = b.PL[p];
+    const uint32_t info = (uint32_t)me.w;
+    if (info & (INFO_BOUNDARY | INFO_PINNED)) continue;
+    const uint32_t m = info & INFO_MAT;
+    if (seal_class(b, m) || matw(b, m, M_phantom) != 0) continue;
+    const int2 pos = b.POS[p];
+    int2 pr = xy(me);
+    const bool liquidI = seal_liquid(b, m);
+    const uint32_t cnt = nn & NBRN_COUNT;
+    if (cnt < (uint32_t)MAXNBR) {
+      const uint32_t* col = b.NBR + p;
+      pr = contain_core(b, [&](uint32_t k) { return col[(size_t)k * stride]; }, cnt, true, pos, pr, liquidI, f);
+    } else {
+      uint32_t seals[MAXNBR];
+      uint32_t sealN = 0;
+      const int32_t loX = sub_sat(min(pos.x, pr.x), SEAL_REACH, f), hiX = add_sat(max(pos.x, pr.x), SEAL_REACH, f);
+      const int32_t loY = sub_sat(min(pos.y, pr.y), SEAL_REACH, f), hiY = add_sat(max(pos.y, pr.y), SEAL_REACH, f);
+      const ScenePar& S = b.scenes[b.SCN[p]];
+      const int2 cc = cell_coord(S, pr);
+      for (int dy = -1; dy <= 1; ++dy) {
+        const int32_t gy = cc.y + dy;
+        if (gy < 0 || gy >= (int32_t)S.gridH) continue;
+        for (int dx = -1; dx <= 1; ++dx) {
+          const int32_t gx = cc.x + dx;
+          if (gx < 0 || gx >= (int32_t)S.gridW) continue;
+          const uint32_t key = key_of(S, gx, gy);
+          for (uint32_t q = b.cellStart[key]; q < b.cellStart[key + 1]; ++q) {
+            const int4 o = b.PL[q];
+            if (((uint32_t)o.w & INFO_BOUNDARY) || !seal_class(b, (uint32_t)o.w & INFO_MAT)) continue;
+            if (o.x < loX || o.x > hiX || o.y < loY || o.y > hiY) continue;
+            if (sealN < (uint32_t)MAXNBR) seals[sealN++] = q;
+          }
+        }
+      }
+      pr = contain_core(b, [&](uint32_t k) { return seals[k]; }, sealN, false, pos, pr, liquidI, f);
+    }
+    *reinterpret_cast<int2*>(b.PL + p) = pr;
+  }
+}
+
+// containStress (src/sim.wgsl:2742-2771), after thermal: a held seal particle
+// sums nearby intrusion and, past its row's burstP, lets go (FLAG_BURST). It
+// writes only its own flags word and reads neighbours' positions and rows.
+template <bool DBG>
+__global__ void __launch_bounds__(256) k_contain_stress(Bufs b) {
+  Flags<DBG> f{b.dbg};
+  const uint32_t nAct = b.world->nAct, stride = b.nbrStride;
+  for (uint32_t p = gtid(); p < nAct; p += gstride()) {
+    if ((uint32_t)b.PL[p].w & INFO_BOUNDARY) continue;
+    int32_t* w = b.state + (size_t)b.sslot[p] * 8;
+    const uint32_t mi = (uint32_t)w[4];
+    const int32_t burstP = matw(b, mi, M_burstP);
+    if (!seal_class(b, mi) || burstP <= 0) continue;
+    const uint32_t fl = (uint32_t)w[5];
+    if (!(fl & (FLAG_ANCHOR | FLAG_RIGID))) continue;
+    const int32_t px = w[0], py = w[1];
+    const uint32_t cnt = b.NBRN[p] & NBRN_COUNT;
+    int32_t stress = 0;
+    for (uint32_t k = 0; k < cnt; ++k) {
+      const uint32_t e = b.NBR[(size_t)k * stride + p];
+      if (e & NBR_BOUNDARY) continue;
+      const int32_t* wj = b.state + (size_t)b.sslot[e] * 8;
+      const uint32_t mj = (uint32_t)wj[4];
+      if (seal_class(b, mj) || matw(b, mj, M_phantom) != 0) continue;
+      const int32_t dx4 = shr_rne<BPRE>(sub_sat(px, wj[0], f)), dy4 = shr_rne<BPRE>(sub_sat(py, wj[1], f));
+      const int32_t d2 = wadd(wmul(dx4, dx4), wmul(dy4, dy4));
+      if (d2 >= SEAL_STRESS4 * SEAL_STRESS4) continue;
+      stress = wadd(stress, SEAL_STRESS4 - (int32_t)isqrt32((uint32_t)d2));
+    }
+    if ((int32_t)((uint32_t)stress << BPRE) > burstP)
+      w[5] = (int32_t)((fl & ~(FLAG_ANCHOR | FLAG_RIGID | WELD_TAG_MASK)) | FLAG_BURST);
+  }
+}
+
 // thermal (src/sim.wgsl:2612-2707) for one particle; updates words 4..7.
 template <bool DBG>
 __device__ __forceinline__ void thermal(const Bufs& b, uint32_t i, int32_t heat, int32_t corr, int32_t* w,
@@ -840,10 +1069,8 @@ __device__ __forceinline__ void thermal(const Bufs& b, uint32_t i, int32_t heat,
   if (froze && mat != mat0 && fuse_row(b, mat)) fl |= FLAG_CONGEAL;
   if (burning) fl |= FLAG_BURNING;
   if (matw(b, mat, M_phantom) != 0) fl |= FLAG_DEAD;
-  if (seal_class(b, mat)) {
-    fl |= FLAG_SEAL;
-    atomicOr(b.err, ERR_UNSUPPORTED_ROW);
-  }
+  if (seal_class(b, mat)) fl |= FLAG_SEAL;
+  if (matw(b, mat, M_solidMode) == SOLID_RIGID) atomicOr(b.err, ERR_UNSUPPORTED_ROW);  // rigid bodies are not built
   w[4] = (int32_t)mat;
   w[5] = (int32_t)fl;
   w[6] = T;

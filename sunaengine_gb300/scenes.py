@@ -121,6 +121,65 @@ def _assemble(fluid_pos, fluid_mat, bnd, dom_w_wu, dom_h_wu, name, vel=None, tem
     return sc
 
 
+FLAG_ANCHOR = 4
+
+
+def sealed_box(spacing: float = 0.6, held: bool = True, seal: str = 'RUBBER', seed: int = 0x5ea1,
+               membrane: bool = False, closed: bool = True) -> Scene:
+    """Containment scenes (build-defined; the reference ships no frozen one).
+
+    ``membrane=False``: a box of seal-class particles (1 wu apart, held with
+    FLAG_ANCHOR when ``held``; without its lid when ``closed`` is False) in a
+    48 x 40 wu walled box, filled with a jittered WATER block at ``spacing``
+    wu. Below rest spacing (1 wu) the block starts compressed: pressure drives
+    it into the seal and crowded rows fill their 48-entry neighbour lists
+    (containOverflow's path).
+    ``membrane=True``: a free horizontal strip of seal particles (welded at
+    load) carrying a WATER block over empty space.
+    """
+    rng = Xorshift32(seed)
+    dom_w, dom_h = 48, 40
+    half = ONE >> 1
+    sm = mat_id(seal)
+    seal_pts = []
+    if membrane:
+        for c in range(10, 39):
+            seal_pts.append((c * ONE + half, 22 * ONE + half))
+        x0, x1, y0, y1 = 11.0, 37.0, 12.0, 21.5
+    else:
+        for c in range(8, 41):
+            seal_pts.append((c * ONE + half, 34 * ONE + half))
+        for r in range(12, 34):
+            seal_pts.append((8 * ONE + half, r * ONE + half))
+            seal_pts.append((40 * ONE + half, r * ONE + half))
+        if closed:
+            for c in range(9, 40):
+                seal_pts.append((c * ONE + half, 11 * ONE + half))
+        x0, x1, y0, y1 = 9.6, 39.4, 14.0, 33.6
+    water = []
+    sp = int(round(spacing * ONE))
+    jit = max(1, sp // 8)
+    y = int(y1 * ONE)
+    while y >= int(y0 * ONE):
+        x = int(x0 * ONE)
+        while x <= int(x1 * ONE):
+            jx = (rng() % (2 * jit + 1)) - jit
+            jy = (rng() % (2 * jit + 1)) - jit
+            water.append((x + jx, y + jy))
+            x += sp
+        y -= sp
+    fl_pos = seal_pts + water
+    fl_mat = np.array([sm] * len(seal_pts) + [MAT_WATER] * len(water), np.uint32)
+    sc = _assemble(fl_pos, fl_mat, boundary_ring(dom_w, dom_h, dom_h - 4), dom_w, dom_h,
+                   f"{'membrane' if membrane else 'sealed_box'}_{seal.lower()}")
+    if held and not membrane:
+        fl = np.zeros(sc.n, np.uint32)
+        fl[:len(seal_pts)] = FLAG_ANCHOR
+        sc.flags = fl
+    sc.meta = {'seal': len(seal_pts), 'water': len(water), 'box': (8, 40, 12, 35) if not membrane else None}
+    return sc
+
+
 def make_scene(name: str, **opts) -> Scene:
     """The reference's canonical scenes (``makeScene``, ``src/engine.js:2469-2648``)."""
     if name == 'dambreak_v1':
