@@ -186,6 +186,36 @@ int sn_last_timing(sn_engine* e, float* ms, uint64_t* launches);
 int sn_profile_substep(sn_engine* e, uint32_t reps, float* ms, uint32_t max_phases, uint32_t* n_phases);
 int sn_batch_profile_substep(sn_batch* b, uint32_t reps, float* ms, uint32_t max_phases, uint32_t* n_phases);
 
+/* ---- authoring edits -----------------------------------------------------------
+ * The device halves of the reference's host-side edits (src/engine.js:
+ * replaceWhere :6191, sliceBondsMany :6240, eraseWhere :6460): the caller
+ * evaluates its predicate on a readState copy, as the reference does in JS.
+ * sn_write_bonds writes nFluid*48 bond words (replaceWhere / sliceBonds
+ * tombstone bonds on the host and write the rows back; call
+ * sn_set_formation_clock(..., dirty = 1) after, as they set _bondDirty).
+ * sn_erase keeps the fluid slots whose keep[i] != 0 (n = nFluid flags):
+ * survivors stay in order, the boundary block follows them, stAcc moves with
+ * its particle, bond partners are renumbered and bonds to erased particles
+ * (and tombstones) are dropped, and formation runs on the next substep;
+ * *removed receives the count. */
+int sn_write_bonds(sn_engine* e, const uint32_t* bonds, size_t words);
+int sn_batch_write_bonds(sn_batch* b, uint32_t id, const uint32_t* bonds, size_t words);
+int sn_erase(sn_engine* e, const uint8_t* keep, size_t n, uint32_t* removed);
+int sn_batch_erase(sn_batch* b, uint32_t id, const uint8_t* keep, size_t n, uint32_t* removed);
+
+/* ---- inputs: jets and the user drive ------------------------------------------
+ * setJets (src/engine.js:4740-4770): up to 8 jets per scene, [x, y, r, fx, fy]
+ * int32 each (ticks; fx/fy in the units of Mat.grav); extra entries are
+ * ignored, as the reference slices to JET_MAX. A particle whose position lies
+ * in a jet's disc gets its acceleration in predict (jet_accel,
+ * src/sim.wgsl:935-949). k = 0 removes them (bit-inert). *n_out = jets kept.
+ * setUserDrive (src/engine.js:4797-4815) is stored clamped to +-USER_A_MAX and
+ * returned; it drives only user-flagged rigid bodies, which this engine does
+ * not build, so it changes no result here. */
+int sn_set_jets(sn_engine* e, const int32_t* jets, uint32_t k, uint32_t* n_out);
+int sn_batch_set_jets(sn_batch* b, uint32_t id, const int32_t* jets, uint32_t k, uint32_t* n_out);
+int sn_set_user_drive(sn_engine* e, int32_t ax, int32_t ay, int32_t out[2]);
+
 /* ---- lane autotuner ----------------------------------------------------------
  * No counterpart in the reference. The neighbour gathers of solveA, the colour
  * passes, post1, post2 and the neighbour-list build can split each particle's list over 1, 2, 4 or 8

@@ -72,6 +72,12 @@ def lib():
         l.sno_spawn.argtypes = [P, i32p, ctypes.c_uint32, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         l.sno_set_walls.restype = ctypes.c_int
         l.sno_set_walls.argtypes = [P, ctypes.c_int]
+        l.sno_write_bonds.restype = ctypes.c_int
+        l.sno_write_bonds.argtypes = [P, u32p, ctypes.c_size_t]
+        l.sno_erase.restype = ctypes.c_int64
+        l.sno_erase.argtypes = [P, np.ctypeslib.ndpointer(np.uint8, flags='C')]
+        l.sno_set_jets.restype = ctypes.c_uint32
+        l.sno_set_jets.argtypes = [P, i32p, ctypes.c_uint32]
         l.sno_impulse.restype = ctypes.c_int64
         l.sno_impulse.argtypes = [P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                   ctypes.c_int32, ctypes.c_uint32]
@@ -122,6 +128,7 @@ class OracleEngine:
         self._mats = np.ascontiguousarray(m, dtype=np.int32).reshape(-1)
         self.mat_count = self._mats.size // 48
         self.h = l.sno_create(max_particles, self._luts, self._mats, self.mat_count, iters, threads)
+        self._mats_rows = self._mats.reshape(-1, 48)
         if not self.h:
             raise ValueError('oracle create failed')
         self.max_particles = max_particles
@@ -236,6 +243,26 @@ class OracleEngine:
 
     def impulse(self, cx, cy, r, ix, iy, limit=3000) -> int:
         return int(lib().sno_impulse(self.h, cx, cy, r, ix, iy, limit))
+
+    def write_state_keep_scratch(self, state):
+        self.write_state(state)  # derived rows (stAcc included) untouched
+
+    def write_bonds(self, bonds):
+        b = np.ascontiguousarray(bonds, dtype=np.uint32).reshape(-1)
+        if lib().sno_write_bonds(self.h, b, b.size) != 0:
+            raise ValueError('oracle write_bonds: wrong size')
+
+    def erase(self, keep) -> int:
+        k = np.ascontiguousarray(np.asarray(keep, dtype=bool).astype(np.uint8))
+        if k.size != self.n_fluid:
+            raise ValueError('erase: one keep flag per fluid slot')
+        return int(lib().sno_erase(self.h, k))
+
+    def set_jets(self, jets) -> int:
+        q = np.array([[j['x'], j['y'], j['r'], j.get('fx', 0), j.get('fy', 0)] for j in jets] or np.zeros((0, 5)),
+                     dtype=np.int32).reshape(-1)
+        q = np.ascontiguousarray(q if q.size else np.zeros(5, np.int32))
+        return int(lib().sno_set_jets(self.h, q, len(jets)))
 
     def set_walls(self, on: bool) -> bool:
         return bool(lib().sno_set_walls(self.h, 1 if on else 0))

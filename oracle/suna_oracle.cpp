@@ -127,6 +127,9 @@ struct SnoEngine {
   bool bondDirty = true;
   bool wallsOn = true;
   uint32_t unsupported = 0;     // nonzero: a transition produced a row this oracle does not restate
+  // §23.B jets (setJets, src/engine.js:4740-4770): [x, y, r, fx, fy] ticks
+  int32_t jets[8][5] = {};
+  uint32_t nJets = 0;
   // the loaded scene's boundary block, for spawnFluid's relocation
   std::vector<int32_t> scenePos, sceneTemp, sceneFuel;
   std::vector<uint32_t> sceneMat;
@@ -234,6 +237,23 @@ inline int32_t iabs(int32_t x) { return x < 0 ? (int32_t)(0u - (uint32_t)x) : x;
 // ---- passes ------------------------------------------------------------------
 
 // src/sim.wgsl:958-1000
+// jet_accel (src/sim.wgsl:935-949): the sum of the accelerations of the jets
+// whose disc holds p; saturating, so overlapping jets never flip sign.
+constexpr uint32_t JET_SH = 9;
+inline V2 jet_accel(const E& e, int32_t px, int32_t py, const Dbg& g) {
+  V2 a{0, 0};
+  for (uint32_t k = 0; k < e.nJets; ++k) {
+    const int32_t* j = e.jets[k];
+    const int32_t dx = fp_sub_sat(px, j[0], g) >> JET_SH, dy = fp_sub_sat(py, j[1], g) >> JET_SH;
+    const int32_t rr = j[2] >> JET_SH;
+    if (wadd(wmul(dx, dx), wmul(dy, dy)) <= wmul(rr, rr)) {
+      a.x = fp_add_sat(a.x, j[3], g);
+      a.y = fp_add_sat(a.y, j[4], g);
+    }
+  }
+  return a;
+}
+
 void pass_predict(E& e, const std::vector<Particle>& in) {
   PFOR for (int64_t ii = 0; ii < (int64_t)e.nFluid; ++ii) {
     uint32_t i = (uint32_t)ii;
@@ -245,9 +265,9 @@ void pass_predict(E& e, const std::vector<Particle>& in) {
     if (p.flags & FLAG_ANCHOR) { d.predx = p.px; d.predy = p.py; continue; }
     if (p.flags & FLAG_RIGID) continue;
     int32_t vmaxN = fp_neg_sat(e.vmax, g);
-    // jets: nJets == 0, jet_accel returns (0,0) and fp_add_sat(x, 0) == x.
-    int32_t vx = fp_add_sat(fp_add_sat(p.vx, d.stx, g), 0, g);
-    int32_t vy = fp_add_sat(fp_add_sat(fp_add_sat(p.vy, d.sty, g), Mt[M_grav], g), 0, g);
+    const V2 jf = jet_accel(e, p.px, p.py, g);
+    int32_t vx = fp_add_sat(fp_add_sat(p.vx, d.stx, g), jf.x, g);
+    int32_t vy = fp_add_sat(fp_add_sat(fp_add_sat(p.vy, d.sty, g), Mt[M_grav], g), jf.y, g);
     vx = clampi(vx, vmaxN, e.vmax);
     vy = clampi(vy, vmaxN, e.vmax);
     V2 pr{fp_add_sat(p.px, vx, g), fp_add_sat(p.py, vy, g)};
@@ -1107,6 +1127,15 @@ SnoEngine* sno_create(uint32_t maxParticles, const int32_t* luts, const int32_t*
 
 void sno_destroy(SnoEngine* e) { delete e; }
 
+// setJets (src/engine.js:4740-4770): the first JET_MAX = 8 jets, [x, y, r, fx, fy] each.
+uint32_t sno_set_jets(SnoEngine* e, const int32_t* q, uint32_t k) {
+  if (k > 8) k = 8;
+  for (uint32_t j = 0; j < k; ++j)
+    for (int w = 0; w < 5; ++w) e->jets[j][w] = q[j * 5 + w];
+  e->nJets = k;
+  return k;
+}
+
 // loadScene, src/engine.js:3704-3951. Returns 0 or a negative error code:
 // -1 bad sizes, -2 matId out of range, -3 position out of range, -4 flags,
 // -5 temp, -6 fuel, -7 cellShift, -8 too many cells, -9 a row this oracle
@@ -1218,6 +1247,59 @@ int sno_write_state(SnoEngine* e, const int32_t* state, const int32_t* derived) 
   if (derived) std::memcpy(e->der.data(), derived, (size_t)e->n * 64);
   return 0;
 }
+int sno_write_bonds(SnoEngine* e, const uint32_t* in, size_t words) {
+  if (words < (size_t)e->nFluid * BOND_CAP) return -1;
+  std::memcpy(e->bond.data(), in, (size_t)e->nFluid * BOND_CAP * 4);
+  return 0;
+}
+
+// eraseWhere's compaction (src/engine.js:6460-6650): keep[i] for each fluid
+// slot; survivors keep their order, the boundary block follows them; state and
+// derived rows are permuted, bond contents are renumbered (tombstones and
+// bonds to erased partners dropped), and formation runs on the next substep.
+// Returns the number of particles removed.
+int64_t sno_erase(SnoEngine* e, const uint8_t* keep) {
+  const uint32_t oldF = e->nFluid, nB = e->n - e->nFluid;
+  std::vector<uint32_t> surv;
+  for (uint32_t i = 0; i < oldF; ++i)
+    if (keep[i]) surv.push_back(i);
+  const uint32_t newF = (uint32_t)surv.size(), removed = oldF - newF;
+  if (removed == 0) return 0;
+  const uint32_t newN = newF + nB;
+  std::vector<Particle>& cur = e->st[e->parity];
+  std::vector<Particle> st(e->maxParticles);
+  std::vector<Derived> dv(e->maxParticles);
+  for (uint32_t k = 0; k < newF; ++k) { st[k] = cur[surv[k]]; dv[k] = e->der[surv[k]]; }
+  for (uint32_t b = 0; b < nB; ++b) { st[newF + b] = cur[oldF + b]; dv[newF + b] = e->der[oldF + b]; }
+  std::vector<int32_t> oldToNew(oldF, -1);
+  for (uint32_t k = 0; k < newF; ++k) oldToNew[surv[k]] = (int32_t)k;
+  std::vector<uint32_t> bo(e->bond.size(), 0), bc(e->bondCand.size(), 0);
+  for (int which = 0; which < 2; ++which) {
+    const std::vector<uint32_t>& src = which ? e->bondCand : e->bond;
+    std::vector<uint32_t>& dst = which ? bc : bo;
+    for (uint32_t k = 0; k < newF; ++k) {
+      uint32_t so = surv[k] * BOND_CAP, c = 0;
+      for (uint32_t q = 0; q < BOND_CAP; ++q) {
+        uint32_t w = src[so + q];
+        if (w == 0u) break;
+        if (w & BOND_TOMB) continue;
+        int32_t nj = oldToNew[w & BOND_J_MASK];
+        if (nj < 0) continue;
+        dst[k * BOND_CAP + c++] = (w & BOND_L0_MASK) | (uint32_t)nj;
+      }
+    }
+  }
+  e->st[0] = st;
+  e->st[1] = st;
+  e->der = dv;
+  e->bond = bo;
+  e->bondCand = bc;
+  e->n = newN;
+  e->nFluid = newF;
+  e->bondDirty = true;
+  return removed;
+}
+
 void sno_set_formation_clock(SnoEngine* e, uint64_t clk, int dirty) {
   e->formationClock = clk;
   e->bondDirty = dirty != 0;

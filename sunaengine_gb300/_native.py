@@ -177,6 +177,13 @@ SIGNATURES = {
     'sn3_get_info': (ctypes.c_int, [P, u32, ctypes.POINTER(Sn3Info)]),
     'sn3_last_timing': (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(u64)]),
     'sn3_profile_substep': (ctypes.c_int, [P, u32, P, u32, ctypes.POINTER(u32)]),
+    'sn_write_bonds': (ctypes.c_int, [P, P, ctypes.c_size_t]),
+    'sn_batch_write_bonds': (ctypes.c_int, [P, u32, P, ctypes.c_size_t]),
+    'sn_erase': (ctypes.c_int, [P, P, ctypes.c_size_t, ctypes.POINTER(u32)]),
+    'sn_batch_erase': (ctypes.c_int, [P, u32, P, ctypes.c_size_t, ctypes.POINTER(u32)]),
+    'sn_set_jets': (ctypes.c_int, [P, P, u32, ctypes.POINTER(u32)]),
+    'sn_batch_set_jets': (ctypes.c_int, [P, u32, P, u32, ctypes.POINTER(u32)]),
+    'sn_set_user_drive': (ctypes.c_int, [P, ctypes.c_int32, ctypes.c_int32, P]),
     'sn_autotune': (ctypes.c_int, [P, u32, ctypes.POINTER(u32)]),
     'sn_batch_autotune': (ctypes.c_int, [P, u32, ctypes.POINTER(u32)]),
     'sn_lanes': (ctypes.c_int, [P, P]),

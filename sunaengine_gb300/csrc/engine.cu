@@ -172,6 +172,7 @@ struct World {
   EvPar* devEp = nullptr;
   bool eventsDirty = false, anyEvents = false;
   bool hasFriction = false, hasBonds = false, hasSeal = false;
+  int32_t userA[2] = {0, 0};  // setUserDrive: drives only user-flagged rigid bodies (none are built)
   bool layoutDirty = true;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
@@ -1092,6 +1093,93 @@ struct World {
     return true;
   }
 
+  // Bond rows of scene s from the host (the write half of the reference's
+  // readBond/writeBuffer(bond) pair that replaceWhere and sliceBonds use).
+  bool write_bonds(uint32_t s, const uint32_t* in, size_t words) {
+    SceneHost& h = sh[s];
+    if (!h.loaded) return fail("writeBonds before loadScene");
+    if (!in || words < (size_t)h.nFluid * BOND_CAP) return fail("bonds: need %u words", h.nFluid * BOND_CAP);
+    accFresh = false;
+    cudaMemcpyAsync(b.bond + (size_t)h.slotBase * BOND_CAP, in, (size_t)h.nFluid * BOND_CAP * 4,
+                    cudaMemcpyHostToDevice, st);
+    return cuda_ok(cudaStreamSynchronize(st), "writeBonds");
+  }
+
+  // eraseWhere's compaction (src/engine.js:6460-6650) for scene s: keep[i]
+  // per fluid slot; survivors keep their order and the boundary block follows
+  // them; state and stAcc are permuted, bond contents are renumbered (bonds to
+  // erased partners and tombstones dropped), and formation runs on the next
+  // substep. Clocks, chain and the impulse queue are untouched.
+  bool erase(uint32_t s, const uint8_t* keep, size_t nkeep, uint32_t* removedOut) {
+    SceneHost& h = sh[s];
+    if (!h.loaded) return fail("eraseWhere before loadScene");
+    if (!keep || nkeep != h.nFluid) return fail("eraseWhere: need %u keep flags", h.nFluid);
+    accFresh = false;
+    const uint32_t oldF = h.nFluid, n = h.n, nB = n - oldF;
+    std::vector<uint32_t> surv;
+    for (uint32_t i = 0; i < oldF; ++i)
+      if (keep[i]) surv.push_back(i);
+    const uint32_t newF = (uint32_t)surv.size();
+    if (removedOut) *removedOut = oldF - newF;
+    if (newF == oldF) return true;
+    std::vector<int32_t> stIn((size_t)n * 8), scIn((size_t)n * 2);
+    std::vector<uint32_t> bIn((size_t)oldF * BOND_CAP);
+    cudaMemcpyAsync(stIn.data(), b.state + (size_t)h.slotBase * 8, stIn.size() * 4, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(scIn.data(), b.stacc + h.slotBase, scIn.size() * 4, cudaMemcpyDeviceToHost, st);
+    if (oldF)
+      cudaMemcpyAsync(bIn.data(), b.bond + (size_t)h.slotBase * BOND_CAP, bIn.size() * 4, cudaMemcpyDeviceToHost, st);
+    if (!cuda_ok(cudaStreamSynchronize(st), "erase read")) return false;
+    const uint32_t newN = newF + nB;
+    std::vector<int32_t> stOut((size_t)newN * 8), scOut((size_t)newN * 2);
+    auto mv = [&](uint32_t src, uint32_t dst) {
+      std::memcpy(&stOut[(size_t)dst * 8], &stIn[(size_t)src * 8], 32);
+      std::memcpy(&scOut[(size_t)dst * 2], &scIn[(size_t)src * 2], 8);
+    };
+    for (uint32_t k = 0; k < newF; ++k) mv(surv[k], k);
+    for (uint32_t bb = 0; bb < nB; ++bb) mv(oldF + bb, newF + bb);
+    std::vector<int32_t> oldToNew(oldF, -1);
+    for (uint32_t k = 0; k < newF; ++k) oldToNew[surv[k]] = (int32_t)k;
+    std::vector<uint32_t> bOut((size_t)oldF * BOND_CAP, 0u);  // the full old extent: rows past newF end zero
+    for (uint32_t k = 0; k < newF; ++k) {
+      uint32_t c = 0;
+      for (uint32_t q = 0; q < (uint32_t)BOND_CAP; ++q) {
+        const uint32_t w = bIn[(size_t)surv[k] * BOND_CAP + q];
+        if (w == 0u) break;
+        if (w & BOND_TOMB) continue;
+        const int32_t nj = oldToNew[w & BOND_J_MASK];
+        if (nj < 0) continue;
+        bOut[(size_t)k * BOND_CAP + c++] = (w & BOND_L0_MASK) | (uint32_t)nj;
+      }
+    }
+    cudaMemcpyAsync(b.state + (size_t)h.slotBase * 8, stOut.data(), stOut.size() * 4, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(b.stacc + h.slotBase, scOut.data(), scOut.size() * 4, cudaMemcpyHostToDevice, st);
+    if (oldF)
+      cudaMemcpyAsync(b.bond + (size_t)h.slotBase * BOND_CAP, bOut.data(), bOut.size() * 4, cudaMemcpyHostToDevice, st);
+    if (!cuda_ok(cudaStreamSynchronize(st), "erase write")) return false;
+    if (!pull_params()) return false;
+    h.n = newN;
+    h.nFluid = newF;
+    hpar[s].n = newN;
+    hpar[s].nFluid = newF;
+    hpar[s].bondDirty = 1;
+    layoutDirty = true;
+    eventsDirty = true;
+    return push_scene(s) && cuda_ok(cudaStreamSynchronize(st), "erase");
+  }
+
+  // setJets (src/engine.js:4740-4770): the first 8 jets, [x, y, r, fx, fy].
+  bool set_jets(uint32_t s, const int32_t* q, uint32_t k, uint32_t* nOut) {
+    if (!sh[s].loaded) return fail("setJets before loadScene");
+    if (k > 0 && !q) return fail("jets is NULL");
+    if (k > 8) k = 8;
+    if (!pull_params()) return false;
+    hpar[s].nJets = k;
+    for (uint32_t j = 0; j < 8; ++j)
+      for (int w = 0; w < 5; ++w) hpar[s].jet[j][w] = j < k ? q[j * 5 + w] : 0;
+    if (nOut) *nOut = k;
+    return push_scene(s) && cuda_ok(cudaStreamSynchronize(st), "setJets");
+  }
+
   // Device checkpoint of scene s: [state n*8][stAcc n*2][chain 8][bond rows nFluid*48 when the
   // world has bonding rows], copied on the engine stream.
   size_t ckpt_bytes(uint32_t s) const {
@@ -1412,6 +1500,38 @@ int sn_batch_write_state(sn_batch* b, uint32_t id, const int32_t* state, const i
   w.hpar[id].substep = (uint32_t)substep_count;
   w.eventsDirty = true;
   return rc_of(w, w.push_scene(id) && w.cuda_ok(cudaStreamSynchronize(w.st), "write"));
+}
+int sn_write_bonds(sn_engine* e, const uint32_t* bonds, size_t words) {
+  if (!e) return SN_E_INVALID;
+  return rc_of(e->w, e->w.write_bonds(0, bonds, words));
+}
+int sn_batch_write_bonds(sn_batch* b, uint32_t id, const uint32_t* bonds, size_t words) {
+  if (!b || id >= b->w.maxScenes) return SN_E_INVALID;
+  return rc_of(b->w, b->w.write_bonds(id, bonds, words));
+}
+int sn_erase(sn_engine* e, const uint8_t* keep, size_t n, uint32_t* removed) {
+  if (!e) return SN_E_INVALID;
+  return rc_of(e->w, e->w.erase(0, keep, n, removed));
+}
+int sn_batch_erase(sn_batch* b, uint32_t id, const uint8_t* keep, size_t n, uint32_t* removed) {
+  if (!b || id >= b->w.maxScenes) return SN_E_INVALID;
+  return rc_of(b->w, b->w.erase(id, keep, n, removed));
+}
+int sn_set_jets(sn_engine* e, const int32_t* jets, uint32_t k, uint32_t* n_out) {
+  if (!e) return SN_E_INVALID;
+  return rc_of(e->w, e->w.set_jets(0, jets, k, n_out));
+}
+int sn_batch_set_jets(sn_batch* b, uint32_t id, const int32_t* jets, uint32_t k, uint32_t* n_out) {
+  if (!b || id >= b->w.maxScenes) return SN_E_INVALID;
+  return rc_of(b->w, b->w.set_jets(id, jets, k, n_out));
+}
+int sn_set_user_drive(sn_engine* e, int32_t ax, int32_t ay, int32_t out[2]) {
+  if (!e) return SN_E_INVALID;
+  const int32_t M = 32768;  // USER_A_MAX, src/engine.js:481
+  e->w.userA[0] = std::max(-M, std::min(M, ax));
+  e->w.userA[1] = std::max(-M, std::min(M, ay));
+  if (out) { out[0] = e->w.userA[0]; out[1] = e->w.userA[1]; }
+  return SN_OK;
 }
 int sn_autotune(sn_engine* e, uint32_t reps, uint32_t* substeps_run) {
   if (!e) return SN_E_INVALID;

@@ -272,6 +272,22 @@ __device__ __forceinline__ int32_t gsum(int32_t v) {
 
 // ---- kernels --------------------------------------------------------------------
 
+// jet_accel (src/sim.wgsl:935-949): the saturating sum of the accelerations
+// of the scene's jets whose disc holds p; (0, 0) with no jets.
+template <bool DBG>
+__device__ __forceinline__ int2 jet_accel(const ScenePar& S, int2 p, const Flags<DBG>& f) {
+  int2 a = make_int2(0, 0);
+  for (uint32_t k = 0; k < S.nJets; ++k) {
+    const int32_t dx = sub_sat(p.x, S.jet[k][0], f) >> 9, dy = sub_sat(p.y, S.jet[k][1], f) >> 9;
+    const int32_t rr = S.jet[k][2] >> 9;
+    if (wadd(wmul(dx, dx), wmul(dy, dy)) <= wmul(rr, rr)) {
+      a.x = add_sat(a.x, S.jet[k][3], f);
+      a.y = add_sat(a.y, S.jet[k][4], f);
+    }
+  }
+  return a;
+}
+
 // predict (src/sim.wgsl:958-1000) + the grid key of every slot.
 template <bool DBG>
 __global__ void __launch_bounds__(256) k_predict_key(Bufs b) {
@@ -293,8 +309,9 @@ __global__ void __launch_bounds__(256) k_predict_key(Bufs b) {
       if (matw(b, m, M_phantom) == 0 && !(fl & (FLAG_ANCHOR | FLAG_RIGID))) {
         int2 st = b.stacc[slot];
         int32_t vmax = S.vmax, vmaxN = neg_sat(vmax, f);
-        int32_t vx = add_sat(a.z, st.x, f);
-        int32_t vy = add_sat(add_sat(a.w, st.y, f), matw(b, m, M_grav), f);
+        const int2 jf = jet_accel(S, pos, f);
+        int32_t vx = add_sat(add_sat(a.z, st.x, f), jf.x, f);
+        int32_t vy = add_sat(add_sat(add_sat(a.w, st.y, f), matw(b, m, M_grav), f), jf.y, f);
         vx = clampi(vx, vmaxN, vmax);
         vy = clampi(vy, vmaxN, vmax);
         pred = wall_clamp(S, make_int2(add_sat(pos.x, vx, f), add_sat(pos.y, vy, f)));

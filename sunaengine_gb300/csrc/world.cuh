@@ -41,6 +41,8 @@ struct ScenePar {
   uint32_t formNow;    // formation runs in the substep in flight (set by predict)
   uint32_t active;     // 0 = slot range reserved but not stepped
   uint32_t substep;    // substeps advanced since load (impulse schedule clock)
+  uint32_t nJets;      // §23.B jets (setJets): 0..8
+  int32_t jet[8][5];   // [x, y, r, fx, fy] ticks
 };
 
 // World-level totals, written by the host when the scene set changes.

@@ -25,6 +25,11 @@ BOND_CAP = 48
 VMAX = 65536
 
 
+def authoring_kerf() -> int:
+    """sliceBondsMany's default kerf, Math.round(ONE * 0.52) (src/engine.js:6240)."""
+    return 34079
+
+
 class EngineError(RuntimeError):
     """Raised for refused input and for errors the device reported."""
 
@@ -109,6 +114,7 @@ class Engine:
                  chain: bool = True, device: int = 0, tables=None, mats=None, lanes: int = 0):
         self._lib = _native.load()
         o, self._keep = _opts(max_particles, max_cells, iters, debug, chain, device, tables, mats, lanes)
+        self._mats_rows = self._keep[1]
         h = ctypes.c_void_p()
         rc = self._lib.sn_create(ctypes.byref(o), ctypes.byref(h))
         if rc != 0:
@@ -199,6 +205,43 @@ class Engine:
         self._check(self._lib.sn_read_bonds(self._h, _ptr(a), a.size), 'readBond')
         return a[:self.n_fluid * BOND_CAP]
 
+    def write_bonds(self, bonds: np.ndarray):
+        b = np.ascontiguousarray(bonds, dtype=np.uint32).reshape(-1)
+        self._check(self._lib.sn_write_bonds(self._h, _ptr(b), b.size), 'writeBonds')
+
+    def write_state_keep_scratch(self, state: np.ndarray):
+        self.write_state(state, self.read_scratch())
+
+    def erase(self, keep) -> int:
+        """The device compaction of eraseWhere: keep one flag per fluid slot."""
+        k = np.ascontiguousarray(np.asarray(keep, dtype=bool).astype(np.uint8))
+        out = ctypes.c_uint32()
+        self._check(self._lib.sn_erase(self._h, _ptr(k), k.size, ctypes.byref(out)), 'eraseWhere')
+        i = self.info()
+        self._n, self._n_fluid = int(i['n']), int(i['n_fluid'])
+        return int(out.value)
+
+    # authoring edits, same host logic as the reference (see authoring.py)
+    def erase_where(self, keep) -> int:
+        from . import authoring
+        return authoring.erase_where(self, keep)
+
+    def replace_where(self, test, new_mat: int) -> int:
+        from . import authoring
+        return authoring.replace_where(self, test, new_mat)
+
+    def slice_bonds_many(self, segments, kerf: int = authoring_kerf()) -> int:
+        from . import authoring
+        return authoring.slice_bonds_many(self, segments, kerf)
+
+    def slice_bonds(self, x0: int, y0: int, x1: int, y1: int) -> int:
+        return self.slice_bonds_many([{'x0': x0, 'y0': y0, 'x1': x1, 'y1': y1}])
+
+    eraseWhere = erase_where
+    replaceWhere = replace_where
+    sliceBondsMany = slice_bonds_many
+    sliceBonds = slice_bonds
+
     def spawn_fluid(self, particles, no_weld: bool = True) -> int:
         arr, k = _particles(particles)
         out = ctypes.c_uint32()
@@ -248,6 +291,32 @@ class Engine:
         l = ctypes.c_uint64()
         self._check(self._lib.sn_last_timing(self._h, ctypes.byref(ms), ctypes.byref(l)), 'timing')
         return float(ms.value), int(l.value)
+
+    @staticmethod
+    def _jet_words(jets):
+        q = np.zeros(max(1, len(jets)) * 5, np.int32)
+        for k, j in enumerate(jets):
+            q[k * 5:k * 5 + 5] = (int(j['x']), int(j['y']), int(j['r']), int(j.get('fx', 0)), int(j.get('fy', 0)))
+        return q
+
+    def set_jets(self, jets) -> int:
+        """setJets (src/engine.js:4740): list of {x, y, r, fx, fy} in ticks; the
+        first 8 are kept. Returns how many the engine holds."""
+        jets = list(jets or [])
+        q = self._jet_words(jets)
+        n = ctypes.c_uint32()
+        self._check(self._lib.sn_set_jets(self._h, _ptr(q), len(jets), ctypes.byref(n)), 'setJets')
+        return int(n.value)
+
+    def set_user_drive(self, ax: int, ay: int):
+        """setUserDrive (src/engine.js:4797): stored clamped to +-32768; it
+        drives only user-flagged rigid bodies, which this engine does not build."""
+        out = np.zeros(2, np.int32)
+        self._check(self._lib.sn_set_user_drive(self._h, int(ax), int(ay), _ptr(out)), 'setUserDrive')
+        return [int(out[0]), int(out[1])]
+
+    setJets = set_jets
+    setUserDrive = set_user_drive
 
     def autotune(self, reps: int = 1) -> int:
         """Pick the gather lanes per kernel class on real substeps (the scene
@@ -411,6 +480,13 @@ class Batch:
     def autotune(self, reps: int = 1) -> int:
         n = ctypes.c_uint32()
         self._check(self._lib.sn_batch_autotune(self._h, int(reps), ctypes.byref(n)), 'autotune')
+        return int(n.value)
+
+    def set_jets(self, sid: int, jets) -> int:
+        jets = list(jets or [])
+        q = Engine._jet_words(jets)
+        n = ctypes.c_uint32()
+        self._check(self._lib.sn_batch_set_jets(self._h, int(sid), _ptr(q), len(jets), ctypes.byref(n)), 'set_jets')
         return int(n.value)
 
     def lanes(self):
