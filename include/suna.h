@@ -121,8 +121,23 @@ int sn_write_state(sn_engine* e, const int32_t* state, const int32_t* scratch, s
 int sn_read_bonds(sn_engine* e, uint32_t* out, size_t words);
 /* Engine.spawnFluid (src/engine.js:5901): append k fluid particles, relocate
  * the boundary block to the tail. *n_out = new n (unchanged when the capacity
- * refuses, as the reference silently does). */
+ * refuses, as the reference silently does). `no_weld` holds the options bits:
+ * SN_SPAWN_NO_WELD ({noWeld: true}: no weld tag), SN_SPAWN_OWN_GROUP
+ * ({ownGroup: true}: its own group even while a gesture is held). */
+#define SN_SPAWN_NO_WELD 1u
+#define SN_SPAWN_OWN_GROUP 2u
 int sn_spawn(sn_engine* e, const sn_particle* list, uint32_t k, uint32_t no_weld, uint32_t* n_out);
+/* Weld groups (src/engine.js:4570-4680): beginWeldGroup opens a gesture (every
+ * spawn joins it until endWeldGroup) and returns its tag; holdWeldGroup holds
+ * an existing tag; endWeldGroup releases (formation runs on the next
+ * substep); armFuse arms draw-time fusion (§18.24) for the open gesture, and
+ * the arm is cleared by the first sn_step after the release.
+ * sn_weld_state: {weldHold, fuseTag, lastWeldTag, weldSeq}. */
+int sn_begin_weld_group(sn_engine* e, uint32_t* tag);
+int sn_hold_weld_group(sn_engine* e, uint32_t tag);
+int sn_end_weld_group(sn_engine* e, uint32_t* was);
+int sn_arm_fuse(sn_engine* e, uint32_t* tag);
+int sn_weld_state(sn_engine* e, uint32_t out[4]);
 /* Engine.applyImpulse (src/engine.js:6077): add (ix, iy) to the velocity of the
  * first `limit` fluid particles in slot order within r of (cx, cy), clamped to
  * +-VMAX. Applied on the device at the current substep boundary. */

@@ -72,6 +72,15 @@ def lib():
         l.sno_spawn.argtypes = [P, i32p, ctypes.c_uint32, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         l.sno_set_walls.restype = ctypes.c_int
         l.sno_set_walls.argtypes = [P, ctypes.c_int]
+        l.sno_hold_weld_group.restype = ctypes.c_int
+        l.sno_hold_weld_group.argtypes = [P, ctypes.c_uint32]
+        l.sno_end_weld_group.restype = ctypes.c_uint32
+        l.sno_end_weld_group.argtypes = [P]
+        l.sno_begin_weld_group.restype = ctypes.c_uint32
+        l.sno_begin_weld_group.argtypes = [P]
+        l.sno_arm_fuse.restype = ctypes.c_int
+        l.sno_arm_fuse.argtypes = [P]
+        l.sno_weld_state.argtypes = [P, u32p]
         l.sno_write_bonds.restype = ctypes.c_int
         l.sno_write_bonds.argtypes = [P, u32p, ctypes.c_size_t]
         l.sno_erase.restype = ctypes.c_int64
@@ -229,14 +238,38 @@ class OracleEngine:
     def set_formation_clock(self, clk: int, dirty: bool):
         lib().sno_set_formation_clock(self.h, clk, 1 if dirty else 0)
 
-    def spawn(self, particles, no_weld: bool = True) -> int:
+    def begin_weld_group(self) -> int:
+        return int(lib().sno_begin_weld_group(self.h))
+
+    def hold_weld_group(self, tag: int) -> int:
+        r = lib().sno_hold_weld_group(self.h, int(tag))
+        if r < 0:
+            raise ValueError('holdWeldGroup(0): use endWeldGroup() to release')
+        return r
+
+    def end_weld_group(self) -> int:
+        return int(lib().sno_end_weld_group(self.h))
+
+    def arm_fuse(self) -> int:
+        r = lib().sno_arm_fuse(self.h)
+        if r < 0:
+            raise ValueError('armFuse(): no weld group is open')
+        return r
+
+    def weld_state(self):
+        a = np.zeros(4, np.uint32)
+        lib().sno_weld_state(self.h, a)
+        return dict(zip(('weld_hold', 'fuse_tag', 'last_weld_tag', 'weld_seq'), (int(x) for x in a)))
+
+    def spawn(self, particles, no_weld: bool = True, own_group: bool = False) -> int:
         rows = np.zeros((len(particles), 8), np.int32)
         has_t = any('temp' in p for p in particles)
         has_f = any('fuel' in p for p in particles)
         for k, p in enumerate(particles):
             rows[k] = (p['x'], p['y'], p.get('vx', 0), p.get('vy', 0), p.get('mat', 0),
                        p.get('flags', 0), p.get('temp', 0), p.get('fuel', 0))
-        r = lib().sno_spawn(self.h, rows.reshape(-1), len(particles), int(has_t), int(has_f), int(no_weld))
+        r = lib().sno_spawn(self.h, rows.reshape(-1), len(particles), int(has_t), int(has_f),
+                            (1 if no_weld else 0) | (2 if own_group else 0))
         if r < 0:
             raise ValueError(f'oracle spawn refused (code {r})')
         return int(r)
@@ -268,8 +301,8 @@ class OracleEngine:
         return bool(lib().sno_set_walls(self.h, 1 if on else 0))
 
     # the Engine method names, so the demo layer can drive either engine
-    def spawn_fluid(self, particles, no_weld: bool = True) -> int:
-        return self.spawn(particles, no_weld)
+    def spawn_fluid(self, particles, no_weld: bool = True, own_group: bool = False) -> int:
+        return self.spawn(particles, no_weld, own_group)
 
     def apply_impulse(self, cx, cy, r, ix, iy, limit=3000) -> int:
         return self.impulse(cx, cy, r, ix, iy, limit)

@@ -114,6 +114,7 @@ struct SnoEngine {
   uint32_t n = 0, nFluid = 0, gridW = 1, gridH = 1, cellTotal = 1, cellShift = 18;
   int32_t originX = 0, originY = 0, domW = 0, domH = 0, vmax = VMAX;
   uint32_t weldHold = 0, fuseTag = 0;
+  uint32_t weldSeq = 1, weldHoldSeq = 0, lastWeldTag = 0;  // weld-group host state (src/engine.js:4570-4680)
   // buffers
   std::vector<Particle> st[2];
   std::vector<Derived> der;
@@ -237,6 +238,15 @@ inline int32_t iabs(int32_t x) { return x < 0 ? (int32_t)(0u - (uint32_t)x) : x;
 // ---- passes ------------------------------------------------------------------
 
 // src/sim.wgsl:958-1000
+// _nextWeldSeq (src/engine.js:4570-4580): the next tag sequence not held open.
+inline uint32_t next_weld_seq(E& e) {
+  const uint32_t MAXS = 4095;
+  uint32_t q = (e.weldSeq % MAXS) + 1;
+  for (uint32_t guard = 0; guard <= MAXS && q == e.weldHoldSeq; ++guard) q = (q % MAXS) + 1;
+  e.weldSeq = q;
+  return q;
+}
+
 // jet_accel (src/sim.wgsl:935-949): the sum of the accelerations of the jets
 // whose disc holds p; saturating, so overlapping jets never flip sign.
 constexpr uint32_t JET_SH = 9;
@@ -1163,6 +1173,7 @@ int sno_load_scene(SnoEngine* e, uint32_t n, uint32_t nFluid, const int32_t* pos
   e->n = n; e->nFluid = nFluid; e->gridW = gW; e->gridH = gH; e->cellTotal = (uint32_t)ct;
   e->cellShift = cellShift; e->domW = domW; e->domH = domH; e->originX = 0; e->originY = 0;
   e->vmax = VMAX; e->weldHold = 0; e->fuseTag = 0; e->wallsOn = true;
+  e->weldSeq = 1; e->weldHoldSeq = 0; e->lastWeldTag = 0;
   e->substepCount = 0; e->parity = 0; e->formationClock = 0; e->bondDirty = true;
   e->unsupported = 0;
   uint32_t cap = e->maxParticles;
@@ -1212,7 +1223,40 @@ int sno_load_scene(SnoEngine* e, uint32_t n, uint32_t nFluid, const int32_t* pos
 int sno_step(SnoEngine* e, uint32_t count) {
   if (e->n == 0) return -1;
   for (uint32_t s = 0; s < count; ++s) substep(*e);
+  // step() (src/engine.js:3990-3997): the arm dies with the formation pass
+  // after its gesture was released.
+  if (count > 0 && e->fuseTag != 0 && e->weldHold == 0) e->fuseTag = 0;
   return e->unsupported ? -9 : 0;
+}
+
+// Weld groups (src/engine.js:4570-4680).
+int sno_hold_weld_group(SnoEngine* e, uint32_t tag) {
+  const uint32_t t = tag & WELD_TAG_MASK;
+  if (t == 0) return -1;
+  e->weldHold = t;
+  e->weldHoldSeq = t >> 8;
+  return (int)t;
+}
+uint32_t sno_end_weld_group(SnoEngine* e) {
+  if (e->weldHold == 0) return 0;
+  const uint32_t was = e->weldHold;
+  e->weldHold = 0;
+  e->weldHoldSeq = 0;
+  e->bondDirty = true;
+  return was;
+}
+uint32_t sno_begin_weld_group(SnoEngine* e) {
+  if (e->weldHold != 0) sno_end_weld_group(e);
+  if (e->fuseTag != 0) e->fuseTag = 0;
+  return (uint32_t)sno_hold_weld_group(e, (next_weld_seq(*e) << 8) & WELD_TAG_MASK);
+}
+int sno_arm_fuse(SnoEngine* e) {
+  if (e->weldHold == 0) return -1;
+  e->fuseTag = e->weldHold;
+  return (int)e->fuseTag;
+}
+void sno_weld_state(SnoEngine* e, uint32_t out[4]) {
+  out[0] = e->weldHold; out[1] = e->fuseTag; out[2] = e->lastWeldTag; out[3] = e->weldSeq;
 }
 
 void sno_digest(SnoEngine* e, uint32_t acc[8]) { digest(*e, e->st[e->parity], acc); }
@@ -1314,15 +1358,17 @@ int64_t sno_spawn(SnoEngine* e, const int32_t* rows, uint32_t k, int hasTemp, in
   uint32_t newFluid = e->nFluid + k, newN = newFluid + nB;
   if (newN > e->maxParticles) return e->n;
   std::vector<Particle>& stb = e->st[e->parity];
-  // weld tag: no gesture API here, so every spawn is its own group; seq 1 is
-  // taken by the loaded scene (src/engine.js `_weldSeq = 1` at load).
-  static_cast<void>(noWeld);
+  // noWeld bit 0: {noWeld: true}; bit 1: {ownGroup: true}
   for (uint32_t i = 0; i < k; ++i) {
     const int32_t* r = rows + 8 * i;
     int32_t mm = r[4] < 0 ? 0 : r[4];
     uint32_t m = (uint32_t)std::min<int32_t>((int32_t)e->matCount - 1, mm);
     if (rigid_row(e->mats[m])) return -9;
   }
+  // §18.2 W1 + §18.22 (src/engine.js:5925-5935): one gesture is one group.
+  const uint32_t seq = (e->weldHoldSeq != 0 && !(noWeld & 2)) ? e->weldHoldSeq : next_weld_seq(*e);
+  const uint32_t tagNow = (seq << 8) & WELD_TAG_MASK;
+  e->lastWeldTag = tagNow;
   for (uint32_t i = 0; i < k; ++i) {
     const int32_t* r = rows + 8 * i;
     int32_t mm = r[4] < 0 ? 0 : r[4];
@@ -1330,8 +1376,7 @@ int64_t sno_spawn(SnoEngine* e, const int32_t* rows, uint32_t k, int hasTemp, in
     const int32_t* row = e->mats[m];
     Particle p;
     p.px = r[0]; p.py = r[1]; p.vx = r[2]; p.vy = r[3]; p.matId = m;
-    uint32_t weldTag = 0;
-    if (!noWeld && spawn_welds(row)) return -10;  // gesture weld tags are not modelled
+    const uint32_t weldTag = (!(noWeld & 1) && spawn_welds(row)) ? tagNow : 0u;
     p.flags = ((uint32_t)r[5] & (FLAG_BURNING | FLAG_ANCHOR)) | (row[M_phantom] != 0 ? FLAG_DEAD : 0u) |
               (seal_class_row(row) ? FLAG_SEAL : 0u) | weldTag;
     int32_t t = hasTemp ? r[6] : row[M_spawnTemp];

@@ -177,6 +177,11 @@ SIGNATURES = {
     'sn3_get_info': (ctypes.c_int, [P, u32, ctypes.POINTER(Sn3Info)]),
     'sn3_last_timing': (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(u64)]),
     'sn3_profile_substep': (ctypes.c_int, [P, u32, P, u32, ctypes.POINTER(u32)]),
+    'sn_begin_weld_group': (ctypes.c_int, [P, ctypes.POINTER(u32)]),
+    'sn_hold_weld_group': (ctypes.c_int, [P, u32]),
+    'sn_end_weld_group': (ctypes.c_int, [P, ctypes.POINTER(u32)]),
+    'sn_arm_fuse': (ctypes.c_int, [P, ctypes.POINTER(u32)]),
+    'sn_weld_state': (ctypes.c_int, [P, P]),
     'sn_write_bonds': (ctypes.c_int, [P, P, ctypes.c_size_t]),
     'sn_batch_write_bonds': (ctypes.c_int, [P, u32, P, ctypes.c_size_t]),
     'sn_erase': (ctypes.c_int, [P, P, ctypes.c_size_t, ctypes.POINTER(u32)]),

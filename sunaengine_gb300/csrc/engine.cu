@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <cstdarg>
 #include <cstdio>
+#include <cstddef>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -143,7 +144,9 @@ struct SceneHost {
   std::vector<uint32_t> mat;
   uint32_t nFluid0 = 0;
   bool hasTemp = false, hasFuel = false;
-  uint32_t weldSeq = 1;
+  uint32_t weldSeq = 1;                   // _weldSeq: the loaded scene holds tag sequence 1
+  uint32_t weldHold = 0, weldHoldSeq = 0;  // the gesture held open
+  uint32_t fuseTag = 0, lastWeldTag = 0;
   bool wallsOn = true;
   std::vector<ImpulseEv> events;
   uint32_t consumed = 0;  // events already applied (at < substeps)
@@ -500,6 +503,7 @@ struct World {
     if (sc->temp) h.temp.assign(sc->temp, sc->temp + sc->n);
     if (sc->fuel) h.fuel.assign(sc->fuel, sc->fuel + sc->n);
     h.weldSeq = 1;
+    h.weldHold = h.weldHoldSeq = h.fuseTag = h.lastWeldTag = 0;
     h.wallsOn = true;
     h.events.clear();
     h.consumed = 0;
@@ -882,6 +886,10 @@ struct World {
     lastLaunches = launchesPerSubstep * count;
     paramsStale = true;
     accFresh = chainOn;
+    // step() (src/engine.js:3990-3997): an armed fusion outlives its gesture
+    // only until the formation pass after release, i.e. this call.
+    for (uint32_t s2 = 0; s2 < maxScenes; ++s2)
+      if (sh[s2].used && sh[s2].loaded && sh[s2].fuseTag != 0 && sh[s2].weldHold == 0 && !set_fuse(s2, 0)) return false;
     return cuda_ok(cudaGetLastError(), "step");
   }
 
@@ -960,7 +968,7 @@ struct World {
   }
 
   // spawnFluid (src/engine.js:5901-6020) for scene s.
-  bool spawn(uint32_t s, const sn_particle* list, uint32_t k, bool noWeld, uint32_t* nOut) {
+  bool spawn(uint32_t s, const sn_particle* list, uint32_t k, bool noWeld, uint32_t* nOut, bool ownGroup = false) {
     accFresh = false;
     SceneHost& h = sh[s];
     if (!h.loaded) return fail("spawn before loadScene");
@@ -975,8 +983,12 @@ struct World {
         return fail("spawn position outside [-2^28, 2^28]");
       int32_t mm = std::min<int32_t>((int32_t)matCount - 1, std::max<int32_t>(0, list[i].mat));
       if (rigid_row((uint32_t)mm)) return fail("spawn of rigid-body row %d (solidMode 2) is not supported", mm);
-      if (!noWeld && spawn_welds((uint32_t)mm)) return fail("weld-group spawns are not supported");
     }
+    // §18.2 W1 + §18.22 (src/engine.js:5925-5935): one gesture is one group;
+    // a spawn outside an open gesture is its own group.
+    const uint32_t seq = (h.weldHoldSeq != 0 && !ownGroup) ? h.weldHoldSeq : next_weld_seq(h);
+    const uint32_t weldTag = (seq << 8) & WELD_TAG_MASK;
+    h.lastWeldTag = weldTag;
     uint32_t total = k + nB;
     std::vector<int32_t> stw((size_t)total * 8, 0);
     for (uint32_t i = 0; i < k; ++i) {
@@ -990,7 +1002,7 @@ struct World {
       w[3] = q.vy;
       w[4] = (int32_t)m;
       w[5] = (int32_t)((q.flags & SPAWN_FLAG_MASK) | (r[M_phantom] != 0 ? FLAG_DEAD : 0u) |
-                       (seal_row(m) ? FLAG_SEAL : 0u));
+                       (seal_row(m) ? FLAG_SEAL : 0u) | ((!noWeld && spawn_welds(m)) ? weldTag : 0u));
       int32_t t = q.has_temp ? q.temp : r[M_spawnTemp];
       w[6] = std::max(TEMP_MIN, std::min(TEMP_MAX, t));
       w[7] = std::max(0, q.has_fuel ? q.fuel : r[M_fuel0]);
@@ -1165,6 +1177,63 @@ struct World {
     layoutDirty = true;
     eventsDirty = true;
     return push_scene(s) && cuda_ok(cudaStreamSynchronize(st), "erase");
+  }
+
+  // ---- weld groups (src/engine.js:4570-4680) -----------------------------------
+  // _nextWeldSeq: the next 12-bit tag sequence not held open (no rigid bodies
+  // exist here to take one).
+  static uint32_t next_weld_seq(SceneHost& h) {
+    const uint32_t MAXS = 4095;
+    uint32_t q = (h.weldSeq % MAXS) + 1;
+    for (uint32_t guard = 0; guard <= MAXS && q == h.weldHoldSeq; ++guard) q = (q % MAXS) + 1;
+    h.weldSeq = q;
+    return q;
+  }
+  // One ScenePar word, written in stream order without touching the clocks.
+  bool put_word(uint32_t s, size_t off, uint32_t v) {
+    return cuda_ok(cudaMemcpyAsync(reinterpret_cast<char*>(b.scenes + s) + off, &v, 4, cudaMemcpyHostToDevice, st),
+                   "param") &&
+           cuda_ok(cudaStreamSynchronize(st), "param");
+  }
+  bool set_weld_hold(uint32_t s, uint32_t tag) {
+    sh[s].weldHold = tag;
+    sh[s].weldHoldSeq = tag >> 8;
+    hpar[s].weldHold = tag;
+    return put_word(s, offsetof(ScenePar, weldHold), tag);
+  }
+  bool set_fuse(uint32_t s, uint32_t tag) {
+    sh[s].fuseTag = tag;
+    hpar[s].fuseTag = tag;
+    return put_word(s, offsetof(ScenePar, fuseTag), tag);
+  }
+  bool hold_weld_group(uint32_t s, uint32_t tag, uint32_t* out) {
+    if (!sh[s].loaded) return fail("holdWeldGroup before loadScene");
+    const uint32_t t = tag & WELD_TAG_MASK;
+    if (t == 0) return fail("holdWeldGroup(0): use endWeldGroup() to release");
+    if (out) *out = t;
+    return set_weld_hold(s, t);
+  }
+  bool end_weld_group(uint32_t s, uint32_t* was) {
+    if (!sh[s].loaded) return fail("endWeldGroup before loadScene");
+    if (was) *was = sh[s].weldHold;
+    if (sh[s].weldHold == 0) return true;
+    if (!set_weld_hold(s, 0)) return false;
+    // the formation pass that clears the released tag runs on the next substep
+    if (!pull_params()) return false;
+    hpar[s].bondDirty = 1;
+    return put_word(s, offsetof(ScenePar, bondDirty), 1u);
+  }
+  bool begin_weld_group(uint32_t s, uint32_t* tag) {
+    if (!sh[s].loaded) return fail("beginWeldGroup before loadScene");
+    if (sh[s].weldHold != 0 && !end_weld_group(s, nullptr)) return false;
+    if (sh[s].fuseTag != 0 && !set_fuse(s, 0)) return false;
+    return hold_weld_group(s, (next_weld_seq(sh[s]) << 8) & WELD_TAG_MASK, tag);
+  }
+  bool arm_fuse(uint32_t s, uint32_t* tag) {
+    if (!sh[s].loaded) return fail("armFuse before loadScene");
+    if (sh[s].weldHold == 0) return fail("armFuse(): no weld group is open");
+    if (tag) *tag = sh[s].weldHold;
+    return set_fuse(s, sh[s].weldHold);
   }
 
   // setJets (src/engine.js:4740-4770): the first 8 jets, [x, y, r, fx, fy].
@@ -1349,7 +1418,8 @@ int sn_read_bonds(sn_engine* e, uint32_t* out, size_t words) {
 }
 int sn_spawn(sn_engine* e, const sn_particle* list, uint32_t k, uint32_t no_weld, uint32_t* n_out) {
   if (!e || (k && !list)) return SN_E_INVALID;
-  return rc_of(e->w, e->w.spawn(0, list, k, no_weld != 0, n_out));
+  return rc_of(e->w, e->w.spawn(0, list, k, (no_weld & SN_SPAWN_NO_WELD) != 0, n_out,
+                                (no_weld & SN_SPAWN_OWN_GROUP) != 0));
 }
 int sn_impulse(sn_engine* e, int32_t cx, int32_t cy, int32_t r, int32_t ix, int32_t iy, uint32_t limit,
                uint32_t* hits) {
@@ -1500,6 +1570,31 @@ int sn_batch_write_state(sn_batch* b, uint32_t id, const int32_t* state, const i
   w.hpar[id].substep = (uint32_t)substep_count;
   w.eventsDirty = true;
   return rc_of(w, w.push_scene(id) && w.cuda_ok(cudaStreamSynchronize(w.st), "write"));
+}
+int sn_begin_weld_group(sn_engine* e, uint32_t* tag) {
+  if (!e) return SN_E_INVALID;
+  return rc_of(e->w, e->w.begin_weld_group(0, tag));
+}
+int sn_hold_weld_group(sn_engine* e, uint32_t tag) {
+  if (!e) return SN_E_INVALID;
+  return rc_of(e->w, e->w.hold_weld_group(0, tag, nullptr));
+}
+int sn_end_weld_group(sn_engine* e, uint32_t* was) {
+  if (!e) return SN_E_INVALID;
+  return rc_of(e->w, e->w.end_weld_group(0, was));
+}
+int sn_arm_fuse(sn_engine* e, uint32_t* tag) {
+  if (!e) return SN_E_INVALID;
+  return rc_of(e->w, e->w.arm_fuse(0, tag));
+}
+int sn_weld_state(sn_engine* e, uint32_t out[4]) {
+  if (!e || !out) return SN_E_INVALID;
+  const SceneHost& h = e->w.sh[0];
+  out[0] = h.weldHold;
+  out[1] = h.fuseTag;
+  out[2] = h.lastWeldTag;
+  out[3] = h.weldSeq;
+  return SN_OK;
 }
 int sn_write_bonds(sn_engine* e, const uint32_t* bonds, size_t words) {
   if (!e) return SN_E_INVALID;

@@ -1283,9 +1283,10 @@ __global__ void __launch_bounds__(256) k_form1(Bufs b) {
       uint32_t tagI = flI & WELD_TAG_MASK;
       int32_t ki = bond_k(b, matI, wi[6], f);
       bool canReform = (!anchoredI && matw(b, matI, M_bondReform) != 0 && ki != 0);
+      bool fuseArmed = S.fuseTag != 0u && fuse_row(b, matI);
       bool congealI = (flI & FLAG_CONGEAL) && fuse_row(b, matI);
       bool congealNear = seen && fuse_row(b, matI);
-      if (canReform || (!anchoredI && tagI != 0u) || congealI || congealNear) {
+      if (canReform || (!anchoredI && tagI != 0u) || fuseArmed || congealI || congealNear) {
         for (uint32_t k = 0; k < cnt; ++k) {
           if (cn >= (uint32_t)BOND_CAP) { f.flag(8); break; }
           uint32_t e = b.NBR[(size_t)k * stride + p];
@@ -1297,10 +1298,14 @@ __global__ void __launch_bounds__(256) k_form1(Bufs b) {
           uint32_t fJ = (uint32_t)wj[5];
           uint32_t tagJ = fJ & WELD_TAG_MASK;
           bool weld = (!anchoredI && tagI != 0u && tagI == tagJ);
+          bool fuse = false;
+          if (fuseArmed && !(fJ & FLAG_RIGID) && fuse_row(b, mj) && (!anchoredI || !(fJ & FLAG_ANCHOR)))
+            fuse = (tagI == S.fuseTag && tagJ == 0u) || (tagJ == S.fuseTag && tagI == 0u) ||
+                   (tagI == S.fuseTag && tagJ == S.fuseTag);
           bool congealJ = (fJ & FLAG_CONGEAL) && fuse_row(b, mj);
-          bool congeal = ((congealI || congealJ) && !weld && mj == matI && !(fJ & FLAG_RIGID));
-          if (!congeal && matw(b, mj, M_bondGroup) != matw(b, matI, M_bondGroup)) continue;
-          if (!weld && !congeal) {
+          bool congeal = ((congealI || congealJ) && !weld && !fuse && mj == matI && !(fJ & FLAG_RIGID));
+          if (!fuse && !congeal && matw(b, mj, M_bondGroup) != matw(b, matI, M_bondGroup)) continue;
+          if (!weld && !fuse && !congeal) {
             if (!canReform) continue;
             if (bond_k(b, mj, wj[6], f) == 0) continue;
           }
@@ -1313,7 +1318,7 @@ __global__ void __launch_bounds__(256) k_form1(Bufs b) {
           if (abs(d4x) > L0_MAX || abs(d4y) > L0_MAX) continue;
           int32_t d2 = wadd(wmul(d4x, d4x), wmul(d4y, d4y));
           if (d2 < D2_FLOOR || d2 > BOND_R2) continue;
-          if (!weld && !congeal) {
+          if (!weld && !fuse && !congeal) {
             int32_t vl = min(matw(b, matI, M_bondFormV), matw(b, mj, M_bondFormV));
             int32_t vl4 = shr_rne<RPRE>(vl);
             int32_t r4x = shr_rne<RPRE>(sub_sat(wi[2], wj[2], f));

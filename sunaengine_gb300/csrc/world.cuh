@@ -33,7 +33,7 @@ struct ScenePar {
   uint32_t n, nFluid;
   uint32_t gridW, gridH, cellShift, cellTotal;
   int32_t domW, domH, vmax;
-  uint32_t weldHold;
+  uint32_t weldHold;   // the weld tag a gesture holds open (0: none)
   uint32_t keyOff[4];  // global key of this scene's first colour-c cell
   uint32_t nA[4];      // colour-c cells per grid row: (gridW + 1 - (c & 1)) / 2
   uint32_t formClock;  // formation clock (the engine's `_substep`), advanced on device
@@ -41,6 +41,7 @@ struct ScenePar {
   uint32_t formNow;    // formation runs in the substep in flight (set by predict)
   uint32_t active;     // 0 = slot range reserved but not stepped
   uint32_t substep;    // substeps advanced since load (impulse schedule clock)
+  uint32_t fuseTag;    // §18.24 armed draw-time fusion tag (0: none)
   uint32_t nJets;      // §23.B jets (setJets): 0..8
   int32_t jet[8][5];   // [x, y, r, fx, fy] ticks
 };

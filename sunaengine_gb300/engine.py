@@ -205,6 +205,36 @@ class Engine:
         self._check(self._lib.sn_read_bonds(self._h, _ptr(a), a.size), 'readBond')
         return a[:self.n_fluid * BOND_CAP]
 
+    # weld groups (src/engine.js:4570-4680)
+    def begin_weld_group(self) -> int:
+        t = ctypes.c_uint32()
+        self._check(self._lib.sn_begin_weld_group(self._h, ctypes.byref(t)), 'beginWeldGroup')
+        return int(t.value)
+
+    def hold_weld_group(self, tag: int) -> int:
+        self._check(self._lib.sn_hold_weld_group(self._h, int(tag)), 'holdWeldGroup')
+        return int(tag) & 0x000fff00
+
+    def end_weld_group(self) -> int:
+        t = ctypes.c_uint32()
+        self._check(self._lib.sn_end_weld_group(self._h, ctypes.byref(t)), 'endWeldGroup')
+        return int(t.value)
+
+    def arm_fuse(self) -> int:
+        t = ctypes.c_uint32()
+        self._check(self._lib.sn_arm_fuse(self._h, ctypes.byref(t)), 'armFuse')
+        return int(t.value)
+
+    def weld_state(self):
+        a = np.zeros(4, np.uint32)
+        self._check(self._lib.sn_weld_state(self._h, _ptr(a)), 'weldState')
+        return dict(zip(('weld_hold', 'fuse_tag', 'last_weld_tag', 'weld_seq'), (int(x) for x in a)))
+
+    beginWeldGroup = begin_weld_group
+    holdWeldGroup = hold_weld_group
+    endWeldGroup = end_weld_group
+    armFuse = arm_fuse
+
     def write_bonds(self, bonds: np.ndarray):
         b = np.ascontiguousarray(bonds, dtype=np.uint32).reshape(-1)
         self._check(self._lib.sn_write_bonds(self._h, _ptr(b), b.size), 'writeBonds')
@@ -242,10 +272,11 @@ class Engine:
     sliceBondsMany = slice_bonds_many
     sliceBonds = slice_bonds
 
-    def spawn_fluid(self, particles, no_weld: bool = True) -> int:
+    def spawn_fluid(self, particles, no_weld: bool = True, own_group: bool = False) -> int:
         arr, k = _particles(particles)
         out = ctypes.c_uint32()
-        self._check(self._lib.sn_spawn(self._h, arr, k, 1 if no_weld else 0, ctypes.byref(out)), 'spawnFluid')
+        opts = (1 if no_weld else 0) | (2 if own_group else 0)
+        self._check(self._lib.sn_spawn(self._h, arr, k, opts, ctypes.byref(out)), 'spawnFluid')
         n = int(out.value)
         if n != self._n:
             self._n_fluid += n - self._n

@@ -43,3 +43,38 @@ def test_edit_sequence_matches_oracle():
     steps(6)
     assert g.digest().hex == r.digest()
     assert list(g.debug_counters()) == list(r.debug_counters())
+
+
+def test_weld_gestures_and_fusion_match_oracle():
+    import test_weld as w
+    sc = w.pole_scene()
+    g = Engine(max_particles=6000, debug=True).load_scene(sc)
+    r = w.oracle(sc)
+
+    def steps(k):
+        g.step(k)
+        r.step(k)
+        assert g.chain_hex() == r.chain_hex()
+        assert g.weld_state() == r.weld_state()
+
+    steps(2)
+    assert g.begin_weld_group() == r.begin_weld_group()
+    for k in range(3):
+        assert g.spawn_fluid(w.stroke(30 * w.ONE + k * 3 * w.ONE, 10 * w.ONE, 3), no_weld=False) == \
+            r.spawn_fluid(w.stroke(30 * w.ONE + k * 3 * w.ONE, 10 * w.ONE, 3), no_weld=False)
+        steps(1)
+    assert g.end_weld_group() == r.end_weld_group()
+    steps(3)
+    g.spawn_fluid(w.stroke(8 * w.ONE, 8 * w.ONE, 4), no_weld=False, own_group=True)
+    r.spawn_fluid(w.stroke(8 * w.ONE, 8 * w.ONE, 4), no_weld=False, own_group=True)
+    steps(2)
+    g.begin_weld_group(), r.begin_weld_group()
+    assert g.arm_fuse() == r.arm_fuse()
+    band = w.stroke(21 * w.ONE, 25 * w.ONE + w.ONE // 2, 6)
+    g.spawn_fluid(band, no_weld=False)
+    r.spawn_fluid(band, no_weld=False)
+    steps(1)
+    g.end_weld_group(), r.end_weld_group()
+    steps(5)
+    assert np.array_equal(g.read_bonds(), r.read_bonds())
+    assert list(g.debug_counters()) == list(r.debug_counters())
