@@ -224,12 +224,53 @@ int sn_batch_erase(sn_batch* b, uint32_t id, const uint8_t* keep, size_t n, uint
  * ignored, as the reference slices to JET_MAX. A particle whose position lies
  * in a jet's disc gets its acceleration in predict (jet_accel,
  * src/sim.wgsl:935-949). k = 0 removes them (bit-inert). *n_out = jets kept.
- * setUserDrive (src/engine.js:4797-4815) is stored clamped to +-USER_A_MAX and
- * returned; it drives only user-flagged rigid bodies, which this engine does
- * not build, so it changes no result here. */
+ * setUserDrive (src/engine.js:4797-4815) is stored clamped to +-USER_A_MAX
+ * (32768) and returned in out[2]; rigidStep adds it to the velocity of every
+ * free body flagged as the user's (RB_USER). */
 int sn_set_jets(sn_engine* e, const int32_t* jets, uint32_t k, uint32_t* n_out);
 int sn_batch_set_jets(sn_batch* b, uint32_t id, const int32_t* jets, uint32_t k, uint32_t* n_out);
 int sn_set_user_drive(sn_engine* e, int32_t ax, int32_t ay, int32_t out[2]);
+
+/* ---- §20 rigid bodies (src/sim.wgsl:3070-3747; host src/engine.js:5452-5811) ---
+ * A body is a set of fluid slots of a solidMode-rigid row wearing FLAG_RIGID
+ * and one weld tag; its record (32 int32 words, the reference's RB_* layout,
+ * src/sim.wgsl:703-793) holds centre, velocity, angle (BAM), spin, carried
+ * remainders, member count and inertia; every member is placed at
+ * c + R(theta) * o each substep from its exact rest offset o.
+ *   sn_make_rigid_body   makeRigidBody(slots, pivot, user) :5722 (pivot NULL:
+ *                        a free body; {x, y} ticks: an axis body, makeAxisBody)
+ *   sn_promote_weld_group promoteWeldGroup(tag, pivot, user) :5584 (tag 0 =
+ *                        the gesture held open)
+ *   sn_end_weld_group_and_promote endWeldGroupAndPromote(pivot, user) :5782
+ *   sn_dissolve_all_bodies dissolveAllBodies() :5789, *count = members freed
+ *   sn_read_bodies       readBodies() :5811: *count records of 32 words (word
+ *                        29 reads 0); out may be NULL to get the count
+ *   sn_read_rest_offsets readRestOffsets() :5817: n*2 words
+ *   sn_set_body_user     setBodyUser(index, on) :5319
+ *   sn_set_body_driver   one body's driver sidecar (the words
+ *                        setBodyConstraint's evaluator uploads, :5343-5412):
+ *                        mask of RD_HAS_* bits (< 512) and nine values
+ *                        {px, py, angle, vx, vy, omega, fx, fy, torque}; they
+ *                        hold until changed or cleared
+ *   sn_drag_body         dragGrab(grab, x, y, vx, vy) for a rigid grab :6111
+ *   sn_restore_bodies    restoreAuthoringSnapshot's body records and rest
+ *                        offsets :5838 (drivers cleared)
+ * Index arguments and *index results are the body's position in readBodies;
+ * *index = -1 where the reference returns null (too few members, no slot).
+ * eraseWhere repairs the bodies (survivors keep their rest offsets); a scene
+ * load dissolves them; checkpoints of a scene with bodies are refused. */
+int sn_make_rigid_body(sn_engine* e, const uint32_t* slots, uint32_t k, const int32_t* pivot, uint32_t user,
+                       int32_t* index);
+int sn_promote_weld_group(sn_engine* e, uint32_t tag, const int32_t* pivot, uint32_t user, int32_t* index);
+int sn_end_weld_group_and_promote(sn_engine* e, const int32_t* pivot, uint32_t user, int32_t* index);
+int sn_dissolve_all_bodies(sn_engine* e, uint32_t* count);
+int sn_read_bodies(sn_engine* e, int32_t* out, size_t words, uint32_t* count);
+int sn_read_rest_offsets(sn_engine* e, int32_t* out, size_t words);
+int sn_set_body_user(sn_engine* e, uint32_t index, uint32_t on, uint32_t* found);
+int sn_set_body_driver(sn_engine* e, uint32_t index, int32_t mask, const int32_t values[9]);
+int sn_clear_body_drivers(sn_engine* e);
+int sn_drag_body(sn_engine* e, uint32_t tag, int32_t x, int32_t y, int32_t vx, int32_t vy, uint32_t* moved);
+int sn_restore_bodies(sn_engine* e, const int32_t* records, uint32_t count, const int32_t* rest, size_t rest_words);
 
 /* ---- lane autotuner ----------------------------------------------------------
  * No counterpart in the reference. The neighbour gathers of solveA, the colour

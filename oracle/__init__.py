@@ -87,6 +87,32 @@ def lib():
         l.sno_erase.argtypes = [P, np.ctypeslib.ndpointer(np.uint8, flags='C')]
         l.sno_set_jets.restype = ctypes.c_uint32
         l.sno_set_jets.argtypes = [P, i32p, ctypes.c_uint32]
+        for f in ('sno_make_rigid_body',):
+            getattr(l, f).restype = ctypes.c_int32
+            getattr(l, f).argtypes = [P, u32p, ctypes.c_uint32, P, ctypes.c_int]
+        l.sno_promote_weld_group.restype = ctypes.c_int32
+        l.sno_promote_weld_group.argtypes = [P, ctypes.c_uint32, P, ctypes.c_int]
+        l.sno_end_weld_group_and_promote.restype = ctypes.c_int32
+        l.sno_end_weld_group_and_promote.argtypes = [P, P, ctypes.c_int]
+        for f in ('sno_dissolve_all_bodies', 'sno_body_count'):
+            getattr(l, f).restype = ctypes.c_uint32
+            getattr(l, f).argtypes = [P]
+        for f in ('sno_read_bodies', 'sno_read_rest'):
+            getattr(l, f).restype = ctypes.c_int
+            getattr(l, f).argtypes = [P, i32p, ctypes.c_size_t]
+        l.sno_set_body_user.restype = ctypes.c_int
+        l.sno_set_body_user.argtypes = [P, ctypes.c_uint32, ctypes.c_int]
+        l.sno_set_body_driver.restype = ctypes.c_int
+        l.sno_set_body_driver.argtypes = [P, ctypes.c_uint32, ctypes.c_int32, i32p]
+        l.sno_clear_body_drivers.restype = ctypes.c_int
+        l.sno_clear_body_drivers.argtypes = [P]
+        l.sno_set_user_drive.restype = ctypes.c_int32
+        l.sno_set_user_drive.argtypes = [P, ctypes.c_int32, ctypes.c_int32]
+        l.sno_drag_body.restype = ctypes.c_int
+        l.sno_drag_body.argtypes = [P, ctypes.c_uint32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                    ctypes.c_int32]
+        l.sno_restore_bodies.restype = ctypes.c_int
+        l.sno_restore_bodies.argtypes = [P, i32p, ctypes.c_uint32, P, ctypes.c_size_t]
         l.sno_impulse.restype = ctypes.c_int64
         l.sno_impulse.argtypes = [P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                   ctypes.c_int32, ctypes.c_uint32]
@@ -299,6 +325,79 @@ class OracleEngine:
 
     def set_walls(self, on: bool) -> bool:
         return bool(lib().sno_set_walls(self.h, 1 if on else 0))
+
+    # §20 rigid bodies (src/engine.js:5452-5811)
+    @staticmethod
+    def _pivot(pivot):
+        if pivot is None:
+            return None, None
+        a = np.ascontiguousarray([int(pivot[0]), int(pivot[1])], dtype=np.int32)
+        return a, a.ctypes.data_as(ctypes.c_void_p)
+
+    def make_rigid_body(self, slots, pivot=None, user: bool = False):
+        s = np.ascontiguousarray(np.asarray(slots, dtype=np.int64).clip(0, 2**32 - 1).astype(np.uint32))
+        keep, pp = self._pivot(pivot)
+        r = lib().sno_make_rigid_body(self.h, s if s.size else np.zeros(1, np.uint32), s.size, pp, int(bool(user)))
+        if r == -2:
+            raise ValueError('[aether] §20: no free weld tag for a new body')
+        return None if r < 0 else int(r)
+
+    def make_axis_body(self, slots, px: int, py: int, user: bool = False):
+        return self.make_rigid_body(slots, (px, py), user)
+
+    def promote_weld_group(self, tag: int = 0, pivot=None, user: bool = False):
+        keep, pp = self._pivot(pivot)
+        r = lib().sno_promote_weld_group(self.h, int(tag), pp, int(bool(user)))
+        return None if r < 0 else int(r)
+
+    def end_weld_group_and_promote(self, pivot=None, user: bool = False):
+        keep, pp = self._pivot(pivot)
+        r = lib().sno_end_weld_group_and_promote(self.h, pp, int(bool(user)))
+        return None if r < 0 else int(r)
+
+    def dissolve_all_bodies(self) -> int:
+        return int(lib().sno_dissolve_all_bodies(self.h))
+
+    @property
+    def body_count(self) -> int:
+        return int(lib().sno_body_count(self.h))
+
+    def read_bodies(self) -> np.ndarray:
+        a = np.zeros(max(1, self.body_count) * 32, np.int32)
+        lib().sno_read_bodies(self.h, a, a.size)
+        return a[:self.body_count * 32].reshape(-1, 32)
+
+    def read_rest_offsets(self) -> np.ndarray:
+        a = np.zeros(max(1, self.n) * 2, np.int32)
+        lib().sno_read_rest(self.h, a, a.size)
+        return a[:self.n * 2]
+
+    def set_body_user(self, index: int, on: bool) -> bool:
+        return bool(lib().sno_set_body_user(self.h, int(index), int(bool(on))))
+
+    def set_body_driver(self, index: int, mask: int, values):
+        v = np.zeros(9, np.int32)
+        v[:len(values)] = np.asarray(values, dtype=np.int64).clip(-2**31, 2**31 - 1)
+        if lib().sno_set_body_driver(self.h, int(index), int(mask), v) != 0:
+            raise ValueError('body driver: no such body or bad mask')
+
+    def clear_body_drivers(self):
+        lib().sno_clear_body_drivers(self.h)
+
+    def set_user_drive(self, ax: int, ay: int):
+        lib().sno_set_user_drive(self.h, int(ax), int(ay))
+
+    def drag_body(self, tag: int, tx: int, ty: int, vx: int = 0, vy: int = 0) -> int:
+        return int(lib().sno_drag_body(self.h, int(tag), int(tx), int(ty), int(vx), int(vy)))
+
+    def restore_bodies(self, records, rest=None):
+        r = np.ascontiguousarray(np.asarray(records, dtype=np.int32).reshape(-1))
+        nb = r.size // 32
+        rr = None if rest is None else np.ascontiguousarray(np.asarray(rest, dtype=np.int32).reshape(-1))
+        if lib().sno_restore_bodies(self.h, r if r.size else np.zeros(32, np.int32), nb,
+                                    None if rr is None else rr.ctypes.data_as(ctypes.c_void_p),
+                                    0 if rr is None else rr.size) != 0:
+            raise ValueError('restore_bodies: bad sizes')
 
     # the Engine method names, so the demo layer can drive either engine
     def spawn_fluid(self, particles, no_weld: bool = True, own_group: bool = False) -> int:

@@ -13,10 +13,9 @@
 //   src/hash/statehash.js                 -> digest(), fold_chain()
 //   src/engine.js loadScene/_encodeSubstep/spawnFluid/applyImpulse
 //
-// Scope: the fluid, friction, bond, thermal and formation passes. Rigid bodies
-// (src/sim.wgsl section 20) and containment (section 29) are not restated;
-// rows that would activate them are refused at load/spawn and a transition
-// into one raises an error word (see `unsupported`).
+// Scope: the fluid, friction, bond, thermal and formation passes, containment
+// (src/sim.wgsl section 29) and rigid bodies (section 20, with the host's body
+// record math from src/engine.js:2050-2150 and 5452-5811).
 //
 // Parity is pinned by the reference's frozen dambreak_v1 chain
 // (test/extraction_gate.md:62-68).
@@ -131,6 +130,17 @@ struct SnoEngine {
   // §23.B jets (setJets, src/engine.js:4740-4770): [x, y, r, fx, fy] ticks
   int32_t jets[8][5] = {};
   uint32_t nJets = 0;
+  // §20 rigid bodies (src/sim.wgsl:670-821): body records in the reference's
+  // 32-word layout, the 10-word driver sidecars, rest offsets per slot, the
+  // Q22 quarter-turn cosine table, and the host's body list (`_bodies`).
+  struct BodyDesc {
+    uint32_t tag = 0, first = 0, last = 0, n = 0;
+    bool axis = false, user = false;
+  };
+  std::vector<int32_t> rbody, rdrive, rest;
+  std::vector<BodyDesc> bodies;
+  int32_t cosT[1026];
+  int32_t userA[2] = {0, 0};
   // the loaded scene's boundary block, for spawnFluid's relocation
   std::vector<int32_t> scenePos, sceneTemp, sceneFuel;
   std::vector<uint32_t> sceneMat;
@@ -238,11 +248,18 @@ inline int32_t iabs(int32_t x) { return x < 0 ? (int32_t)(0u - (uint32_t)x) : x;
 // ---- passes ------------------------------------------------------------------
 
 // src/sim.wgsl:958-1000
-// _nextWeldSeq (src/engine.js:4570-4580): the next tag sequence not held open.
+// _nextWeldSeq (src/engine.js:4570-4580): the next tag sequence that is neither
+// held open nor worn by a body of the host's body list.
+inline bool weld_seq_taken(const E& e, uint32_t q) {
+  if (q == e.weldHoldSeq) return true;
+  for (const auto& b : e.bodies)
+    if ((b.tag >> 8) == q) return true;
+  return false;
+}
 inline uint32_t next_weld_seq(E& e) {
   const uint32_t MAXS = 4095;
   uint32_t q = (e.weldSeq % MAXS) + 1;
-  for (uint32_t guard = 0; guard <= MAXS && q == e.weldHoldSeq; ++guard) q = (q % MAXS) + 1;
+  for (uint32_t guard = 0; guard <= MAXS && weld_seq_taken(e, q); ++guard) q = (q % MAXS) + 1;
   e.weldSeq = q;
   return q;
 }
@@ -725,12 +742,6 @@ void pass_thermal(E& e, std::vector<Particle>& out) {
     if (burning) fl |= FLAG_BURNING;
     if (e.M(mat)[M_phantom] != 0) fl |= FLAG_DEAD;
     if (seal_class_row(e.M(mat))) fl |= FLAG_SEAL;
-    if (rigid_row(e.M(mat))) {
-#ifdef _OPENMP
-#pragma omp atomic
-#endif
-      e.unsupported |= 1u;
-    }
     p.matId = mat; p.flags = fl; p.temp = T; p.fuel = fuel;
   }
 }
@@ -1077,10 +1088,585 @@ void pass_containStress(E& e, std::vector<Particle>& out) {
   }
 }
 
+// ---- §20 rigid bodies (src/sim.wgsl:670-821, 3070-3747) ----------------------
+// One body at a time, members enumerated by [first, last] plus the tag, sums
+// in wrapping i32 (the reference's workgroup tree is exact integer addition,
+// so the order of the terms does not matter).
+constexpr uint32_t RB_LIVE = 0, RB_TAG = 1, RB_FIRST = 2, RB_LAST = 3, RB_CX = 4, RB_CY = 5, RB_VX = 6,
+                   RB_VY = 7, RB_THETA = 8, RB_OMEGA = 9, RB_RESX = 10, RB_RESY = 11, RB_RESVX = 12,
+                   RB_RESVY = 13, RB_N = 14, RB_SUMIS2 = 15, RB_GSUM = 16, RB_INVI = 17, RB_IQ = 18,
+                   RB_RSH = 19, RB_ISH = 20, RB_OMEGAM = 21, RB_RMAX = 22, RB_OSH = 23, RB_CQX = 24,
+                   RB_CQY = 25, RB_THETAQ = 26, RB_AXIS = 27, RB_USER = 28;
+constexpr uint32_t RG_BODY_WORDS = 32, RG_MAX_BODIES = 1024, RG_DRIVER_WORDS = 10;
+constexpr uint32_t RD_MASK = 0, RD_PX = 1, RD_PY = 2, RD_A = 3, RD_VX = 4, RD_VY = 5, RD_W = 6, RD_FX = 7,
+                   RD_FY = 8, RD_TQ = 9;
+constexpr int32_t RD_HAS_PX = 1, RD_HAS_PY = 2, RD_HAS_A = 4, RD_HAS_VX = 8, RD_HAS_VY = 16, RD_HAS_W = 32,
+                  RD_HAS_FX = 64, RD_HAS_FY = 128, RD_HAS_TQ = 256;
+constexpr int32_t BAM_QUARTER = 1073741824, BAM_PER_RAD = 683565276;
+constexpr uint32_t RG_QSH = 20, COS_Q = 22, RG_QN = 1024;
+constexpr int32_t RG_QMASK = 1048575, COS_ONE = 4194304;
+constexpr int32_t RS_TARGET = 2048, TQ_TERM_R = 134217728, NEG_TQ_TERM = -134217728;
+constexpr uint32_t TQ_HI_SH = 15;
+constexpr int32_t RIGID_MIN_MEMBERS = 4, SUMI_MAX = 1073741824;
+constexpr int32_t RG_IQ_MIN = 16, RG_IQ_MAX = 31;
+constexpr int32_t SEAL_R4 = 1126;
+
+// fp_shr_rne with a per-body shift: WGSL takes a shift amount modulo 32, so
+// s = 0 returns x unchanged (rem = 0 and the half-point is 2^31).
+inline int32_t shr_rne_rt(int32_t x, uint32_t s) { return s == 0 ? x : fp_shr_rne(x, s); }
+
+// rg_cos (src/sim.wgsl:836-852): quarter-turn fold + linear interpolation.
+inline int32_t rg_cos(const E& e, int32_t a, const Dbg& g) {
+  const uint32_t q = ((uint32_t)a >> 30) & 3u;
+  const int32_t w = a & 1073741823;
+  int32_t u;
+  bool neg;
+  if (q == 0u) { u = w; neg = false; }
+  else if (q == 1u) { u = BAM_QUARTER - w; neg = true; }
+  else if (q == 2u) { u = w; neg = true; }
+  else { u = BAM_QUARTER - w; neg = false; }
+  const uint32_t idx = (uint32_t)u >> RG_QSH;
+  const int32_t frac = u & RG_QMASK;
+  const int32_t c0 = e.cosT[idx], c1 = e.cosT[idx + 1];
+  const int32_t v = wadd(c0, fp_mul_s(wsub(c1, c0), frac, RG_QSH, g));
+  return neg ? wsub(0, v) : v;
+}
+inline int32_t rg_sin(const E& e, int32_t a, const Dbg& g) { return rg_cos(e, wsub(a, BAM_QUARTER), g); }
+
+// rg_idiv_rne (src/sim.wgsl:862-872): round-half-even divide, sign-symmetric.
+inline int32_t rg_idiv_rne(int32_t a, int32_t n) {
+  if (n <= 0) return 0;
+  const bool neg = a < 0;
+  const int32_t x = neg ? wsub(0, a) : a;
+  int32_t q = (int32_t)((int64_t)x / n);
+  const int32_t r2 = wmul(2, wsub(x, wmul(q, n)));
+  if (r2 > n || (r2 == n && (q & 1) == 1)) q = wadd(q, 1);
+  return neg ? wsub(0, q) : q;
+}
+
+// rg_inv_inertia (src/sim.wgsl:3141-3154)
+inline void rg_inv_inertia(int32_t s, int32_t rsh, int32_t ish, int32_t& invI, int32_t& iq, const Dbg& g) {
+  invI = 0;
+  iq = 0;
+  if (s <= 0) return;
+  const int32_t bl = 32 - (int32_t)clz32((uint32_t)s);
+  const int32_t iqNat = bl - 1 + 2 * ish - rsh;
+  const int32_t q = std::min(iqNat, RG_IQ_MAX);
+  const int32_t E_ = q + rsh - 2 * ish;
+  if (iqNat < RG_IQ_MIN || E_ < 1 || E_ > 62) { g.flag(10); return; }
+  invI = fp_div_s(BAM_PER_RAD, s, (uint32_t)E_, g);
+  iq = q;
+}
+// rg_mul_shr (src/sim.wgsl:3167-3169)
+inline int32_t rg_mul_shr(int32_t a, int32_t b, int32_t s, const Dbg& g) {
+  return i64_shr_rne_sat((int64_t)a * (int64_t)b, (uint32_t)clampi(s, 1, 31), g);
+}
+inline bool rg_is_member(const std::vector<Particle>& st, uint32_t i, int32_t tag) {
+  const uint32_t f = st[i].flags;
+  return (f & FLAG_RIGID) != 0u && (int32_t)weld_tag(f) == tag;
+}
+inline int32_t* body_rec(E& e, uint32_t b) { return e.rbody.data() + (size_t)b * RG_BODY_WORDS; }
+inline const int32_t* body_drv(const E& e, uint32_t b) { return e.rdrive.data() + (size_t)b * RG_DRIVER_WORDS; }
+
+// rg_place (src/sim.wgsl:3193-3206): pred = c + R(theta) * o for every member.
+void rg_place(E& e, const std::vector<Particle>& in, int32_t tag, uint32_t first, uint32_t last, int32_t cx,
+              int32_t cy, int32_t th, const Dbg& g) {
+  const int32_t c = rg_cos(e, th, g), s = rg_sin(e, th, g);
+  for (uint32_t i = first; i <= last && i < e.nFluid; ++i) {
+    if (!rg_is_member(in, i, tag)) continue;
+    const int32_t ox = e.rest[2 * (size_t)i], oy = e.rest[2 * (size_t)i + 1];
+    e.der[i].predx = fp_add_sat(cx, fp_sub_sat(fp_mul_s(ox, c, COS_Q, g), fp_mul_s(oy, s, COS_Q, g), g), g);
+    e.der[i].predy = fp_add_sat(cy, fp_add_sat(fp_mul_s(ox, s, COS_Q, g), fp_mul_s(oy, c, COS_Q, g), g), g);
+  }
+}
+
+// rigidStep (src/sim.wgsl:3226-3440), before predict.
+void pass_rigidStep(E& e, const std::vector<Particle>& in) {
+  Dbg g = e.D();
+  for (uint32_t b = 0; b < (uint32_t)e.bodies.size(); ++b) {
+    int32_t* R = body_rec(e, b);
+    const int32_t* D = body_drv(e, b);
+    const int32_t tag = R[RB_TAG], n = R[RB_N], axis = R[RB_AXIS], usr = R[RB_USER], dmask = D[RD_MASK];
+    const uint32_t first = (uint32_t)R[RB_FIRST], last = (uint32_t)R[RB_LAST], rsh = (uint32_t)R[RB_RSH];
+    const bool ok = R[RB_LIVE] != 0 && n >= RIGID_MIN_MEMBERS;
+    if (!ok) continue;
+    int32_t cx = R[RB_CX], cy = R[RB_CY];
+    if (dmask & RD_HAS_PX) cx = D[RD_PX];
+    if (dmask & RD_HAS_PY) cy = D[RD_PY];
+    int32_t fx = 0, fy = 0, thi = 0, tlo = 0;
+    for (uint32_t i = first; i <= last && i < e.nFluid; ++i) {
+      if (!rg_is_member(in, i, tag)) continue;
+      const Derived& d = e.der[i];
+      const int32_t gI = axis != 0 ? e.M(in[i].matId)[M_grav] : 0;
+      const int32_t sy0 = fp_add_sat(d.sty, gI, g);
+      const V2 jm = jet_accel(e, in[i].px, in[i].py, g);
+      const int32_t jx0 = fp_add_sat(d.stx, jm.x, g), jy0 = fp_add_sat(sy0, jm.y, g);
+      const int32_t sx = clampi(jx0, -32768, 32768), sy = clampi(jy0, -32768, 32768);
+      if (sx != jx0 || sy != jy0) g.flag(11);
+      fx = wadd(fx, sx);
+      fy = wadd(fy, sy);
+      const int32_t rx = shr_rne_rt(fp_sub_sat(in[i].px, cx, g), rsh);
+      const int32_t ry = shr_rne_rt(fp_sub_sat(in[i].py, cy, g), rsh);
+      const int32_t raw = wsub(wmul(rx, sy), wmul(ry, sx));
+      if (raw > TQ_TERM_R || raw < NEG_TQ_TERM) g.flag(9);
+      const int32_t t = clampi(raw, NEG_TQ_TERM, TQ_TERM_R);
+      const int32_t hi = t >> TQ_HI_SH;
+      thi = wadd(thi, hi);
+      tlo = wadd(tlo, wsub(t, (int32_t)((uint32_t)hi << TQ_HI_SH)));
+    }
+    const int32_t invI = R[RB_INVI], iq = R[RB_IQ], gS = R[RB_GSUM];
+    const bool holdX = axis != 0 || (dmask & RD_HAS_PX), holdY = axis != 0 || (dmask & RD_HAS_PY);
+    int32_t dvx = 0, dvy = 0;
+    if (axis == 0) {
+      const int32_t ax = wadd(R[RB_RESVX], fx), ay = wadd(wadd(R[RB_RESVY], fy), gS);
+      dvx = rg_idiv_rne(ax, n);
+      dvy = rg_idiv_rne(ay, n);
+      R[RB_RESVX] = wsub(ax, wmul(dvx, n));
+      R[RB_RESVY] = wsub(ay, wmul(dvy, n));
+      const int32_t uax = usr != 0 ? e.userA[0] : 0, uay = usr != 0 ? e.userA[1] : 0;
+      dvx = fp_add_sat(dvx, uax, g);
+      dvy = fp_add_sat(dvy, uay, g);
+    }
+    if (dmask & RD_HAS_FX) dvx = fp_add_sat(dvx, D[RD_FX], g);
+    if (dmask & RD_HAS_FY) dvy = fp_add_sat(dvy, D[RD_FY], g);
+    int32_t vx0 = R[RB_VX], vy0 = R[RB_VY];
+    if (dmask & RD_HAS_VX) vx0 = D[RD_VX];
+    if (dmask & RD_HAS_VY) vy0 = D[RD_VY];
+    const int32_t vmaxN = fp_neg_sat(e.vmax, g);
+    const int32_t vx = clampi(fp_add_sat(vx0, dvx, g), vmaxN, e.vmax);
+    const int32_t vy = clampi(fp_add_sat(vy0, dvy, g), vmaxN, e.vmax);
+    if (holdX) {
+      R[RB_VX] = 0; R[RB_RESVX] = 0; R[RB_CQX] = cx; R[RB_CX] = cx;
+    } else {
+      R[RB_VX] = vx;
+      R[RB_CQX] = clampi(fp_add_sat(cx, vx, g), WALL, wsub(e.domW, WALL));
+    }
+    if (holdY) {
+      R[RB_VY] = 0; R[RB_RESVY] = 0; R[RB_CQY] = cy; R[RB_CY] = cy;
+    } else {
+      R[RB_VY] = vy;
+      R[RB_CQY] = clampi(fp_add_sat(cy, vy, g), WALL, wsub(e.domH, WALL));
+    }
+    int32_t dth = 0;
+    if (invI != 0)
+      dth = fp_add_sat(rg_mul_shr(thi, invI, iq - (int32_t)TQ_HI_SH, g), rg_mul_shr(tlo, invI, iq, g), g);
+    if (dmask & RD_HAS_TQ) dth = fp_add_sat(dth, D[RD_TQ], g);
+    int32_t theta = R[RB_THETA], w0 = R[RB_OMEGA];
+    if (dmask & RD_HAS_A) theta = D[RD_A];
+    if (dmask & RD_HAS_W) w0 = D[RD_W];
+    const int32_t om = R[RB_OMEGAM];
+    const int32_t w = clampi(fp_add_sat(w0, dth, g), wsub(0, om), om);
+    if (dmask & RD_HAS_A) {
+      R[RB_THETA] = theta; R[RB_THETAQ] = theta; R[RB_OMEGA] = 0;
+    } else {
+      R[RB_OMEGA] = w;
+      R[RB_THETAQ] = wadd(theta, w);
+    }
+    rg_place(e, in, tag, first, last, R[RB_CQX], R[RB_CQY], R[RB_THETAQ], g);
+  }
+}
+
+// rigid_seal_delta (src/sim.wgsl:2001-2051): a member's swept segment against
+// the anchored seal particles of the cells its expanded AABB touches; a hit
+// returns the reversion pos - pred, which rigidSolve folds into the body.
+V2 rigid_seal_delta(const E& e, const std::vector<Particle>& in, uint32_t i, int32_t bodyTag, const Dbg& g) {
+  const V2 pos{in[i].px, in[i].py}, pr{e.der[i].predx, e.der[i].predy};
+  const int32_t mx4 = fp_shr_rne(fp_sub_sat(pr.x, pos.x, g), BPRE), my4 = fp_shr_rne(fp_sub_sat(pr.y, pos.y, g), BPRE);
+  const int32_t ml2 = wadd(wmul(mx4, mx4), wmul(my4, my4));
+  const V2 lo = cell_coord(e, V2{fp_sub_sat(std::min(pos.x, pr.x), SEAL_REACH, g),
+                                 fp_sub_sat(std::min(pos.y, pr.y), SEAL_REACH, g)});
+  const V2 hi = cell_coord(e, V2{fp_add_sat(std::max(pos.x, pr.x), SEAL_REACH, g),
+                                 fp_add_sat(std::max(pos.y, pr.y), SEAL_REACH, g)});
+  for (int32_t gy = lo.y; gy <= hi.y; ++gy)
+    for (int32_t gx = lo.x; gx <= hi.x; ++gx) {
+      const uint32_t c = (uint32_t)gy * e.gridW + (uint32_t)gx;
+      for (uint32_t t = e.cellStart[c]; t < e.cellStart[c + 1]; ++t) {
+        const uint32_t j = e.sortedIds[t];
+        if (j == i || is_boundary(e, j)) continue;
+        const uint32_t fj = in[j].flags;
+        if ((fj & (FLAG_ANCHOR | FLAG_SEAL)) != (FLAG_ANCHOR | FLAG_SEAL) || !seal_class_row(e.M(in[j].matId)))
+          continue;
+        if ((fj & FLAG_RIGID) && (int32_t)weld_tag(fj) == bodyTag) continue;
+        const int32_t px4 = fp_shr_rne(fp_sub_sat(e.der[j].predx, pos.x, g), BPRE);
+        const int32_t py4 = fp_shr_rne(fp_sub_sat(e.der[j].predy, pos.y, g), BPRE);
+        int32_t dx4 = px4, dy4 = py4;
+        if (ml2 > 0) {
+          const int32_t dot = wadd(wmul(px4, mx4), wmul(py4, my4));
+          if (dot >= ml2) {
+            dx4 = wsub(px4, mx4);
+            dy4 = wsub(py4, my4);
+          } else if (dot > 0) {
+            const int32_t tq = fp_div_s(dot, ml2, 16, g);
+            dx4 = wsub(px4, fp_mul_s(mx4, tq, 16, g));
+            dy4 = wsub(py4, fp_mul_s(my4, tq, 16, g));
+          }
+        }
+        if (wadd(wmul(dx4, dx4), wmul(dy4, dy4)) < SEAL_R4 * SEAL_R4)
+          return V2{fp_sub_sat(pos.x, pr.x, g), fp_sub_sat(pos.y, pr.y, g)};
+      }
+    }
+  return V2{0, 0};
+}
+
+// rigidSolve (src/sim.wgsl:3459-3573), once per iteration after applyFric.
+void pass_rigidSolve(E& e, const std::vector<Particle>& in) {
+  Dbg g = e.D();
+  for (uint32_t b = 0; b < (uint32_t)e.bodies.size(); ++b) {
+    int32_t* R = body_rec(e, b);
+    const int32_t* D = body_drv(e, b);
+    const int32_t tag = R[RB_TAG], n = R[RB_N], axis = R[RB_AXIS], dmask = D[RD_MASK];
+    const uint32_t first = (uint32_t)R[RB_FIRST], last = (uint32_t)R[RB_LAST], rsh = (uint32_t)R[RB_RSH];
+    const int32_t cqx = R[RB_CQX], cqy = R[RB_CQY];
+    if (!(R[RB_LIVE] != 0 && n >= RIGID_MIN_MEMBERS)) continue;
+    int32_t fx = 0, fy = 0, sx = 0, sy = 0, sn = 0, thi = 0, tlo = 0;
+    for (uint32_t i = first; i <= last && i < e.nFluid; ++i) {
+      if (!rg_is_member(in, i, tag)) continue;
+      const int32_t dm = e.M(in[i].matId)[M_dpMax], dmN = fp_neg_sat(dm, g);
+      const Derived& d = e.der[i];
+      const V2 seal = rigid_seal_delta(e, in, i, tag, g);
+      const int32_t dx = clampi(fp_shr_rne(d.dpx, ACC), dmN, dm), dy = clampi(fp_shr_rne(d.dpy, ACC), dmN, dm);
+      fx = wadd(fx, dx);
+      fy = wadd(fy, dy);
+      if (seal.x != 0 || seal.y != 0) {
+        sx = wadd(sx, seal.x);
+        sy = wadd(sy, seal.y);
+        sn = wadd(sn, 1);
+      }
+      const int32_t tx = fp_add_sat(dx, seal.x, g), ty = fp_add_sat(dy, seal.y, g);
+      const int32_t rx = shr_rne_rt(fp_sub_sat(d.predx, cqx, g), rsh);
+      const int32_t ry = shr_rne_rt(fp_sub_sat(d.predy, cqy, g), rsh);
+      const int32_t raw = wsub(wmul(rx, ty), wmul(ry, tx));
+      if (raw > TQ_TERM_R || raw < NEG_TQ_TERM) g.flag(9);
+      const int32_t t = clampi(raw, NEG_TQ_TERM, TQ_TERM_R);
+      const int32_t hi = t >> TQ_HI_SH;
+      thi = wadd(thi, hi);
+      tlo = wadd(tlo, wsub(t, (int32_t)((uint32_t)hi << TQ_HI_SH)));
+    }
+    const int32_t invI = R[RB_INVI], iq = R[RB_IQ];
+    if (axis == 0) {
+      const int32_t ax = wadd(R[RB_RESX], fx), ay = wadd(R[RB_RESY], fy);
+      int32_t dcx = rg_idiv_rne(ax, n), dcy = rg_idiv_rne(ay, n);
+      R[RB_RESX] = wsub(ax, wmul(dcx, n));
+      R[RB_RESY] = wsub(ay, wmul(dcy, n));
+      if (sn > 0) {
+        dcx = fp_add_sat(dcx, rg_idiv_rne(sx, sn), g);
+        dcy = fp_add_sat(dcy, rg_idiv_rne(sy, sn), g);
+      }
+      if (!(dmask & RD_HAS_PX)) R[RB_CQX] = clampi(fp_add_sat(cqx, dcx, g), WALL, wsub(e.domW, WALL));
+      else R[RB_RESX] = 0;
+      if (!(dmask & RD_HAS_PY)) R[RB_CQY] = clampi(fp_add_sat(cqy, dcy, g), WALL, wsub(e.domH, WALL));
+      else R[RB_RESY] = 0;
+    }
+    int32_t dth = 0;
+    if (invI != 0)
+      dth = fp_add_sat(rg_mul_shr(thi, invI, iq - (int32_t)TQ_HI_SH, g), rg_mul_shr(tlo, invI, iq, g), g);
+    if (!(dmask & RD_HAS_A)) R[RB_THETAQ] = wadd(R[RB_THETAQ], dth);
+    rg_place(e, in, tag, first, last, R[RB_CQX], R[RB_CQY], R[RB_THETAQ], g);
+  }
+}
+
+// rigidMember (src/sim.wgsl:3610-3747), after containStress. The leave step
+// decides every member against the membership the pass began with, then
+// clears: the reference's workgroup clears FLAG_RIGID in the same loop that
+// other lanes read it, which only matters when a leaving member is another
+// member's sole same-body neighbour within bond range; here that read is
+// defined as the state at the start of the pass.
+void pass_rigidMember(E& e, std::vector<Particle>& out) {
+  Dbg g = e.D();
+  for (uint32_t b = 0; b < (uint32_t)e.bodies.size(); ++b) {
+    int32_t* R = body_rec(e, b);
+    if (R[RB_LIVE] == 0) continue;
+    const int32_t tag = R[RB_TAG], axis = R[RB_AXIS];
+    const uint32_t first = (uint32_t)R[RB_FIRST], last = (uint32_t)R[RB_LAST];
+    const uint32_t ish = (uint32_t)R[RB_ISH], osh = (uint32_t)R[RB_OSH];
+    // 1. close the substep
+    const int32_t vmaxN = fp_neg_sat(e.vmax, g);
+    R[RB_VX] = clampi(fp_sub_sat(R[RB_CQX], R[RB_CX], g), vmaxN, e.vmax);
+    R[RB_VY] = clampi(fp_sub_sat(R[RB_CQY], R[RB_CY], g), vmaxN, e.vmax);
+    R[RB_OMEGA] = wsub(R[RB_THETAQ], R[RB_THETA]);
+    R[RB_CX] = R[RB_CQX];
+    R[RB_CY] = R[RB_CQY];
+    R[RB_THETA] = R[RB_THETAQ];
+    // 2. leave
+    std::vector<uint32_t> leaving;
+    for (uint32_t i = first; i <= last && i < e.nFluid; ++i) {
+      if (!rg_is_member(out, i, tag)) continue;
+      const int32_t* M = e.M(out[i].matId);
+      bool leave = M[M_solidMode] != SOLID_RIGID || M[M_phantom] != 0;
+      if (!leave) {
+        bool touched = false;
+        const uint32_t cnt = nbr_count(e, i);
+        for (uint32_t k = 0; k < cnt; ++k) {
+          const uint32_t j = e.nbr[(size_t)i * MAXNBR + k];
+          if (j >= e.nFluid) continue;
+          if (!rg_is_member(out, j, tag)) continue;
+          const int32_t dx = fp_shr_rne(fp_sub_sat(out[i].px, out[j].px, g), BPRE);
+          const int32_t dy = fp_shr_rne(fp_sub_sat(out[i].py, out[j].py, g), BPRE);
+          if (iabs(dx) > L0_MAX || iabs(dy) > L0_MAX) continue;
+          if (wadd(wmul(dx, dx), wmul(dy, dy)) <= BOND_R2) { touched = true; break; }
+        }
+        leave = !touched;
+      }
+      if (leave) leaving.push_back(i);
+    }
+    for (uint32_t i : leaving) out[i].flags &= ~FLAG_RIGID;
+    // 3. recount and re-base
+    int32_t cn = 0, sox = 0, soy = 0, si2 = 0, gsm = 0;
+    for (uint32_t i = first; i <= last && i < e.nFluid; ++i) {
+      if (!rg_is_member(out, i, tag)) continue;
+      const int32_t ox = e.rest[2 * (size_t)i], oy = e.rest[2 * (size_t)i + 1];
+      cn = wadd(cn, 1);
+      sox = wadd(sox, ox >> osh);
+      soy = wadd(soy, oy >> osh);
+      const int32_t a = ox >> ish, c = oy >> ish;
+      si2 = wadd(si2, wadd(wmul(a, a), wmul(c, c)));
+      gsm = wadd(gsm, e.M(out[i].matId)[M_grav]);
+    }
+    const int32_t nLive = cn;
+    const bool dissolve = nLive < RIGID_MIN_MEMBERS;
+    int32_t dx = 0, dy = 0;
+    if (!dissolve && axis == 0) {
+      dx = (int32_t)((uint32_t)rg_idiv_rne(sox, nLive) << osh);
+      dy = (int32_t)((uint32_t)rg_idiv_rne(soy, nLive) << osh);
+    }
+    if (dissolve) {
+      R[RB_LIVE] = 0;
+      R[RB_N] = 0;
+    } else {
+      if (dx != 0 || dy != 0) {
+        const int32_t th = R[RB_THETA];
+        const int32_t c = rg_cos(e, th, g), s = rg_sin(e, th, g);
+        R[RB_CX] = fp_add_sat(R[RB_CX], fp_sub_sat(fp_mul_s(dx, c, COS_Q, g), fp_mul_s(dy, s, COS_Q, g), g), g);
+        R[RB_CY] = fp_add_sat(R[RB_CY], fp_add_sat(fp_mul_s(dx, s, COS_Q, g), fp_mul_s(dy, c, COS_Q, g), g), g);
+      }
+      R[RB_N] = nLive;
+      R[RB_SUMIS2] = si2;
+      R[RB_GSUM] = gsm;
+      int32_t invI, iq;
+      rg_inv_inertia(si2, R[RB_RSH], R[RB_ISH], invI, iq, g);
+      R[RB_INVI] = invI;
+      R[RB_IQ] = iq;
+    }
+    for (uint32_t i = first; i <= last && i < e.nFluid; ++i) {
+      if (!rg_is_member(out, i, tag)) continue;
+      if (dissolve) {
+        out[i].flags &= ~FLAG_RIGID;
+      } else if (dx != 0 || dy != 0) {
+        e.rest[2 * (size_t)i] = wsub(e.rest[2 * (size_t)i], dx);
+        e.rest[2 * (size_t)i + 1] = wsub(e.rest[2 * (size_t)i + 1], dy);
+      }
+    }
+  }
+}
+
+// ---- §20 host math (src/engine.js:2050-2150, 5452-5811) ------------------------
+// Math.round: the integral value closest to x, ties towards +infinity.
+inline double js_round(double x) {
+  const double r = std::floor(x);
+  return (x - r >= 0.5) ? r + 1.0 : r;
+}
+// buildCosTable (src/engine.js:2062-2068)
+void build_cos_table(int32_t T[1026]) {
+  for (uint32_t k = 0; k <= RG_QN; ++k)
+    T[k] = (int32_t)js_round(std::cos(((double)k * M_PI) / (double)(2 * RG_QN)) * (double)COS_ONE);
+  T[RG_QN] = 0;
+  T[RG_QN + 1] = 0;
+}
+// idivRne (src/engine.js:2074-2080) on the host's exact integers.
+inline int64_t idiv_rne64(int64_t a, int64_t n) {
+  if (n <= 0) return 0;
+  const bool neg = a < 0;
+  const int64_t x = neg ? -a : a;
+  int64_t q = x / n;
+  const int64_t r2 = 2 * (x - q * n);
+  if (r2 > n || (r2 == n && (q & 1) == 1)) q += 1;
+  return neg ? -q : q;
+}
+// isqrt64 (src/engine.js:2083-2089) on a double, with the reference's own
+// float seed and integer correction.
+inline double isqrt_js(double x) {
+  if (x <= 0) return 0;
+  double r = std::floor(std::sqrt(x));
+  while (r > 0 && r * r > x) r -= 1;
+  while ((r + 1) * (r + 1) <= x) r += 1;
+  return r;
+}
+struct Shifts { int32_t rMax, rsh, ish, osh; };
+// rigidShifts (src/engine.js:2106-2128), in the same double arithmetic.
+bool rigid_shifts(const std::vector<int32_t>& ox, const std::vector<int32_t>& oy, Shifts& out) {
+  const size_t N = ox.size();
+  double rMax = 0;
+  for (size_t k = 0; k < N; ++k) {
+    const double a = std::fabs((double)ox[k]), b = std::fabs((double)oy[k]);
+    const double m = isqrt_js(a * a + b * b);
+    if (m > rMax) rMax = m;
+  }
+  const int32_t rm = (int32_t)(int64_t)rMax;
+  int32_t rsh = 0;
+  while ((rm >> rsh) > RS_TARGET) ++rsh;
+  int32_t ish = 0;
+  for (;;) {
+    double sum = 0;
+    for (size_t k = 0; k < N; ++k) {
+      const double a = (double)(ox[k] >> ish), b = (double)(oy[k] >> ish);
+      sum += a * a + b * b;
+    }
+    if (sum < (double)SUMI_MAX) break;
+    if (++ish > 30) return false;
+  }
+  int32_t osh = 0;
+  while ((double)N * (double)(rm >> osh) >= (double)SUMI_MAX) ++osh;
+  out = Shifts{rm, rsh, ish, osh};
+  return true;
+}
+// rigidInvInertia (src/engine.js:2135-2150): exact, like the BigInt original.
+void rigid_inv_inertia_host(int32_t s, int32_t rsh, int32_t ish, int32_t& invI, int32_t& iq) {
+  invI = 0;
+  iq = 0;
+  if (s <= 0) return;
+  const int32_t bl = 32 - (int32_t)clz32((uint32_t)s);
+  const int32_t iqNat = bl - 1 + 2 * ish - rsh;
+  const int32_t q0 = std::min(iqNat, RG_IQ_MAX);
+  const int32_t E_ = q0 + rsh - 2 * ish;
+  if (iqNat < RG_IQ_MIN || E_ < 1 || E_ > 62) return;
+  const unsigned __int128 num = (unsigned __int128)BAM_PER_RAD << E_, den = (unsigned __int128)s;
+  unsigned __int128 q = num / den;
+  const unsigned __int128 r = num - q * den;
+  if (2 * r > den || (2 * r == den && (q & 1))) q += 1;
+  if (q > 2147483647u) q = 2147483647u;
+  invI = (int32_t)q;
+  iq = q0;
+}
+
+// _writeBodyRecord (src/engine.js:5452-5580). `st` is the current state;
+// `members` ascending fluid slots. Returns the body index or -1.
+int32_t write_body_record(E& e, const std::vector<uint32_t>& members, const std::vector<Particle>& st, uint32_t tag,
+                          const int32_t* pivot, bool user) {
+  const size_t N = members.size();
+  if (N < (size_t)RIGID_MIN_MEMBERS) return -1;
+  if (e.bodies.size() >= RG_MAX_BODIES) return -1;
+  int64_t sx = 0, sy = 0, svx = 0, svy = 0;
+  for (uint32_t i : members) { sx += st[i].px; sy += st[i].py; svx += st[i].vx; svy += st[i].vy; }
+  const bool axis = pivot != nullptr;
+  const int32_t cx = axis ? pivot[0] : (int32_t)idiv_rne64(sx, (int64_t)N);
+  const int32_t cy = axis ? pivot[1] : (int32_t)idiv_rne64(sy, (int64_t)N);
+  const int32_t vx = axis ? 0 : (int32_t)idiv_rne64(svx, (int64_t)N);
+  const int32_t vy = axis ? 0 : (int32_t)idiv_rne64(svy, (int64_t)N);
+  std::vector<int32_t> ox(N), oy(N);
+  for (size_t k = 0; k < N; ++k) {
+    ox[k] = (int32_t)((int64_t)st[members[k]].px - cx);
+    oy[k] = (int32_t)((int64_t)st[members[k]].py - cy);
+  }
+  Shifts sh;
+  if (!rigid_shifts(ox, oy, sh)) return -1;
+  int64_t sumIs2 = 0, gSum = 0;
+  for (size_t k = 0; k < N; ++k) {
+    const int64_t a = ox[k] >> sh.ish, b = oy[k] >> sh.ish;
+    sumIs2 += a * a + b * b;
+    gSum += e.M(st[members[k]].matId)[M_grav];
+  }
+  int32_t invI, iq;
+  rigid_inv_inertia_host((int32_t)sumIs2, sh.rsh, sh.ish, invI, iq);
+  int64_t acc = 0;
+  for (size_t k = 0; k < N; ++k) {
+    const Particle& p = st[members[k]];
+    acc += (int64_t)(ox[k] >> sh.rsh) * ((int64_t)p.vy - vy) - (int64_t)(oy[k] >> sh.rsh) * ((int64_t)p.vx - vx);
+  }
+  int64_t omega = 0;
+  if (invI != 0) {
+    const __int128 num = (__int128)acc * invI, den = (__int128)1 << iq;
+    __int128 q = num / den, r = num - q * den;
+    if (r < 0) { q -= 1; r += den; }
+    if (2 * r > den || (2 * r == den && (q & 1))) q += 1;
+    omega = (int64_t)q;
+  }
+  const int64_t omegaMax =
+      std::max<int64_t>(1, std::min<int64_t>(BAM_QUARTER, ((int64_t)VMAX * BAM_PER_RAD) / std::max<int64_t>(1, sh.rMax)));
+  omega = std::max(-omegaMax, std::min(omegaMax, omega));
+  const uint32_t idx = (uint32_t)e.bodies.size();
+  e.rbody.resize((size_t)(idx + 1) * RG_BODY_WORDS, 0);
+  e.rdrive.resize((size_t)(idx + 1) * RG_DRIVER_WORDS, 0);
+  int32_t* R = body_rec(e, idx);
+  std::fill(R, R + RG_BODY_WORDS, 0);
+  std::fill(e.rdrive.begin() + (size_t)idx * RG_DRIVER_WORDS, e.rdrive.begin() + (size_t)(idx + 1) * RG_DRIVER_WORDS, 0);
+  R[RB_LIVE] = 1; R[RB_TAG] = (int32_t)tag;
+  R[RB_FIRST] = (int32_t)members.front(); R[RB_LAST] = (int32_t)members.back();
+  R[RB_CX] = cx; R[RB_CY] = cy; R[RB_VX] = vx; R[RB_VY] = vy;
+  R[RB_THETA] = 0; R[RB_OMEGA] = (int32_t)omega;
+  R[RB_N] = (int32_t)N; R[RB_SUMIS2] = (int32_t)sumIs2; R[RB_GSUM] = (int32_t)(uint32_t)(uint64_t)gSum;
+  R[RB_INVI] = invI; R[RB_IQ] = iq; R[RB_RSH] = sh.rsh; R[RB_ISH] = sh.ish; R[RB_OSH] = sh.osh;
+  R[RB_OMEGAM] = (int32_t)omegaMax; R[RB_RMAX] = sh.rMax;
+  R[RB_CQX] = cx; R[RB_CQY] = cy; R[RB_THETAQ] = 0;
+  R[RB_AXIS] = axis ? 1 : 0; R[RB_USER] = user ? 1 : 0;
+  for (size_t k = 0; k < N; ++k) {
+    e.rest[2 * (size_t)members[k]] = ox[k];
+    e.rest[2 * (size_t)members[k] + 1] = oy[k];
+  }
+  E::BodyDesc d;
+  d.tag = tag; d.first = members.front(); d.last = members.back(); d.n = (uint32_t)N; d.axis = axis; d.user = user;
+  e.bodies.push_back(d);
+  return (int32_t)idx;
+}
+
+// eraseWhere's body repair (src/engine.js:6526-6610) after a compaction with
+// survivors `surv` (old slots, ascending).
+void repair_bodies_after_erase(E& e, const std::vector<uint32_t>& surv) {
+  if (e.bodies.empty()) return;
+  std::vector<Particle>& st = e.st[e.parity];
+  const uint32_t newF = (uint32_t)surv.size();
+  std::vector<int32_t> restOut(e.rest.size(), 0);
+  for (uint32_t k = 0; k < newF; ++k) {
+    restOut[2 * (size_t)k] = e.rest[2 * (size_t)surv[k]];
+    restOut[2 * (size_t)k + 1] = e.rest[2 * (size_t)surv[k] + 1];
+  }
+  std::vector<int32_t> recs, drvs;
+  std::vector<E::BodyDesc> kept;
+  Dbg g = e.D();
+  for (size_t bi = 0; bi < e.bodies.size(); ++bi) {
+    const E::BodyDesc& b = e.bodies[bi];
+    std::vector<uint32_t> mem;
+    for (uint32_t k = 0; k < newF; ++k) {
+      const uint32_t f = st[k].flags;
+      if ((f & FLAG_RIGID) && (f & WELD_TAG_MASK) == b.tag) mem.push_back(k);
+    }
+    if (mem.size() < (size_t)RIGID_MIN_MEMBERS) {
+      for (uint32_t k : mem) {
+        st[k].flags &= ~FLAG_RIGID;
+        e.st[1 - e.parity][k].flags &= ~FLAG_RIGID;
+      }
+      continue;
+    }
+    std::vector<int32_t> rec(e.rbody.begin() + bi * RG_BODY_WORDS, e.rbody.begin() + (bi + 1) * RG_BODY_WORDS);
+    const int32_t ish = rec[RB_ISH];
+    int64_t sumIs2 = 0, gSum = 0;
+    for (uint32_t k : mem) {
+      const int64_t a = restOut[2 * (size_t)k] >> ish, c = restOut[2 * (size_t)k + 1] >> ish;
+      sumIs2 += a * a + c * c;
+      gSum += e.M(st[k].matId)[M_grav];
+    }
+    int32_t invI, iq;
+    rigid_inv_inertia_host((int32_t)sumIs2, rec[RB_RSH], ish, invI, iq);
+    rec[RB_FIRST] = (int32_t)mem.front(); rec[RB_LAST] = (int32_t)mem.back();
+    rec[RB_N] = (int32_t)mem.size(); rec[RB_SUMIS2] = (int32_t)sumIs2;
+    rec[RB_GSUM] = (int32_t)(uint32_t)(uint64_t)gSum; rec[RB_INVI] = invI; rec[RB_IQ] = iq;
+    recs.insert(recs.end(), rec.begin(), rec.end());
+    drvs.insert(drvs.end(), e.rdrive.begin() + bi * RG_DRIVER_WORDS, e.rdrive.begin() + (bi + 1) * RG_DRIVER_WORDS);
+    E::BodyDesc d = b;
+    d.first = mem.front(); d.last = mem.back(); d.n = (uint32_t)mem.size();
+    kept.push_back(d);
+  }
+  (void)g;
+  e.rbody = recs;
+  e.rdrive = drvs;
+  e.bodies = kept;
+  e.rest = restOut;
+}
+
 // One substep, in _encodeSubstep's order (src/engine.js:4003-4155).
 void substep(E& e) {
   std::vector<Particle>& in = e.st[e.parity];
   std::vector<Particle>& out = e.st[1 - e.parity];
+  pass_rigidStep(e, in);
   pass_predict(e, in);
   pass_grid(e);
   pass_buildNbr(e, in);
@@ -1092,6 +1678,7 @@ void substep(E& e) {
     }
     pass_friction(e, in);
     pass_applyDp(e, in, -1);
+    pass_rigidSolve(e, in);
   }
   pass_contain(e, in);
   pass_finalize(e, in, out);
@@ -1101,7 +1688,7 @@ void substep(E& e) {
   pass_conduct(e, out);
   pass_thermal(e, out);
   pass_containStress(e, out);
-  // rigidMember: inert (no rigid-body rows are admitted)
+  pass_rigidMember(e, out);
   if ((e.formationClock % BOND_PERIOD) == 0 || e.bondDirty) {
     pass_markCongealNbr(e, out);
     pass_bondForm1(e, out);
@@ -1132,6 +1719,7 @@ SnoEngine* sno_create(uint32_t maxParticles, const int32_t* luts, const int32_t*
   std::memcpy(e->mats, mats, sizeof(int32_t) * MAT_WORDS * matCount);
   e->matCount = matCount;
   std::memset(e->dbg, 0, sizeof(e->dbg));
+  build_cos_table(e->cosT);
   return e;
 }
 
@@ -1162,7 +1750,6 @@ int sno_load_scene(SnoEngine* e, uint32_t n, uint32_t nFluid, const int32_t* pos
     if (flags && (flags[i] & ~7u)) return -4;
     if (temp && (temp[i] < TEMP_MIN || temp[i] > TEMP_MAX)) return -5;
     if (fuel && fuel[i] < 0) return -6;
-    if (rigid_row(e->mats[matId[i]])) return -9;
   }
   if (cellShift < 1 || cellShift > 27 || (1u << cellShift) < (uint32_t)H) return -7;
   uint32_t cs = 1u << cellShift;
@@ -1177,6 +1764,12 @@ int sno_load_scene(SnoEngine* e, uint32_t n, uint32_t nFluid, const int32_t* pos
   e->substepCount = 0; e->parity = 0; e->formationClock = 0; e->bondDirty = true;
   e->unsupported = 0;
   uint32_t cap = e->maxParticles;
+  // a scene load dissolves every body and resets the drive (src/engine.js:3811-3813, 3849)
+  e->bodies.clear();
+  e->rbody.clear();
+  e->rdrive.clear();
+  e->rest.assign((size_t)cap * 2, 0);
+  e->userA[0] = e->userA[1] = 0;
   for (int p = 0; p < 2; ++p) e->st[p].assign(cap, Particle{});
   e->der.assign(cap, Derived{});
   e->cellCount.assign(ct + 1, 0);
@@ -1341,6 +1934,7 @@ int64_t sno_erase(SnoEngine* e, const uint8_t* keep) {
   e->n = newN;
   e->nFluid = newF;
   e->bondDirty = true;
+  repair_bodies_after_erase(*e, surv);
   return removed;
 }
 
@@ -1359,12 +1953,6 @@ int64_t sno_spawn(SnoEngine* e, const int32_t* rows, uint32_t k, int hasTemp, in
   if (newN > e->maxParticles) return e->n;
   std::vector<Particle>& stb = e->st[e->parity];
   // noWeld bit 0: {noWeld: true}; bit 1: {ownGroup: true}
-  for (uint32_t i = 0; i < k; ++i) {
-    const int32_t* r = rows + 8 * i;
-    int32_t mm = r[4] < 0 ? 0 : r[4];
-    uint32_t m = (uint32_t)std::min<int32_t>((int32_t)e->matCount - 1, mm);
-    if (rigid_row(e->mats[m])) return -9;
-  }
   // §18.2 W1 + §18.22 (src/engine.js:5925-5935): one gesture is one group.
   const uint32_t seq = (e->weldHoldSeq != 0 && !(noWeld & 2)) ? e->weldHoldSeq : next_weld_seq(*e);
   const uint32_t tagNow = (seq << 8) & WELD_TAG_MASK;
@@ -1454,6 +2042,152 @@ int64_t sno_impulse(SnoEngine* e, int32_t cx, int32_t cy, int32_t radius, int32_
     hits++;
   }
   return hits;
+}
+
+
+// ---- §20 rigid bodies: the host calls (src/engine.js:5452-5811) ----------------
+// pivot: NULL for a free body, else {x, y} ticks (an axis body, §19.B).
+// Each returns the new body's index, or -1 where the reference returns null.
+int32_t sno_make_rigid_body(SnoEngine* e, const uint32_t* slots, uint32_t k, const int32_t* pivot, int user) {
+  if (k == 0 || e->nFluid == 0) return -1;
+  std::vector<Particle>& st = e->st[e->parity];
+  std::vector<uint32_t> members;
+  for (uint32_t q = 0; q < k; ++q) {
+    const uint32_t i = slots[q];
+    if (i >= e->nFluid) continue;
+    if (e->M(st[i].matId)[M_solidMode] != SOLID_RIGID) continue;
+    if (st[i].flags & (FLAG_RIGID | FLAG_ANCHOR)) continue;
+    members.push_back(i);
+  }
+  std::sort(members.begin(), members.end());
+  if (members.size() < (size_t)RIGID_MIN_MEMBERS) return -1;
+  std::vector<bool> inUse(4096, false);
+  for (uint32_t i = 0; i < e->nFluid; ++i) inUse[(st[i].flags & WELD_TAG_MASK) >> 8] = true;
+  uint32_t seq = 0;
+  for (uint32_t g = 0; g <= 4095; ++g) {
+    const uint32_t q = next_weld_seq(*e);
+    if (!inUse[q]) { seq = q; break; }
+  }
+  if (seq == 0) return -2;
+  const uint32_t tag = (seq << 8) & WELD_TAG_MASK;
+  std::vector<Particle> st2 = st;
+  for (uint32_t i : members) st2[i].flags = (st2[i].flags & ~WELD_TAG_MASK) | tag | FLAG_RIGID;
+  const int32_t idx = write_body_record(*e, members, st2, tag, pivot, user != 0);
+  if (idx < 0) return -1;
+  st = st2;
+  e->st[1 - e->parity] = st2;
+  e->bondDirty = true;
+  return idx;
+}
+int32_t sno_promote_weld_group(SnoEngine* e, uint32_t tag, const int32_t* pivot, int user) {
+  const uint32_t t = (tag == 0 ? e->weldHold : tag) & WELD_TAG_MASK;
+  if (t == 0 || e->nFluid == 0) return -1;
+  std::vector<Particle>& st = e->st[e->parity];
+  std::vector<uint32_t> members;
+  for (uint32_t i = 0; i < e->nFluid; ++i) {
+    const uint32_t f = st[i].flags;
+    if ((f & WELD_TAG_MASK) != t) continue;
+    if (f & (FLAG_RIGID | FLAG_ANCHOR)) continue;
+    if (e->M(st[i].matId)[M_solidMode] != SOLID_RIGID) continue;
+    members.push_back(i);
+  }
+  const int32_t idx = write_body_record(*e, members, st, t, pivot, user != 0);
+  if (idx < 0) return -1;
+  for (uint32_t i : members) {
+    st[i].flags |= FLAG_RIGID;
+    e->st[1 - e->parity][i].flags = st[i].flags;
+  }
+  e->bondDirty = true;
+  return idx;
+}
+int32_t sno_end_weld_group_and_promote(SnoEngine* e, const int32_t* pivot, int user) {
+  const uint32_t was = sno_end_weld_group(e);
+  if (was == 0) return -1;
+  return sno_promote_weld_group(e, was, pivot, user);
+}
+uint32_t sno_dissolve_all_bodies(SnoEngine* e) {
+  if (e->bodies.empty()) return 0;
+  uint32_t k = 0;
+  for (uint32_t i = 0; i < e->nFluid; ++i) {
+    if (!(e->st[e->parity][i].flags & FLAG_RIGID)) continue;
+    e->st[0][i].flags &= ~FLAG_RIGID;
+    e->st[1][i].flags &= ~FLAG_RIGID;
+    ++k;
+  }
+  e->bodies.clear();
+  e->rbody.clear();
+  e->rdrive.clear();
+  return k;
+}
+uint32_t sno_body_count(SnoEngine* e) { return (uint32_t)e->bodies.size(); }
+int sno_read_bodies(SnoEngine* e, int32_t* out, size_t words) {
+  if (words < e->rbody.size()) return -1;
+  std::memcpy(out, e->rbody.data(), e->rbody.size() * 4);
+  return 0;
+}
+int sno_read_rest(SnoEngine* e, int32_t* out, size_t words) {
+  if (words < (size_t)e->n * 2) return -1;
+  std::memcpy(out, e->rest.data(), (size_t)e->n * 8);
+  return 0;
+}
+int sno_set_body_user(SnoEngine* e, uint32_t index, int on) {
+  if (index >= e->bodies.size()) return 0;
+  e->bodies[index].user = on != 0;
+  body_rec(*e, index)[RB_USER] = on ? 1 : 0;
+  return 1;
+}
+// One body's driver sidecar: mask (RD_HAS_* bits) and the nine values.
+int sno_set_body_driver(SnoEngine* e, uint32_t index, int32_t mask, const int32_t* values) {
+  if (index >= e->bodies.size() || mask < 0 || mask >= 512) return -1;
+  int32_t* D = e->rdrive.data() + (size_t)index * RG_DRIVER_WORDS;
+  D[0] = mask;
+  for (int q = 0; q < 9; ++q) D[1 + q] = values ? values[q] : 0;
+  return 0;
+}
+int sno_clear_body_drivers(SnoEngine* e) {
+  std::fill(e->rdrive.begin(), e->rdrive.end(), 0);
+  return 0;
+}
+int32_t sno_set_user_drive(SnoEngine* e, int32_t ax, int32_t ay) {
+  const int32_t M = 32768;
+  e->userA[0] = std::max(-M, std::min(M, ax));
+  e->userA[1] = std::max(-M, std::min(M, ay));
+  return 0;
+}
+// dragGrab's rigid branch (src/engine.js:6111-6140): the body wearing `tag`
+// is put one velocity behind the target and its translational remainders are
+// dropped. Returns 1 if a free body was moved.
+int sno_drag_body(SnoEngine* e, uint32_t tag, int32_t tx, int32_t ty, int32_t vx, int32_t vy) {
+  for (size_t b = 0; b < e->bodies.size(); ++b) {
+    if (e->bodies[b].tag != tag) continue;
+    if (e->bodies[b].axis) return 0;
+    const int32_t cvx = std::max(-VMAX, std::min(VMAX, vx)), cvy = std::max(-VMAX, std::min(VMAX, vy));
+    const int32_t ONE = 65536;
+    const int32_t cx = (int32_t)std::max<int64_t>(ONE, std::min<int64_t>((int64_t)e->domW - ONE, (int64_t)tx - cvx));
+    const int32_t cy = (int32_t)std::max<int64_t>(ONE, std::min<int64_t>((int64_t)e->domH - ONE, (int64_t)ty - cvy));
+    int32_t* R = body_rec(*e, (uint32_t)b);
+    R[RB_CX] = cx; R[RB_CY] = cy; R[RB_VX] = cvx; R[RB_VY] = cvy;
+    R[RB_RESX] = R[RB_RESY] = R[RB_RESVX] = R[RB_RESVY] = 0;
+    return 1;
+  }
+  return 0;
+}
+// restoreAuthoringSnapshot's rigid part (src/engine.js:5838-5880): body
+// records (n x 32 words) and rest offsets (n_particles x 2); drivers cleared.
+int sno_restore_bodies(SnoEngine* e, const int32_t* records, uint32_t nBodies, const int32_t* rest, size_t restWords) {
+  if (nBodies > RG_MAX_BODIES || restWords > e->rest.size()) return -1;
+  e->rbody.assign(records, records + (size_t)nBodies * RG_BODY_WORDS);
+  e->rdrive.assign((size_t)nBodies * RG_DRIVER_WORDS, 0);
+  e->bodies.clear();
+  for (uint32_t b = 0; b < nBodies; ++b) {
+    const int32_t* R = records + (size_t)b * RG_BODY_WORDS;
+    E::BodyDesc d;
+    d.tag = (uint32_t)R[RB_TAG]; d.first = (uint32_t)R[RB_FIRST]; d.last = (uint32_t)R[RB_LAST];
+    d.n = (uint32_t)R[RB_N]; d.axis = R[RB_AXIS] != 0; d.user = R[RB_USER] != 0;
+    e->bodies.push_back(d);
+  }
+  if (rest) std::copy(rest, rest + restWords, e->rest.begin());
+  return 0;
 }
 
 }  // extern "C"

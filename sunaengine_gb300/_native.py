@@ -189,6 +189,18 @@ SIGNATURES = {
     'sn_set_jets': (ctypes.c_int, [P, P, u32, ctypes.POINTER(u32)]),
     'sn_batch_set_jets': (ctypes.c_int, [P, u32, P, u32, ctypes.POINTER(u32)]),
     'sn_set_user_drive': (ctypes.c_int, [P, ctypes.c_int32, ctypes.c_int32, P]),
+    'sn_make_rigid_body': (ctypes.c_int, [P, P, u32, P, u32, ctypes.POINTER(ctypes.c_int32)]),
+    'sn_promote_weld_group': (ctypes.c_int, [P, u32, P, u32, ctypes.POINTER(ctypes.c_int32)]),
+    'sn_end_weld_group_and_promote': (ctypes.c_int, [P, P, u32, ctypes.POINTER(ctypes.c_int32)]),
+    'sn_dissolve_all_bodies': (ctypes.c_int, [P, ctypes.POINTER(u32)]),
+    'sn_read_bodies': (ctypes.c_int, [P, P, ctypes.c_size_t, ctypes.POINTER(u32)]),
+    'sn_read_rest_offsets': (ctypes.c_int, [P, P, ctypes.c_size_t]),
+    'sn_set_body_user': (ctypes.c_int, [P, u32, u32, ctypes.POINTER(u32)]),
+    'sn_set_body_driver': (ctypes.c_int, [P, u32, ctypes.c_int32, P]),
+    'sn_clear_body_drivers': (ctypes.c_int, [P]),
+    'sn_drag_body': (ctypes.c_int, [P, u32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                    ctypes.POINTER(u32)]),
+    'sn_restore_bodies': (ctypes.c_int, [P, P, u32, P, ctypes.c_size_t]),
     'sn_autotune': (ctypes.c_int, [P, u32, ctypes.POINTER(u32)]),
     'sn_batch_autotune': (ctypes.c_int, [P, u32, ctypes.POINTER(u32)]),
     'sn_lanes': (ctypes.c_int, [P, P]),

@@ -18,6 +18,8 @@
 #include "ckptpool.h"
 #include "radix.cuh"
 #include "sim2d.cuh"
+#include "rigid.cuh"
+#include <cmath>
 
 using namespace sn;
 using namespace sn::d2;
@@ -175,7 +177,6 @@ struct World {
   EvPar* devEp = nullptr;
   bool eventsDirty = false, anyEvents = false;
   bool hasFriction = false, hasBonds = false, hasSeal = false;
-  int32_t userA[2] = {0, 0};  // setUserDrive: drives only user-flagged rigid bodies (none are built)
   bool layoutDirty = true;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
@@ -297,7 +298,18 @@ struct World {
     hits = dalloc<uint32_t>(1, err);
     accTmp = dalloc<uint32_t>((size_t)scenesCap * 8, err);
     devEp = dalloc<EvPar>(scenesCap, err);
+    b.rbody = dalloc<int32_t>((size_t)RG_MAX_BODIES * RG_BODY_WORDS, err);
+    b.rdrv = dalloc<int32_t>((size_t)RG_MAX_BODIES * RG_DRIVER_WORDS, err);
+    b.rest = dalloc<int2>(C, err);
+    b.rmark = dalloc<uint32_t>(C, err);
+    int32_t* dcos = dalloc<int32_t>(RG_COS_N, err);
     if (!err.empty()) return false;
+    {
+      int32_t T[RG_COS_N];
+      build_cos_table(T);
+      cudaMemcpy(dcos, T, sizeof(T), cudaMemcpyHostToDevice);
+      b.cosT = dcos;
+    }
     for (int i = 4 * TN; i < 5 * TN; ++i)
       if (o->luts[i] != 0) return fail("the s_corr kernel table must be all zero (scorrK = 0 in the frozen tables)");
     cudaMemcpy(dl, o->luts, sizeof(int32_t) * LUT_WORDS, cudaMemcpyHostToDevice);
@@ -332,12 +344,8 @@ struct World {
     return r[M_bondK] != 0 && r[M_bondReform] == 0 && r[M_solidMode] != 0 && r[M_phantom] == 0;
   }
   bool spawn_welds(uint32_t m) const { return row(m)[M_bondGroup] >= 0 && row(m)[M_bondReform] == 0; }
-  // Rigid-body rows (solidMode 2: ICE, WOOD, STONE, METAL, BEDROCK in MATS)
-  // need §20's body solve, which this engine does not run.
-  bool rigid_row(uint32_t m) const { return row(m)[M_solidMode] == SOLID_RIGID; }
-
   // Which optional passes the loaded rows (and every row a transition can turn
-  // them into, except the unsupported rigid-body rows) need.
+  // them into) need.
   void update_features() {
     std::vector<bool> seen(matCount, false);
     std::vector<uint32_t> stack;
@@ -352,12 +360,12 @@ struct World {
       stack.pop_back();
       for (int f : {M_meltTo, M_freezeTo, M_boilTo, M_condTo, M_burnTo, M_splitTo, M_corrTo}) {
         uint32_t t = (uint32_t)row(m)[f];
-        if (t < matCount && !seen[t] && !rigid_row(t)) { seen[t] = true; stack.push_back(t); }
+        if (t < matCount && !seen[t]) { seen[t] = true; stack.push_back(t); }
       }
     }
     bool fr = false, bo = false, se = false;
     for (uint32_t m = 0; m < matCount; ++m) {
-      if (!seen[m] || rigid_row(m)) continue;
+      if (!seen[m]) continue;
       if (row(m)[M_fric] != 0 || row(m)[M_bondK] != 0) fr = true;
       if (row(m)[M_bondK] != 0) bo = true;
       if (seal_row(m)) se = true;
@@ -464,9 +472,6 @@ struct World {
       if (sc->flags && (sc->flags[i] & ~FLAG_MASK)) return fail("flags[%u] sets a reserved bit", i);
       if (sc->temp && (sc->temp[i] < TEMP_MIN || sc->temp[i] > TEMP_MAX)) return fail("temp[%u] out of range", i);
       if (sc->fuel && sc->fuel[i] < 0) return fail("fuel[%u] < 0", i);
-      if (rigid_row(sc->mat_id[i]))
-        return fail("matId[%u] = %u is a rigid-body row (solidMode 2); rigid bodies are not built", i,
-                    sc->mat_id[i]);
       uint32_t want = row(sc->mat_id[i])[M_phantom] != 0 ? FLAG_DEAD : 0u;
       if (sc->flags && (sc->flags[i] & FLAG_DEAD) && !want) return fail("flags[%u] sets FLAG_DEAD on a live row", i);
     }
@@ -481,6 +486,8 @@ struct World {
     accFresh = false;
     SceneHost& h = sh[s];
     if (!validate_scene(sc, h.cap)) return false;
+    // a scene load dissolves every body of the scene (src/engine.js:3811-3813)
+    if (!drop_scene_bodies(s)) return false;
     uint32_t cs = 1u << sc->cell_shift;
     uint32_t gW = std::max<uint32_t>(1, (uint32_t)(((int64_t)sc->dom_w + cs - 1) / cs));
     uint32_t gH = std::max<uint32_t>(1, (uint32_t)(((int64_t)sc->dom_h + cs - 1) / cs));
@@ -662,6 +669,13 @@ struct World {
     mark();
     k_predict_key<DBG><<<gs, 256, 0, st>>>(b);
     ++Lc;
+    // §20: rigidStep runs before predict in the reference; predict leaves
+    // members at pred = pos, so placing them after it is the same substep.
+    const uint32_t nB = (uint32_t)bodies.size();
+    if (nB) {
+      k_rigid_step<DBG><<<nB, RG_THREADS, 0, st>>>(b);
+      ++Lc;
+    }
     mark();
     int bits = 1;
     while ((1ull << bits) <= hw.K) ++bits;
@@ -686,6 +700,10 @@ struct World {
         k_apply_fric<DBG><<<ga, 256, 0, st>>>(b);
         Lc += 2;
       }
+      if (nB) {
+        k_rigid_solve<DBG><<<nB, RG_THREADS, 0, st>>>(b, hasSeal ? 1 : 0);
+        ++Lc;
+      }
       mark();
     }
     if (hasSeal) {
@@ -695,10 +713,14 @@ struct World {
     SN_LANES(lc.p1, (launch_post1<DBG, L_>()));
     ++Lc;
     mark();
-    if (hasBonds) {
+    if (hasBonds || nB) {
       SN_LANES(lc.p2, (launch_post2<DBG, false, L_>(0)));
       if (hasSeal) {
         k_contain_stress<DBG><<<ga, 256, 0, st>>>(b);
+        ++Lc;
+      }
+      if (nB) {
+        k_rigid_member<DBG><<<nB, RG_THREADS, 0, st>>>(b);
         ++Lc;
       }
       k_form1<DBG><<<ga, 256, 0, st>>>(b);
@@ -981,12 +1003,10 @@ struct World {
       // solver forms then stays inside i32 (see the range note in sim2d.cuh).
       if (list[i].x < -(1 << 28) || list[i].x > (1 << 28) || list[i].y < -(1 << 28) || list[i].y > (1 << 28))
         return fail("spawn position outside [-2^28, 2^28]");
-      int32_t mm = std::min<int32_t>((int32_t)matCount - 1, std::max<int32_t>(0, list[i].mat));
-      if (rigid_row((uint32_t)mm)) return fail("spawn of rigid-body row %d (solidMode 2) is not supported", mm);
     }
     // §18.2 W1 + §18.22 (src/engine.js:5925-5935): one gesture is one group;
     // a spawn outside an open gesture is its own group.
-    const uint32_t seq = (h.weldHoldSeq != 0 && !ownGroup) ? h.weldHoldSeq : next_weld_seq(h);
+    const uint32_t seq = (h.weldHoldSeq != 0 && !ownGroup) ? h.weldHoldSeq : next_weld_seq(s);
     const uint32_t weldTag = (seq << 8) & WELD_TAG_MASK;
     h.lastWeldTag = weldTag;
     uint32_t total = k + nB;
@@ -1163,6 +1183,7 @@ struct World {
         bOut[(size_t)k * BOND_CAP + c++] = (w & BOND_L0_MASK) | (uint32_t)nj;
       }
     }
+    if (!repair_bodies_after_erase(s, surv, stOut)) return false;
     cudaMemcpyAsync(b.state + (size_t)h.slotBase * 8, stOut.data(), stOut.size() * 4, cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(b.stacc + h.slotBase, scOut.data(), scOut.size() * 4, cudaMemcpyHostToDevice, st);
     if (oldF)
@@ -1179,13 +1200,491 @@ struct World {
     return push_scene(s) && cuda_ok(cudaStreamSynchronize(st), "erase");
   }
 
+  // ---- §20 rigid bodies: host side (src/engine.js:2050-2150, 5452-5811) ----------
+  // Device records are in world order (`bodies`); a scene's bodies keep their
+  // relative order, and a body's index in the reference's API is its position
+  // among its scene's bodies.
+  struct BodyHost {
+    uint32_t scene = 0, tag = 0, first = 0, last = 0, n = 0;
+    bool axis = false, user = false;
+  };
+  std::vector<BodyHost> bodies;
+
+  static double js_round(double x) {  // Math.round: ties towards +infinity
+    const double r = std::floor(x);
+    return (x - r >= 0.5) ? r + 1.0 : r;
+  }
+  // buildCosTable (src/engine.js:2062-2068): Q22 cos over a quarter turn, 1024 steps.
+  static void build_cos_table(int32_t* T) {
+    for (int k = 0; k <= 1024; ++k)
+      T[k] = (int32_t)js_round(std::cos(((double)k * 3.141592653589793) / 2048.0) * 4194304.0);
+    T[1024] = 0;
+    T[1025] = 0;
+  }
+  static int64_t idiv_rne64(int64_t a, int64_t n) {  // idivRne (src/engine.js:2074-2080)
+    if (n <= 0) return 0;
+    const bool neg = a < 0;
+    const int64_t x = neg ? -a : a;
+    int64_t q = x / n;
+    const int64_t r2 = 2 * (x - q * n);
+    if (r2 > n || (r2 == n && (q & 1) == 1)) q += 1;
+    return neg ? -q : q;
+  }
+  static double isqrt_js(double x) {  // isqrt64 (src/engine.js:2083-2089), on the same doubles
+    if (x <= 0) return 0;
+    double r = std::floor(std::sqrt(x));
+    while (r > 0 && r * r > x) r -= 1;
+    while ((r + 1) * (r + 1) <= x) r += 1;
+    return r;
+  }
+  // rigidShifts (src/engine.js:2106-2128)
+  static bool rigid_shifts(const std::vector<int32_t>& ox, const std::vector<int32_t>& oy, int32_t& rMax,
+                           int32_t& rsh, int32_t& ish, int32_t& osh) {
+    const size_t N = ox.size();
+    double rm = 0;
+    for (size_t k = 0; k < N; ++k) {
+      const double a = std::fabs((double)ox[k]), c = std::fabs((double)oy[k]);
+      const double m = isqrt_js(a * a + c * c);
+      if (m > rm) rm = m;
+    }
+    rMax = (int32_t)(int64_t)rm;
+    rsh = 0;
+    while ((rMax >> rsh) > 2048) ++rsh;
+    ish = 0;
+    for (;;) {
+      double sum = 0;
+      for (size_t k = 0; k < N; ++k) {
+        const double a = (double)(ox[k] >> ish), c = (double)(oy[k] >> ish);
+        sum += a * a + c * c;
+      }
+      if (sum < 1073741824.0) break;
+      if (++ish > 30) return false;
+    }
+    osh = 0;
+    while ((double)N * (double)(rMax >> osh) >= 1073741824.0) ++osh;
+    return true;
+  }
+  // rigidInvInertia (src/engine.js:2135-2150), exact.
+  static void rigid_inv_inertia(int32_t s, int32_t rsh, int32_t ish, int32_t& invI, int32_t& iq) {
+    invI = 0;
+    iq = 0;
+    if (s <= 0) return;
+    const int32_t bl = 32 - __builtin_clz((uint32_t)s);
+    const int32_t iqNat = bl - 1 + 2 * ish - rsh;
+    const int32_t q0 = std::min(iqNat, 31);
+    const int32_t E = q0 + rsh - 2 * ish;
+    if (iqNat < 16 || E < 1 || E > 62) return;
+    const unsigned __int128 num = (unsigned __int128)683565276u << E, den = (unsigned __int128)(uint32_t)s;
+    unsigned __int128 q = num / den;
+    const unsigned __int128 r = num - q * den;
+    if (2 * r > den || (2 * r == den && (q & 1))) q += 1;
+    if (q > 2147483647u) q = 2147483647u;
+    invI = (int32_t)q;
+    iq = q0;
+  }
+
+  uint32_t scene_bodies(uint32_t s) const {
+    uint32_t k = 0;
+    for (const BodyHost& bh : bodies) k += bh.scene == s;
+    return k;
+  }
+  int world_body(uint32_t s, uint32_t k) const {  // scene-local index -> record index
+    for (size_t i = 0; i < bodies.size(); ++i)
+      if (bodies[i].scene == s && k-- == 0) return (int)i;
+    return -1;
+  }
+  bool read_records(std::vector<int32_t>& rec, std::vector<int32_t>& drv) {
+    rec.assign(bodies.size() * RG_BODY_WORDS, 0);
+    drv.assign(bodies.size() * RG_DRIVER_WORDS, 0);
+    if (bodies.empty()) return true;
+    return cuda_ok(cudaMemcpyAsync(rec.data(), b.rbody, rec.size() * 4, cudaMemcpyDeviceToHost, st), "bodies") &&
+           cuda_ok(cudaMemcpyAsync(drv.data(), b.rdrv, drv.size() * 4, cudaMemcpyDeviceToHost, st), "drivers") &&
+           cuda_ok(cudaStreamSynchronize(st), "bodies");
+  }
+  bool write_records(const std::vector<int32_t>& rec, const std::vector<int32_t>& drv) {
+    graphValid = false;
+    hw.nBodies = (uint32_t)bodies.size();
+    if (bodies.empty()) return true;
+    return cuda_ok(cudaMemcpyAsync(b.rbody, rec.data(), rec.size() * 4, cudaMemcpyHostToDevice, st), "bodies") &&
+           cuda_ok(cudaMemcpyAsync(b.rdrv, drv.data(), drv.size() * 4, cudaMemcpyHostToDevice, st), "drivers") &&
+           cuda_ok(cudaStreamSynchronize(st), "bodies");
+  }
+  // Replace scene s's bodies by (recS, drvS, descS), keeping every other
+  // scene's records as they are on the device.
+  bool replace_scene_bodies(uint32_t s, const std::vector<int32_t>& recS, const std::vector<int32_t>& drvS,
+                            const std::vector<BodyHost>& descS) {
+    std::vector<int32_t> rec, drv;
+    if (!read_records(rec, drv)) return false;
+    std::vector<int32_t> r2, d2;
+    std::vector<BodyHost> b2;
+    for (size_t i = 0; i < bodies.size(); ++i) {
+      if (bodies[i].scene == s) continue;
+      r2.insert(r2.end(), rec.begin() + i * RG_BODY_WORDS, rec.begin() + (i + 1) * RG_BODY_WORDS);
+      d2.insert(d2.end(), drv.begin() + i * RG_DRIVER_WORDS, drv.begin() + (i + 1) * RG_DRIVER_WORDS);
+      b2.push_back(bodies[i]);
+    }
+    r2.insert(r2.end(), recS.begin(), recS.end());
+    d2.insert(d2.end(), drvS.begin(), drvS.end());
+    b2.insert(b2.end(), descS.begin(), descS.end());
+    if (b2.size() > (size_t)RG_MAX_BODIES) return fail("more than %d rigid bodies", RG_MAX_BODIES);
+    bodies = b2;
+    return write_records(r2, d2);
+  }
+  bool drop_scene_bodies(uint32_t s) {
+    if (scene_bodies(s) == 0) return true;
+    return replace_scene_bodies(s, {}, {}, {});
+  }
+  bool read_scene_state(uint32_t s, std::vector<int32_t>& stw) {
+    const SceneHost& h = sh[s];
+    stw.assign((size_t)h.n * 8, 0);
+    if (h.n == 0) return true;
+    return cuda_ok(cudaMemcpyAsync(stw.data(), b.state + (size_t)h.slotBase * 8, stw.size() * 4,
+                                   cudaMemcpyDeviceToHost, st), "state") &&
+           cuda_ok(cudaStreamSynchronize(st), "state");
+  }
+  bool write_scene_state(uint32_t s, const std::vector<int32_t>& stw, uint32_t lo, uint32_t hi) {
+    const SceneHost& h = sh[s];
+    if (hi < lo) return true;
+    accFresh = false;
+    return cuda_ok(cudaMemcpyAsync(b.state + ((size_t)h.slotBase + lo) * 8, stw.data() + (size_t)lo * 8,
+                                   ((size_t)hi - lo + 1) * 32, cudaMemcpyHostToDevice, st), "state") &&
+           cuda_ok(cudaStreamSynchronize(st), "state");
+  }
+  bool mark_bond_dirty(uint32_t s) {
+    if (!pull_params()) return false;
+    hpar[s].bondDirty = 1;
+    return put_word(s, offsetof(ScenePar, bondDirty), 1u);
+  }
+
+  // _writeBodyRecord (src/engine.js:5452-5580): members ascending fluid slots
+  // of scene s, `stw` its state words. *idx = the body's index in scene s, or
+  // -1 where the reference returns null.
+  bool write_body_record(uint32_t s, const std::vector<uint32_t>& members, const std::vector<int32_t>& stw,
+                         uint32_t tag, const int32_t* pivot, bool user, int32_t* idx) {
+    *idx = -1;
+    const size_t N = members.size();
+    if (N < 4 || scene_bodies(s) >= (uint32_t)RG_MAX_BODIES || bodies.size() >= (size_t)RG_MAX_BODIES) return true;
+    auto W = [&](uint32_t i, int w) { return (int64_t)stw[(size_t)i * 8 + w]; };
+    int64_t sx = 0, sy = 0, svx = 0, svy = 0;
+    for (uint32_t i : members) { sx += W(i, 0); sy += W(i, 1); svx += W(i, 2); svy += W(i, 3); }
+    const bool axis = pivot != nullptr;
+    const int32_t cx = axis ? pivot[0] : (int32_t)idiv_rne64(sx, (int64_t)N);
+    const int32_t cy = axis ? pivot[1] : (int32_t)idiv_rne64(sy, (int64_t)N);
+    const int32_t vx = axis ? 0 : (int32_t)idiv_rne64(svx, (int64_t)N);
+    const int32_t vy = axis ? 0 : (int32_t)idiv_rne64(svy, (int64_t)N);
+    std::vector<int32_t> ox(N), oy(N);
+    for (size_t k = 0; k < N; ++k) {
+      ox[k] = (int32_t)(W(members[k], 0) - cx);
+      oy[k] = (int32_t)(W(members[k], 1) - cy);
+    }
+    int32_t rMax, rsh, ish, osh;
+    if (!rigid_shifts(ox, oy, rMax, rsh, ish, osh)) return fail("body too large for an i32 inertia sum");
+    int64_t sumIs2 = 0, gSum = 0;
+    for (size_t k = 0; k < N; ++k) {
+      const int64_t a = ox[k] >> ish, c = oy[k] >> ish;
+      sumIs2 += a * a + c * c;
+      gSum += row((uint32_t)W(members[k], 4))[M_grav];
+    }
+    int32_t invI, iq;
+    rigid_inv_inertia((int32_t)sumIs2, rsh, ish, invI, iq);
+    int64_t acc = 0;
+    for (size_t k = 0; k < N; ++k)
+      acc += (int64_t)(ox[k] >> rsh) * (W(members[k], 3) - vy) - (int64_t)(oy[k] >> rsh) * (W(members[k], 2) - vx);
+    int64_t omega = 0;
+    if (invI != 0) {
+      const __int128 num = (__int128)acc * invI, den = (__int128)1 << iq;
+      __int128 q = num / den, r = num - q * den;
+      if (r < 0) { q -= 1; r += den; }
+      if (2 * r > den || (2 * r == den && (q & 1))) q += 1;
+      omega = (int64_t)q;
+    }
+    const int64_t omegaMax = std::max<int64_t>(
+        1, std::min<int64_t>(1073741824, ((int64_t)VMAX * 683565276) / std::max<int64_t>(1, rMax)));
+    omega = std::max(-omegaMax, std::min(omegaMax, omega));
+    std::vector<int32_t> rec(RG_BODY_WORDS, 0), drv(RG_DRIVER_WORDS, 0);
+    rec[RB_LIVE] = 1; rec[RB_TAG] = (int32_t)tag;
+    rec[RB_FIRST] = (int32_t)members.front(); rec[RB_LAST] = (int32_t)members.back();
+    rec[RB_CX] = cx; rec[RB_CY] = cy; rec[RB_VX] = vx; rec[RB_VY] = vy;
+    rec[RB_OMEGA] = (int32_t)omega; rec[RB_N] = (int32_t)N;
+    rec[RB_SUMIS2] = (int32_t)sumIs2; rec[RB_GSUM] = (int32_t)(uint32_t)(uint64_t)gSum;
+    rec[RB_INVI] = invI; rec[RB_IQ] = iq; rec[RB_RSH] = rsh; rec[RB_ISH] = ish; rec[RB_OSH] = osh;
+    rec[RB_OMEGAM] = (int32_t)omegaMax; rec[RB_RMAX] = rMax;
+    rec[RB_CQX] = cx; rec[RB_CQY] = cy; rec[RB_AXIS] = axis ? 1 : 0; rec[RB_USER] = user ? 1 : 0;
+    rec[RB_SCENE] = (int32_t)s;
+    // rest offsets, one copy per contiguous run of member slots
+    const uint32_t base = sh[s].slotBase;
+    for (size_t k0 = 0; k0 < N;) {
+      size_t k1 = k0 + 1;
+      while (k1 < N && members[k1] == members[k1 - 1] + 1) ++k1;
+      std::vector<int2> win(k1 - k0);
+      for (size_t q = k0; q < k1; ++q) win[q - k0] = make_int2(ox[q], oy[q]);
+      if (!cuda_ok(cudaMemcpyAsync(b.rest + base + members[k0], win.data(), win.size() * sizeof(int2),
+                                   cudaMemcpyHostToDevice, st), "rest") ||
+          !cuda_ok(cudaStreamSynchronize(st), "rest"))
+        return false;
+      k0 = k1;
+    }
+    const uint32_t at = (uint32_t)bodies.size();
+    BodyHost bh;
+    bh.scene = s; bh.tag = tag; bh.first = members.front(); bh.last = members.back(); bh.n = (uint32_t)N;
+    bh.axis = axis; bh.user = user;
+    bodies.push_back(bh);
+    *idx = (int32_t)scene_bodies(s) - 1;
+    graphValid = false;
+    hw.nBodies = (uint32_t)bodies.size();
+    return cuda_ok(cudaMemcpyAsync(b.rbody + (size_t)at * RG_BODY_WORDS, rec.data(), RG_BODY_WORDS * 4,
+                                   cudaMemcpyHostToDevice, st), "body") &&
+           cuda_ok(cudaMemcpyAsync(b.rdrv + (size_t)at * RG_DRIVER_WORDS, drv.data(), RG_DRIVER_WORDS * 4,
+                                   cudaMemcpyHostToDevice, st), "driver") &&
+           cuda_ok(cudaStreamSynchronize(st), "body");
+  }
+
+  // makeRigidBody / makeAxisBody (src/engine.js:5722-5780)
+  bool make_rigid_body(uint32_t s, const uint32_t* slots, uint32_t k, const int32_t* pivot, bool user, int32_t* idx) {
+    *idx = -1;
+    SceneHost& h = sh[s];
+    if (!h.loaded) return fail("makeRigidBody before loadScene");
+    if (k == 0 || h.nFluid == 0) return true;
+    if (!slots) return fail("slots is NULL");
+    std::vector<int32_t> stw;
+    if (!read_scene_state(s, stw)) return false;
+    std::vector<uint32_t> members;
+    for (uint32_t q = 0; q < k; ++q) {
+      const uint32_t i = slots[q];
+      if (i >= h.nFluid) continue;
+      if (row((uint32_t)stw[(size_t)i * 8 + 4])[M_solidMode] != SOLID_RIGID) continue;
+      if ((uint32_t)stw[(size_t)i * 8 + 5] & (FLAG_RIGID | FLAG_ANCHOR)) continue;
+      members.push_back(i);
+    }
+    std::sort(members.begin(), members.end());
+    members.erase(std::unique(members.begin(), members.end()), members.end());
+    if (members.size() < 4) return true;
+    std::vector<bool> inUse(4096, false);
+    for (uint32_t i = 0; i < h.nFluid; ++i) inUse[((uint32_t)stw[(size_t)i * 8 + 5] & WELD_TAG_MASK) >> 8] = true;
+    uint32_t seq = 0;
+    for (uint32_t g = 0; g <= 4095; ++g) {
+      const uint32_t q = next_weld_seq(s);
+      if (!inUse[q]) { seq = q; break; }
+    }
+    if (seq == 0) return fail("§20: no free weld tag for a new body");
+    const uint32_t tag = (seq << 8) & WELD_TAG_MASK;
+    for (uint32_t i : members) {
+      uint32_t& fl = reinterpret_cast<uint32_t&>(stw[(size_t)i * 8 + 5]);
+      fl = (fl & ~WELD_TAG_MASK) | tag | FLAG_RIGID;
+    }
+    if (!write_body_record(s, members, stw, tag, pivot, user, idx)) return false;
+    if (*idx < 0) return true;
+    return write_scene_state(s, stw, members.front(), members.back()) && mark_bond_dirty(s);
+  }
+  // promoteWeldGroup (src/engine.js:5584-5622): the held (or given) tag's
+  // rigid-row particles that are neither anchored nor already in a body.
+  bool promote_weld_group(uint32_t s, uint32_t tag, const int32_t* pivot, bool user, int32_t* idx) {
+    *idx = -1;
+    SceneHost& h = sh[s];
+    if (!h.loaded) return fail("promoteWeldGroup before loadScene");
+    const uint32_t t = (tag == 0 ? h.weldHold : tag) & WELD_TAG_MASK;
+    if (t == 0 || h.nFluid == 0) return true;
+    std::vector<int32_t> stw;
+    if (!read_scene_state(s, stw)) return false;
+    std::vector<uint32_t> members;
+    for (uint32_t i = 0; i < h.nFluid; ++i) {
+      const uint32_t fl = (uint32_t)stw[(size_t)i * 8 + 5];
+      if ((fl & WELD_TAG_MASK) != t || (fl & (FLAG_RIGID | FLAG_ANCHOR))) continue;
+      if (row((uint32_t)stw[(size_t)i * 8 + 4])[M_solidMode] != SOLID_RIGID) continue;
+      members.push_back(i);
+    }
+    if (!write_body_record(s, members, stw, t, pivot, user, idx)) return false;
+    if (*idx < 0) return true;
+    for (uint32_t i : members) stw[(size_t)i * 8 + 5] |= (int32_t)FLAG_RIGID;
+    return write_scene_state(s, stw, members.front(), members.back()) && mark_bond_dirty(s);
+  }
+  bool end_weld_group_and_promote(uint32_t s, const int32_t* pivot, bool user, int32_t* idx) {
+    *idx = -1;
+    uint32_t was = 0;
+    if (!end_weld_group(s, &was)) return false;
+    if (was == 0) return true;
+    return promote_weld_group(s, was, pivot, user, idx);
+  }
+  // dissolveAllBodies (src/engine.js:5789-5808)
+  bool dissolve_all_bodies(uint32_t s, uint32_t* count) {
+    if (count) *count = 0;
+    if (!sh[s].loaded) return fail("dissolveAllBodies before loadScene");
+    if (scene_bodies(s) == 0) return true;
+    std::vector<int32_t> stw;
+    if (!read_scene_state(s, stw)) return false;
+    uint32_t k = 0;
+    for (uint32_t i = 0; i < sh[s].nFluid; ++i) {
+      int32_t& fl = stw[(size_t)i * 8 + 5];
+      if (!((uint32_t)fl & FLAG_RIGID)) continue;
+      fl &= ~(int32_t)FLAG_RIGID;
+      ++k;
+    }
+    if (count) *count = k;
+    return write_scene_state(s, stw, 0, sh[s].n - 1) && drop_scene_bodies(s);
+  }
+  bool set_body_user(uint32_t s, uint32_t k, bool on, bool* found) {
+    *found = false;
+    const int wi = world_body(s, k);
+    if (wi < 0) return true;
+    bodies[wi].user = on;
+    *found = true;
+    const int32_t v = on ? 1 : 0;
+    return cuda_ok(cudaMemcpyAsync(b.rbody + (size_t)wi * RG_BODY_WORDS + RB_USER, &v, 4, cudaMemcpyHostToDevice, st),
+                   "user") &&
+           cuda_ok(cudaStreamSynchronize(st), "user");
+  }
+  // A body's driver sidecar (the words `_serviceBodyConstraints` uploads,
+  // src/engine.js:5370-5412): mask of RD_HAS_* bits and the nine values.
+  bool set_body_driver(uint32_t s, uint32_t k, int32_t mask, const int32_t* values) {
+    const int wi = world_body(s, k);
+    if (wi < 0) return fail("body %u is not live", k);
+    if (mask < 0 || mask >= 512) return fail("driver mask %d outside 0..511", mask);
+    int32_t d[RG_DRIVER_WORDS] = {mask};
+    for (int q = 0; q < 9; ++q) d[1 + q] = values ? values[q] : 0;
+    return cuda_ok(cudaMemcpyAsync(b.rdrv + (size_t)wi * RG_DRIVER_WORDS, d, sizeof(d), cudaMemcpyHostToDevice, st),
+                   "driver") &&
+           cuda_ok(cudaStreamSynchronize(st), "driver");
+  }
+  bool clear_body_drivers(uint32_t s) {
+    const int32_t z[RG_DRIVER_WORDS] = {0};
+    for (size_t i = 0; i < bodies.size(); ++i)
+      if (bodies[i].scene == s &&
+          !cuda_ok(cudaMemcpyAsync(b.rdrv + i * RG_DRIVER_WORDS, z, sizeof(z), cudaMemcpyHostToDevice, st), "driver"))
+        return false;
+    return cuda_ok(cudaStreamSynchronize(st), "driver");
+  }
+  // dragGrab's rigid branch (src/engine.js:6111-6140)
+  bool drag_body(uint32_t s, uint32_t tag, int32_t tx, int32_t ty, int32_t vx, int32_t vy, bool* moved) {
+    *moved = false;
+    for (size_t i = 0; i < bodies.size(); ++i) {
+      if (bodies[i].scene != s || bodies[i].tag != tag) continue;
+      if (bodies[i].axis) return true;
+      const int32_t cvx = std::max(-VMAX, std::min(VMAX, vx)), cvy = std::max(-VMAX, std::min(VMAX, vy));
+      const int64_t ONE = 65536;
+      const int32_t w4[4] = {
+          (int32_t)std::max<int64_t>(ONE, std::min<int64_t>((int64_t)sh[s].domW - ONE, (int64_t)tx - cvx)),
+          (int32_t)std::max<int64_t>(ONE, std::min<int64_t>((int64_t)sh[s].domH - ONE, (int64_t)ty - cvy)), cvx, cvy};
+      const int32_t z4[4] = {0, 0, 0, 0};
+      *moved = true;
+      return cuda_ok(cudaMemcpyAsync(b.rbody + i * RG_BODY_WORDS + RB_CX, w4, 16, cudaMemcpyHostToDevice, st), "drag") &&
+             cuda_ok(cudaMemcpyAsync(b.rbody + i * RG_BODY_WORDS + RB_RESX, z4, 16, cudaMemcpyHostToDevice, st), "drag") &&
+             cuda_ok(cudaStreamSynchronize(st), "drag");
+    }
+    return true;
+  }
+  // readBodies: scene s's records in the reference's layout (word 29 zero).
+  bool read_bodies(uint32_t s, int32_t* out, size_t words, uint32_t* count) {
+    std::vector<int32_t> rec, drv;
+    if (!read_records(rec, drv)) return false;
+    const uint32_t nb = scene_bodies(s);
+    if (count) *count = nb;
+    if (!out) return true;
+    if (words < (size_t)nb * RG_BODY_WORDS) return fail("readBodies needs %u words", nb * RG_BODY_WORDS);
+    size_t o = 0;
+    for (size_t i = 0; i < bodies.size(); ++i) {
+      if (bodies[i].scene != s) continue;
+      std::memcpy(out + o, rec.data() + i * RG_BODY_WORDS, RG_BODY_WORDS * 4);
+      out[o + RB_SCENE] = 0;
+      o += RG_BODY_WORDS;
+    }
+    return true;
+  }
+  bool read_rest(uint32_t s, int32_t* out, size_t words) {
+    const SceneHost& h = sh[s];
+    if (!out || words < (size_t)h.n * 2) return fail("readRestOffsets needs n*2 words");
+    return h.n == 0 || (cuda_ok(cudaMemcpyAsync(out, b.rest + h.slotBase, (size_t)h.n * 8, cudaMemcpyDeviceToHost, st),
+                                "rest") &&
+                        cuda_ok(cudaStreamSynchronize(st), "rest"));
+  }
+  // restoreAuthoringSnapshot's rigid part (src/engine.js:5838-5880).
+  bool restore_bodies(uint32_t s, const int32_t* records, uint32_t nb, const int32_t* rest, size_t restWords) {
+    if (!sh[s].loaded) return fail("restore before loadScene");
+    if (nb > (uint32_t)RG_MAX_BODIES || (nb && !records)) return fail("bad body records");
+    if (rest && restWords > (size_t)sh[s].cap * 2) return fail("rest offsets exceed the scene's slots");
+    std::vector<int32_t> rec(records, records + (size_t)nb * RG_BODY_WORDS), drv((size_t)nb * RG_DRIVER_WORDS, 0);
+    std::vector<BodyHost> desc(nb);
+    for (uint32_t k = 0; k < nb; ++k) {
+      int32_t* R = rec.data() + (size_t)k * RG_BODY_WORDS;
+      R[RB_SCENE] = (int32_t)s;
+      desc[k].scene = s; desc[k].tag = (uint32_t)R[RB_TAG]; desc[k].first = (uint32_t)R[RB_FIRST];
+      desc[k].last = (uint32_t)R[RB_LAST]; desc[k].n = (uint32_t)R[RB_N];
+      desc[k].axis = R[RB_AXIS] != 0; desc[k].user = R[RB_USER] != 0;
+    }
+    if (rest && restWords &&
+        (!cuda_ok(cudaMemcpyAsync(b.rest + sh[s].slotBase, rest, restWords * 4, cudaMemcpyHostToDevice, st), "rest") ||
+         !cuda_ok(cudaStreamSynchronize(st), "rest")))
+      return false;
+    return replace_scene_bodies(s, rec, drv, desc);
+  }
+  // eraseWhere's body repair (src/engine.js:6526-6610), on the host copy of
+  // the compacted state `stOut` (its flags change here) before it is written.
+  bool repair_bodies_after_erase(uint32_t s, const std::vector<uint32_t>& surv, std::vector<int32_t>& stOut) {
+    if (scene_bodies(s) == 0) return true;
+    const SceneHost& h = sh[s];
+    std::vector<int32_t> rec, drv;
+    if (!read_records(rec, drv)) return false;
+    std::vector<int2> restIn(h.nFluid > 0 ? h.nFluid : 1), restOut(h.cap);
+    if (h.nFluid &&
+        (!cuda_ok(cudaMemcpyAsync(restIn.data(), b.rest + h.slotBase, (size_t)h.nFluid * 8, cudaMemcpyDeviceToHost, st),
+                  "rest") ||
+         !cuda_ok(cudaStreamSynchronize(st), "rest")))
+      return false;
+    const uint32_t newF = (uint32_t)surv.size();
+    for (uint32_t k = 0; k < (uint32_t)h.cap; ++k) restOut[k] = make_int2(0, 0);
+    for (uint32_t k = 0; k < newF; ++k) restOut[k] = restIn[surv[k]];
+    std::vector<int32_t> recS, drvS;
+    std::vector<BodyHost> descS;
+    for (size_t i = 0; i < bodies.size(); ++i) {
+      if (bodies[i].scene != s) continue;
+      std::vector<uint32_t> mem;
+      for (uint32_t k = 0; k < newF; ++k) {
+        const uint32_t fl = (uint32_t)stOut[(size_t)k * 8 + 5];
+        if ((fl & FLAG_RIGID) && (fl & WELD_TAG_MASK) == bodies[i].tag) mem.push_back(k);
+      }
+      if (mem.size() < 4) {
+        for (uint32_t k : mem) stOut[(size_t)k * 8 + 5] &= ~(int32_t)FLAG_RIGID;
+        continue;
+      }
+      std::vector<int32_t> r(rec.begin() + i * RG_BODY_WORDS, rec.begin() + (i + 1) * RG_BODY_WORDS);
+      const int32_t ish = r[RB_ISH];
+      int64_t sumIs2 = 0, gSum = 0;
+      for (uint32_t k : mem) {
+        const int64_t a = restOut[k].x >> ish, c = restOut[k].y >> ish;
+        sumIs2 += a * a + c * c;
+        gSum += row((uint32_t)stOut[(size_t)k * 8 + 4])[M_grav];
+      }
+      int32_t invI, iq;
+      rigid_inv_inertia((int32_t)sumIs2, r[RB_RSH], ish, invI, iq);
+      r[RB_FIRST] = (int32_t)mem.front(); r[RB_LAST] = (int32_t)mem.back(); r[RB_N] = (int32_t)mem.size();
+      r[RB_SUMIS2] = (int32_t)sumIs2; r[RB_GSUM] = (int32_t)(uint32_t)(uint64_t)gSum;
+      r[RB_INVI] = invI; r[RB_IQ] = iq;
+      recS.insert(recS.end(), r.begin(), r.end());
+      drvS.insert(drvS.end(), drv.begin() + i * RG_DRIVER_WORDS, drv.begin() + (i + 1) * RG_DRIVER_WORDS);
+      BodyHost d = bodies[i];
+      d.first = mem.front(); d.last = mem.back(); d.n = (uint32_t)mem.size();
+      descS.push_back(d);
+    }
+    if (!cuda_ok(cudaMemcpyAsync(b.rest + h.slotBase, restOut.data(), (size_t)h.cap * 8, cudaMemcpyHostToDevice, st),
+                 "rest") ||
+        !cuda_ok(cudaStreamSynchronize(st), "rest"))
+      return false;
+    return replace_scene_bodies(s, recS, drvS, descS);
+  }
+
   // ---- weld groups (src/engine.js:4570-4680) -----------------------------------
-  // _nextWeldSeq: the next 12-bit tag sequence not held open (no rigid bodies
-  // exist here to take one).
-  static uint32_t next_weld_seq(SceneHost& h) {
+  // _nextWeldSeq: the next 12-bit tag sequence that is neither held open nor
+  // worn by one of the scene's bodies.
+  bool weld_seq_taken(uint32_t s, uint32_t q) const {
+    if (q == sh[s].weldHoldSeq) return true;
+    for (const BodyHost& bh : bodies)
+      if (bh.scene == s && (bh.tag >> 8) == q) return true;
+    return false;
+  }
+  uint32_t next_weld_seq(uint32_t s) {
+    SceneHost& h = sh[s];
     const uint32_t MAXS = 4095;
     uint32_t q = (h.weldSeq % MAXS) + 1;
-    for (uint32_t guard = 0; guard <= MAXS && q == h.weldHoldSeq; ++guard) q = (q % MAXS) + 1;
+    for (uint32_t guard = 0; guard <= MAXS && weld_seq_taken(s, q); ++guard) q = (q % MAXS) + 1;
     h.weldSeq = q;
     return q;
   }
@@ -1227,13 +1726,27 @@ struct World {
     if (!sh[s].loaded) return fail("beginWeldGroup before loadScene");
     if (sh[s].weldHold != 0 && !end_weld_group(s, nullptr)) return false;
     if (sh[s].fuseTag != 0 && !set_fuse(s, 0)) return false;
-    return hold_weld_group(s, (next_weld_seq(sh[s]) << 8) & WELD_TAG_MASK, tag);
+    return hold_weld_group(s, (next_weld_seq(s) << 8) & WELD_TAG_MASK, tag);
   }
   bool arm_fuse(uint32_t s, uint32_t* tag) {
     if (!sh[s].loaded) return fail("armFuse before loadScene");
     if (sh[s].weldHold == 0) return fail("armFuse(): no weld group is open");
     if (tag) *tag = sh[s].weldHold;
     return set_fuse(s, sh[s].weldHold);
+  }
+
+  // setUserDrive (src/engine.js:4797-4806): clamped to +-USER_A_MAX (32768),
+  // read by user-flagged bodies in rigidStep.
+  bool set_user_drive(uint32_t s, int32_t ax, int32_t ay, int32_t* out) {
+    if (!sh[s].loaded) return fail("setUserDrive before loadScene");
+    const int32_t M = 32768;
+    const int32_t q[2] = {std::max(-M, std::min(M, ax)), std::max(-M, std::min(M, ay))};
+    if (out) { out[0] = q[0]; out[1] = q[1]; }
+    if (q[0] == hpar[s].userA[0] && q[1] == hpar[s].userA[1]) return true;
+    hpar[s].userA[0] = q[0];
+    hpar[s].userA[1] = q[1];
+    return put_word(s, offsetof(ScenePar, userA), (uint32_t)q[0]) &&
+           put_word(s, offsetof(ScenePar, userA) + 4, (uint32_t)q[1]);
   }
 
   // setJets (src/engine.js:4740-4770): the first 8 jets, [x, y, r, fx, fy].
@@ -1258,6 +1771,7 @@ struct World {
   bool ckpt_save(uint32_t s, sn_ckpt_pool* pool, uint64_t* handle) {
     SceneHost& h = sh[s];
     if (!h.loaded) return fail("checkpoint of a scene that is not loaded");
+    if (scene_bodies(s) != 0) return fail("checkpoints of scenes with rigid bodies are not supported");
     if (pool->device != device) return fail("checkpoint pool is on device %d, the engine on %d", pool->device, device);
     if (layoutDirty && !relayout()) return false;
     if (!pull_params()) return false;
@@ -1517,6 +2031,7 @@ int sn_batch_add_scene(sn_batch* b, const sn_scene* sc, uint32_t capacity, uint3
 int sn_batch_remove_scene(sn_batch* b, uint32_t id) {
   if (!b || id >= b->w.maxScenes || !b->w.sh[id].used) return SN_E_INVALID;
   World& w = b->w;
+  if (!w.drop_scene_bodies(id)) return rc_of(w, false);
   w.sh[id] = SceneHost{};
   w.hpar[id] = ScenePar{};
   w.layoutDirty = true;
@@ -1622,11 +2137,7 @@ int sn_batch_set_jets(sn_batch* b, uint32_t id, const int32_t* jets, uint32_t k,
 }
 int sn_set_user_drive(sn_engine* e, int32_t ax, int32_t ay, int32_t out[2]) {
   if (!e) return SN_E_INVALID;
-  const int32_t M = 32768;  // USER_A_MAX, src/engine.js:481
-  e->w.userA[0] = std::max(-M, std::min(M, ax));
-  e->w.userA[1] = std::max(-M, std::min(M, ay));
-  if (out) { out[0] = e->w.userA[0]; out[1] = e->w.userA[1]; }
-  return SN_OK;
+  return rc_of(e->w, e->w.set_user_drive(0, ax, ay, out));
 }
 int sn_autotune(sn_engine* e, uint32_t reps, uint32_t* substeps_run) {
   if (!e) return SN_E_INVALID;
@@ -1718,6 +2229,60 @@ int sn_batch_last_timing(sn_batch* b, float* ms, uint64_t* launches) {
   if (ms && !b->w.timing(ms)) return SN_E_CUDA;
   if (launches) *launches = b->w.lastLaunches;
   return SN_OK;
+}
+
+
+// ---- §20 rigid bodies (src/engine.js:5452-5811) -------------------------------
+int sn_make_rigid_body(sn_engine* e, const uint32_t* slots, uint32_t k, const int32_t* pivot, uint32_t user,
+                       int32_t* index) {
+  if (!e || !index) return SN_E_INVALID;
+  return rc_of(e->w, e->w.make_rigid_body(0, slots, k, pivot, user != 0, index));
+}
+int sn_promote_weld_group(sn_engine* e, uint32_t tag, const int32_t* pivot, uint32_t user, int32_t* index) {
+  if (!e || !index) return SN_E_INVALID;
+  return rc_of(e->w, e->w.promote_weld_group(0, tag, pivot, user != 0, index));
+}
+int sn_end_weld_group_and_promote(sn_engine* e, const int32_t* pivot, uint32_t user, int32_t* index) {
+  if (!e || !index) return SN_E_INVALID;
+  return rc_of(e->w, e->w.end_weld_group_and_promote(0, pivot, user != 0, index));
+}
+int sn_dissolve_all_bodies(sn_engine* e, uint32_t* count) {
+  if (!e) return SN_E_INVALID;
+  return rc_of(e->w, e->w.dissolve_all_bodies(0, count));
+}
+int sn_read_bodies(sn_engine* e, int32_t* out, size_t words, uint32_t* count) {
+  if (!e) return SN_E_INVALID;
+  return rc_of(e->w, e->w.read_bodies(0, out, words, count));
+}
+int sn_read_rest_offsets(sn_engine* e, int32_t* out, size_t words) {
+  if (!e) return SN_E_INVALID;
+  return rc_of(e->w, e->w.read_rest(0, out, words));
+}
+int sn_set_body_user(sn_engine* e, uint32_t index, uint32_t on, uint32_t* found) {
+  if (!e) return SN_E_INVALID;
+  bool f = false;
+  const bool ok = e->w.set_body_user(0, index, on != 0, &f);
+  if (found) *found = f ? 1u : 0u;
+  return rc_of(e->w, ok);
+}
+int sn_set_body_driver(sn_engine* e, uint32_t index, int32_t mask, const int32_t values[9]) {
+  if (!e) return SN_E_INVALID;
+  return rc_of(e->w, e->w.set_body_driver(0, index, mask, values));
+}
+int sn_clear_body_drivers(sn_engine* e) {
+  if (!e) return SN_E_INVALID;
+  return rc_of(e->w, e->w.clear_body_drivers(0));
+}
+int sn_drag_body(sn_engine* e, uint32_t tag, int32_t x, int32_t y, int32_t vx, int32_t vy, uint32_t* moved) {
+  if (!e) return SN_E_INVALID;
+  bool m = false;
+  const bool ok = e->w.drag_body(0, tag, x, y, vx, vy, &m);
+  if (moved) *moved = m ? 1u : 0u;
+  return rc_of(e->w, ok);
+}
+int sn_restore_bodies(sn_engine* e, const int32_t* records, uint32_t count, const int32_t* rest, size_t rest_words) {
+  if (!e) return SN_E_INVALID;
+  return rc_of(e->w, e->w.restore_bodies(0, records, count, rest, rest_words));
 }
 
 }  // extern "C"

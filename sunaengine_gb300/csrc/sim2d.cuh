@@ -89,6 +89,7 @@ constexpr uint32_t INFO_PINNED = 0x10000000u;    // FLAG_ANCHOR | FLAG_RIGID: ne
 constexpr uint32_t INFO_BURST = 0x08000000u;     // FLAG_BURST
 constexpr uint32_t INFO_RIGID = 0x04000000u;     // FLAG_RIGID
 constexpr uint32_t INFO_SEAL = 0x02000000u;      // FLAG_SEAL
+constexpr uint32_t INFO_TAG = 0x000fff00u;       // a rigid member's weld tag (its body id); 0 otherwise
 
 // material words (src/engine.js:678-705)
 enum : int {
@@ -145,6 +146,12 @@ struct Bufs {
   uint32_t* dbg;        // [16]
   uint32_t* err;        // [4]
   uint32_t* work;       // [4] per-substep flags: [0] = some particle has a friction/bond row
+  // §20 rigid bodies
+  int32_t* rbody;       // [bodies * 32] body records (the reference's RB_* words; word 29 = scene)
+  int32_t* rdrv;        // [bodies * 10] driver sidecars (RD_* words)
+  int2* rest;           // [cap] rest offsets, slot space
+  const int32_t* cosT;  // [1026] Q22 quarter-turn cosine table
+  uint32_t* rmark;      // [cap] rigidMember's leave marks, slot space
 };
 
 enum : uint32_t { ERR_UNSUPPORTED_ROW = 1u, ERR_BOND_PARTNER = 2u };
@@ -254,7 +261,12 @@ __device__ __forceinline__ uint32_t info_of(uint32_t matId, uint32_t flags, bool
   return (matId & INFO_MAT) | (boundary ? INFO_BOUNDARY : 0u) | ((flags & FLAG_DEAD) ? INFO_DEAD : 0u) |
          ((flags & FLAG_CONGEAL) ? INFO_CONGEAL : 0u) | ((flags & (FLAG_ANCHOR | FLAG_RIGID)) ? INFO_PINNED : 0u) |
          ((flags & FLAG_BURST) ? INFO_BURST : 0u) | ((flags & FLAG_RIGID) ? INFO_RIGID : 0u) |
-         ((flags & FLAG_SEAL) ? INFO_SEAL : 0u);
+         ((flags & FLAG_SEAL) ? INFO_SEAL : 0u) | ((flags & FLAG_RIGID) ? (flags & INFO_TAG) : 0u);
+}
+// rg_same_body (src/sim.wgsl:891-894) on two info words: both rigid members
+// wearing the same nonzero body tag.
+__device__ __forceinline__ bool same_body(uint32_t infoI, uint32_t infoJ) {
+  return (infoI & infoJ & INFO_RIGID) != 0u && ((infoI ^ infoJ) & INFO_TAG) == 0u && (infoI & INFO_TAG) != 0u;
 }
 __device__ __forceinline__ int2 xy(int4 v) { return make_int2(v.x, v.y); }
 __device__ __forceinline__ int2 ld_pred(const int4* PL, uint32_t q) {
@@ -547,9 +559,12 @@ __global__ void __launch_bounds__(256) k_solveA(Bufs b, int lastIter) {
 // solveB_at (src/sim.wgsl:1337-1372) for one particle. The S table is all
 // zeros in the frozen tables (scorrK = 0, checked at load), so the release
 // build drops its term; debug builds still read it.
-template <bool DBG, int L>
+// RIG: the warp holds a rigid member, whose own correction skips the members
+// of its body (src/sim.wgsl:1355-1358).
+template <bool DBG, int L, bool RIG = false>
 __device__ __forceinline__ int2 solveB_dp(const Bufs& b, const int4* __restrict__ src, uint32_t p, uint32_t cnt,
-                                          uint32_t sub, int2 pi, int32_t li, const Flags<DBG>& f) {
+                                          uint32_t sub, int2 pi, int32_t li, const Flags<DBG>& f,
+                                          uint32_t infoI = 0u) {
   const uint32_t stride = b.nbrStride;
   int32_t dpx = 0, dpy = 0;
   const uint32_t* np = b.NBR + p;
@@ -561,6 +576,9 @@ __device__ __forceinline__ int2 solveB_dp(const Bufs& b, const int4* __restrict_
     if (k + L < cnt) {
       en = np[(size_t)(k + L) * stride];
       on = src[en & ~NBR_BOUNDARY];
+    }
+    if constexpr (RIG) {
+      if (!(e & NBR_BOUNDARY) && same_body(infoI, (uint32_t)o.w)) continue;
     }
     int2 d = pdelta(pi, xy(o), f);
     int id = lut_index(d, f);
@@ -620,9 +638,17 @@ __global__ void __launch_bounds__(256, 8) k_colour(Bufs b, int colour, const int
     const uint32_t info = (uint32_t)me.w;
     const bool act = mine && !(info & INFO_BOUNDARY);  // walls are identical in both buffers
     const uint32_t cnt = act ? (b.NBRN[p] & NBRN_COUNT) : 0u;
-    int2 dp = solveB_dp<DBG, L>(b, src, act ? p : 0u, cnt, sub, xy(me), me.z, f);
+    const bool rigidI = act && (info & INFO_RIGID);
+    int2 dp;
+    if (__any_sync(0xffffffffu, rigidI))
+      dp = solveB_dp<DBG, L, true>(b, src, act ? p : 0u, cnt, sub, xy(me), me.z, f, rigidI ? info : 0u);
+    else
+      dp = solveB_dp<DBG, L>(b, src, act ? p : 0u, cnt, sub, xy(me), me.z, f);
     if (sub != 0 || !act) continue;
     int2 pr = xy(me);
+    // a rigid member's dp is not applied: rigidSolve folds it into its body
+    // at the end of the iteration (src/sim.wgsl:1418-1429)
+    if (rigidI) b.DP[p] = dp;
     if (!(info & INFO_PINNED)) {
       const ScenePar& S = b.scenes[b.SCN[p]];
       pr = apply_dp(b, S, info & INFO_MAT, pr, dp, f);
@@ -655,7 +681,9 @@ __global__ void __launch_bounds__(256) k_friction(Bufs b) {
     if (info & INFO_BOUNDARY) continue;
     uint32_t m = info & INFO_MAT;
     if (!friction_row(b, m)) continue;
-    if (info & INFO_RIGID) continue;
+    // a rigid member skips its own body, gathers no bonds and ADDS its friction
+    // to the solver dp waiting for rigidSolve (src/sim.wgsl:1680-1688, 1925-1929)
+    const bool rigidI = (info & INFO_RIGID) != 0u;
     int32_t fi = matw(b, m, M_fric);
     int32_t bondKi = matw(b, m, M_bondK);
     int2 pi = xy(me);
@@ -667,6 +695,7 @@ __global__ void __launch_bounds__(256) k_friction(Bufs b) {
         uint32_t e = b.NBR[(size_t)k * stride + p];
         uint32_t q = e & ~NBR_BOUNDARY;
         int4 o = b.PL[q];
+        if (rigidI && !(e & NBR_BOUNDARY) && same_body(info, (uint32_t)o.w)) continue;
         int2 pq = xy(o);
         int2 d = pdelta(pi, pq, f);
         int id = lut_index(d, f);
@@ -693,6 +722,11 @@ __global__ void __launch_bounds__(256) k_friction(Bufs b) {
         fx = wsub(fx, clampi(sx, -FR_TERM, FR_TERM));
         fy = wsub(fy, clampi(sy, -FR_TERM, FR_TERM));
       }
+    }
+    if (rigidI) {
+      const int2 d0 = b.DP[p];
+      b.DP[p] = make_int2(add_sat(d0.x, fx, f), add_sat(d0.y, fy, f));
+      continue;
     }
     int32_t bx = 0, by = 0;
     if (bondKi != 0 && !(info & INFO_BURST)) {
@@ -1087,7 +1121,6 @@ __device__ __forceinline__ void thermal(const Bufs& b, uint32_t i, int32_t heat,
   if (burning) fl |= FLAG_BURNING;
   if (matw(b, mat, M_phantom) != 0) fl |= FLAG_DEAD;
   if (seal_class(b, mat)) fl |= FLAG_SEAL;
-  if (matw(b, mat, M_solidMode) == SOLID_RIGID) atomicOr(b.err, ERR_UNSUPPORTED_ROW);  // rigid bodies are not built
   w[4] = (int32_t)mat;
   w[5] = (int32_t)fl;
   w[6] = T;
@@ -1133,6 +1166,8 @@ __global__ void __launch_bounds__(256, 6) k_post2(Bufs b, int formFlags) {
         on = b.PL[en & ~NBR_BOUNDARY];
       }
       const uint32_t q = e & ~NBR_BOUNDARY;
+      // a rigid member's cohesion skips its own body (src/sim.wgsl:2450-2457)
+      if ((info & INFO_RIGID) && !(e & NBR_BOUNDARY) && same_body(info, (uint32_t)o.w)) continue;
       const int2 d = pdelta(pi, xy(o), f);
       const int id = lut_index(d, f);
       if (id < 0) continue;

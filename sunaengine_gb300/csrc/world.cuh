@@ -44,6 +44,7 @@ struct ScenePar {
   uint32_t fuseTag;    // §18.24 armed draw-time fusion tag (0: none)
   uint32_t nJets;      // §23.B jets (setJets): 0..8
   int32_t jet[8][5];   // [x, y, r, fx, fy] ticks
+  int32_t userA[2];    // §24 setUserDrive: the drive of user-flagged rigid bodies
 };
 
 // World-level totals, written by the host when the scene set changes.
@@ -55,6 +56,7 @@ struct WorldPar {
   uint32_t nAct;           // active particles (sorted-space length)
   uint32_t hasFriction;    // some material has fric != 0 or bondK != 0
   uint32_t hasBonds;       // some material has bondK != 0
+  uint32_t nBodies;        // §20 body records (all scenes)
 };
 
 }  // namespace sn

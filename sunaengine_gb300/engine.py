@@ -340,14 +340,113 @@ class Engine:
         return int(n.value)
 
     def set_user_drive(self, ax: int, ay: int):
-        """setUserDrive (src/engine.js:4797): stored clamped to +-32768; it
-        drives only user-flagged rigid bodies, which this engine does not build."""
+        """setUserDrive (src/engine.js:4797): stored clamped to +-32768; added
+        to the velocity of free bodies flagged as the user's."""
         out = np.zeros(2, np.int32)
         self._check(self._lib.sn_set_user_drive(self._h, int(ax), int(ay), _ptr(out)), 'setUserDrive')
         return [int(out[0]), int(out[1])]
 
     setJets = set_jets
     setUserDrive = set_user_drive
+
+    # ---- §20 rigid bodies (src/engine.js:5452-5811) ------------------------------
+    @staticmethod
+    def _pivot(pivot):
+        if pivot is None:
+            return None
+        return np.ascontiguousarray([int(pivot[0]), int(pivot[1])], dtype=np.int32)
+
+    def make_rigid_body(self, slots, pivot=None, user: bool = False) -> Optional[int]:
+        """makeRigidBody(slots, pivot, user) (src/engine.js:5722): one body of
+        the listed fluid slots whose row is solidMode rigid (not anchored, not
+        already in a body) under a fresh tag; ``pivot`` = (x, y) ticks makes
+        an axis body. Returns the body index, or None below 4 members."""
+        s = np.ascontiguousarray(np.asarray(slots, dtype=np.int64).reshape(-1).clip(0, 2**32 - 1).astype(np.uint32))
+        pv = self._pivot(pivot)
+        out = ctypes.c_int32()
+        self._check(self._lib.sn_make_rigid_body(self._h, _ptr(s), s.size, _ptr(pv), int(bool(user)),
+                                                 ctypes.byref(out)), 'makeRigidBody')
+        return None if out.value < 0 else int(out.value)
+
+    def make_axis_body(self, slots, px: int, py: int, user: bool = False) -> Optional[int]:
+        return self.make_rigid_body(slots, (px, py), user)
+
+    def promote_weld_group(self, tag: int = 0, pivot=None, user: bool = False) -> Optional[int]:
+        """promoteWeldGroup(tag = held, pivot, user) (src/engine.js:5584)."""
+        pv = self._pivot(pivot)
+        out = ctypes.c_int32()
+        self._check(self._lib.sn_promote_weld_group(self._h, int(tag), _ptr(pv), int(bool(user)),
+                                                    ctypes.byref(out)), 'promoteWeldGroup')
+        return None if out.value < 0 else int(out.value)
+
+    def end_weld_group_and_promote(self, pivot=None, user: bool = False) -> Optional[int]:
+        pv = self._pivot(pivot)
+        out = ctypes.c_int32()
+        self._check(self._lib.sn_end_weld_group_and_promote(self._h, _ptr(pv), int(bool(user)), ctypes.byref(out)),
+                    'endWeldGroupAndPromote')
+        return None if out.value < 0 else int(out.value)
+
+    def dissolve_all_bodies(self) -> int:
+        out = ctypes.c_uint32()
+        self._check(self._lib.sn_dissolve_all_bodies(self._h, ctypes.byref(out)), 'dissolveAllBodies')
+        return int(out.value)
+
+    @property
+    def body_count(self) -> int:
+        out = ctypes.c_uint32()
+        self._check(self._lib.sn_read_bodies(self._h, None, 0, ctypes.byref(out)), 'readBodies')
+        return int(out.value)
+
+    def read_bodies(self) -> np.ndarray:
+        """readBodies(): one row of 32 record words per body."""
+        nb = self.body_count
+        a = np.zeros(max(1, nb) * 32, np.int32)
+        out = ctypes.c_uint32()
+        self._check(self._lib.sn_read_bodies(self._h, _ptr(a), a.size, ctypes.byref(out)), 'readBodies')
+        return a[:int(out.value) * 32].reshape(-1, 32)
+
+    def read_rest_offsets(self) -> np.ndarray:
+        a = np.zeros(max(1, self.n) * 2, np.int32)
+        self._check(self._lib.sn_read_rest_offsets(self._h, _ptr(a), a.size), 'readRestOffsets')
+        return a[:self.n * 2]
+
+    def set_body_user(self, index: int, on: bool) -> bool:
+        out = ctypes.c_uint32()
+        self._check(self._lib.sn_set_body_user(self._h, int(index), int(bool(on)), ctypes.byref(out)), 'setBodyUser')
+        return bool(out.value)
+
+    def set_body_driver(self, index: int, mask: int, values):
+        """The driver sidecar of one body: RD_HAS_* mask and the nine values
+        {px, py, angle, vx, vy, omega, fx, fy, torque}, held until changed."""
+        v = np.zeros(9, np.int32)
+        v[:len(values)] = np.asarray(values, dtype=np.int64).clip(-2**31, 2**31 - 1)
+        self._check(self._lib.sn_set_body_driver(self._h, int(index), int(mask), _ptr(v)), 'setBodyConstraint')
+
+    def clear_body_drivers(self):
+        self._check(self._lib.sn_clear_body_drivers(self._h), 'clearBodyConstraints')
+
+    def drag_body(self, tag: int, x: int, y: int, vx: int = 0, vy: int = 0) -> bool:
+        """dragGrab's rigid branch (src/engine.js:6111): the free body wearing
+        ``tag`` is put one velocity behind (x, y)."""
+        out = ctypes.c_uint32()
+        self._check(self._lib.sn_drag_body(self._h, int(tag), int(x), int(y), int(vx), int(vy), ctypes.byref(out)),
+                    'dragGrab')
+        return bool(out.value)
+
+    def restore_bodies(self, records, rest=None):
+        r = np.ascontiguousarray(np.asarray(records, dtype=np.int32).reshape(-1))
+        rr = None if rest is None else np.ascontiguousarray(np.asarray(rest, dtype=np.int32).reshape(-1))
+        self._check(self._lib.sn_restore_bodies(self._h, _ptr(r) if r.size else None, r.size // 32, _ptr(rr),
+                                                0 if rr is None else rr.size), 'restoreAuthoringSnapshot')
+
+    makeRigidBody = make_rigid_body
+    makeAxisBody = make_axis_body
+    promoteWeldGroup = promote_weld_group
+    endWeldGroupAndPromote = end_weld_group_and_promote
+    dissolveAllBodies = dissolve_all_bodies
+    readBodies = read_bodies
+    readRestOffsets = read_rest_offsets
+    setBodyUser = set_body_user
 
     def autotune(self, reps: int = 1) -> int:
         """Pick the gather lanes per kernel class on real substeps (the scene

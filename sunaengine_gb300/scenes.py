@@ -180,6 +180,83 @@ def sealed_box(spacing: float = 0.6, held: bool = True, seal: str = 'RUBBER', se
     return sc
 
 
+def rigid_tank(plank: str = 'METAL', wheel: str = 'WOOD', rail: bool = True, seed: int = 0x71a9,
+               plank_temp: Optional[int] = None, water: bool = True) -> Scene:
+    """Rigid-body scenes (build-defined; the reference ships no frozen one).
+
+    A 64 x 44 wu walled tank with a jittered WATER pool (y 30.5..41.5 wu), an
+    L-shaped plank of ``plank`` (a 16 x 3 bar with a 3 x 5 leg, 1 wu lattice)
+    above it, a disc of radius 5 wu of ``wheel`` at (46, 20) and, with
+    ``rail``, a held STONE rail (FLAG_ANCHOR; STONE is seal class, so it also
+    wears FLAG_SEAL) under the plank. ``meta`` names the slot lists; a body is
+    made from them with ``makeRigidBody`` / ``makeAxisBody`` after the load.
+    """
+    rng = Xorshift32(seed)
+    dom_w, dom_h = 64, 44
+    half = ONE >> 1
+    pos, mat, temp = [], [], []
+    meta = {}
+    if plank:
+        pm = mat_id(plank)
+        sl = []
+        for r in range(3):
+            for c in range(16):
+                sl.append(len(pos))
+                pos.append((8 * ONE + half + c * ONE, 14 * ONE + half + r * ONE))
+                mat.append(pm)
+        for r in range(3, 8):
+            for c in range(3):
+                sl.append(len(pos))
+                pos.append((21 * ONE + half + c * ONE, 14 * ONE + half + r * ONE))
+                mat.append(pm)
+        meta['plank'] = sl
+    if wheel:
+        wm = mat_id(wheel)
+        sl = []
+        for r in range(-5, 6):
+            for c in range(-5, 6):
+                if r * r + c * c <= 25:
+                    sl.append(len(pos))
+                    pos.append((46 * ONE + c * ONE, 20 * ONE + r * ONE))
+                    mat.append(wm)
+        meta['wheel'] = sl
+        meta['wheel_centre'] = (46 * ONE, 20 * ONE)
+    if rail:
+        sl = []
+        for c in range(7):
+            sl.append(len(pos))
+            pos.append((9 * ONE + half + c * ONE, 24 * ONE + half))
+            mat.append(mat_id('STONE'))
+        meta['rail'] = sl
+    if water:
+        jit = ONE // 8
+        y = 30 * ONE + half
+        w = []
+        while y <= 41 * ONE + half:
+            x = 3 * ONE + half
+            while x <= 60 * ONE + half:
+                jx = (rng() % (2 * jit + 1)) - jit
+                jy = (rng() % (2 * jit + 1)) - jit
+                w.append(len(pos))
+                pos.append((x + jx, y + jy))
+                mat.append(MAT_WATER)
+                x += ONE
+            y += ONE
+        meta['water'] = w
+    sc = _assemble(pos, np.array(mat, np.uint32), boundary_ring(dom_w, dom_h, dom_h - 4), dom_w, dom_h,
+                   f'rigid_tank_{plank.lower() if plank else "none"}')
+    fl = np.zeros(sc.n, np.uint32)
+    for i in meta.get('rail', []):
+        fl[i] = FLAG_ANCHOR
+    sc.flags = fl
+    if plank_temp is not None and plank:
+        t = np.full(sc.n, AMBIENT, np.int32)
+        t[meta['plank']] = plank_temp
+        sc.temp = t
+    sc.meta = meta
+    return sc
+
+
 def make_scene(name: str, **opts) -> Scene:
     """The reference's canonical scenes (``makeScene``, ``src/engine.js:2469-2648``)."""
     if name == 'dambreak_v1':

@@ -16,6 +16,8 @@ CASES = {
     'burst': dict(sc=dict(spacing=0.5), mats=dict(burstP=30000)),
     'permeable': dict(sc=dict(spacing=0.6), mats=dict(sealMode=1)),
     'photo_seal': dict(sc=dict(spacing=0.6, seal='PHOTO')),
+    'stone_seal': dict(sc=dict(spacing=0.6, seal='STONE')),
+    'bedrock_seal': dict(sc=dict(spacing=0.6, seal='BEDROCK')),
 }
 
 
@@ -43,9 +45,3 @@ def test_containment_lanes_and_release_build(lanes):
     g.step(30)
     r.step(30)
     assert g.chain_hex() == r.chain_hex()
-
-
-def test_rigid_rows_are_refused_on_the_gpu():
-    from sunaengine_gb300.engine import EngineError
-    with pytest.raises(EngineError):
-        Engine(max_particles=4096).load_scene(scenes.sealed_box(seal='STONE'))

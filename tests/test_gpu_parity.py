@@ -260,10 +260,11 @@ def test_refuses_bad_input():
     bad.matId[0] = 99
     with pytest.raises(EngineError):
         e.load_scene(bad)
-    seal = sc.copy()
-    seal.matId[0] = M('STONE')
+    flags = sc.copy()
+    flags.flags = np.zeros(sc.n, np.uint32)
+    flags.flags[0] = 16  # FLAG_RIGID is the engine's to set, never the scene's
     with pytest.raises(EngineError):
-        e.load_scene(seal)
+        e.load_scene(flags)
     big = scenes.make_scene('dambreak_v1')
     with pytest.raises(EngineError):
         e.load_scene(big)  # n > maxParticles

@@ -1,0 +1,183 @@
+"""§20 rigid bodies on the GPU against the oracle, through the C ABI.
+
+Every comparison is bit-exact: the chain after each batch of substeps, the
+state words, the body records, the rest offsets and (debug builds) the
+debug counters."""
+import numpy as np
+import pytest
+
+from sunaengine_gb300 import data, scenes
+from sunaengine_gb300.engine import Engine
+
+import test_oracle_rigid as t
+
+pytestmark = pytest.mark.gpu
+ONE = 65536
+
+
+def both(sc, mats=None, debug=True, lanes=0, extra=256):
+    g = Engine(max_particles=sc.n + extra, debug=debug, mats=mats, lanes=lanes).load_scene(sc)
+    r = t.oracle(sc, mats=mats, threads=16)
+    return g, r
+
+
+def same(g, r, debug=True):
+    assert g.chain_hex() == r.chain_hex()
+    assert np.array_equal(g.read_state(), r.read_state())
+    assert np.array_equal(g.read_bodies(), r.read_bodies())
+    assert np.array_equal(g.read_rest_offsets(), r.read_rest_offsets())
+    if debug:
+        assert np.array_equal(g.debug_counters(), r.debug_counters())
+    g.check_errors()
+
+
+def run(g, r, ks=(1, 2, 5, 12, 30)):
+    for k in ks:
+        g.step(k)
+        r.step(k)
+        assert g.chain_hex() == r.chain_hex(), f'diverged by substep {r.substep_count}'
+
+
+def test_free_and_axis_bodies_in_water():
+    sc = scenes.rigid_tank()
+    g, r = both(sc)
+    cx, cy = sc.meta['wheel_centre']
+    for x in (g, r):
+        assert x.make_rigid_body(sc.meta['plank']) == 0
+        assert x.make_axis_body(sc.meta['wheel'], cx + 2 * ONE, cy) == 1
+    same(g, r)
+    run(g, r, (1, 2, 5, 12, 30, 60, 90))
+    same(g, r)
+    assert g.read_bodies()[0][5] > 20 * ONE
+
+
+@pytest.mark.parametrize('lanes', [1, 2, 4])
+def test_release_build_and_lane_splits(lanes):
+    sc = scenes.rigid_tank(seed=0x5151)
+    g, r = both(sc, debug=False, lanes=lanes)
+    for x in (g, r):
+        x.make_rigid_body(sc.meta['plank'])
+        x.make_rigid_body(sc.meta['wheel'])
+    run(g, r, (3, 17, 40))
+    same(g, r, debug=False)
+
+
+def test_dry_symmetric_body_and_centroid_axle():
+    sc = scenes.rigid_tank(plank='', rail=False, water=False)
+    g, r = both(sc)
+    for x in (g, r):
+        x.make_rigid_body(sc.meta['wheel'])
+    run(g, r, (10, 50, 100))
+    same(g, r)
+    assert g.read_bodies()[0][8] == 0
+    g2, r2 = both(sc)
+    for x in (g2, r2):
+        x.make_axis_body(sc.meta['wheel'], *sc.meta['wheel_centre'])
+    run(g2, r2, (100, 100))
+    same(g2, r2)
+    assert g2.read_bodies()[0][8] == 0
+
+
+def test_user_drive_and_drivers():
+    sc = scenes.rigid_tank(rail=False)
+    g, r = both(sc)
+    cx, cy = sc.meta['wheel_centre']
+    for x in (g, r):
+        x.make_rigid_body(sc.meta['plank'], user=True)
+        x.make_axis_body(sc.meta['wheel'], cx, cy - ONE, user=True)
+        x.set_user_drive(700, -300)
+    run(g, r, (4, 8))
+    same(g, r)
+    R0 = g.read_bodies()[0]
+    for x in (g, r):
+        x.set_body_driver(0, 1 | 4 | 256, [R0[4] + ONE, 0, 5000000, 0, 0, 0, 0, 0, 40000])
+        x.set_body_driver(1, 32 | 64, [0, 0, 0, 0, 0, 3000000, 900, 0, 0])
+    run(g, r, (3, 9))
+    same(g, r)
+    for x in (g, r):
+        x.set_body_user(0, False)
+        x.clear_body_drivers()
+        x.set_user_drive(0, 0)
+    run(g, r, (10,))
+    same(g, r)
+
+
+def _ice_mats():
+    m = data.mats().copy()
+    m[data.mat_id('ICE'), data.MAT_FIELDS.index('meltPt')] = 10 * ONE
+    return m
+
+
+@pytest.mark.parametrize('cold', [32, 3])
+def test_members_leave_and_bodies_dissolve(cold):
+    m = _ice_mats()
+    sc = scenes.rigid_tank(plank='ICE')
+    pl = sc.meta['plank']
+    tt = np.full(sc.n, scenes.AMBIENT, np.int32)
+    tt[pl[:cold]] = -10 * ONE
+    sc.temp = tt
+    g, r = both(sc, mats=m)
+    for x in (g, r):
+        x.make_rigid_body(pl)
+        x.make_rigid_body(sc.meta['wheel'])
+    run(g, r, (1, 1, 8, 30))
+    same(g, r)
+    assert g.read_bodies()[0][0] == (1 if cold >= 4 else 0)
+
+
+def test_erase_repair_and_gesture_promotion():
+    sc = scenes.rigid_tank(rail=False)
+    g, r = both(sc)
+    for x in (g, r):
+        x.make_rigid_body(sc.meta['plank'])
+        x.make_rigid_body(sc.meta['wheel'])
+    run(g, r, (6,))
+    keep = np.ones(sc.nFluid, bool)
+    keep[sc.meta['plank'][5:15]] = False
+    keep[sc.meta['wheel'][:-2]] = False
+    keep[sc.meta['water'][::7]] = False
+    assert g.erase(keep) == r.erase(keep)
+    same(g, r)
+    run(g, r, (1, 9))
+    metal = data.mat_id('WOOD')
+    pts = [{'x': (30 + c) * ONE + ONE // 2, 'y': (8 + rr) * ONE + ONE // 2, 'mat': metal}
+           for rr in range(4) for c in range(6)]
+    for x in (g, r):
+        x.begin_weld_group()
+        x.spawn_fluid(pts, no_weld=False)
+        assert x.end_weld_group_and_promote() == 1
+    same(g, r)
+    run(g, r, (1, 4, 20))
+    same(g, r)
+
+
+def test_restore_and_drag():
+    sc = scenes.rigid_tank()
+    g, r = both(sc)
+    for x in (g, r):
+        x.make_rigid_body(sc.meta['plank'])
+        x.make_axis_body(sc.meta['wheel'], *sc.meta['wheel_centre'])
+    run(g, r, (20,))
+    tag = int(g.read_bodies()[0][1])
+    for x in (g, r):
+        assert x.drag_body(tag, 40 * ONE, 10 * ONE, -2000, 500)
+    run(g, r, (1, 10))
+    same(g, r)
+    # keyframe: state, stAcc, bonds, bodies, rest offsets, formation clock
+    key = (g.read_state(), g.read_scratch(), g.read_bonds(), g.read_bodies(), g.read_rest_offsets())
+    clk = g.info()['formation_clock']
+    g.step(15)
+    r.step(15)
+    ahead = g.read_state().copy(), g.read_bodies().copy()
+    h = Engine(max_particles=sc.n + 256, debug=True).load_scene(sc)
+    h.write_state(key[0], key[1])
+    h.write_bonds(key[2])
+    h.restore_bodies(key[3], key[4])
+    h.set_formation_clock(clk, False)
+    h.step(15)
+    assert np.array_equal(h.read_state(), ahead[0])
+    assert np.array_equal(h.read_bodies(), ahead[1])
+    assert g.dissolve_all_bodies() == r.dissolve_all_bodies()
+    run(g, r, (5,))
+    assert g.body_count == 0 == r.body_count
+    assert np.array_equal(g.read_state(), r.read_state())

@@ -69,7 +69,17 @@ def test_finite_burst_pressure_releases_held_particles():
     assert not (held.read_state().reshape(-1, 8)[:sc.meta['seal'], 5].astype(np.uint32) & 64).any()
 
 
-def test_rigid_rows_stay_refused():
-    sc = scenes.sealed_box(seal='STONE')
-    with pytest.raises(ValueError):
-        oracle(sc)
+def test_loose_rigid_rows_seal_like_any_seal_row():
+    # BEDROCK and STONE are rigid-body rows; outside a body they are ordinary
+    # seal matter: BEDROCK (burstP 0) holds the compressed water, STONE
+    # (burstP 2.5) bursts under it
+    sc = scenes.sealed_box(seal='BEDROCK', spacing=0.6)
+    o = oracle(sc)
+    o.step(60)
+    got, total = inside_box(o.read_state().reshape(-1, 8), sc)
+    assert got == total
+    sc = scenes.sealed_box(seal='STONE', spacing=0.6)
+    o = oracle(sc)
+    o.step(60)
+    fl = o.read_state().reshape(-1, 8)[:sc.meta['seal'], 5].astype(np.uint32)
+    assert (fl & 64).any()

@@ -1,0 +1,246 @@
+"""§20 rigid bodies on the CPU oracle (build-defined scenes: the reference
+ships no frozen rigid-body vectors). Behaviour checks of the restatement and
+the exact invariants the reference states for it: a dry symmetric body and a
+wheel pinned at its own centroid never turn, an axis body's centre never
+moves, a body's members keep their shape, momentum folds carry remainders."""
+import math
+
+import numpy as np
+import pytest
+
+from sunaengine_gb300 import data, scenes
+
+ONE = 65536
+BAM_PER_RAD = 683565276
+
+
+def oracle(sc, mats=None, threads=8):
+    import oracle as o
+    return o.OracleEngine(sc.n + 256, threads=threads, mats=mats).load_scene(sc)
+
+
+def members(e, slots):
+    st = e.read_state().reshape(-1, 8)
+    return st[slots]
+
+
+def test_cos_table_is_robust_to_the_cos_implementation():
+    # Math.round(cos(k*pi/2048) * 2^22): every product sits far from a .5 tie,
+    # so any faithfully rounded cos gives the same table.
+    worst = min(abs(math.cos(k * math.pi / 2048) * 4194304 % 1 - 0.5) for k in range(1, 1024))
+    assert worst > 1e-6
+
+
+def test_free_body_keeps_its_shape_and_lands():
+    sc = scenes.rigid_tank()
+    e = oracle(sc)
+    pl = sc.meta['plank']
+    assert e.make_rigid_body(pl) == 0
+    p0 = members(e, pl)[:, :2].astype(np.float64)
+    d0 = np.hypot(*(p0[:, None, :] - p0[None, :, :]).transpose(2, 0, 1))
+    e.step(200)
+    R = e.read_bodies()[0]
+    assert R[0] == 1 and R[14] == len(pl)            # live, every member kept
+    p1 = members(e, pl)[:, :2].astype(np.float64)
+    d1 = np.hypot(*(p1[:, None, :] - p1[None, :, :]).transpose(2, 0, 1))
+    assert np.abs(d1 - d0).max() < 0.01 * ONE          # rigid up to the Q22 rotation rounding
+    assert R[5] > 20 * ONE                             # fell from y ~ 16 wu onto the rail/pool
+    st = members(e, pl)
+    assert (st[:, 5] & 16).all()                       # FLAG_RIGID
+    over_rail = (st[:, 0] > 9 * ONE) & (st[:, 0] < 16 * ONE)
+    assert (st[over_rail, 1] < 24.5 * ONE).all()       # the held STONE rail was not crossed
+    assert (e.debug_counters()[[0, 1, 2, 5, 9, 10, 11]] == 0).all()
+
+
+def test_dry_symmetric_body_never_turns():
+    sc = scenes.rigid_tank(plank='', rail=False, water=False)
+    e = oracle(sc)
+    assert e.make_rigid_body(sc.meta['wheel']) == 0
+    for _ in range(4):
+        e.step(60)
+        R = e.read_bodies()[0]
+        assert R[8] == 0 and R[9] == 0                 # theta, omega exactly 0
+    assert R[5] > 30 * ONE                             # it fell to the floor
+
+
+def test_axis_body_swings_about_a_fixed_pivot():
+    sc = scenes.rigid_tank(plank='', rail=False)
+    e = oracle(sc)
+    cx, cy = sc.meta['wheel_centre']
+    assert e.make_axis_body(sc.meta['wheel'], cx + 2 * ONE, cy) == 0
+    thetas = []
+    for _ in range(6):
+        e.step(25)
+        R = e.read_bodies()[0]
+        assert (R[4], R[5], R[6], R[7]) == (cx + 2 * ONE, cy, 0, 0)
+        thetas.append(int(R[8]))
+    assert len(set(thetas)) > 3 and min(thetas) < -BAM_PER_RAD // 2   # an unbalanced wheel swings
+
+
+def test_wheel_pinned_at_its_centroid_stays_still():
+    sc = scenes.rigid_tank(plank='', rail=False, water=False)
+    e = oracle(sc)
+    cx, cy = sc.meta['wheel_centre']
+    assert e.make_axis_body(sc.meta['wheel'], cx, cy) == 0
+    e.step(300)
+    R = e.read_bodies()[0]
+    assert R[8] == 0 and R[9] == 0
+
+
+def test_user_drive_moves_only_free_user_bodies():
+    sc = scenes.rigid_tank(plank='METAL', wheel='WOOD', rail=False, water=False)
+    e = oracle(sc)
+    cx, cy = sc.meta['wheel_centre']
+    b0 = e.make_rigid_body(sc.meta['plank'], user=True)
+    b1 = e.make_axis_body(sc.meta['wheel'], cx, cy, user=True)
+    x0 = int(e.read_bodies()[b0][4])
+    e.set_user_drive(-900, 0)
+    e.step(10)
+    R = e.read_bodies()
+    assert R[b0][6] == -9000 and R[b0][4] == x0 - 900 * 55  # an acceleration of the whole body, in the air
+    assert R[b1][8] == 0 and R[b1][9] == 0            # the axle absorbs the drive
+    # the same body without the flag does not feel it
+    f = oracle(sc)
+    f.make_rigid_body(sc.meta['plank'], user=False)
+    f.set_user_drive(-900, 0)
+    f.step(10)
+    assert f.read_bodies()[0][6] == 0
+
+
+def test_drivers_hold_position_and_angle():
+    sc = scenes.rigid_tank(rail=False)
+    e = oracle(sc)
+    b = e.make_rigid_body(sc.meta['plank'])
+    R0 = e.read_bodies()[0]
+    e.set_body_driver(b, 1 | 2 | 4, [R0[4], R0[5], 123456789, 0, 0, 0, 0, 0, 0])
+    e.step(30)
+    R = e.read_bodies()[0]
+    assert (R[4], R[5], R[8]) == (R0[4], R0[5], 123456789)
+    e.clear_body_drivers()
+    e.step(30)
+    assert e.read_bodies()[0][5] > R0[5]
+
+
+def test_members_leave_when_their_row_changes():
+    # ICE that melts at 10 degrees; half the plank starts at -10 and half at
+    # 20: the warm half turns to water on the first substep and leaves.
+    m = data.mats().copy()
+    ice = data.mat_id('ICE')
+    m[ice, data.MAT_FIELDS.index('meltPt')] = 10 * ONE
+    sc = scenes.rigid_tank(plank='ICE', rail=False, water=False)
+    pl = sc.meta['plank']
+    t = np.full(sc.n, scenes.AMBIENT, np.int32)
+    cold = pl[:32]
+    t[cold] = -10 * ONE
+    sc.temp = t
+    e = oracle(sc, mats=m)
+    assert e.make_rigid_body(pl) == 0
+    rest0 = e.read_rest_offsets().reshape(-1, 2)[cold].copy()
+    e.step(1)
+    R = e.read_bodies()[0]
+    st = e.read_state().reshape(-1, 8)
+    assert R[0] == 1 and R[14] == len(cold)
+    assert not (st[pl[32:], 5] & 16).any() and (st[cold, 5] & 16).all()
+    rest1 = e.read_rest_offsets().reshape(-1, 2)[cold]
+    d = rest0 - rest1                                  # the re-base moved every offset by one vector
+    assert (d == d[0]).all() and (d[0] != 0).any()
+    e.step(20)
+    assert e.read_bodies()[0][0] == 1
+
+
+def test_body_dissolves_below_four_members():
+    m = data.mats().copy()
+    ice = data.mat_id('ICE')
+    m[ice, data.MAT_FIELDS.index('meltPt')] = 10 * ONE
+    sc = scenes.rigid_tank(plank='ICE', rail=False, water=False)
+    pl = sc.meta['plank']
+    t = np.full(sc.n, scenes.AMBIENT, np.int32)
+    t[pl[:3]] = -10 * ONE
+    sc.temp = t
+    e = oracle(sc, mats=m)
+    e.make_rigid_body(pl)
+    e.step(1)
+    R = e.read_bodies()[0]
+    assert R[0] == 0 and R[14] == 0
+    assert not (e.read_state().reshape(-1, 8)[pl, 5] & 16).any()
+
+
+def test_make_rigid_body_refusals_and_fresh_tags():
+    sc = scenes.rigid_tank()
+    e = oracle(sc)
+    assert e.make_rigid_body(sc.meta['plank'][:3]) is None          # below RIGID_MIN_MEMBERS
+    assert e.make_rigid_body(sc.meta['water'][:20]) is None         # not a rigid row
+    assert e.make_rigid_body(sc.meta['rail']) is None               # anchored matter is never promoted
+    a = e.make_rigid_body(sc.meta['plank'])
+    b = e.make_rigid_body(sc.meta['wheel'])
+    assert (a, b) == (0, 1)
+    assert e.make_rigid_body(sc.meta['plank']) is None              # already in a body
+    R = e.read_bodies()
+    assert R[0][1] != R[1][1] and R[0][1] & 0xfff00 and R[1][1] & 0xfff00
+    st = e.read_state().reshape(-1, 8)
+    assert ((st[sc.meta['plank'], 5] & 0xfff00) == R[0][1]).all()
+
+
+def test_promote_a_drawn_gesture():
+    sc = scenes.rigid_tank(plank='', wheel='', rail=False)
+    e = oracle(sc)
+    tag = e.begin_weld_group()
+    metal = data.mat_id('METAL')
+    pts = [{'x': (20 + c) * ONE + ONE // 2, 'y': (10 + r) * ONE + ONE // 2, 'mat': metal}
+           for r in range(3) for c in range(8)]
+    e.spawn(pts, no_weld=False)
+    idx = e.end_weld_group_and_promote()
+    assert idx == 0
+    R = e.read_bodies()[0]
+    assert R[1] == tag and R[14] == 24
+    e.step(50)
+    assert e.read_bodies()[0][5] > R[5]
+
+
+def test_erase_repairs_bodies():
+    sc = scenes.rigid_tank(rail=False)
+    e = oracle(sc)
+    e.make_rigid_body(sc.meta['plank'])
+    e.make_rigid_body(sc.meta['wheel'])
+    e.step(10)
+    keep = np.ones(sc.nFluid, bool)
+    keep[sc.meta['plank'][:10]] = False                # cut a piece off the plank
+    keep[sc.meta['wheel'][:-3]] = False                # leave 3 of the wheel: it dissolves
+    assert e.erase(keep) == 10 + len(sc.meta['wheel']) - 3
+    R = e.read_bodies()
+    assert len(R) == 1 and R[0][14] == len(sc.meta['plank']) - 10
+    st = e.read_state().reshape(-1, 8)
+    assert ((st[:, 5] & 16) != 0).sum() == len(sc.meta["plank"]) - 10
+    e.step(20)
+    assert e.read_bodies()[0][0] == 1
+
+
+def test_restore_rejoins():
+    sc = scenes.rigid_tank()
+    e = oracle(sc)
+    e.make_rigid_body(sc.meta['plank'])
+    e.make_axis_body(sc.meta['wheel'], *sc.meta['wheel_centre'])
+    e.step(30)
+    key = (e.read_state(), e.read_derived(), e.read_bonds(), e.read_bodies(), e.read_rest_offsets(),
+           e.formation_clock)
+    e.step(20)
+    ahead = (e.read_state().copy(), e.read_bodies().copy())
+    f = oracle(sc)
+    f.write_state(key[0], key[1])
+    f.write_bonds(key[2])
+    f.restore_bodies(key[3], key[4])
+    f.set_formation_clock(key[5], False)
+    f.step(20)
+    assert np.array_equal(f.read_state(), ahead[0])
+    assert np.array_equal(f.read_bodies(), ahead[1])
+
+
+def test_drag_moves_a_free_body():
+    sc = scenes.rigid_tank(rail=False)
+    e = oracle(sc)
+    e.make_rigid_body(sc.meta['plank'])
+    tag = int(e.read_bodies()[0][1])
+    assert e.drag_body(tag, 30 * ONE, 12 * ONE, 1000, 0)
+    R = e.read_bodies()[0]
+    assert (R[4], R[5], R[6], R[7]) == (30 * ONE - 1000, 12 * ONE, 1000, 0)
+    assert not e.drag_body(0x55500, 0, 0)
