@@ -42,7 +42,9 @@ def build(force: bool = False, verbose: bool = False) -> Path:
             return LIB
         BUILD.mkdir(exist_ok=True)
         tag = os.getpid()
-        flags = [*ARCH, '-lineinfo', '-O3', '-std=c++17', '-Xcompiler', '-fPIC', '-diag-suppress', '550']
+        # host floating point (the rigid-body record math restates JS doubles) without FMA contraction
+        flags = [*ARCH, '-lineinfo', '-O3', '-std=c++17', '-Xcompiler', '-fPIC', '-Xcompiler', '-ffp-contract=off',
+                 '-diag-suppress', '550']
         if verbose:
             flags.append('-Xptxas=-v')
         units = sorted(CSRC.glob('*.cu'))
