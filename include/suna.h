@@ -271,6 +271,13 @@ int sn_set_body_driver(sn_engine* e, uint32_t index, int32_t mask, const int32_t
 int sn_clear_body_drivers(sn_engine* e);
 int sn_drag_body(sn_engine* e, uint32_t tag, int32_t x, int32_t y, int32_t vx, int32_t vy, uint32_t* moved);
 int sn_restore_bodies(sn_engine* e, const int32_t* records, uint32_t count, const int32_t* rest, size_t rest_words);
+/* _writeBodyRecord (src/engine.js:5452) for host-side rebuilds that choose
+ * their members themselves (splitDisconnectedBodies :6313,
+ * promoteLooseRigidComponents :5636): members are taken as given, tag 0 draws
+ * a fresh tag; FLAG_RIGID and the tag are set on them. *index = -1 below 4
+ * members or at 1024 bodies; *tag_out receives the tag used. */
+int sn_write_body(sn_engine* e, const uint32_t* members, uint32_t k, uint32_t tag, const int32_t* pivot, uint32_t user,
+                  int32_t* index, uint32_t* tag_out);
 
 /* ---- lane autotuner ----------------------------------------------------------
  * No counterpart in the reference. The neighbour gathers of solveA, the colour

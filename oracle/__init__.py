@@ -111,6 +111,9 @@ def lib():
         l.sno_drag_body.restype = ctypes.c_int
         l.sno_drag_body.argtypes = [P, ctypes.c_uint32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                     ctypes.c_int32]
+        l.sno_write_body.restype = ctypes.c_int32
+        l.sno_write_body.argtypes = [P, u32p, ctypes.c_uint32, ctypes.c_uint32, P, ctypes.c_int,
+                                     ctypes.POINTER(ctypes.c_uint32)]
         l.sno_restore_bodies.restype = ctypes.c_int
         l.sno_restore_bodies.argtypes = [P, i32p, ctypes.c_uint32, P, ctypes.c_size_t]
         l.sno_impulse.restype = ctypes.c_int64
@@ -341,6 +344,16 @@ class OracleEngine:
         if r == -2:
             raise ValueError('[aether] §20: no free weld tag for a new body')
         return None if r < 0 else int(r)
+
+    def write_body(self, members, tag: int = 0, pivot=None, user: bool = False):
+        s = np.ascontiguousarray(np.asarray(members, dtype=np.int64).reshape(-1).astype(np.uint32))
+        keep, pp = self._pivot(pivot)
+        t = ctypes.c_uint32()
+        r = lib().sno_write_body(self.h, s if s.size else np.zeros(1, np.uint32), s.size, int(tag), pp,
+                                 int(bool(user)), ctypes.byref(t))
+        if r == -3:
+            raise ValueError('body member outside the fluid slots')
+        return (None if r < 0 else int(r)), int(t.value)
 
     def make_axis_body(self, slots, px: int, py: int, user: bool = False):
         return self.make_rigid_body(slots, (px, py), user)

@@ -2100,6 +2100,25 @@ int32_t sno_promote_weld_group(SnoEngine* e, uint32_t tag, const int32_t* pivot,
   e->bondDirty = true;
   return idx;
 }
+// _writeBodyRecord as the host-side rebuilds call it (members as given, tag 0
+// draws _nextWeldSeq, FLAG_RIGID and the tag set). *tagOut = the tag.
+int32_t sno_write_body(SnoEngine* e, const uint32_t* slots, uint32_t k, uint32_t tag, const int32_t* pivot, int user,
+                       uint32_t* tagOut) {
+  std::vector<uint32_t> members(slots, slots + k);
+  std::sort(members.begin(), members.end());
+  members.erase(std::unique(members.begin(), members.end()), members.end());
+  if (!members.empty() && members.back() >= e->nFluid) return -3;
+  const uint32_t t = tag != 0 ? (tag & WELD_TAG_MASK) : ((next_weld_seq(*e) << 8) & WELD_TAG_MASK);
+  if (tagOut) *tagOut = t;
+  if (members.empty()) return -1;
+  std::vector<Particle>& st = e->st[e->parity];
+  for (uint32_t i : members) {
+    st[i].flags = (st[i].flags & ~WELD_TAG_MASK) | t | FLAG_RIGID;
+    e->st[1 - e->parity][i].flags = st[i].flags;
+  }
+  e->bondDirty = true;
+  return write_body_record(*e, members, st, t, pivot, user != 0);
+}
 int32_t sno_end_weld_group_and_promote(SnoEngine* e, const int32_t* pivot, int user) {
   const uint32_t was = sno_end_weld_group(e);
   if (was == 0) return -1;

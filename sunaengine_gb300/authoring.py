@@ -10,6 +10,8 @@ doubles in the same operation order as the reference's JavaScript numbers.
 """
 from __future__ import annotations
 
+import math
+
 import numpy as np
 
 from . import data
@@ -166,3 +168,210 @@ def erase_where(eng, keep) -> int:
     st = eng.read_state().reshape(-1, 8)
     mask = np.array([bool(keep(_fields(st, i))) for i in range(nf)], bool)
     return eng.erase(mask)
+
+
+# ---- §20 host-side body rebuilds ---------------------------------------------------
+ONE = 65536
+FLAG_ANCHOR = 4
+RIGID_MIN_MEMBERS = 4
+RG_MAX_BODIES = 1024
+RB_TAG, RB_FIRST, RB_LAST, RB_CX, RB_CY, RB_AXIS, RB_USER = 1, 2, 3, 4, 5, 27, 28
+
+
+def _js_round(x: float) -> int:
+    """Math.round: ties towards +infinity."""
+    r = math.floor(x)
+    return int(r + 1 if x - r >= 0.5 else r)
+
+
+def _i32(v) -> int:
+    """JS `x | 0` on an integral number."""
+    v = int(v) & 0xffffffff
+    return v - (1 << 32) if v & 0x80000000 else v
+
+
+def _components(st, members, link_ticks, severed):
+    """The connected pieces of `members` (src/engine.js:6353-6383): a 3x3 scan
+    of link-sized cells, pairs within the link radius and not severed."""
+    if len(members) < 2:
+        return [list(members)]
+    cell = max(1, link_ticks)
+    lim2 = float(link_ticks) * float(link_ticks)
+    grid = {}
+    for i in members:
+        k = (math.floor(float(st[i, 0]) / cell), math.floor(float(st[i, 1]) / cell))
+        grid.setdefault(k, []).append(i)
+    seen, out = set(), []
+    for seed in members:
+        if seed in seen:
+            continue
+        comp, q = [], [seed]
+        seen.add(seed)
+        while q:
+            i = q.pop()
+            comp.append(i)
+            xi, yi = float(st[i, 0]), float(st[i, 1])
+            cx, cy = math.floor(xi / cell), math.floor(yi / cell)
+            for dy in (-1, 0, 1):
+                for dx in (-1, 0, 1):
+                    for j in grid.get((cx + dx, cy + dy), ()):
+                        if j in seen:
+                            continue
+                        ex, ey = float(st[j, 0]) - xi, float(st[j, 1]) - yi
+                        if ex * ex + ey * ey > lim2 or severed(xi, yi, float(st[j, 0]), float(st[j, 1])):
+                            continue
+                        seen.add(j)
+                        q.append(j)
+        comp.sort()
+        out.append(comp)
+    out.sort(key=lambda c: (-len(c), c[0]))
+    return out
+
+
+def split_disconnected_bodies(eng, link_ticks: int = None, cuts=(), kerf: int = None) -> dict:
+    """splitDisconnectedBodies (src/engine.js:6312-6440): after a cut, every
+    body whose members fall into several connected pieces (1.65 wu links, no
+    link across a cut line or within the kerf of one) is rebuilt as one body
+    per piece of at least 4 members; only the largest piece keeps the axle
+    and the user flag. Returns {'split': pieces added, 'bodies': bodies now}."""
+    link_ticks = _js_round(1.65 * ONE) if link_ticks is None else int(link_ticks)
+    kerf = _js_round(ONE * 0.52) if kerf is None else int(kerf)
+    nb = eng.body_count
+    nf = eng.n_fluid
+    if nb == 0 or nf == 0:
+        return {'split': 0, 'bodies': nb}
+    st = eng.read_state().reshape(-1, 8).copy()
+    recs = eng.read_bodies()
+    segs = [(float(_i32(s['x0'])), float(_i32(s['y0'])), float(_i32(s['x1'])), float(_i32(s['y1']))) for s in cuts]
+    kerf2 = float(max(0, _i32(kerf))) ** 2
+
+    def point_seg_d2(px, py, ax, ay, bx, by):
+        ex, ey = bx - ax, by - ay
+        den = ex * ex + ey * ey
+        t = max(0.0, min(1.0, ((px - ax) * ex + (py - ay) * ey) / den)) if den > 0 else 0.0
+        dx, dy = px - (ax + ex * t), py - (ay + ey * t)
+        return dx * dx + dy * dy
+
+    def orient(ax, ay, bx, by, cx, cy):
+        return (bx - ax) * (cy - ay) - (by - ay) * (cx - ax)
+
+    def crosses(ax, ay, bx, by, cx, cy, dx, dy):
+        if (max(ax, bx) < min(cx, dx) or max(cx, dx) < min(ax, bx) or
+                max(ay, by) < min(cy, dy) or max(cy, dy) < min(ay, by)):
+            return False
+        a, b = orient(ax, ay, bx, by, cx, cy), orient(ax, ay, bx, by, dx, dy)
+        c, d = orient(cx, cy, dx, dy, ax, ay), orient(cx, cy, dx, dy, bx, by)
+        return ((a == 0 or b == 0 or (a < 0) != (b < 0)) and (c == 0 or d == 0 or (c < 0) != (d < 0)))
+
+    def severed(ax, ay, bx, by):
+        for x0, y0, x1, y1 in segs:
+            if (crosses(ax, ay, bx, by, x0, y0, x1, y1) or point_seg_d2(ax, ay, x0, y0, x1, y1) <= kerf2 or
+                    point_seg_d2(bx, by, x0, y0, x1, y1) <= kerf2 or point_seg_d2(x0, y0, ax, ay, bx, by) <= kerf2 or
+                    point_seg_d2(x1, y1, ax, ay, bx, by) <= kerf2):
+                return True
+        return False
+
+    fl = st[:, 5].astype(np.int64) & 0xffffffff
+    specs, split = [], 0
+    for R in recs:
+        tag = int(R[RB_TAG]) & 0xffffffff
+        members = [i for i in range(int(R[RB_FIRST]), min(int(R[RB_LAST]) + 1, nf))
+                   if (fl[i] & FLAG_RIGID) and (fl[i] & WELD_TAG_MASK) == tag]
+        if not members:
+            continue
+        parts = _components(st, members, link_ticks, severed)
+        split += len(parts) - 1
+        axis = bool(R[RB_AXIS])
+        specs.append((parts, axis, bool(R[RB_USER]), (int(R[RB_CX]), int(R[RB_CY])) if axis else None))
+    if not split:
+        return {'split': 0, 'bodies': nb}
+    rigid = (fl[:nf] & FLAG_RIGID) != 0
+    st[:nf, 5] = np.where(rigid, (fl[:nf] & ~(FLAG_RIGID | WELD_TAG_MASK)), fl[:nf]).astype(np.uint32).view(np.int32)
+    eng.write_state_keep_scratch(st.reshape(-1))
+    eng.restore_bodies(np.zeros((0, 32), np.int32))
+    made = 0
+    for parts, axis, user, pivot in specs:
+        for p, members in enumerate(parts):
+            if len(members) < RIGID_MIN_MEMBERS or made >= RG_MAX_BODIES:
+                continue
+            idx, _ = eng.write_body(members, 0, pivot if (p == 0 and axis) else None, p == 0 and user)
+            made += idx is not None
+    _mark_dirty(eng)
+    return {'split': split, 'bodies': eng.body_count}
+
+
+def promote_loose_rigid_components(eng, link_ticks: int = None, eligible=()) -> int:
+    """promoteLooseRigidComponents (src/engine.js:5636-5710): clusters of loose
+    rigid-row matter (not anchored, not in a body) of one material, linked
+    within 1.65 wu, that hold a live bond and one of the caller's freshly
+    congealed witnesses ({'slot', 'mat'}) become bodies. Returns how many."""
+    link_ticks = _js_round(1.65 * ONE) if link_ticks is None else int(link_ticks)
+    nf = eng.n_fluid
+    if nf == 0 or eng.body_count >= RG_MAX_BODIES:
+        return 0
+    wit = {int(w['slot']): int(w['mat']) & 0xffffffff for w in eligible
+           if isinstance(w.get('slot'), int) and isinstance(w.get('mat'), int)}
+    if not wit:
+        return 0
+    st = eng.read_state().reshape(-1, 8)
+    bonds = eng.read_bonds().reshape(-1, BOND_CAP)
+    solid = data.MAT_FIELDS.index('solidMode')
+    cell = max(1, _i32(link_ticks))
+    live = np.zeros(nf, bool)
+    for i in range(nf):
+        for w in bonds[i]:
+            w = int(w) & 0xffffffff
+            if not w:
+                break
+            if not (w & BOND_TOMB):
+                live[i] = True
+                break
+    grid, cand = {}, []
+    fl = st[:, 5].astype(np.int64) & 0xffffffff
+    for i in range(nf):
+        m = int(st[i, 4]) & 0xffffffff
+        if (fl[i] & (FLAG_ANCHOR | FLAG_RIGID)) or _row(eng, m)[solid] != 2:
+            continue
+        k = (math.floor(float(st[i, 0]) / cell), math.floor(float(st[i, 1]) / cell), m)
+        grid.setdefault(k, []).append(i)
+        cand.append(i)
+    if not cand:
+        return 0
+    lim2 = float(cell) * float(cell)
+    seen, groups = set(), []
+    for seed in cand:
+        if seed in seen:
+            continue
+        mat = int(st[seed, 4]) & 0xffffffff
+        part, todo = [], [seed]
+        bonded = congealed = False
+        seen.add(seed)
+        while todo:
+            i = todo.pop()
+            part.append(i)
+            bonded = bonded or bool(live[i])
+            congealed = congealed or wit.get(i) == (int(st[i, 4]) & 0xffffffff)
+            xi, yi = float(st[i, 0]), float(st[i, 1])
+            cx, cy = math.floor(xi / cell), math.floor(yi / cell)
+            for dy in (-1, 0, 1):
+                for dx in (-1, 0, 1):
+                    for j in grid.get((cx + dx, cy + dy, mat), ()):
+                        if j in seen:
+                            continue
+                        ex, ey = float(st[j, 0]) - xi, float(st[j, 1]) - yi
+                        if ex * ex + ey * ey > lim2:
+                            continue
+                        seen.add(j)
+                        todo.append(j)
+        part.sort()
+        if bonded and congealed and len(part) >= RIGID_MIN_MEMBERS:
+            groups.append(part)
+    made = 0
+    for members in groups:
+        if eng.body_count >= RG_MAX_BODIES:
+            break
+        idx, _ = eng.write_body(members, 0)
+        made += idx is not None
+    if made:
+        _mark_dirty(eng)
+    return made

@@ -1476,6 +1476,33 @@ struct World {
     if (*idx < 0) return true;
     return write_scene_state(s, stw, members.front(), members.back()) && mark_bond_dirty(s);
   }
+  // The body-record writer the reference's host-side rebuilds call directly
+  // (splitDisconnectedBodies, promoteLooseRigidComponents: src/engine.js:
+  // 5630-5700, 6313-6430): `members` as given (the caller filtered them), a
+  // fresh tag from _nextWeldSeq when tag == 0, FLAG_RIGID and the tag set on
+  // them, formation on the next substep.
+  bool write_body(uint32_t s, const uint32_t* slots, uint32_t k, uint32_t tag, const int32_t* pivot, bool user,
+                  int32_t* idx, uint32_t* tagOut) {
+    *idx = -1;
+    SceneHost& h = sh[s];
+    if (!h.loaded) return fail("writeBodyRecord before loadScene");
+    if (k > 0 && !slots) return fail("slots is NULL");
+    std::vector<uint32_t> members(slots, slots + k);
+    std::sort(members.begin(), members.end());
+    members.erase(std::unique(members.begin(), members.end()), members.end());
+    if (!members.empty() && members.back() >= h.nFluid) return fail("body member outside the fluid slots");
+    const uint32_t t = tag != 0 ? (tag & WELD_TAG_MASK) : ((next_weld_seq(s) << 8) & WELD_TAG_MASK);
+    if (tagOut) *tagOut = t;
+    if (members.empty()) return true;
+    std::vector<int32_t> stw;
+    if (!read_scene_state(s, stw)) return false;
+    for (uint32_t i : members) {
+      uint32_t& fl = reinterpret_cast<uint32_t&>(stw[(size_t)i * 8 + 5]);
+      fl = (fl & ~WELD_TAG_MASK) | t | FLAG_RIGID;
+    }
+    if (!write_body_record(s, members, stw, t, pivot, user, idx)) return false;
+    return write_scene_state(s, stw, members.front(), members.back()) && mark_bond_dirty(s);
+  }
   // promoteWeldGroup (src/engine.js:5584-5622): the held (or given) tag's
   // rigid-row particles that are neither anchored nor already in a body.
   bool promote_weld_group(uint32_t s, uint32_t tag, const int32_t* pivot, bool user, int32_t* idx) {
@@ -2279,6 +2306,11 @@ int sn_drag_body(sn_engine* e, uint32_t tag, int32_t x, int32_t y, int32_t vx, i
   const bool ok = e->w.drag_body(0, tag, x, y, vx, vy, &m);
   if (moved) *moved = m ? 1u : 0u;
   return rc_of(e->w, ok);
+}
+int sn_write_body(sn_engine* e, const uint32_t* members, uint32_t k, uint32_t tag, const int32_t* pivot, uint32_t user,
+                  int32_t* index, uint32_t* tag_out) {
+  if (!e || !index) return SN_E_INVALID;
+  return rc_of(e->w, e->w.write_body(0, members, k, tag, pivot, user != 0, index, tag_out));
 }
 int sn_restore_bodies(sn_engine* e, const int32_t* records, uint32_t count, const int32_t* rest, size_t rest_words) {
   if (!e) return SN_E_INVALID;

@@ -368,6 +368,16 @@ class Engine:
                                                  ctypes.byref(out)), 'makeRigidBody')
         return None if out.value < 0 else int(out.value)
 
+    def write_body(self, members, tag: int = 0, pivot=None, user: bool = False):
+        """_writeBodyRecord for host-side rebuilds (members as given, tag 0 =
+        a fresh tag); returns (index or None, tag)."""
+        s = np.ascontiguousarray(np.asarray(members, dtype=np.int64).reshape(-1).astype(np.uint32))
+        pv = self._pivot(pivot)
+        out, t = ctypes.c_int32(), ctypes.c_uint32()
+        self._check(self._lib.sn_write_body(self._h, _ptr(s) if s.size else None, s.size, int(tag), _ptr(pv),
+                                            int(bool(user)), ctypes.byref(out), ctypes.byref(t)), 'writeBodyRecord')
+        return (None if out.value < 0 else int(out.value)), int(t.value)
+
     def make_axis_body(self, slots, px: int, py: int, user: bool = False) -> Optional[int]:
         return self.make_rigid_body(slots, (px, py), user)
 

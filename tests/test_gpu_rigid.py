@@ -181,3 +181,29 @@ def test_restore_and_drag():
     run(g, r, (5,))
     assert g.body_count == 0 == r.body_count
     assert np.array_equal(g.read_state(), r.read_state())
+
+
+def test_split_and_loose_promotion_match():
+    from sunaengine_gb300 import authoring
+    sc = scenes.rigid_tank()
+    g, r = both(sc)
+    cx, cy = sc.meta['wheel_centre']
+    for x in (g, r):
+        x.make_rigid_body(sc.meta['plank'], user=True)
+        x.make_axis_body(sc.meta['wheel'], cx + ONE, cy)
+    run(g, r, (2, 7))
+    cut = [{'x0': 16 * ONE, 'y0': 5 * ONE, 'x1': 17 * ONE, 'y1': 40 * ONE},
+           {'x0': 40 * ONE, 'y0': 20 * ONE, 'x1': 52 * ONE, 'y1': 21 * ONE}]
+    assert authoring.split_disconnected_bodies(g, cuts=cut) == authoring.split_disconnected_bodies(r, cuts=cut)
+    same(g, r)
+    run(g, r, (1, 10))
+    same(g, r)
+    s2 = scenes.rigid_tank(wheel='', rail=False, plank='STONE', seed=0x3131)
+    g2, r2 = both(s2)
+    run(g2, r2, (1,))
+    w = [{'slot': s2.meta['plank'][7], 'mat': data.mat_id('STONE')}]
+    assert authoring.promote_loose_rigid_components(g2, eligible=w) == \
+        authoring.promote_loose_rigid_components(r2, eligible=w) == 1
+    same(g2, r2)
+    run(g2, r2, (1, 12))
+    same(g2, r2)

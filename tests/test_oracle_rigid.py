@@ -244,3 +244,42 @@ def test_drag_moves_a_free_body():
     R = e.read_bodies()[0]
     assert (R[4], R[5], R[6], R[7]) == (30 * ONE - 1000, 12 * ONE, 1000, 0)
     assert not e.drag_body(0x55500, 0, 0)
+
+
+def test_split_disconnected_bodies_after_a_cut():
+    from sunaengine_gb300 import authoring
+    sc = scenes.rigid_tank(rail=False)
+    e = oracle(sc)
+    cx, cy = sc.meta['wheel_centre']
+    e.make_rigid_body(sc.meta['plank'], user=True)
+    e.make_axis_body(sc.meta['wheel'], cx, cy)
+    cut = [{'x0': 16 * ONE, 'y0': 5 * ONE, 'x1': 16 * ONE, 'y1': 30 * ONE}]
+    assert authoring.split_disconnected_bodies(e, cuts=[]) == {'split': 0, 'bodies': 2}
+    out = authoring.split_disconnected_bodies(e, cuts=cut)
+    # the columns at 15.5 and 16.5 wu lie inside the kerf: six single chips,
+    # which stay loose, and two pieces of 21 and 36 members
+    assert out == {'split': 7, 'bodies': 3}
+    R = e.read_bodies()
+    assert sorted(R[:, 14].tolist()) == sorted([36, 21, len(sc.meta['wheel'])])
+    st = e.read_state().reshape(-1, 8)
+    assert ((st[sc.meta['plank'], 5] & 16) != 0).sum() == 57
+    assert R[0][28] == 1 and R[1][28] == 0            # the larger piece keeps the user flag
+    assert R[2][27] == 1 and (R[2][4], R[2][5]) == (cx, cy)
+    e.step(30)
+    assert (e.read_bodies()[:, 0] == 1).all()
+
+
+def test_promote_loose_rigid_components():
+    from sunaengine_gb300 import authoring
+    sc = scenes.rigid_tank(wheel='', rail=False, plank='STONE')
+    e = oracle(sc)
+    e.step(1)                                          # the loaded STONE welds (scene weld tag)
+    pl = sc.meta['plank']
+    assert authoring.promote_loose_rigid_components(e, eligible=[]) == 0
+    stone = data.mat_id('STONE')
+    n = authoring.promote_loose_rigid_components(e, eligible=[{'slot': pl[5], 'mat': stone}])
+    assert n == 1
+    R = e.read_bodies()[0]
+    assert R[14] == len(pl)
+    e.step(20)
+    assert e.read_bodies()[0][0] == 1
