@@ -279,6 +279,21 @@ int sn_restore_bodies(sn_engine* e, const int32_t* records, uint32_t count, cons
 int sn_write_body(sn_engine* e, const uint32_t* members, uint32_t k, uint32_t tag, const int32_t* pivot, uint32_t user,
                   int32_t* index, uint32_t* tag_out);
 
+/* ---- material rows at run time ---------------------------------------------------
+ * §25 interned rows (src/engine.js:4981-5245): the host's composition algebra
+ * (synth) and intern cache decide a row's 48 words and its row id; the engine
+ * only holds the table. sn_set_material writes one row past the authored ones
+ * (row == the current count appends; *mat_count receives the new count) with
+ * rampInv baked from rampHi - rampLo and grav scaled by the gravity scale, as
+ * _internUpload does; sn_clear_materials drops every row past the authored
+ * ones (clearInterned). §26.C setGravityScale (src/engine.js:4843): q in Q16,
+ * clamped to [0, 4 x 65536]; every row's grav becomes RNE(grav * q / 65536).
+ * All three hold for every scene loaded afterwards. */
+int sn_set_material(sn_engine* e, uint32_t row, const int32_t words[48], uint32_t* mat_count);
+int sn_clear_materials(sn_engine* e);
+int sn_set_gravity_scale(sn_engine* e, int32_t q, int32_t* out);
+int sn_batch_set_material(sn_batch* b, uint32_t row, const int32_t words[48], uint32_t* mat_count);
+
 /* ---- lane autotuner ----------------------------------------------------------
  * No counterpart in the reference. The neighbour gathers of solveA, the colour
  * passes, post1, post2 and the neighbour-list build can split each particle's list over 1, 2, 4 or 8

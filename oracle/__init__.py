@@ -114,6 +114,13 @@ def lib():
         l.sno_write_body.restype = ctypes.c_int32
         l.sno_write_body.argtypes = [P, u32p, ctypes.c_uint32, ctypes.c_uint32, P, ctypes.c_int,
                                      ctypes.POINTER(ctypes.c_uint32)]
+        l.sno_set_material.restype = ctypes.c_int
+        l.sno_set_material.argtypes = [P, ctypes.c_uint32, i32p]
+        l.sno_clear_materials.argtypes = [P]
+        l.sno_set_gravity_scale.restype = ctypes.c_int32
+        l.sno_set_gravity_scale.argtypes = [P, ctypes.c_int32]
+        l.sno_mat_count.restype = ctypes.c_uint32
+        l.sno_mat_count.argtypes = [P]
         l.sno_restore_bodies.restype = ctypes.c_int
         l.sno_restore_bodies.argtypes = [P, i32p, ctypes.c_uint32, P, ctypes.c_size_t]
         l.sno_impulse.restype = ctypes.c_int64
@@ -344,6 +351,20 @@ class OracleEngine:
         if r == -2:
             raise ValueError('[aether] §20: no free weld tag for a new body')
         return None if r < 0 else int(r)
+
+    # runtime material rows (src/engine.js:4843-4855, 5115-5245)
+    def set_material(self, row: int, words) -> int:
+        w = np.ascontiguousarray(np.asarray(words, dtype=np.int64).reshape(48).astype(np.int32))
+        r = lib().sno_set_material(self.h, int(row), w)
+        if r < 0:
+            raise ValueError(f'set_material refused (code {r})')
+        return int(r)
+
+    def clear_materials(self):
+        lib().sno_clear_materials(self.h)
+
+    def set_gravity_scale(self, q: int) -> int:
+        return int(lib().sno_set_gravity_scale(self.h, int(q)))
 
     def write_body(self, members, tag: int = 0, pivot=None, user: bool = False):
         s = np.ascontiguousarray(np.asarray(members, dtype=np.int64).reshape(-1).astype(np.uint32))

@@ -106,8 +106,10 @@ struct V2 { int32_t x, y; };
 struct SnoEngine {
   uint32_t maxParticles = 0, iters = 4;
   int32_t luts[5 * 3202];
-  int32_t mats[MAT_MAX][MAT_WORDS];
-  uint32_t matCount = 0;
+  int32_t mats[MAT_MAX][MAT_WORDS];      // the table the passes read (grav scaled)
+  int32_t matsAuth[MAT_MAX][MAT_WORDS];  // rows as authored or minted
+  uint32_t matCount = 0, authoredCount = 0;
+  int32_t gravQ = 65536;                 // setGravityScale (src/engine.js:4843), Q16
   int threads = 1;
   // params
   uint32_t n = 0, nFluid = 0, gridW = 1, gridH = 1, cellTotal = 1, cellShift = 18;
@@ -1717,7 +1719,8 @@ SnoEngine* sno_create(uint32_t maxParticles, const int32_t* luts, const int32_t*
   std::memcpy(e->luts, luts, sizeof(e->luts));
   std::memset(e->mats, 0, sizeof(e->mats));
   std::memcpy(e->mats, mats, sizeof(int32_t) * MAT_WORDS * matCount);
-  e->matCount = matCount;
+  std::memcpy(e->matsAuth, e->mats, sizeof(e->mats));
+  e->matCount = e->authoredCount = matCount;
   std::memset(e->dbg, 0, sizeof(e->dbg));
   build_cos_table(e->cosT);
   return e;
@@ -2208,5 +2211,39 @@ int sno_restore_bodies(SnoEngine* e, const int32_t* records, uint32_t nBodies, c
   if (rest) std::copy(rest, rest + restWords, e->rest.begin());
   return 0;
 }
+
+
+// ---- material rows at run time (src/engine.js:4843-4855, 5115-5245) -----------
+// _internUpload: a row past the authored ones (the next free row appends),
+// rampInv baked, grav scaled by the gravity scale. Returns the table size or
+// a negative code (-1 bad row id, -2 a product outside the table).
+int sno_set_material(SnoEngine* e, uint32_t row, const int32_t* w) {
+  if (row < e->authoredCount || row > e->matCount || row >= MAT_MAX) return -1;
+  const uint32_t count = std::max(e->matCount, row + 1);
+  for (int f : {M_meltTo, M_freezeTo, M_boilTo, M_condTo, M_burnTo, M_splitTo, M_corrTo})
+    if (w[f] < 0 || (uint32_t)w[f] >= count) return -2;
+  std::memcpy(e->matsAuth[row], w, sizeof(int32_t) * MAT_WORDS);
+  const int64_t span = (int64_t)w[M_rampHi] - w[M_rampLo];
+  e->matsAuth[row][M_rampInv] = span > 0 ? (int32_t)(4294967296LL / span) : 0;
+  std::memcpy(e->mats[row], e->matsAuth[row], sizeof(int32_t) * MAT_WORDS);
+  e->mats[row][M_grav] = (int32_t)idiv_rne64((int64_t)w[M_grav] * e->gravQ, 65536);
+  e->matCount = count;
+  return (int)count;
+}
+void sno_clear_materials(SnoEngine* e) {
+  for (uint32_t m = e->authoredCount; m < MAT_MAX; ++m) {
+    std::memset(e->mats[m], 0, sizeof(e->mats[m]));
+    std::memset(e->matsAuth[m], 0, sizeof(e->matsAuth[m]));
+  }
+  e->matCount = e->authoredCount;
+}
+int32_t sno_set_gravity_scale(SnoEngine* e, int32_t q) {
+  const int32_t qq = std::max(0, std::min(4 * 65536, q));
+  e->gravQ = qq;
+  for (uint32_t m = 0; m < e->matCount; ++m)
+    e->mats[m][M_grav] = (int32_t)idiv_rne64((int64_t)e->matsAuth[m][M_grav] * qq, 65536);
+  return qq;
+}
+uint32_t sno_mat_count(SnoEngine* e) { return e->matCount; }
 
 }  // extern "C"

@@ -164,8 +164,10 @@ struct World {
   uint32_t capSlots = 0, maxCells = 0, maxScenes = 0;
   int numSMs = 152;
   std::string err;
-  int32_t hmats[MAT_MAX * MAT_WORDS];
-  uint32_t matCount = 0;
+  int32_t hmats[MAT_MAX * MAT_WORDS];  // the device image (grav scaled by gravQ)
+  int32_t hauth[MAT_MAX * MAT_WORDS];  // the rows as authored or minted
+  uint32_t matCount = 0, authoredCount = 0;
+  int32_t gravQ = 65536;               // setGravityScale, Q16
   std::vector<SceneHost> sh;
   std::vector<ScenePar> hpar;
   WorldPar hw{};
@@ -238,7 +240,8 @@ struct World {
     maxScenes = scenesCap;
     std::memset(hmats, 0, sizeof(hmats));
     std::memcpy(hmats, o->mats, sizeof(int32_t) * MAT_WORDS * o->mat_count);
-    matCount = o->mat_count;
+    std::memcpy(hauth, hmats, sizeof(hauth));
+    matCount = authoredCount = o->mat_count;
     for (uint32_t m = 0; m < matCount; ++m) {
       const int32_t* r = hmats + m * MAT_WORDS;
       if (r[M_eps] < 32768) return fail("mats[%u].eps < 32768", m);
@@ -1698,6 +1701,64 @@ struct World {
     return replace_scene_bodies(s, recS, drvS, descS);
   }
 
+  // ---- material rows at run time: §25 interned rows, §26.C gravity scale ------
+  // _internUpload (src/engine.js:5190-5205): one row into the table, rampInv
+  // baked from its ramp, grav scaled by the world gravity. `row` may be the
+  // next free row (the table grows) or an existing row past the authored ones.
+  bool upload_mats(uint32_t lo, uint32_t hi) {
+    if (hi <= lo) return true;
+    graphValid = false;
+    accFresh = false;
+    return cuda_ok(cudaMemcpyAsync(const_cast<int32_t*>(b.mats) + (size_t)lo * MAT_WORDS, hmats + (size_t)lo * MAT_WORDS,
+                                   sizeof(int32_t) * MAT_WORDS * (hi - lo), cudaMemcpyHostToDevice, st),
+                   "mats") &&
+           cuda_ok(cudaStreamSynchronize(st), "mats");
+  }
+  int32_t scaled_grav(int32_t g) const { return (int32_t)idiv_rne64((int64_t)g * gravQ, 65536); }
+  bool set_material(uint32_t rowId, const int32_t* w) {
+    if (!w) return fail("material words are NULL");
+    if (rowId < authoredCount) return fail("row %u is an authored row", rowId);
+    if (rowId > matCount || rowId >= (uint32_t)MAT_MAX) return fail("row %u is not the next free row or a minted one", rowId);
+    const uint32_t count = std::max(matCount, rowId + 1);
+    if (w[M_eps] < 32768) return fail("row %u: eps < 32768", rowId);
+    if (w[M_dpMax] <= 0) return fail("row %u: dpMax <= 0", rowId);
+    if (w[M_burstP] < 0) return fail("row %u: burstP < 0", rowId);
+    if (w[M_sealMode] != 0 && w[M_sealMode] != 1) return fail("row %u: sealMode must be 0 or 1", rowId);
+    if ((int64_t)w[M_rampHi] - w[M_rampLo] < 65536) return fail("row %u: ramp narrower than 1 degree", rowId);
+    for (int f : {M_meltTo, M_freezeTo, M_boilTo, M_condTo, M_burnTo, M_splitTo, M_corrTo})
+      if (w[f] < 0 || (uint32_t)w[f] >= count) return fail("row %u names a product outside the table", rowId);
+    int32_t* a = hauth + (size_t)rowId * MAT_WORDS;
+    std::memcpy(a, w, sizeof(int32_t) * MAT_WORDS);
+    const int64_t span = (int64_t)a[M_rampHi] - a[M_rampLo];
+    a[M_rampInv] = span > 0 ? (int32_t)((int64_t)4294967296LL / span) : 0;
+    int32_t* d = hmats + (size_t)rowId * MAT_WORDS;
+    std::memcpy(d, a, sizeof(int32_t) * MAT_WORDS);
+    d[M_grav] = scaled_grav(a[M_grav]);
+    matCount = count;
+    update_features();
+    return upload_mats(rowId, rowId + 1);
+  }
+  // clearInterned (src/engine.js:5235-5245): drop every row past the authored ones.
+  bool clear_materials() {
+    for (uint32_t m = authoredCount; m < (uint32_t)MAT_MAX; ++m) {
+      std::memset(hauth + (size_t)m * MAT_WORDS, 0, sizeof(int32_t) * MAT_WORDS);
+      std::memset(hmats + (size_t)m * MAT_WORDS, 0, sizeof(int32_t) * MAT_WORDS);
+    }
+    matCount = authoredCount;
+    update_features();
+    return upload_mats(authoredCount, MAT_MAX);
+  }
+  // setGravityScale (src/engine.js:4843-4855): q in Q16, clamped to [0, 4].
+  bool set_gravity_scale(int32_t q, int32_t* out) {
+    const int32_t qq = std::max(0, std::min(4 * 65536, q));
+    if (out) *out = qq;
+    if (qq == gravQ) return true;
+    gravQ = qq;
+    for (uint32_t m = 0; m < matCount; ++m)
+      hmats[(size_t)m * MAT_WORDS + M_grav] = scaled_grav(hauth[(size_t)m * MAT_WORDS + M_grav]);
+    return upload_mats(0, matCount);
+  }
+
   // ---- weld groups (src/engine.js:4570-4680) -----------------------------------
   // _nextWeldSeq: the next 12-bit tag sequence that is neither held open nor
   // worn by one of the scene's bodies.
@@ -2311,6 +2372,26 @@ int sn_write_body(sn_engine* e, const uint32_t* members, uint32_t k, uint32_t ta
                   int32_t* index, uint32_t* tag_out) {
   if (!e || !index) return SN_E_INVALID;
   return rc_of(e->w, e->w.write_body(0, members, k, tag, pivot, user != 0, index, tag_out));
+}
+int sn_set_material(sn_engine* e, uint32_t row, const int32_t words[48], uint32_t* mat_count) {
+  if (!e) return SN_E_INVALID;
+  const bool ok = e->w.set_material(row, words);
+  if (mat_count) *mat_count = e->w.matCount;
+  return rc_of(e->w, ok);
+}
+int sn_clear_materials(sn_engine* e) {
+  if (!e) return SN_E_INVALID;
+  return rc_of(e->w, e->w.clear_materials());
+}
+int sn_set_gravity_scale(sn_engine* e, int32_t q, int32_t* out) {
+  if (!e) return SN_E_INVALID;
+  return rc_of(e->w, e->w.set_gravity_scale(q, out));
+}
+int sn_batch_set_material(sn_batch* b, uint32_t row, const int32_t words[48], uint32_t* mat_count) {
+  if (!b) return SN_E_INVALID;
+  const bool ok = b->w.set_material(row, words);
+  if (mat_count) *mat_count = b->w.matCount;
+  return rc_of(b->w, ok);
 }
 int sn_restore_bodies(sn_engine* e, const int32_t* records, uint32_t count, const int32_t* rest, size_t rest_words) {
   if (!e) return SN_E_INVALID;

@@ -368,6 +368,25 @@ class Engine:
                                                  ctypes.byref(out)), 'makeRigidBody')
         return None if out.value < 0 else int(out.value)
 
+    # ---- runtime material rows (src/engine.js:4843-4855, 5115-5245) -------------
+    def set_material(self, row: int, words) -> int:
+        """_internUpload: write one row past the authored ones (rampInv baked,
+        grav scaled by the gravity scale); returns the table size."""
+        w = np.ascontiguousarray(np.asarray(words, dtype=np.int64).reshape(48).astype(np.int32))
+        out = ctypes.c_uint32()
+        self._check(self._lib.sn_set_material(self._h, int(row), _ptr(w), ctypes.byref(out)), 'internUpload')
+        return int(out.value)
+
+    def clear_materials(self):
+        self._check(self._lib.sn_clear_materials(self._h), 'clearInterned')
+
+    def set_gravity_scale(self, q: int) -> int:
+        out = ctypes.c_int32()
+        self._check(self._lib.sn_set_gravity_scale(self._h, int(q), ctypes.byref(out)), 'setGravityScale')
+        return int(out.value)
+
+    setGravityScale = set_gravity_scale
+
     def write_body(self, members, tag: int = 0, pivot=None, user: bool = False):
         """_writeBodyRecord for host-side rebuilds (members as given, tag 0 =
         a fresh tag); returns (index or None, tag)."""
