@@ -15,7 +15,9 @@ through the public API (scene upload from host memory, a digest read back
 after every substep, final state read back), the per-phase roofline of the
 dominant kernel, the CPU baseline, the batched workload (256 scenes of
 1k-64k particles with stir impulses) against the same scenes stepped one at a
-time on the plain path, and GPU clock samples.
+time on the plain path, the 3D dam break, the serving stream, the
+construction site (rigid bodies and containment at scale, with and without
+its bodies) and GPU clock samples.
 
 --impl reference times the reference's algorithm on the host cores: the
 reference itself is JavaScript + WGSL for WebGPU and cannot run here (no JS
@@ -366,6 +368,57 @@ def batched_workload(steps: int, warmup: int, device: int, plain_sample: int = 2
             'batched_vs_plain': batched / plain}
 
 
+def construction_workload(steps: int, warmup: int, device: int, with_cpu: bool = True, cpu_seconds: float = 4.0):
+    """The widened rows at scale: 24 bays of a METAL plank (free rigid body), a
+    WOOD disc (axis body) and a held STONE rail (containment) over one WATER
+    pool, 74,384 particles, 48 bodies, ITERS 4, chain on. The same scene
+    without bodies (the planks and discs loose) shows what the three rigid
+    passes cost."""
+    from sunaengine_gb300 import scenes
+    from sunaengine_gb300.engine import Engine
+    sc = scenes.construction_site()
+    out = {'workload': 'construction site: 24 bays of a METAL plank (free body, 63 members), a WOOD disc '
+                       '(axis body, 81 members) and a held STONE rail over a 44-row WATER pool; '
+                       f'{sc.n} particles, 48 bodies, ITERS 4, H_set||H_slot every substep',
+           'particles': sc.n, 'steps': steps, 'unit': UNIT}
+    for label, bodies in (('with_bodies', True), ('without_bodies', False)):
+        e = Engine(max_particles=sc.n, device=device).load_scene(sc)
+        if bodies:
+            for pl, wh, pv in zip(sc.meta['planks'], sc.meta['wheels'], sc.meta['wheel_pivots']):
+                e.make_rigid_body(pl)
+                e.make_axis_body(wh, *pv)
+        e.step(warmup)
+        e.sync()
+        e.step(steps)
+        e.sync()
+        ms, launches = e.last_timing()
+        e.check_errors()
+        out[label] = {'value': sc.n * steps / (ms / 1e3), 'ms_per_step': ms / steps,
+                      'gpu_launches_per_step': launches / steps}
+        if bodies:
+            out['bodies_live'] = int((e.read_bodies()[:, 0] == 1).sum())
+            out['chain'] = e.chain_hex()
+        e.destroy()
+    out['rigid_share'] = 1.0 - out['without_bodies']['ms_per_step'] / out['with_bodies']['ms_per_step']
+    if with_cpu:
+        import oracle
+        small = scenes.construction_site(tiles=2)
+        o = oracle.OracleEngine(small.n, threads=os.cpu_count() or 1).load_scene(small)
+        for pl, wh, pv in zip(small.meta['planks'], small.meta['wheels'], small.meta['wheel_pivots']):
+            o.make_rigid_body(pl)
+            o.make_axis_body(wh, *pv)
+        o.step(2)
+        k, t0 = 0, time.perf_counter()
+        while time.perf_counter() - t0 < cpu_seconds:
+            o.step(5)
+            k += 5
+        dt = time.perf_counter() - t0
+        out['cpu_baseline'] = {'value': small.n * k / dt, 'unit': UNIT, 'cores': os.cpu_count() or 1, 'kind': 'port',
+                               'sample': f'the same bays, 2 of 24 ({small.n} particles, 4 bodies), {k} substeps, '
+                                         f'{dt:.1f} s'}
+    return out
+
+
 def sections_only(args):
     """--no-2d: the 3D / batched / serving sections alone (a profiling aid; the
     line carries no headline value)."""
@@ -378,6 +431,8 @@ def sections_only(args):
         line['cfg3_3d'] = workload_3d(args.steps, args.warmup, local, with_cpu=not args.no_cpu)
     if rank == 0 and not args.no_serving:
         line['serving'] = serving_workload(local)
+    if rank == 0 and not args.no_construction:
+        line['construction'] = construction_workload(args.steps, args.warmup, local, with_cpu=not args.no_cpu)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:
@@ -480,6 +535,8 @@ def ours(args):
         line['cfg3_3d'] = workload_3d(args.steps, args.warmup, local, with_cpu=not args.no_cpu)
     if rank == 0 and not args.no_serving:
         line['serving'] = serving_workload(local)
+    if rank == 0 and not args.no_construction:
+        line['construction'] = construction_workload(args.steps, args.warmup, local, with_cpu=not args.no_cpu)
     if rank == 0 and not args.no_cpu:
         line['cpu_baseline'] = run_cpu_baseline(seconds=args.cpu_seconds)
     if rank == 0:
@@ -502,6 +559,7 @@ def main():
     ap.add_argument('--no-autotune', action='store_true',
                     help='keep the rule-based lanes (profiling runs: a tuner under ncu sees serialised timings)')
     ap.add_argument('--no-serving', action='store_true')
+    ap.add_argument('--no-construction', action='store_true')
     ap.add_argument('--cpu-seconds', type=float, default=12.0)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)

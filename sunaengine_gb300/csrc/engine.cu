@@ -727,12 +727,9 @@ struct World {
         ++Lc;
       }
       k_form1<DBG><<<ga, 256, 0, st>>>(b);
-      k_form2<<<gs, 256, 0, st>>>(b);
+      if (chainOn) k_form2<true><<<gs, 256, 0, st>>>(b, b.acc);
+      else k_form2<false><<<gs, 256, 0, st>>>(b, nullptr);
       Lc += 3;
-      if (chainOn) {
-        k_hash<<<gs, 256, 0, st>>>(b, b.acc);
-        ++Lc;
-      }
     } else if (chainOn) {
       SN_LANES(lc.p2, (launch_post2<DBG, true, L_>(1)));
       ++Lc;

@@ -1053,18 +1053,22 @@ __global__ void __launch_bounds__(256) k_contain(Bufs b) {
 // containStress (src/sim.wgsl:2742-2771), after thermal: a held seal particle
 // sums nearby intrusion and, past its row's burstP, lets go (FLAG_BURST). It
 // writes only its own flags word and reads neighbours' positions and rows.
+// Walks slots (one coalesced read of the two words that decide) and visits
+// the neighbour list only for held seal particles.
 template <bool DBG>
 __global__ void __launch_bounds__(256) k_contain_stress(Bufs b) {
   Flags<DBG> f{b.dbg};
-  const uint32_t nAct = b.world->nAct, stride = b.nbrStride;
-  for (uint32_t p = gtid(); p < nAct; p += gstride()) {
-    if ((uint32_t)b.PL[p].w & INFO_BOUNDARY) continue;
-    int32_t* w = b.state + (size_t)b.sslot[p] * 8;
-    const uint32_t mi = (uint32_t)w[4];
+  const uint32_t slotEnd = b.world->slotEnd, stride = b.nbrStride;
+  for (uint32_t slot = gtid(); slot < slotEnd; slot += gstride()) {
+    int32_t* w = b.state + (size_t)slot * 8;
+    const int2 mf = *reinterpret_cast<const int2*>(w + 4);
+    const uint32_t mi = (uint32_t)mf.x, fl = (uint32_t)mf.y;
+    if (!(fl & (FLAG_ANCHOR | FLAG_RIGID))) continue;
+    const ScenePar& S = b.scenes[b.sceneOf[slot]];
+    if (!S.active || slot - S.slotBase >= S.nFluid) continue;
     const int32_t burstP = matw(b, mi, M_burstP);
     if (!seal_class(b, mi) || burstP <= 0) continue;
-    const uint32_t fl = (uint32_t)w[5];
-    if (!(fl & (FLAG_ANCHOR | FLAG_RIGID))) continue;
+    const uint32_t p = b.inv[slot];
     const int32_t px = w[0], py = w[1];
     const uint32_t cnt = b.NBRN[p] & NBRN_COUNT;
     int32_t stress = 0;
@@ -1290,6 +1294,15 @@ __global__ void __launch_bounds__(256) k_form1(Bufs b) {
     const int32_t* wi = b.state + (size_t)slot * 8;
     uint32_t* cand = b.bondCand + (size_t)slot * BOND_CAP;
     const uint32_t* brow = b.bond + (size_t)slot * BOND_CAP;
+    const uint32_t flI = (uint32_t)wi[5], matI = (uint32_t)wi[4];
+    // Rigid members and rows that do not bond propose nothing: their list is
+    // empty. Candidate rows are dense (entries first, zeros after), so a row
+    // whose first word is zero is already empty and is not rewritten.
+    if ((flI & FLAG_RIGID) || matw(b, matI, M_bondK) == 0 || matw(b, matI, M_bondGroup) < 0) {
+      if (cand[0] != 0u)
+        for (int k = 0; k < BOND_CAP; ++k) cand[k] = 0;
+      continue;
+    }
     uint32_t cnt = b.NBRN[p] & NBRN_COUNT;
     // markCongealNbr: refresh the congeal bit from the post-thermal flags
     bool seen = false;
@@ -1299,15 +1312,9 @@ __global__ void __launch_bounds__(256) k_form1(Bufs b) {
       uint32_t qs = b.sslot[e];
       if ((uint32_t)b.state[(size_t)qs * 8 + 5] & FLAG_CONGEAL) { seen = true; break; }
     }
-    uint32_t flI = (uint32_t)wi[5];
-    if (flI & FLAG_RIGID) {
-      for (int k = 0; k < BOND_CAP; ++k) cand[k] = 0;
-      continue;
-    }
     bool anchoredI = (flI & FLAG_ANCHOR) != 0;
-    uint32_t matI = (uint32_t)wi[4];
     uint32_t cn = 0;
-    if (matw(b, matI, M_bondK) != 0 && matw(b, matI, M_bondGroup) >= 0) {
+    {
       for (int k = 0; k < BOND_CAP; ++k) {
         uint32_t w = brow[k];
         if (w == 0u) break;
@@ -1374,35 +1381,56 @@ __global__ void __launch_bounds__(256) k_form1(Bufs b) {
   }
 }
 
-// bondForm2 (src/sim.wgsl:3001-3068): keep mutual proposals, clear weld tags.
-__global__ void __launch_bounds__(256) k_form2(Bufs b) {
+// bondForm2 (src/sim.wgsl:3001-3068): keep mutual proposals, clear weld
+// tags. It is the last pass of the substep that writes hashed words, so with
+// HASH it also folds every particle's digest (the state hash of the substep).
+template <bool HASH>
+__global__ void __launch_bounds__(256) k_form2(Bufs b, uint32_t* __restrict__ acc) {
+  __shared__ uint32_t dsacc[8], dsscene;
+  if (HASH) digest_block_begin(dsacc, &dsscene);
   const uint32_t slotEnd = b.world->slotEnd;
-  for (uint32_t slot = gtid(); slot < slotEnd; slot += gstride()) {
-    const ScenePar& S = b.scenes[b.sceneOf[slot]];
-    uint32_t i = slot - S.slotBase;
-    if (!S.active || i >= S.nFluid || !S.formNow) continue;
-    const uint32_t* cand = b.bondCand + (size_t)slot * BOND_CAP;
-    uint32_t* row = b.bond + (size_t)slot * BOND_CAP;
-    uint32_t nn = 0;
-    for (int k = 0; k < BOND_CAP; ++k) {
-      uint32_t w = cand[k];
-      if (w == 0u) break;
-      uint32_t j = w & BOND_J_MASK;
-      const uint32_t* cj = b.bondCand + (size_t)(S.slotBase + j) * BOND_CAP;
-      bool ok = false;
-      for (int q = 0; q < BOND_CAP; ++q) {
-        uint32_t v = cj[q];
-        if (v == 0u) break;
-        if ((v & BOND_J_MASK) == i) { ok = ((v & BOND_L0_MASK) == (w & BOND_L0_MASK)); break; }
+  const uint32_t nIter = HASH ? (slotEnd + gstride() - 1) / gstride() * gstride() : slotEnd;
+  for (uint32_t slot = gtid(); slot < nIter; slot += gstride()) {
+    bool valid = false;
+    uint32_t s = 0;
+    uint32_t h[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (slot < slotEnd) {
+      s = b.sceneOf[slot];
+      const ScenePar& S = b.scenes[s];
+      const uint32_t i = slot - S.slotBase;
+      uint32_t* row = b.bond + (size_t)slot * BOND_CAP;
+      if (S.active && i < S.nFluid && S.formNow) {
+        const uint32_t* cand = b.bondCand + (size_t)slot * BOND_CAP;
+        uint32_t nn = 0;
+        for (int k = 0; k < BOND_CAP; ++k) {
+          uint32_t w = cand[k];
+          if (w == 0u) break;
+          uint32_t j = w & BOND_J_MASK;
+          const uint32_t* cj = b.bondCand + (size_t)(S.slotBase + j) * BOND_CAP;
+          bool ok = false;
+          for (int q = 0; q < BOND_CAP; ++q) {
+            uint32_t v = cj[q];
+            if (v == 0u) break;
+            if ((v & BOND_J_MASK) == i) { ok = ((v & BOND_L0_MASK) == (w & BOND_L0_MASK)); break; }
+          }
+          if (ok) row[nn++] = w & ~BOND_TOMB;
+        }
+        // bond rows are dense too: an empty row stays as it is
+        if (nn != 0u || row[0] != 0u)
+          for (int k = nn; k < BOND_CAP; ++k) row[k] = 0;
+        int32_t* w = b.state + (size_t)slot * 8;
+        uint32_t fo = (uint32_t)w[5] & ~FLAG_CONGEAL;
+        if (!(fo & FLAG_RIGID) && (fo & WELD_TAG_MASK) != S.weldHold) fo &= ~WELD_TAG_MASK;
+        w[5] = (int32_t)fo;
       }
-      if (ok) row[nn++] = w & ~BOND_TOMB;
+      if (HASH) {
+        valid = S.active && i < S.n;
+        if (valid) particle_digest(b.state + (size_t)slot * 8, i, i < S.nFluid ? row : nullptr, h);
+      }
     }
-    for (int k = nn; k < BOND_CAP; ++k) row[k] = 0;
-    int32_t* w = b.state + (size_t)slot * 8;
-    uint32_t fo = (uint32_t)w[5] & ~FLAG_CONGEAL;
-    if (!(fo & FLAG_RIGID) && (fo & WELD_TAG_MASK) != S.weldHold) fo &= ~WELD_TAG_MASK;
-    w[5] = (int32_t)fo;
+    if (HASH) digest_add_block(acc, dsacc, &dsscene, valid, s, h);
   }
+  if (HASH) digest_block_end(acc, dsacc, &dsscene);
 }
 
 }  // namespace d2

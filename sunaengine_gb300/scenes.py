@@ -257,6 +257,67 @@ def rigid_tank(plank: str = 'METAL', wheel: str = 'WOOD', rail: bool = True, see
     return sc
 
 
+def construction_site(tiles: int = 24, depth: int = 44, seed: int = 0xc0457) -> Scene:
+    """The widened rows at scale (build-defined): ``tiles`` 64-wu bays side by
+    side, each with an L-shaped METAL plank (63 members), a WOOD disc of
+    radius 5 wu (81 members) and a held STONE rail (seal class: containment
+    runs) above one WATER pool ``depth`` rows deep spanning the whole width.
+    ``meta`` lists each bay's plank and wheel slots and the wheel centres, so
+    a caller makes one free body per plank and one axis body per wheel."""
+    rng = Xorshift32(seed)
+    dom_w, dom_h = 64 * tiles, depth + 52
+    half = ONE >> 1
+    pos, mat = [], []
+    planks, wheels, centres, rails = [], [], [], []
+    metal, wood, stone = mat_id('METAL'), mat_id('WOOD'), mat_id('STONE')
+    for t in range(tiles):
+        ox = t * 64 * ONE
+        sl = []
+        for r in range(3):
+            for c in range(16):
+                sl.append(len(pos))
+                pos.append((ox + 8 * ONE + half + c * ONE, 14 * ONE + half + r * ONE))
+                mat.append(metal)
+        for r in range(3, 8):
+            for c in range(3):
+                sl.append(len(pos))
+                pos.append((ox + 21 * ONE + half + c * ONE, 14 * ONE + half + r * ONE))
+                mat.append(metal)
+        planks.append(sl)
+        sl = []
+        cx, cy = ox + 46 * ONE, 20 * ONE
+        for r in range(-5, 6):
+            for c in range(-5, 6):
+                if r * r + c * c <= 25:
+                    sl.append(len(pos))
+                    pos.append((cx + c * ONE, cy + r * ONE))
+                    mat.append(wood)
+        wheels.append(sl)
+        centres.append((cx + ONE, cy))
+        for c in range(7):
+            rails.append(len(pos))
+            pos.append((ox + 9 * ONE + half + c * ONE, 28 * ONE + half))
+            mat.append(stone)
+    jit = ONE // 8
+    y = (dom_h - 2 - depth) * ONE + half
+    while y <= (dom_h - 3) * ONE + half:
+        x = 3 * ONE + half
+        while x <= (dom_w - 4) * ONE + half:
+            jx = (rng() % (2 * jit + 1)) - jit
+            jy = (rng() % (2 * jit + 1)) - jit
+            pos.append((x + jx, y + jy))
+            mat.append(MAT_WATER)
+            x += ONE
+        y += ONE
+    sc = _assemble(pos, np.array(mat, np.uint32), boundary_ring(dom_w, dom_h, dom_h - 4), dom_w, dom_h,
+                   f'construction_site_{tiles}')
+    fl = np.zeros(sc.n, np.uint32)
+    fl[rails] = FLAG_ANCHOR
+    sc.flags = fl
+    sc.meta = {'planks': planks, 'wheels': wheels, 'wheel_pivots': centres, 'rails': rails}
+    return sc
+
+
 def make_scene(name: str, **opts) -> Scene:
     """The reference's canonical scenes (``makeScene``, ``src/engine.js:2469-2648``)."""
     if name == 'dambreak_v1':
