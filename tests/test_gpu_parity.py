@@ -57,6 +57,17 @@ def _hot_rice():
     return sc
 
 
+def _walls_only():
+    """No fluid at all: the boundary block alone (nFluid = 0)."""
+    return scenes._assemble([], np.zeros(0, np.uint32), scenes.boundary_ring(40, 24, 20), 40, 24, 'walls_only')
+
+
+def _one_drop():
+    """A single WATER particle falling onto the floor of an empty box."""
+    return scenes._assemble([(20 * ONE + 777, 5 * ONE)], np.zeros(1, np.uint32), scenes.boundary_ring(40, 24, 20),
+                            40, 24, 'one_drop')
+
+
 def _anchored():
     sc = _pool('SAND', 30, 10)
     fl = np.zeros(sc.n, np.uint32)
@@ -78,6 +89,8 @@ SCENES = {
     'anchored_sand': (_anchored, 30),
     'two_fluid_48': (lambda: scenes.large_two_fluid(side=48, band=8), 30),
     'lattice_dambreak_64': (lambda: scenes.lattice_dambreak(), 30),
+    'walls_only': (_walls_only, 10),
+    'one_drop': (_one_drop, 60),
 }
 
 
@@ -249,6 +262,16 @@ def test_batch_remove_and_add_keeps_others_exact(oracle_mod):
     rc.step(15)
     assert b.chain_hex(ia) == ra.chain_hex()
     assert b.chain_hex(ic) == rc.chain_hex()
+
+
+def test_empty_scene_steps_and_hashes():
+    sc = scenes._assemble([], np.zeros(0, np.uint32), np.zeros((0, 2), np.int32), 40, 24, 'empty')
+    e = Engine(max_particles=1024).load_scene(sc)
+    d0 = e.digest().hex
+    e.step(5)
+    assert e.digest().hex == d0 and e.info()['substep_count'] == 5
+    assert e.read_state().size == 0
+    e.check_errors()
 
 
 def test_refuses_bad_input():
