@@ -162,7 +162,7 @@ BYTES = {
 
 
 # ncu summaries under profiles/ that carry the DRAM traffic of a dominant kernel
-PROFILE_OF = {'colour x4': 'k_colour_2d_large.md', 'solve+apply': 'k3_solve_3d_dam.md'}
+PROFILE_OF = {'colour x4': 'k_colour_2d_large.md', 'solve+apply': 'k3_solve_3d_dam.md', 'density': 'k3_density_3d_dam.md'}
 
 
 def profiled_traffic(phase: str):

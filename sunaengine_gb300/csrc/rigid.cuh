@@ -279,7 +279,9 @@ __device__ int2 rigid_seal_delta(const Bufs& b, const ScenePar& S, uint32_t p, i
         if (t == p) continue;
         const int4 o = b.PL[t];
         const uint32_t info = (uint32_t)o.w;
-        if (info & INFO_BOUNDARY) continue;
+        // a held seal particle wears FLAG_SEAL and FLAG_ANCHOR, so its sorted
+        // record carries INFO_SEAL and INFO_PINNED; only those read their flags
+        if ((info & INFO_BOUNDARY) || !(info & INFO_SEAL) || !(info & INFO_PINNED)) continue;
         const uint32_t fj = (uint32_t)b.state[(size_t)b.sslot[t] * 8 + 5];
         if ((fj & (FLAG_ANCHOR | FLAG_SEAL)) != (FLAG_ANCHOR | FLAG_SEAL) || !seal_class(b, info & INFO_MAT)) continue;
         if ((fj & FLAG_RIGID) && (int32_t)(fj & WELD_TAG_MASK) == tag) continue;
