@@ -338,7 +338,7 @@ def batched_workload(steps: int, warmup: int, device: int, plain_sample: int = 2
         for (at, cx, cy, r, ix, iy) in ev:
             b.schedule_impulse(sid, at, cx, cy, r, ix, iy)
     b.step(warmup)
-    tuned = b.autotune(1)
+    tuned = b.autotune(2)
     b.sync()
     b.step(steps)
     ms, launches = b.last_timing()
@@ -451,7 +451,7 @@ def ours(args):
     e.load_scene(sc)
     e.step(args.warmup)
     if not args.no_autotune:
-        e.autotune(1)   # lane split per gather class, tuned on real (untimed) substeps
+        e.autotune(3)   # lane split per gather class, tuned on real (untimed) substeps
     e.sync()
     _barrier(dist)
     with ClockSampler(local) as clk:

@@ -300,7 +300,8 @@ int sn_batch_set_material(sn_batch* b, uint32_t row, const int32_t words[48], ui
  * lanes; results are identical for every choice, speed is not. With
  * opts.lanes == 0 each class starts from a rule on the active particle count
  * (re-applied when the scene set changes by more than 2x); sn_autotune runs
- * 4 x reps REAL substeps of every loaded scene (they advance the scenes and
+ * 4 x (reps + 1) REAL substeps of every loaded scene (the first of each lane
+ * count untimed) (they advance the scenes and
  * their chains exactly like sn_step) under each lane count with phase timers
  * and keeps the fastest count per class. *substeps_run receives how many
  * substeps it ran. With opts.lanes != 0 the lanes are pinned and it runs none.

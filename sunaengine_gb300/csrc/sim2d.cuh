@@ -520,12 +520,11 @@ __global__ void __launch_bounds__(256) k_solveA(Bufs b, int lastIter) {
     // current pair is computed
     uint32_t qn = sub < cnt ? (np[(size_t)sub * stride] & ~NBR_BOUNDARY) : 0u;
     int2 pn = ld_pred(b.PL, qn);
+    uint32_t qn2 = sub + L < cnt ? (np[(size_t)(sub + L) * stride] & ~NBR_BOUNDARY) : 0u;
     for (uint32_t k = sub; k < cnt; k += L) {
       int2 pj = pn;
-      if (k + L < cnt) {
-        qn = np[(size_t)(k + L) * stride] & ~NBR_BOUNDARY;
-        pn = ld_pred(b.PL, qn);
-      }
+      if (k + L < cnt) pn = ld_pred(b.PL, qn2);
+      if (k + 2 * L < cnt) qn2 = np[(size_t)(k + 2 * L) * stride] & ~NBR_BOUNDARY;
       int2 d = pdelta(pi, pj, f);
       int id = lut_index(d, f);
       if (id < 0) continue;
@@ -570,13 +569,15 @@ __device__ __forceinline__ int2 solveB_dp(const Bufs& b, const int4* __restrict_
   const uint32_t* np = b.NBR + p;
   uint32_t en = sub < cnt ? np[(size_t)sub * stride] : 0u;
   int4 on = src[en & ~NBR_BOUNDARY];
+  uint32_t en2 = sub + L < cnt ? np[(size_t)(sub + L) * stride] : 0u;
   for (uint32_t k = sub; k < cnt; k += L) {
     uint32_t e = en;
     int4 o = on;
     if (k + L < cnt) {
-      en = np[(size_t)(k + L) * stride];
+      en = en2;
       on = src[en & ~NBR_BOUNDARY];
     }
+    if (k + 2 * L < cnt) en2 = np[(size_t)(k + 2 * L) * stride];
     if constexpr (RIG) {
       if (!(e & NBR_BOUNDARY) && same_body(infoI, (uint32_t)o.w)) continue;
     }

@@ -11,7 +11,7 @@ def test_autotune_keeps_the_chain():
     sc = scenes.large_two_fluid(side=192)
     a = Engine(max_particles=sc.n).load_scene(sc)
     ran = a.autotune(1)
-    assert ran == 4
+    assert ran == 8          # 4 lane counts x (1 untimed + 1 timed)
     lanes = a.lanes()
     assert set(lanes) == {'solveA', 'colours', 'post1', 'post2', 'nbr'}
     assert all(v in (1, 2, 4, 8) for v in lanes.values())
