@@ -310,6 +310,11 @@ int sn_autotune(sn_engine* e, uint32_t reps, uint32_t* substeps_run);
 int sn_batch_autotune(sn_batch* b, uint32_t reps, uint32_t* substeps_run);
 int sn_lanes(sn_engine* e, uint32_t out[5]);
 int sn_batch_lanes(sn_batch* b, uint32_t out[5]);
+/* Pin {solveA, colours, post1, post2, neighbour lists} lanes (each 1, 2, 4 or
+ * 8), e.g. a split tuned on another run of the same workload; afterwards
+ * neither the size rule nor sn_autotune changes them. */
+int sn_set_lanes(sn_engine* e, const uint32_t lanes[5]);
+int sn_batch_set_lanes(sn_batch* b, const uint32_t lanes[5]);
 
 /* ---- digest without device allocation ------------------------------------ */
 /* No counterpart in the reference. For callers that cannot allocate device

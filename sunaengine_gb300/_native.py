@@ -203,6 +203,8 @@ SIGNATURES = {
     'sn_drag_body': (ctypes.c_int, [P, u32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                     ctypes.POINTER(u32)]),
     'sn_restore_bodies': (ctypes.c_int, [P, P, u32, P, ctypes.c_size_t]),
+    'sn_set_lanes': (ctypes.c_int, [P, P]),
+    'sn_batch_set_lanes': (ctypes.c_int, [P, P]),
     'sn_set_material': (ctypes.c_int, [P, u32, P, ctypes.POINTER(u32)]),
     'sn_clear_materials': (ctypes.c_int, [P]),
     'sn_set_gravity_scale': (ctypes.c_int, [P, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]),

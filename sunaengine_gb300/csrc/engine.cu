@@ -621,8 +621,8 @@ struct World {
   struct LaneCfg {
     int a = 1, c = 1, p1 = 1, p2 = 1, n = 1;
   };
-  LaneCfg lanesCfg;
-  bool autoLanes = true, lanesTuned = false;
+  LaneCfg lanesCfg, pinnedLanes;
+  bool autoLanes = true, lanesTuned = false, setLanes = false;
   uint32_t tunedAtN = 0;
 
   template <bool DBG, int L>
@@ -757,7 +757,8 @@ struct World {
   }
   void default_lanes() {
     if (!autoLanes) {
-      lanesCfg = LaneCfg{lanesOverride, lanesOverride, lanesOverride, lanesOverride, lanesOverride};
+      lanesCfg = setLanes ? pinnedLanes
+                          : LaneCfg{lanesOverride, lanesOverride, lanesOverride, lanesOverride, lanesOverride};
       return;
     }
     if (lanesTuned && hw.nAct * 2 >= tunedAtN && hw.nAct <= tunedAtN * 2ull) return;
@@ -770,6 +771,21 @@ struct World {
   // phase events, then keep the fastest count per gather class. Every lane
   // count gives the same results, so the tuning substeps are ordinary
   // substeps of the scenes (they count toward the caller's request).
+  // Pin the lanes of every gather class (e.g. ones tuned on another run of
+  // the same workload); the size rule and the tuner stop changing them.
+  bool set_lanes(const uint32_t* v) {
+    if (!v) return fail("lanes are NULL");
+    for (int k = 0; k < 5; ++k)
+      if (v[k] != 1 && v[k] != 2 && v[k] != 4 && v[k] != 8) return fail("lanes must be 1, 2, 4 or 8");
+    lanesCfg = LaneCfg{(int)v[0], (int)v[1], (int)v[2], (int)v[3], (int)v[4]};
+    pinnedLanes = lanesCfg;
+    setLanes = true;
+    autoLanes = false;
+    lanesTuned = true;
+    graphValid = false;
+    return true;
+  }
+
   bool autotune(uint32_t per, uint32_t* used) {
     if (used) *used = 0;
     if (!autoLanes) return true;  // lanes were pinned at create
@@ -2239,6 +2255,14 @@ int sn_lanes(sn_engine* e, uint32_t out[5]) {
   const auto& c = e->w.lanesCfg;
   out[0] = c.a; out[1] = c.c; out[2] = c.p1; out[3] = c.p2; out[4] = c.n;
   return SN_OK;
+}
+int sn_set_lanes(sn_engine* e, const uint32_t lanes[5]) {
+  if (!e) return SN_E_INVALID;
+  return rc_of(e->w, e->w.set_lanes(lanes));
+}
+int sn_batch_set_lanes(sn_batch* b, const uint32_t lanes[5]) {
+  if (!b) return SN_E_INVALID;
+  return rc_of(b->w, b->w.set_lanes(lanes));
 }
 int sn_batch_lanes(sn_batch* b, uint32_t out[5]) {
   if (!b || !out) return SN_E_INVALID;

@@ -829,13 +829,15 @@ __global__ void __launch_bounds__(256, 5) k_post1(Bufs b) {
     const uint32_t* np = b.NBR + pp;
     uint32_t en = sub < cnt ? np[(size_t)sub * stride] : 0u;
     int4 on = b.PL[en & ~NBR_BOUNDARY];
+    uint32_t en2 = sub + L < cnt ? np[(size_t)(sub + L) * stride] : 0u;
     for (uint32_t k = sub; k < cnt; k += L) {
       const uint32_t e = en;
       const int4 o = on;
       if (k + L < cnt) {
-        en = np[(size_t)(k + L) * stride];
+        en = en2;
         on = b.PL[en & ~NBR_BOUNDARY];
       }
+      if (k + 2 * L < cnt) en2 = np[(size_t)(k + 2 * L) * stride];
       if (e & NBR_BOUNDARY) continue;
       const uint32_t q = e;
       const int2 pq = xy(o);
@@ -1163,13 +1165,15 @@ __global__ void __launch_bounds__(256, 6) k_post2(Bufs b, int formFlags) {
     const uint32_t* np = b.NBR + pp;
     uint32_t en = sub < cnt ? np[(size_t)sub * stride] : 0u;
     int4 on = b.PL[en & ~NBR_BOUNDARY];
+    uint32_t en2 = sub + L < cnt ? np[(size_t)(sub + L) * stride] : 0u;
     for (uint32_t k = sub; k < cnt; k += L) {
       const uint32_t e = en;
       const int4 o = on;
       if (k + L < cnt) {
-        en = np[(size_t)(k + L) * stride];
+        en = en2;
         on = b.PL[en & ~NBR_BOUNDARY];
       }
+      if (k + 2 * L < cnt) en2 = np[(size_t)(k + 2 * L) * stride];
       const uint32_t q = e & ~NBR_BOUNDARY;
       // a rigid member's cohesion skips its own body (src/sim.wgsl:2450-2457)
       if ((info & INFO_RIGID) && !(e & NBR_BOUNDARY) && same_body(info, (uint32_t)o.w)) continue;

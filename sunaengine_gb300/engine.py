@@ -489,6 +489,11 @@ class Engine:
         self._check(self._lib.sn_lanes(self._h, _ptr(a)), 'lanes')
         return dict(zip(('solveA', 'colours', 'post1', 'post2', 'nbr'), (int(x) for x in a)))
 
+    def set_lanes(self, lanes: dict):
+        """Pin the per-class lane split (the dict `lanes()` returns)."""
+        a = np.array([lanes[k] for k in ('solveA', 'colours', 'post1', 'post2', 'nbr')], np.uint32)
+        self._check(self._lib.sn_set_lanes(self._h, _ptr(a)), 'setLanes')
+
     def profile_substep(self, reps: int = 3) -> np.ndarray:
         """Mean device ms per kernel phase over `reps` real substeps (profileSubstep)."""
         out = np.zeros(64, np.float32)
@@ -652,6 +657,10 @@ class Batch:
         a = np.zeros(5, np.uint32)
         self._check(self._lib.sn_batch_lanes(self._h, _ptr(a)), 'lanes')
         return dict(zip(('solveA', 'colours', 'post1', 'post2', 'nbr'), (int(x) for x in a)))
+
+    def set_lanes(self, lanes: dict):
+        a = np.array([lanes[k] for k in ('solveA', 'colours', 'post1', 'post2', 'nbr')], np.uint32)
+        self._check(self._lib.sn_batch_set_lanes(self._h, _ptr(a)), 'setLanes')
 
     # device keyframes (sn_batch_ckpt_*): see checkpoints.CheckpointPool
     def ckpt_bytes(self, sid: int) -> int:

@@ -38,3 +38,15 @@ def test_batch_autotune_keeps_every_scene():
     ref.step(30)
     for i, j in zip(ids, rid):
         assert bt.chain_hex(i) == ref.chain_hex(j)
+
+
+def test_pinned_lanes_survive_a_load():
+    sc = scenes.make_scene('dambreak_v1')
+    e = Engine(max_particles=sc.n + 64)
+    want = {'solveA': 2, 'colours': 4, 'post1': 1, 'post2': 8, 'nbr': 2}
+    e.set_lanes(want)
+    e.load_scene(sc)
+    assert e.lanes() == want
+    e.step(3)
+    e.autotune(1)
+    assert e.lanes() == want
