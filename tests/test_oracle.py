@@ -2,26 +2,27 @@
 
 Golden values: the frozen dambreak_v1 chain and checkpoint digests recorded in
 the reference's test/extraction_gate.md:62-68 (also test/site_gates.mjs:53-61),
-and the frozen LUT hash (src/engine.js:501).
+and the frozen LUT hash (src/engine.js:501), carried in
+tests/golden/reference_dambreak_v1.json (written from those files by
+tests/golden/extract_reference_golden.py).
 """
+import json
+from pathlib import Path
+
 import numpy as np
 import pytest
 
 from sunaengine_gb300 import data, scenes
 
-GOLDEN_CHAIN = '20918f97fbcbb409e7d058ebcae6f6725973b9a19042168742b07e8c17126d14'
-GOLDEN_CHECKPOINTS = {
-    1: 'c31aa57fb218829e3b78250e5909ddbbbb872c7d60e5b674f78d1a7164d8e0be',
-    10: '95984e71128a222a27f285a340d178384a588ca74d27abb2448e08d3c4239c04',
-    100: '320e900be986aa4e63ee1d110a4fb798d7e07e39ca7828782c475c1f206204eb',
-    1000: 'b1844e32b4d2bd4b3dbd91cd4ffb7ead0bf568d6fea0dc53c8d555134f946d9b',
-}
+GOLDEN = json.loads((Path(__file__).parent / 'golden' / 'reference_dambreak_v1.json').read_text())
+GOLDEN_CHAIN = GOLDEN['chain']
+GOLDEN_CHECKPOINTS = {int(k): v for k, v in GOLDEN['checkpoints'].items()}
 
 
 def test_table_hash_and_layout():
     w = data.luts()
     assert w.size == 5 * 3202
-    assert data.table_hash(w) == data.TABLE_HASH
+    assert data.table_hash(w) == data.TABLE_HASH == GOLDEN['table_hash']
     # the s_corr table is all zeros (scorrK = 0, src/tables.js:41)
     assert not w[4 * 3202:].any()
 
