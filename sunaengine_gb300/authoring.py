@@ -375,3 +375,86 @@ def promote_loose_rigid_components(eng, link_ticks: int = None, eligible=()) -> 
     if made:
         _mark_dirty(eng)
     return made
+
+
+# ---- exact authoring saves (.suna with bonds, bodies and composed rows) -------------
+RG_BODY_WORDS = 32
+
+
+def authoring_snapshot(eng) -> dict:
+    """The engine-owned parts of an exact save (the payload of encodeSuna,
+    src/suna.js:46-84, and the input of restoreAuthoringSnapshot,
+    src/engine.js:5838): state, bond rows (also as the candidate table),
+    the body-record image (RG_MAX_BODIES x 32 words), rest offsets, the body
+    descriptors and the formation clock."""
+    n, nf = eng.n, eng.n_fluid
+    recs = eng.read_bodies()
+    image = np.zeros(RG_MAX_BODIES * RG_BODY_WORDS, np.int32)
+    image[:recs.size] = recs.reshape(-1)
+    bonds = np.zeros(n * BOND_CAP, np.uint32)
+    if nf:
+        bonds[:nf * BOND_CAP] = np.asarray(eng.read_bonds(), dtype=np.uint32).reshape(-1)[:nf * BOND_CAP]
+    bodies = [{'tag': int(R[RB_TAG]) & 0xffffffff, 'first': int(R[RB_FIRST]), 'last': int(R[RB_LAST]),
+               'n': int(R[14]), 'index': k, 'axis': bool(R[RB_AXIS]), 'user': bool(R[RB_USER])}
+              for k, R in enumerate(recs)]
+    return {'state': np.ascontiguousarray(eng.read_state(), dtype=np.int32), 'bonds': bonds, 'bondCand': bonds.copy(),
+            'bodyRecords': image, 'restOffsets': np.ascontiguousarray(eng.read_rest_offsets(), dtype=np.int32),
+            'bodies': bodies, 'formationClock': int(eng.formation_clock)}
+
+
+def restore_authoring_snapshot(eng, snap: dict):
+    """restoreAuthoringSnapshot (src/engine.js:5838-5888) after load_scene:
+    state, bond rows, body records and rest offsets, formation clock (no
+    pending formation)."""
+    n, nf = eng.n, eng.n_fluid
+    state = np.ascontiguousarray(snap['state'], dtype=np.int32).reshape(-1)
+    if state.size != n * 8:
+        raise ValueError(f'snapshot state has {state.size} words; expected {n * 8}')
+    eng.write_state_keep_scratch(state)
+    bonds = np.ascontiguousarray(snap['bonds'], dtype=np.uint32).reshape(-1)
+    if nf:
+        eng.write_bonds(bonds[:nf * BOND_CAP])
+    k = len(snap.get('bodies') or [])
+    recs = np.ascontiguousarray(snap['bodyRecords'], dtype=np.int32).reshape(-1)[:k * RG_BODY_WORDS]
+    eng.restore_bodies(recs.reshape(-1, RG_BODY_WORDS), snap.get('restOffsets'))
+    eng.set_formation_clock(int(snap.get('formationClock', 0)), False)
+
+
+def save_suna(eng, scene, interner=None, app=None) -> str:
+    """An exact `.suna` save of the engine's scene (`scene` gives the domain:
+    domW, domH, cellShift) with its composed-material record."""
+    from . import formats
+    snap = authoring_snapshot(eng)
+    header = {'n': int(eng.n), 'nFluid': int(eng.n_fluid), 'domW': int(scene.domW), 'domH': int(scene.domH),
+              'cellShift': int(scene.cellShift), 'formationClock': snap['formationClock']}
+    payload = dict(snap, scene=header, tints=np.zeros(int(eng.n), np.uint32), app=app,
+                   materials={'events': list(interner.events) if interner is not None else []})
+    return formats.encode_suna(payload)
+
+
+def load_suna(text, new_engine):
+    """Load an exact `.suna`: a fresh engine from `new_engine()`, the composed
+    rows re-derived from the record (applyMintEvents refuses any mismatch),
+    the scene loaded from the saved words, then restoreAuthoringSnapshot.
+    Returns (engine, interner)."""
+    from . import formats, materials, scenes as sc_mod
+    doc = formats.decode_suna(text)
+    s = doc['scene']
+    n, nf = int(s['n']), int(s['nFluid'])
+    st = np.asarray(doc['state'], dtype=np.int32).reshape(n, 8)
+    sc = sc_mod.Scene(n=n, nFluid=nf, pos=st[:, 0:2].copy(), vel=st[:, 2:4].copy(),
+                      matId=st[:, 4].astype(np.uint32), domW=int(s['domW']), domH=int(s['domH']),
+                      cellShift=int(s['cellShift']), flags=(st[:, 5].astype(np.uint32) & 5),
+                      temp=st[:, 6].copy(), fuel=st[:, 7].copy(), name='suna')
+    eng = new_engine()
+    it = materials.Interner(eng)
+    it.apply_events((doc.get('materials') or {}).get('events') or [])
+    eng.load_scene(sc)
+    if doc.get('bonds') is not None:
+        restore_authoring_snapshot(eng, {'state': doc['state'], 'bonds': doc['bonds'],
+                                         'bodyRecords': doc['bodyRecords'], 'restOffsets': doc['restOffsets'],
+                                         'bodies': doc.get('bodies') or [],
+                                         'formationClock': int(s.get('formationClock', 0))})
+    else:
+        eng.write_state_keep_scratch(np.asarray(doc['state'], dtype=np.int32))
+    return eng, it

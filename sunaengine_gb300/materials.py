@@ -211,7 +211,13 @@ class Interner:
         self.spawned: Dict[int, int] = {}
         self.events: List[dict] = []
         self.tick = 0
-        self.substep = lambda: int(getattr(eng, 'formation_clock', 0))
+        self.substep = self._clock
+
+    def _clock(self) -> int:
+        try:
+            return int(self.eng.formation_clock)
+        except Exception:  # no scene loaded yet (a replay applies its record first)
+            return 0
 
     @staticmethod
     def _key(base, bits, mask):

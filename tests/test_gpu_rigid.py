@@ -207,3 +207,25 @@ def test_split_and_loose_promotion_match():
     same(g2, r2)
     run(g2, r2, (1, 12))
     same(g2, r2)
+
+
+def test_exact_suna_save_loads_on_both_engines():
+    import oracle as o
+    from sunaengine_gb300 import authoring, materials
+    sc = scenes.rigid_tank()
+    e = Engine(max_particles=sc.n + 256, debug=True).load_scene(sc)
+    it = materials.Interner(e)
+    row = it.intern(data.mat_id('SAND'), materials.MOD['E'])['rowId']
+    e.spawn_fluid([{'x': (50 + c) * ONE, 'y': 6 * ONE, 'mat': row} for c in range(8)], no_weld=False)
+    e.make_rigid_body(sc.meta['plank'])
+    e.make_axis_body(sc.meta['wheel'], *sc.meta['wheel_centre'])
+    e.step(25)
+    text = authoring.save_suna(e, sc, it)
+    g, _ = authoring.load_suna(text, lambda: Engine(max_particles=sc.n + 256, debug=True))
+    r, _ = authoring.load_suna(text, lambda: o.OracleEngine(sc.n + 256, threads=16))
+    e.write_state(e.read_state(), np.zeros(e.n * 2, np.int32))   # a save carries no scratch
+    for x in (e, g, r):
+        x.step(20)
+    assert np.array_equal(g.read_state(), r.read_state()) and np.array_equal(g.read_state(), e.read_state())
+    assert np.array_equal(g.read_bodies(), r.read_bodies())
+    assert np.array_equal(g.debug_counters(), r.debug_counters())
