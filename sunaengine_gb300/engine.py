@@ -518,7 +518,21 @@ class Engine:
     def formation_clock(self) -> int:
         return int(self.info()['formation_clock'])
 
+    def frame(self) -> int:
+        """frame() (src/engine.js:4001): SUBSTEPS_PER_FRAME = 2 substeps."""
+        return self.step(2)
+
+    def sync_mirror(self):
+        """syncMirror(): the reference copies the state to a host mirror before
+        applyImpulse reads it; here impulses are applied on the device at the
+        substep boundary and readState is always current, so there is nothing
+        to wait for beyond the queued work."""
+        self.sync()
+
     # camelCase aliases: the reference's method names
+    syncMirror = sync_mirror
+    readDerived = read_scratch   # the derived words that cross substeps (stAcc), n x 2
+    readBond = read_bonds
     setWalls = set_walls
     loadScene = load_scene
     chainHex = chain_hex
