@@ -342,7 +342,7 @@ def batched_workload(steps: int, warmup: int, device: int, plain_sample: int = 2
     # lanes tuned on a separate run advanced to the middle of the timed window
     t = make()
     t.step(warmup + steps // 2)
-    tuned = t.autotune(2)
+    t.autotune(2)
     pick = t.lanes()
     t.destroy()
     b = make()
