@@ -692,10 +692,23 @@ __global__ void __launch_bounds__(256) k_friction(Bufs b) {
     uint32_t cnt = b.NBRN[p] & NBRN_COUNT;
     int32_t fx = 0, fy = 0;
     if (fi != 0) {
+      // one neighbour ahead (record and old position), two ahead (index): a
+      // friction row is one thread per particle, so the gathers would
+      // otherwise form one serial chain of dependent loads
+      uint32_t en = cnt > 0u ? b.NBR[p] : 0u;
+      int4 on = b.PL[en & ~NBR_BOUNDARY];
+      int2 sn = b.POS[en & ~NBR_BOUNDARY];
+      uint32_t en2 = cnt > 1u ? b.NBR[(size_t)stride + p] : 0u;
       for (uint32_t k = 0; k < cnt; ++k) {
-        uint32_t e = b.NBR[(size_t)k * stride + p];
-        uint32_t q = e & ~NBR_BOUNDARY;
-        int4 o = b.PL[q];
+        const uint32_t e = en;
+        const int4 o = on;
+        const int2 so = sn;
+        if (k + 1u < cnt) {
+          en = en2;
+          on = b.PL[en & ~NBR_BOUNDARY];
+          sn = b.POS[en & ~NBR_BOUNDARY];
+        }
+        if (k + 2u < cnt) en2 = b.NBR[(size_t)(k + 2u) * stride + p];
         if (rigidI && !(e & NBR_BOUNDARY) && same_body(info, (uint32_t)o.w)) continue;
         int2 pq = xy(o);
         int2 d = pdelta(pi, pq, f);
@@ -707,7 +720,7 @@ __global__ void __launch_bounds__(256) k_friction(Bufs b) {
         int2 rel = dxi;
         int32_t mu = fi;
         if (!(e & NBR_BOUNDARY)) {
-          int2 dq = delta(pq, b.POS[q], f);
+          int2 dq = delta(pq, so, f);
           rel = make_int2(sub_sat(dxi.x, dq.x, f), sub_sat(dxi.y, dq.y, f));
           mu = mat_mix(fi, matw(b, (uint32_t)o.w & INFO_MAT, M_fric));
         }

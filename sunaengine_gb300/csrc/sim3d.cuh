@@ -308,9 +308,13 @@ __global__ void __launch_bounds__(256) k3_density(Bufs3 b, const int4* __restric
     const int4 me = valid ? PW[s] : make_int4(0, 0, 0, 0);
     int32_t rho = 0, St = 0, sgx = 0, sgy = 0, sgz = 0;
     const uint32_t cnt = valid ? b.NBRN[s] : 0u;
+    // one neighbour record and two indices ahead (as in the 2D sweeps)
+    int4 on = PW[sub < cnt ? b.NBR[(size_t)sub * stride + s] : 0u];
+    uint32_t tn2 = sub + L < cnt ? b.NBR[(size_t)(sub + L) * stride + s] : 0u;
     for (uint32_t k = sub; k < cnt; k += L) {
-      uint32_t t = b.NBR[(size_t)k * stride + s];
-      int4 o = PW[t];
+      const int4 o = on;
+      if (k + L < cnt) on = PW[tn2];
+      if (k + 2 * L < cnt) tn2 = b.NBR[(size_t)(k + 2 * L) * stride + s];
       int32_t dx = wsub(o.x, me.x), dy = wsub(o.y, me.y), dz = wsub(o.z, me.z);
       int32_t r2q = r2q_of(dx, dy, dz);
       if (r2q >= H2Q) continue;
@@ -400,9 +404,12 @@ __global__ void __launch_bounds__(256) k3_solve(Bufs3 b, const int4* __restrict_
     const uint32_t cnt = valid ? b.NBRN[s] : 0u;
     int32_t ax = 0, ay = 0, az = 0;
     uint32_t mag = 0;
+    int4 on = b.PL[sub < cnt ? b.NBR[(size_t)sub * stride + s] : 0u];
+    uint32_t tn2 = sub + L < cnt ? b.NBR[(size_t)(sub + L) * stride + s] : 0u;
     for (uint32_t k = sub; k < cnt; k += L) {
-      uint32_t t = b.NBR[(size_t)k * stride + s];
-      int4 o = b.PL[t];
+      const int4 o = on;
+      if (k + L < cnt) on = b.PL[tn2];
+      if (k + 2 * L < cnt) tn2 = b.NBR[(size_t)(k + 2 * L) * stride + s];
       int32_t tx, ty, tz;
       if (!dp_term(b, me, o, tx, ty, tz, f)) continue;
       if constexpr (DBG) {
