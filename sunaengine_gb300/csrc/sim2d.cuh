@@ -811,7 +811,7 @@ __global__ void __launch_bounds__(256) k_apply_fric(Bufs b) {
 // over the neighbour list. vtmp_j = clamp(pred_j - pos_j) is finalize's
 // velocity, recomputed where it is needed.
 template <bool DBG, int L>
-__global__ void __launch_bounds__(256, 5) k_post1(Bufs b) {
+__global__ void __launch_bounds__(256, 4) k_post1(Bufs b) {
   Flags<DBG> f{b.dbg};
   __shared__ int4 smat[MAT_MAX];  // {xsph, cond, corrode, corrPt}
   for (int m = threadIdx.x; m < MAT_MAX; m += blockDim.x)
@@ -840,32 +840,38 @@ __global__ void __launch_bounds__(256, 5) k_post1(Bufs b) {
     const uint32_t cnt = act ? (b.NBRN[p] & NBRN_COUNT) : 0u;
     int32_t ax = 0, ay = 0, sx = 0, sy = 0, hq = 0, hc = 0;
     const uint32_t* np = b.NBR + pp;
+    // the neighbour's three records (pred/info, rho/rinv/T, old position)
+    // one ahead, its index two ahead
     uint32_t en = sub < cnt ? np[(size_t)sub * stride] : 0u;
     int4 on = b.PL[en & ~NBR_BOUNDARY];
+    int4 rn = b.RX[en & ~NBR_BOUNDARY];
+    int2 sn = b.POS[en & ~NBR_BOUNDARY];
     uint32_t en2 = sub + L < cnt ? np[(size_t)(sub + L) * stride] : 0u;
     for (uint32_t k = sub; k < cnt; k += L) {
       const uint32_t e = en;
       const int4 o = on;
+      const int4 rx = rn;
+      const int2 so = sn;
       if (k + L < cnt) {
         en = en2;
         on = b.PL[en & ~NBR_BOUNDARY];
+        rn = b.RX[en & ~NBR_BOUNDARY];
+        sn = b.POS[en & ~NBR_BOUNDARY];
       }
       if (k + 2 * L < cnt) en2 = np[(size_t)(k + 2 * L) * stride];
       if (e & NBR_BOUNDARY) continue;
-      const uint32_t q = e;
       const int2 pq = xy(o);
       const int2 d = pdelta(pi, pq, f);
       const int id = lut_index(d, f);
       if (id < 0) continue;
       const int2 wg = __ldg(b.WG + id);
       const int32_t W = wg.x;
-      const int4 rx = b.RX[q];
       const int4 mj = smat[(uint32_t)o.w & INFO_MAT];
       if (doX) {
         int32_t K = sym_k(rhoi, rx.x, b.rcp, f);
         int32_t wk = mulf<16>(W, K, f);
         int32_t cij = mat_mix(mi.x, mj.x);
-        int2 vj = delta(pq, b.POS[q], f);
+        int2 vj = delta(pq, so, f);
         vj.x = clampi(vj.x, vmaxN, vmax);
         vj.y = clampi(vj.y, vmaxN, vmax);
         ax = wadd(ax, mulfc<16>(mulf<12>(sub_sat(vj.x, vi.x, f), wk, f), cij, -XS_TERM, XS_TERM, f));
@@ -1152,7 +1158,7 @@ __device__ __forceinline__ void thermal(const Bufs& b, uint32_t i, int32_t heat,
 // 3059-3067) + the state digest. HASH=false when bond formation runs as its
 // own kernels (the digest then follows them).
 template <bool DBG, bool HASH, int L>
-__global__ void __launch_bounds__(256, 6) k_post2(Bufs b, int formFlags) {
+__global__ void __launch_bounds__(256, 5) k_post2(Bufs b, int formFlags) {
   Flags<DBG> f{b.dbg};
   __shared__ int4 smat[MAT_MAX];  // {gammaCoh, gammaCur, adhesion, 0}
   for (int m = threadIdx.x; m < MAT_MAX; m += blockDim.x)
@@ -1176,18 +1182,21 @@ __global__ void __launch_bounds__(256, 6) k_post2(Bufs b, int formFlags) {
     const uint32_t cnt = act ? (b.NBRN[p] & NBRN_COUNT) : 0u;
     int32_t ax = 0, ay = 0;
     const uint32_t* np = b.NBR + pp;
+    // the neighbour's record and normal/density one ahead, its index two ahead
     uint32_t en = sub < cnt ? np[(size_t)sub * stride] : 0u;
     int4 on = b.PL[en & ~NBR_BOUNDARY];
+    int4 nn = b.NQ[en & ~NBR_BOUNDARY];
     uint32_t en2 = sub + L < cnt ? np[(size_t)(sub + L) * stride] : 0u;
     for (uint32_t k = sub; k < cnt; k += L) {
       const uint32_t e = en;
       const int4 o = on;
+      const int4 nq = nn;
       if (k + L < cnt) {
         en = en2;
         on = b.PL[en & ~NBR_BOUNDARY];
+        nn = b.NQ[en & ~NBR_BOUNDARY];
       }
       if (k + 2 * L < cnt) en2 = np[(size_t)(k + 2 * L) * stride];
-      const uint32_t q = e & ~NBR_BOUNDARY;
       // a rigid member's cohesion skips its own body (src/sim.wgsl:2450-2457)
       if ((info & INFO_RIGID) && !(e & NBR_BOUNDARY) && same_body(info, (uint32_t)o.w)) continue;
       const int2 d = pdelta(pi, xy(o), f);
@@ -1199,7 +1208,6 @@ __global__ void __launch_bounds__(256, 6) k_post2(Bufs b, int formFlags) {
         ay = wsub(ay, mulfc<8>(mulf<22>(ca.y, d.y, f), mi.z, -ST_TERM, ST_TERM, f));
         continue;
       }
-      const int4 nq = b.NQ[q];
       const int32_t K = sym_k(rhoi, nq.z, b.rcp, f);
       const int4 mj = smat[(uint32_t)o.w & INFO_MAT];
       const int32_t gCoh = mat_mix(mi.x, mj.x);
