@@ -638,6 +638,11 @@ struct World {
       k_colour<DBG, L><<<g, 256, 0, st>>>(b, c, src, dst);
     }
   }
+  // friction splits each list like the colour passes and takes their lanes
+  template <bool DBG, int L>
+  void launch_friction() {
+    k_friction<DBG, L><<<grid_occ((const void*)k_friction<DBG, L>, (uint64_t)hw.nAct * L), 256, 0, st>>>(b);
+  }
   template <bool DBG, int L>
   void launch_nbr() {
     k_nbr<DBG, L><<<grid_occ((const void*)k_nbr<DBG, L>, (uint64_t)hw.nAct * L), 256, 0, st>>>(b);
@@ -699,7 +704,7 @@ struct World {
       mark();
       Lc += 5;
       if (hasFriction) {
-        k_friction<DBG><<<ga, 256, 0, st>>>(b);
+        SN_LANES(lc.c, (launch_friction<DBG, L_>()));
         k_apply_fric<DBG><<<ga, 256, 0, st>>>(b);
         Lc += 2;
       }

@@ -671,77 +671,86 @@ __global__ void __launch_bounds__(256, 8) k_colour(Bufs b, int colour, const int
 __device__ __forceinline__ bool friction_row(const Bufs& b, uint32_t m) {
   return matw(b, m, M_fric) != 0 || matw(b, m, M_bondK) != 0;
 }
-template <bool DBG>
+// L lanes share one particle's neighbour list (the friction sums wrap, so
+// any split is exact); a friction row's cost is one chain of dependent
+// gathers, which the split shortens L-fold. The bond gather stays on the
+// particle's first lane.
+template <bool DBG, int L>
 __global__ void __launch_bounds__(256) k_friction(Bufs b) {
   if (*b.work == 0u) return;  // no particle has a friction or bond row this substep
   Flags<DBG> f{b.dbg};
   const uint32_t nAct = b.world->nAct, stride = b.nbrStride;
-  for (uint32_t p = gtid(); p < nAct; p += gstride()) {
-    int4 me = b.PL[p];
-    uint32_t info = (uint32_t)me.w;
-    if (info & INFO_BOUNDARY) continue;
-    uint32_t m = info & INFO_MAT;
-    if (!friction_row(b, m)) continue;
+  const uint32_t sub = threadIdx.x & (L - 1), G = gstride() / L;
+  for (uint32_t p = gtid() / L;; p += G) {
+    if (__shfl_sync(0xffffffffu, p, 0) >= nAct) break;  // warp-uniform exit
+    const bool valid = p < nAct;
+    const int4 me = valid ? b.PL[p] : make_int4(0, 0, 0, (int32_t)INFO_BOUNDARY);
+    const uint32_t info = (uint32_t)me.w;
+    const uint32_t m = info & INFO_MAT;
+    const bool act = valid && !(info & INFO_BOUNDARY) && friction_row(b, m);
     // a rigid member skips its own body, gathers no bonds and ADDS its friction
     // to the solver dp waiting for rigidSolve (src/sim.wgsl:1680-1688, 1925-1929)
     const bool rigidI = (info & INFO_RIGID) != 0u;
-    int32_t fi = matw(b, m, M_fric);
-    int32_t bondKi = matw(b, m, M_bondK);
-    int2 pi = xy(me);
-    int2 dxi = delta(pi, b.POS[p], f);
-    uint32_t cnt = b.NBRN[p] & NBRN_COUNT;
+    const int32_t fi = act ? matw(b, m, M_fric) : 0;
+    const int2 pi = xy(me);
+    const uint32_t pp = act ? p : 0u;
+    const int2 dxi = delta(pi, b.POS[pp], f);
+    const uint32_t cnt = fi != 0 ? (b.NBRN[p] & NBRN_COUNT) : 0u;
     int32_t fx = 0, fy = 0;
-    if (fi != 0) {
-      // one neighbour ahead (record and old position), two ahead (index): a
-      // friction row is one thread per particle, so the gathers would
-      // otherwise form one serial chain of dependent loads
-      uint32_t en = cnt > 0u ? b.NBR[p] : 0u;
-      int4 on = b.PL[en & ~NBR_BOUNDARY];
-      int2 sn = b.POS[en & ~NBR_BOUNDARY];
-      uint32_t en2 = cnt > 1u ? b.NBR[(size_t)stride + p] : 0u;
-      for (uint32_t k = 0; k < cnt; ++k) {
-        const uint32_t e = en;
-        const int4 o = on;
-        const int2 so = sn;
-        if (k + 1u < cnt) {
-          en = en2;
-          on = b.PL[en & ~NBR_BOUNDARY];
-          sn = b.POS[en & ~NBR_BOUNDARY];
-        }
-        if (k + 2u < cnt) en2 = b.NBR[(size_t)(k + 2u) * stride + p];
-        if (rigidI && !(e & NBR_BOUNDARY) && same_body(info, (uint32_t)o.w)) continue;
-        int2 pq = xy(o);
-        int2 d = pdelta(pi, pq, f);
-        int id = lut_index(d, f);
-        if (id < 0) continue;
-        int32_t d4x = shr_rne<FPRE>(d.x), d4y = shr_rne<FPRE>(d.y);
-        int32_t d2 = wadd(wmul(d4x, d4x), wmul(d4y, d4y));
-        if (d2 < D2_FLOOR) continue;
-        int2 rel = dxi;
-        int32_t mu = fi;
-        if (!(e & NBR_BOUNDARY)) {
-          int2 dq = delta(pq, so, f);
-          rel = make_int2(sub_sat(dxi.x, dq.x, f), sub_sat(dxi.y, dq.y, f));
-          mu = mat_mix(fi, matw(b, (uint32_t)o.w & INFO_MAT, M_fric));
-        }
-        if (mu == 0) continue;
-        int32_t r4x = shr_rne<RPRE>(rel.x), r4y = shr_rne<RPRE>(rel.y);
-        int32_t dot = wadd(wmul(d4x, r4x), wmul(d4y, r4y));
-        int32_t qq = divshift<16>(dot, d2, b.rcp, f);
-        int32_t tx = sub_sat(r4x, mul<16>(d4x, qq, f), f);
-        int32_t ty = sub_sat(r4y, mul<16>(d4y, qq, f), f);
-        int32_t wq = shr_rne<4>(__ldg(b.WG + id).x);
-        int32_t sx = mul<16>(mul<5>(tx, wq, f), mu, f);
-        int32_t sy = mul<16>(mul<5>(ty, wq, f), mu, f);
-        fx = wsub(fx, clampi(sx, -FR_TERM, FR_TERM));
-        fy = wsub(fy, clampi(sy, -FR_TERM, FR_TERM));
+    // one neighbour ahead (record and old position), two ahead (index)
+    const uint32_t* np = b.NBR + pp;
+    uint32_t en = sub < cnt ? np[(size_t)sub * stride] : 0u;
+    int4 on = b.PL[en & ~NBR_BOUNDARY];
+    int2 sn = b.POS[en & ~NBR_BOUNDARY];
+    uint32_t en2 = sub + L < cnt ? np[(size_t)(sub + L) * stride] : 0u;
+    for (uint32_t k = sub; k < cnt; k += L) {
+      const uint32_t e = en;
+      const int4 o = on;
+      const int2 so = sn;
+      if (k + L < cnt) {
+        en = en2;
+        on = b.PL[en & ~NBR_BOUNDARY];
+        sn = b.POS[en & ~NBR_BOUNDARY];
       }
+      if (k + 2 * L < cnt) en2 = np[(size_t)(k + 2 * L) * stride];
+      if (rigidI && !(e & NBR_BOUNDARY) && same_body(info, (uint32_t)o.w)) continue;
+      int2 pq = xy(o);
+      int2 d = pdelta(pi, pq, f);
+      int id = lut_index(d, f);
+      if (id < 0) continue;
+      int32_t d4x = shr_rne<FPRE>(d.x), d4y = shr_rne<FPRE>(d.y);
+      int32_t d2 = wadd(wmul(d4x, d4x), wmul(d4y, d4y));
+      if (d2 < D2_FLOOR) continue;
+      int2 rel = dxi;
+      int32_t mu = fi;
+      if (!(e & NBR_BOUNDARY)) {
+        int2 dq = delta(pq, so, f);
+        rel = make_int2(sub_sat(dxi.x, dq.x, f), sub_sat(dxi.y, dq.y, f));
+        mu = mat_mix(fi, matw(b, (uint32_t)o.w & INFO_MAT, M_fric));
+      }
+      if (mu == 0) continue;
+      int32_t r4x = shr_rne<RPRE>(rel.x), r4y = shr_rne<RPRE>(rel.y);
+      int32_t dot = wadd(wmul(d4x, r4x), wmul(d4y, r4y));
+      int32_t qq = divshift<16>(dot, d2, b.rcp, f);
+      int32_t tx = sub_sat(r4x, mul<16>(d4x, qq, f), f);
+      int32_t ty = sub_sat(r4y, mul<16>(d4y, qq, f), f);
+      int32_t wq = shr_rne<4>(__ldg(b.WG + id).x);
+      int32_t sx = mul<16>(mul<5>(tx, wq, f), mu, f);
+      int32_t sy = mul<16>(mul<5>(ty, wq, f), mu, f);
+      fx = wsub(fx, clampi(sx, -FR_TERM, FR_TERM));
+      fy = wsub(fy, clampi(sy, -FR_TERM, FR_TERM));
     }
+    if (L > 1) {
+      fx = gsum<L>(fx);
+      fy = gsum<L>(fy);
+    }
+    if (!act || sub != 0) continue;
     if (rigidI) {
       const int2 d0 = b.DP[p];
       b.DP[p] = make_int2(add_sat(d0.x, fx, f), add_sat(d0.y, fy, f));
       continue;
     }
+    const int32_t bondKi = matw(b, m, M_bondK);
     int32_t bx = 0, by = 0;
     if (bondKi != 0 && !(info & INFO_BURST)) {
       uint32_t slot = b.sslot[p];
