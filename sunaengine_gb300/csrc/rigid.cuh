@@ -264,10 +264,12 @@ __global__ void __launch_bounds__(RG_THREADS) k_rigid_step(Bufs b) {
 
 // rigid_seal_delta (src/sim.wgsl:2001-2051): the member's swept segment
 // against held seal particles in the cells its expanded AABB touches. Every
-// hit returns the same reversion, so the scan order does not matter.
+// hit returns the same reversion (pos - pred), so the scan is an existence
+// test and its order does not matter: lane `sub` of a group of L lanes tests
+// every L-th candidate of each cell, and the group ORs the answers.
 template <bool DBG>
-__device__ int2 rigid_seal_delta(const Bufs& b, const ScenePar& S, uint32_t p, int2 pos, int2 pr, int32_t tag,
-                                 const Flags<DBG>& f) {
+__device__ bool rigid_seal_hit(const Bufs& b, const ScenePar& S, uint32_t p, int2 pos, int2 pr, int32_t tag,
+                               uint32_t sub, uint32_t L, const Flags<DBG>& f) {
   const int32_t mx4 = shr_rne<BPRE>(sub_sat(pr.x, pos.x, f)), my4 = shr_rne<BPRE>(sub_sat(pr.y, pos.y, f));
   const int32_t ml2 = wadd(wmul(mx4, mx4), wmul(my4, my4));
   const int2 lo = cell_coord(S, make_int2(sub_sat(min(pos.x, pr.x), SEAL_REACH, f), sub_sat(min(pos.y, pr.y), SEAL_REACH, f)));
@@ -275,7 +277,7 @@ __device__ int2 rigid_seal_delta(const Bufs& b, const ScenePar& S, uint32_t p, i
   for (int32_t gy = lo.y; gy <= hi.y; ++gy)
     for (int32_t gx = lo.x; gx <= hi.x; ++gx) {
       const uint32_t key = key_of(S, gx, gy);
-      for (uint32_t t = b.cellStart[key]; t < b.cellStart[key + 1]; ++t) {
+      for (uint32_t t = b.cellStart[key] + sub; t < b.cellStart[key + 1]; t += L) {
         if (t == p) continue;
         const int4 o = b.PL[t];
         const uint32_t info = (uint32_t)o.w;
@@ -299,16 +301,16 @@ __device__ int2 rigid_seal_delta(const Bufs& b, const ScenePar& S, uint32_t p, i
           }
         }
         if (wadd(wmul(dx4, dx4), wmul(dy4, dy4)) < SEAL_R4 * SEAL_R4)
-          return make_int2(sub_sat(pos.x, pr.x, f), sub_sat(pos.y, pr.y, f));
+          return true;
       }
     }
-  return make_int2(0, 0);
+  return false;
 }
 
 // rigidSolve (src/sim.wgsl:3459-3573), after each iteration's friction pass.
 // `seal`: the world has seal-class rows (else no contact can exist).
 template <bool DBG>
-__global__ void __launch_bounds__(RG_THREADS) k_rigid_solve(Bufs b, int seal) {
+__global__ void __launch_bounds__(RG_THREADS, 1) k_rigid_solve(Bufs b, int seal) {
   Flags<DBG> f{b.dbg};
   __shared__ int32_t sh[RG_THREADS / 32][7];
   int32_t* R = b.rbody + (size_t)blockIdx.x * RG_BODY_WORDS;
@@ -319,15 +321,29 @@ __global__ void __launch_bounds__(RG_THREADS) k_rigid_solve(Bufs b, int seal) {
   const uint32_t first = (uint32_t)R[RB_FIRST], last = (uint32_t)R[RB_LAST], rsh = (uint32_t)R[RB_RSH];
   const int32_t cqx = R[RB_CQX], cqy = R[RB_CQY];
   int32_t v[7] = {0, 0, 0, 0, 0, 0, 0};  // fx, fy, thi, tlo, sn, sx, sy
-  for (uint32_t i = first + threadIdx.x; i <= last && i < S.nFluid; i += RG_THREADS) {
+  // With seal contacts possible, a body whose slot range leaves threads idle
+  // gives each member a group of L lanes for the contact search (debug builds
+  // keep one lane, so their event counts follow the sequential scan).
+  const uint32_t span = last >= first ? last - first + 1u : 0u;
+  uint32_t L = 1;
+  if (!DBG && seal)
+    while (L < 8u && span * (L * 2u) <= (uint32_t)RG_THREADS) L *= 2u;
+  const uint32_t lane = threadIdx.x & 31u, sub = threadIdx.x & (L - 1u);
+  const uint32_t gmask = ((1u << L) - 1u) << (lane & ~(L - 1u));
+  for (uint32_t base = first; base <= last && base < S.nFluid; base += RG_THREADS / L) {
+    const uint32_t i = base + threadIdx.x / L;
     const uint32_t slot = S.slotBase + i;
-    if (!rg_member(b, slot, tag)) continue;
-    const int32_t* w = b.state + (size_t)slot * 8;
-    const uint32_t p = b.inv[slot];
+    const bool mem = i <= last && i < S.nFluid && rg_member(b, slot, tag);
+    const int32_t* w = b.state + (size_t)(mem ? slot : S.slotBase) * 8;
+    const uint32_t p = mem ? b.inv[slot] : 0u;
+    const int2 pr = ld_pred(b.PL, p);
+    const int2 pos = make_int2(w[0], w[1]);
+    bool hit = seal && mem && rigid_seal_hit(b, S, p, pos, pr, tag, sub, L, f);
+    if (L > 1u) hit = (__ballot_sync(0xffffffffu, hit) & gmask) != 0u;
+    if (!mem || sub != 0u) continue;
     const int32_t dm = matw(b, (uint32_t)w[4], M_dpMax), dmN = neg_sat(dm, f);
     const int2 dp = b.DP[p];
-    const int2 pr = ld_pred(b.PL, p);
-    const int2 sd = seal ? rigid_seal_delta(b, S, p, make_int2(w[0], w[1]), pr, tag, f) : make_int2(0, 0);
+    const int2 sd = hit ? make_int2(sub_sat(pos.x, pr.x, f), sub_sat(pos.y, pr.y, f)) : make_int2(0, 0);
     const int32_t dx = clampi(shr_rne<8>(dp.x), dmN, dm), dy = clampi(shr_rne<8>(dp.y), dmN, dm);
     v[0] = wadd(v[0], dx);
     v[1] = wadd(v[1], dy);
