@@ -296,15 +296,16 @@ int sn_batch_set_material(sn_batch* b, uint32_t row, const int32_t words[48], ui
 
 /* ---- lane autotuner ----------------------------------------------------------
  * No counterpart in the reference. The neighbour gathers of solveA, the colour
- * passes, post1, post2 and the neighbour-list build can split each particle's list over 1, 2, 4 or 8
- * lanes; results are identical for every choice, speed is not. With
+ * passes, post1, post2 and the neighbour-list build can split each particle's
+ * list over 1, 2, 4 or 8 lanes; the friction pass takes the colour passes'
+ * count. Results are identical for every choice, speed is not. With
  * opts.lanes == 0 each class starts from a rule on the active particle count
  * (re-applied when the scene set changes by more than 2x); sn_autotune runs
  * 4 x (reps + 1) REAL substeps of every loaded scene (the first of each lane
- * count untimed) (they advance the scenes and
- * their chains exactly like sn_step) under each lane count with phase timers
- * and keeps the fastest count per class. *substeps_run receives how many
- * substeps it ran. With opts.lanes != 0 the lanes are pinned and it runs none.
+ * count untimed; they advance the scenes and their chains exactly like
+ * sn_step) under each lane count with phase timers and keeps the fastest
+ * count per class. *substeps_run receives how many substeps it ran. With
+ * opts.lanes != 0 the lanes are pinned and it runs none.
  * sn_lanes reports {solveA, colours, post1, post2, neighbour lists}. */
 int sn_autotune(sn_engine* e, uint32_t reps, uint32_t* substeps_run);
 int sn_batch_autotune(sn_batch* b, uint32_t reps, uint32_t* substeps_run);
