@@ -638,6 +638,11 @@ struct World {
       k_colour<DBG, L><<<g, 256, 0, st>>>(b, c, src, dst);
     }
   }
+  template <bool DBG, int L>
+  void launch_contain_stress() {
+    k_contain_stress<DBG, L>
+        <<<grid_occ((const void*)k_contain_stress<DBG, L>, (uint64_t)hw.slotEnd * L), 256, 0, st>>>(b);
+  }
   // friction splits each list like the colour passes and takes their lanes
   template <bool DBG, int L>
   void launch_friction() {
@@ -724,7 +729,8 @@ struct World {
     if (hasBonds || nB) {
       SN_LANES(lc.p2, (launch_post2<DBG, false, L_>(0)));
       if (hasSeal) {
-        k_contain_stress<DBG><<<ga, 256, 0, st>>>(b);
+        // the members of seal bodies walk their lists: split them like friction
+        SN_LANES(nB ? lc.c : 1, (launch_contain_stress<DBG, L_>()));
         ++Lc;
       }
       if (nB) {

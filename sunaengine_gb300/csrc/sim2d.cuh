@@ -1085,25 +1085,33 @@ __global__ void __launch_bounds__(256) k_contain(Bufs b) {
 // sums nearby intrusion and, past its row's burstP, lets go (FLAG_BURST). It
 // writes only its own flags word and reads neighbours' positions and rows.
 // Walks slots (one coalesced read of the two words that decide) and visits
-// the neighbour list only for held seal particles.
-template <bool DBG>
+// the neighbour list only for held seal particles. L lanes share one slot's
+// list (the stress sum wraps, so any split is exact): a seal body's members
+// each walk a list, and the split shortens that serial gather chain.
+template <bool DBG, int L>
 __global__ void __launch_bounds__(256) k_contain_stress(Bufs b) {
   Flags<DBG> f{b.dbg};
   const uint32_t slotEnd = b.world->slotEnd, stride = b.nbrStride;
-  for (uint32_t slot = gtid(); slot < slotEnd; slot += gstride()) {
-    int32_t* w = b.state + (size_t)slot * 8;
+  const uint32_t sub = threadIdx.x & (L - 1), G = gstride() / L;
+  for (uint32_t slot = gtid() / L;; slot += G) {
+    if (__shfl_sync(0xffffffffu, slot, 0) >= slotEnd) break;  // warp-uniform exit
+    bool act = slot < slotEnd;
+    int32_t* w = b.state + (size_t)(act ? slot : 0u) * 8;
     const int2 mf = *reinterpret_cast<const int2*>(w + 4);
     const uint32_t mi = (uint32_t)mf.x, fl = (uint32_t)mf.y;
-    if (!(fl & (FLAG_ANCHOR | FLAG_RIGID))) continue;
-    const ScenePar& S = b.scenes[b.sceneOf[slot]];
-    if (!S.active || slot - S.slotBase >= S.nFluid) continue;
-    const int32_t burstP = matw(b, mi, M_burstP);
-    if (!seal_class(b, mi) || burstP <= 0) continue;
-    const uint32_t p = b.inv[slot];
-    const int32_t px = w[0], py = w[1];
-    const uint32_t cnt = b.NBRN[p] & NBRN_COUNT;
+    act = act && (fl & (FLAG_ANCHOR | FLAG_RIGID));
+    int32_t burstP = 0;
+    if (act) {
+      const ScenePar& S = b.scenes[b.sceneOf[slot]];
+      act = S.active && slot - S.slotBase < S.nFluid;
+      burstP = act ? matw(b, mi, M_burstP) : 0;
+      act = act && seal_class(b, mi) && burstP > 0;
+    }
+    const uint32_t p = act ? b.inv[slot] : 0u;
+    const int32_t px = act ? w[0] : 0, py = act ? w[1] : 0;
+    const uint32_t cnt = act ? (b.NBRN[p] & NBRN_COUNT) : 0u;
     int32_t stress = 0;
-    for (uint32_t k = 0; k < cnt; ++k) {
+    for (uint32_t k = sub; k < cnt; k += L) {
       const uint32_t e = b.NBR[(size_t)k * stride + p];
       if (e & NBR_BOUNDARY) continue;
       const int32_t* wj = b.state + (size_t)b.sslot[e] * 8;
@@ -1114,7 +1122,8 @@ __global__ void __launch_bounds__(256) k_contain_stress(Bufs b) {
       if (d2 >= SEAL_STRESS4 * SEAL_STRESS4) continue;
       stress = wadd(stress, SEAL_STRESS4 - (int32_t)isqrt32((uint32_t)d2));
     }
-    if ((int32_t)((uint32_t)stress << BPRE) > burstP)
+    if (L > 1) stress = gsum<L>(stress);
+    if (act && sub == 0 && (int32_t)((uint32_t)stress << BPRE) > burstP)
       w[5] = (int32_t)((fl & ~(FLAG_ANCHOR | FLAG_RIGID | WELD_TAG_MASK)) | FLAG_BURST);
   }
 }
