@@ -10,9 +10,10 @@
 // shared memory never see a conflicting write.
 //
 // Per pass: hist (per tile, per digit) -> exclusive scan of every digit's row
-// of tile counts (one CTA per digit) -> exclusive scan of the digit totals ->
-// scatter. The tile (512 threads x IT items) is picked per sort so that even a
-// few hundred thousand keys spread over ~128 CTAs.
+// of tile counts (one CTA per digit) -> scatter, whose prologue scans the
+// digit totals itself (one thread per digit). The tile (512 threads x IT
+// items) is picked per sort so that even a few hundred thousand keys spread
+// over ~128 CTAs.
 #pragma once
 #include <algorithm>
 #include <cstdint>
@@ -96,26 +97,6 @@ __global__ void __launch_bounds__(ROW_T) k_scan_rows(uint32_t* __restrict__ hist
   if (tid == 0) totals[blockIdx.x] = carry;
 }
 
-// Exclusive scan of the RADIX digit totals, one CTA of RADIX threads.
-__global__ void __launch_bounds__(RADIX) k_scan_totals(uint32_t* __restrict__ totals) {
-  __shared__ uint32_t ws[RADIX / 32];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const uint32_t v = totals[tid];
-  uint32_t x = v;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    uint32_t t = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= o) x += t;
-  }
-  if (lane == 31) ws[warp] = x;
-  __syncthreads();
-  uint32_t before = 0;
-#pragma unroll
-  for (int w = 0; w < RADIX / 32; ++w)
-    if (w < warp) before += ws[w];
-  totals[tid] = before + x - v;
-}
-
 // valsIn == nullptr means the values are the input indices (first pass).
 template <int IT>
 __global__ void __launch_bounds__(TPB) k_scatter(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ valsIn,
@@ -123,14 +104,26 @@ __global__ void __launch_bounds__(TPB) k_scatter(const uint32_t* __restrict__ ke
                                                  const uint32_t* __restrict__ totals, uint32_t numTiles,
                                                  uint32_t* __restrict__ keysOut, uint32_t* __restrict__ valsOut) {
   __shared__ uint32_t cnt[WARPS][RADIX + 1];
+  __shared__ uint32_t wsum[WARPS];
   int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   for (int i = tid; i < WARPS * (RADIX + 1); i += TPB) (&cnt[0][0])[i] = 0;
+  // exclusive scan of the digit totals (k_scan_rows left each row's sum)
+  const uint32_t tv = totals[tid];
+  uint32_t tx = tv;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xffffffffu, tx, o);
+    if (lane >= o) tx += t;
+  }
+  if (lane == 31) wsum[warp] = tx;
   __syncthreads();
+  uint32_t digitBase = tx - tv;
+  for (int w = 0; w < warp; ++w) digitBase += wsum[w];
   uint32_t tile = blockIdx.x, tileBase = tile * (TPB * IT);
   warp_counts<IT>(keys, n, shift, tileBase, cnt, warp, lane);
   __syncthreads();
   {
-    uint32_t run = totals[tid] + offs[(uint32_t)tid * numTiles + tile];
+    uint32_t run = digitBase + offs[(uint32_t)tid * numTiles + tile];
     for (int w = 0; w < WARPS; ++w) {
       uint32_t t = cnt[w][tid];
       cnt[w][tid] = run;
@@ -171,13 +164,12 @@ inline void sort_pass(const uint32_t* kin, const uint32_t* vin, uint32_t n, int 
   uint32_t* totals = hist + (size_t)RADIX * numTiles;
   k_hist<IT><<<numTiles, TPB, 0, st>>>(kin, n, shift, hist, numTiles);
   k_scan_rows<<<RADIX, ROW_T, 0, st>>>(hist, numTiles, totals);
-  k_scan_totals<<<1, RADIX, 0, st>>>(totals);
   k_scatter<IT><<<numTiles, TPB, 0, st>>>(kin, vin, n, shift, hist, totals, numTiles, ko, vo);
 }
 
 // Sort n pairs. keys0 is consumed; the result lands in (outKeys, outVals).
 // tmpK/tmpV are scratch of n words; hist needs hist_words(n) words.
-// Kernel launches: 4 per pass of RBITS key bits.
+// Kernel launches: 3 per pass of RBITS key bits.
 inline void sort_pairs(uint32_t* keys0, uint32_t n, int keyBits, uint32_t* outKeys, uint32_t* outVals,
                        uint32_t* tmpK, uint32_t* tmpV, uint32_t* hist, cudaStream_t st) {
   if (n == 0) return;
@@ -204,7 +196,7 @@ inline void sort_pairs(uint32_t* keys0, uint32_t n, int keyBits, uint32_t* outKe
   }
 }
 
-constexpr int LAUNCHES_PER_PASS = 4;
+constexpr int LAUNCHES_PER_PASS = 3;
 
 // Words of `hist` a sort of up to n keys needs (tile counts plus the digit totals).
 inline size_t hist_words(uint32_t n) {
