@@ -271,6 +271,22 @@ int sn_set_body_driver(sn_engine* e, uint32_t index, int32_t mask, const int32_t
 int sn_clear_body_drivers(sn_engine* e);
 int sn_drag_body(sn_engine* e, uint32_t tag, int32_t x, int32_t y, int32_t vx, int32_t vy, uint32_t* moved);
 int sn_restore_bodies(sn_engine* e, const int32_t* records, uint32_t count, const int32_t* rest, size_t rest_words);
+/* The body calls above on scene `id` of a batch (same arguments and results;
+ * body indices count that scene's bodies only). Removing the scene, or a
+ * load into it, drops its bodies; a checkpoint of a scene with bodies is
+ * refused, as on the plain engine. */
+int sn_batch_make_rigid_body(sn_batch* b, uint32_t id, const uint32_t* slots, uint32_t k, const int32_t* pivot,
+                             uint32_t user, int32_t* index);
+int sn_batch_promote_weld_group(sn_batch* b, uint32_t id, uint32_t tag, const int32_t* pivot, uint32_t user,
+                                int32_t* index);
+int sn_batch_dissolve_all_bodies(sn_batch* b, uint32_t id, uint32_t* count);
+int sn_batch_read_bodies(sn_batch* b, uint32_t id, int32_t* out, size_t words, uint32_t* count);
+int sn_batch_read_rest_offsets(sn_batch* b, uint32_t id, int32_t* out, size_t words);
+int sn_batch_set_body_user(sn_batch* b, uint32_t id, uint32_t index, uint32_t on, uint32_t* found);
+int sn_batch_set_body_driver(sn_batch* b, uint32_t id, uint32_t index, int32_t mask, const int32_t values[9]);
+int sn_batch_clear_body_drivers(sn_batch* b, uint32_t id);
+int sn_batch_drag_body(sn_batch* b, uint32_t id, uint32_t tag, int32_t x, int32_t y, int32_t vx, int32_t vy,
+                       uint32_t* moved);
 /* _writeBodyRecord (src/engine.js:5452) for host-side rebuilds that choose
  * their members themselves (splitDisconnectedBodies :6313,
  * promoteLooseRigidComponents :5636): members are taken as given, tag 0 draws

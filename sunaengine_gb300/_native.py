@@ -203,6 +203,16 @@ SIGNATURES = {
     'sn_drag_body': (ctypes.c_int, [P, u32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                     ctypes.POINTER(u32)]),
     'sn_restore_bodies': (ctypes.c_int, [P, P, u32, P, ctypes.c_size_t]),
+    'sn_batch_make_rigid_body': (ctypes.c_int, [P, u32, P, u32, P, u32, ctypes.POINTER(ctypes.c_int32)]),
+    'sn_batch_promote_weld_group': (ctypes.c_int, [P, u32, u32, P, u32, ctypes.POINTER(ctypes.c_int32)]),
+    'sn_batch_dissolve_all_bodies': (ctypes.c_int, [P, u32, ctypes.POINTER(u32)]),
+    'sn_batch_read_bodies': (ctypes.c_int, [P, u32, P, ctypes.c_size_t, ctypes.POINTER(u32)]),
+    'sn_batch_read_rest_offsets': (ctypes.c_int, [P, u32, P, ctypes.c_size_t]),
+    'sn_batch_set_body_user': (ctypes.c_int, [P, u32, u32, u32, ctypes.POINTER(u32)]),
+    'sn_batch_set_body_driver': (ctypes.c_int, [P, u32, u32, ctypes.c_int32, P]),
+    'sn_batch_clear_body_drivers': (ctypes.c_int, [P, u32]),
+    'sn_batch_drag_body': (ctypes.c_int, [P, u32, u32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                          ctypes.POINTER(u32)]),
     'sn_set_lanes': (ctypes.c_int, [P, P]),
     'sn_batch_set_lanes': (ctypes.c_int, [P, P]),
     'sn_set_material': (ctypes.c_int, [P, u32, P, ctypes.POINTER(u32)]),

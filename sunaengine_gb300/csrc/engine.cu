@@ -2407,6 +2407,58 @@ int sn_write_body(sn_engine* e, const uint32_t* members, uint32_t k, uint32_t ta
   if (!e || !index) return SN_E_INVALID;
   return rc_of(e->w, e->w.write_body(0, members, k, tag, pivot, user != 0, index, tag_out));
 }
+// The same body calls on one scene of a batch (bodies belong to their scene;
+// removing the scene drops them).
+#define SN_BATCH_SCENE(b, id) \
+  if (!(b) || (id) >= (b)->w.maxScenes) return SN_E_INVALID
+int sn_batch_make_rigid_body(sn_batch* b, uint32_t id, const uint32_t* slots, uint32_t k, const int32_t* pivot,
+                             uint32_t user, int32_t* index) {
+  SN_BATCH_SCENE(b, id);
+  if (!index) return SN_E_INVALID;
+  return rc_of(b->w, b->w.make_rigid_body(id, slots, k, pivot, user != 0, index));
+}
+int sn_batch_promote_weld_group(sn_batch* b, uint32_t id, uint32_t tag, const int32_t* pivot, uint32_t user,
+                                int32_t* index) {
+  SN_BATCH_SCENE(b, id);
+  if (!index) return SN_E_INVALID;
+  return rc_of(b->w, b->w.promote_weld_group(id, tag, pivot, user != 0, index));
+}
+int sn_batch_dissolve_all_bodies(sn_batch* b, uint32_t id, uint32_t* count) {
+  SN_BATCH_SCENE(b, id);
+  return rc_of(b->w, b->w.dissolve_all_bodies(id, count));
+}
+int sn_batch_read_bodies(sn_batch* b, uint32_t id, int32_t* out, size_t words, uint32_t* count) {
+  SN_BATCH_SCENE(b, id);
+  return rc_of(b->w, b->w.read_bodies(id, out, words, count));
+}
+int sn_batch_read_rest_offsets(sn_batch* b, uint32_t id, int32_t* out, size_t words) {
+  SN_BATCH_SCENE(b, id);
+  return rc_of(b->w, b->w.read_rest(id, out, words));
+}
+int sn_batch_set_body_user(sn_batch* b, uint32_t id, uint32_t index, uint32_t on, uint32_t* found) {
+  SN_BATCH_SCENE(b, id);
+  bool f = false;
+  const bool ok = b->w.set_body_user(id, index, on != 0, &f);
+  if (found) *found = f ? 1u : 0u;
+  return rc_of(b->w, ok);
+}
+int sn_batch_set_body_driver(sn_batch* b, uint32_t id, uint32_t index, int32_t mask, const int32_t values[9]) {
+  SN_BATCH_SCENE(b, id);
+  return rc_of(b->w, b->w.set_body_driver(id, index, mask, values));
+}
+int sn_batch_clear_body_drivers(sn_batch* b, uint32_t id) {
+  SN_BATCH_SCENE(b, id);
+  return rc_of(b->w, b->w.clear_body_drivers(id));
+}
+int sn_batch_drag_body(sn_batch* b, uint32_t id, uint32_t tag, int32_t x, int32_t y, int32_t vx, int32_t vy,
+                       uint32_t* moved) {
+  SN_BATCH_SCENE(b, id);
+  bool m = false;
+  const bool ok = b->w.drag_body(id, tag, x, y, vx, vy, &m);
+  if (moved) *moved = m ? 1u : 0u;
+  return rc_of(b->w, ok);
+}
+#undef SN_BATCH_SCENE
 int sn_set_material(sn_engine* e, uint32_t row, const int32_t words[48], uint32_t* mat_count) {
   if (!e) return SN_E_INVALID;
   const bool ok = e->w.set_material(row, words);

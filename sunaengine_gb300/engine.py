@@ -636,6 +636,71 @@ class Batch:
         self._check(self._lib.sn_batch_read_state(self._h, int(sid), _ptr(a), a.size), 'read_state')
         return a
 
+    # ---- rigid bodies of one scene (the Engine calls, src/engine.js:5319-6111) ----
+    def make_rigid_body(self, sid: int, slots, pivot=None, user: bool = False) -> Optional[int]:
+        """makeRigidBody on scene ``sid``; the index counts that scene's bodies."""
+        s = np.ascontiguousarray(np.asarray(slots, dtype=np.int64).reshape(-1).clip(0, 2**32 - 1).astype(np.uint32))
+        pv = Engine._pivot(pivot)
+        out = ctypes.c_int32()
+        self._check(self._lib.sn_batch_make_rigid_body(self._h, int(sid), _ptr(s), s.size, _ptr(pv),
+                                                       int(bool(user)), ctypes.byref(out)), 'makeRigidBody')
+        return None if out.value < 0 else int(out.value)
+
+    def make_axis_body(self, sid: int, slots, px: int, py: int, user: bool = False) -> Optional[int]:
+        return self.make_rigid_body(sid, slots, (px, py), user)
+
+    def promote_weld_group(self, sid: int, tag: int = 0, pivot=None, user: bool = False) -> Optional[int]:
+        pv = Engine._pivot(pivot)
+        out = ctypes.c_int32()
+        self._check(self._lib.sn_batch_promote_weld_group(self._h, int(sid), int(tag), _ptr(pv), int(bool(user)),
+                                                          ctypes.byref(out)), 'promoteWeldGroup')
+        return None if out.value < 0 else int(out.value)
+
+    def dissolve_all_bodies(self, sid: int) -> int:
+        out = ctypes.c_uint32()
+        self._check(self._lib.sn_batch_dissolve_all_bodies(self._h, int(sid), ctypes.byref(out)), 'dissolveAllBodies')
+        return int(out.value)
+
+    def body_count(self, sid: int) -> int:
+        out = ctypes.c_uint32()
+        self._check(self._lib.sn_batch_read_bodies(self._h, int(sid), None, 0, ctypes.byref(out)), 'readBodies')
+        return int(out.value)
+
+    def read_bodies(self, sid: int) -> np.ndarray:
+        nb = self.body_count(sid)
+        a = np.zeros(max(1, nb) * 32, np.int32)
+        out = ctypes.c_uint32()
+        self._check(self._lib.sn_batch_read_bodies(self._h, int(sid), _ptr(a), a.size, ctypes.byref(out)),
+                    'readBodies')
+        return a[:int(out.value) * 32].reshape(-1, 32)
+
+    def read_rest_offsets(self, sid: int) -> np.ndarray:
+        n = self.info(sid)['n']
+        a = np.zeros(max(1, n) * 2, np.int32)
+        self._check(self._lib.sn_batch_read_rest_offsets(self._h, int(sid), _ptr(a), a.size), 'readRestOffsets')
+        return a[:n * 2]
+
+    def set_body_user(self, sid: int, index: int, on: bool) -> bool:
+        out = ctypes.c_uint32()
+        self._check(self._lib.sn_batch_set_body_user(self._h, int(sid), int(index), int(bool(on)), ctypes.byref(out)),
+                    'setBodyUser')
+        return bool(out.value)
+
+    def set_body_driver(self, sid: int, index: int, mask: int, values):
+        v = np.zeros(9, np.int32)
+        v[:len(values)] = np.asarray(values, dtype=np.int64).clip(-2**31, 2**31 - 1)
+        self._check(self._lib.sn_batch_set_body_driver(self._h, int(sid), int(index), int(mask), _ptr(v)),
+                    'setBodyConstraint')
+
+    def clear_body_drivers(self, sid: int):
+        self._check(self._lib.sn_batch_clear_body_drivers(self._h, int(sid)), 'clearBodyConstraints')
+
+    def drag_body(self, sid: int, tag: int, x: int, y: int, vx: int = 0, vy: int = 0) -> bool:
+        out = ctypes.c_uint32()
+        self._check(self._lib.sn_batch_drag_body(self._h, int(sid), int(tag), int(x), int(y), int(vx), int(vy),
+                                                 ctypes.byref(out)), 'dragGrab')
+        return bool(out.value)
+
     def read_scratch(self, sid: int) -> np.ndarray:
         n = self.info(sid)['n']
         a = np.zeros(n * 2, np.int32)

@@ -232,3 +232,37 @@ def test_exact_suna_save_loads_on_both_engines():
     assert np.array_equal(g.read_state(), r.read_state()) and np.array_equal(g.read_state(), e.read_state())
     assert np.array_equal(g.read_bodies(), r.read_bodies())
     assert np.array_equal(g.debug_counters(), r.debug_counters())
+
+
+def test_bodies_in_a_batch_match_each_scene_alone():
+    """Rigid bodies in a batched world: two rigid tanks (different seeds, one
+    with a held rail, one with a driven wheel) in one batch, each against its
+    own oracle; removing the first keeps the second exact."""
+    from sunaengine_gb300.engine import Batch
+    a = scenes.rigid_tank(seed=0x1111)
+    c = scenes.rigid_tank(seed=0x2222, rail=False)
+    bt = Batch(max_particles=a.n + c.n + 512, max_scenes=3)
+    ia, ic = bt.add_scene(a), bt.add_scene(c)
+    ra, rc = t.oracle(a, threads=16), t.oracle(c, threads=16)
+    assert bt.make_rigid_body(ia, a.meta['plank']) == 0 and ra.make_rigid_body(a.meta['plank']) == 0
+    assert bt.make_rigid_body(ia, a.meta['wheel']) == 1 and ra.make_rigid_body(a.meta['wheel']) == 1
+    cx, cy = c.meta['wheel_centre']
+    assert bt.make_axis_body(ic, c.meta['wheel'], cx, cy) == 0 and rc.make_axis_body(c.meta['wheel'], cx, cy) == 0
+    spin = [0, 0, 0, 0, 0, 40000, 0, 0, 0]                # RD_HAS_W (32): drive the wheel's spin
+    bt.set_body_driver(ic, 0, 32, spin)
+    rc.set_body_driver(0, 32, spin)
+    assert bt.body_count(ia) == 2 and bt.body_count(ic) == 1
+    for k in (5, 20, 35):
+        bt.step(k)
+        ra.step(k)
+        rc.step(k)
+        assert bt.chain_hex(ia) == ra.chain_hex() and bt.chain_hex(ic) == rc.chain_hex()
+    assert np.array_equal(bt.read_bodies(ia), ra.read_bodies())
+    assert np.array_equal(bt.read_bodies(ic), rc.read_bodies())
+    assert np.array_equal(bt.read_rest_offsets(ic), rc.read_rest_offsets())
+    bt.remove_scene(ia)
+    bt.step(20)
+    rc.step(20)
+    assert bt.chain_hex(ic) == rc.chain_hex()
+    assert np.array_equal(bt.read_bodies(ic), rc.read_bodies())
+    bt.check_errors()
