@@ -258,7 +258,7 @@ int sn_set_user_drive(sn_engine* e, int32_t ax, int32_t ay, int32_t out[2]);
  * Index arguments and *index results are the body's position in readBodies;
  * *index = -1 where the reference returns null (too few members, no slot).
  * eraseWhere repairs the bodies (survivors keep their rest offsets); a scene
- * load dissolves them; checkpoints of a scene with bodies are refused. */
+ * load dissolves them; a device checkpoint carries them. */
 int sn_make_rigid_body(sn_engine* e, const uint32_t* slots, uint32_t k, const int32_t* pivot, uint32_t user,
                        int32_t* index);
 int sn_promote_weld_group(sn_engine* e, uint32_t tag, const int32_t* pivot, uint32_t user, int32_t* index);
@@ -273,8 +273,7 @@ int sn_drag_body(sn_engine* e, uint32_t tag, int32_t x, int32_t y, int32_t vx, i
 int sn_restore_bodies(sn_engine* e, const int32_t* records, uint32_t count, const int32_t* rest, size_t rest_words);
 /* The body calls above on scene `id` of a batch (same arguments and results;
  * body indices count that scene's bodies only). Removing the scene, or a
- * load into it, drops its bodies; a checkpoint of a scene with bodies is
- * refused, as on the plain engine. */
+ * load into it, drops its bodies; a device checkpoint carries them. */
 int sn_batch_make_rigid_body(sn_batch* b, uint32_t id, const uint32_t* slots, uint32_t k, const int32_t* pivot,
                              uint32_t user, int32_t* index);
 int sn_batch_promote_weld_group(sn_batch* b, uint32_t id, uint32_t tag, const int32_t* pivot, uint32_t user,
@@ -443,7 +442,9 @@ int sn3_profile_substep(sn3_engine* e, uint32_t reps, float* ms, uint32_t max_ph
  * checkpoint of a scene (2D: state, scratch, chain, bond rows and the
  * formation/substep clocks; 3D: state, chain and the substep clock) is copied
  * into it on the engine's stream without a host round trip and restored the
- * same way. Loading a checkpoint into a scene rewinds (or advances) that
+ * same way. A 2D scene's rigid bodies travel too: their rest offsets in the
+ * pool, their records and drivers on the host (saving and loading such a
+ * scene waits for the stream once). Loading a checkpoint into a scene rewinds (or advances) that
  * scene exactly: every later substep equals the one after the save. A 2D
  * checkpoint loads only into a scene with the same n and n_fluid. The pool
  * orders copies across engines with events, so one pool may serve several

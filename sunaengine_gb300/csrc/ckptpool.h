@@ -10,6 +10,7 @@
 #include <map>
 #include <string>
 #include <unordered_map>
+#include <vector>
 
 struct sn_ckpt_pool {
   struct Rec {
@@ -19,6 +20,10 @@ struct sn_ckpt_pool {
     uint64_t substeps = 0, formClock = 0;
     uint32_t dirty = 0;
     cudaEvent_t done = nullptr;
+    // a 2D scene's rigid bodies: their records and driver sidecars travel on
+    // the host (a few hundred bytes each), their rest offsets in the pool
+    uint32_t nBodies = 0;
+    std::vector<int32_t> bodyRec, bodyDrv;
   };
   int device = 0;
   char* base = nullptr;

@@ -1658,6 +1658,16 @@ struct World {
     if (nb > (uint32_t)RG_MAX_BODIES || (nb && !records)) return fail("bad body records");
     if (rest && restWords > (size_t)sh[s].cap * 2) return fail("rest offsets exceed the scene's slots");
     std::vector<int32_t> rec(records, records + (size_t)nb * RG_BODY_WORDS), drv((size_t)nb * RG_DRIVER_WORDS, 0);
+    if (rest && restWords &&
+        (!cuda_ok(cudaMemcpyAsync(b.rest + sh[s].slotBase, rest, restWords * 4, cudaMemcpyHostToDevice, st), "rest") ||
+         !cuda_ok(cudaStreamSynchronize(st), "rest")))
+      return false;
+    return bodies_from_records(s, rec, drv);
+  }
+  // Scene s's bodies become the given records (their scene word set to s)
+  // and driver sidecars.
+  bool bodies_from_records(uint32_t s, std::vector<int32_t> rec, const std::vector<int32_t>& drv) {
+    const uint32_t nb = (uint32_t)(rec.size() / RG_BODY_WORDS);
     std::vector<BodyHost> desc(nb);
     for (uint32_t k = 0; k < nb; ++k) {
       int32_t* R = rec.data() + (size_t)k * RG_BODY_WORDS;
@@ -1666,10 +1676,6 @@ struct World {
       desc[k].last = (uint32_t)R[RB_LAST]; desc[k].n = (uint32_t)R[RB_N];
       desc[k].axis = R[RB_AXIS] != 0; desc[k].user = R[RB_USER] != 0;
     }
-    if (rest && restWords &&
-        (!cuda_ok(cudaMemcpyAsync(b.rest + sh[s].slotBase, rest, restWords * 4, cudaMemcpyHostToDevice, st), "rest") ||
-         !cuda_ok(cudaStreamSynchronize(st), "rest")))
-      return false;
     return replace_scene_bodies(s, rec, drv, desc);
   }
   // eraseWhere's body repair (src/engine.js:6526-6610), on the host copy of
@@ -1878,14 +1884,17 @@ struct World {
 
   // Device checkpoint of scene s: [state n*8][stAcc n*2][chain 8][bond rows nFluid*48 when the
   // world has bonding rows], copied on the engine stream.
+  // Pool layout of a 2D checkpoint: state (n x 32 B), stAcc (n x 8 B), the
+  // chain (32 B), bond rows when the world has bonds, rest offsets (n x 8 B)
+  // when the scene has rigid bodies.
   size_t ckpt_bytes(uint32_t s) const {
     const SceneHost& h = sh[s];
-    return (size_t)h.n * 40 + 32 + (hasBonds ? (size_t)h.nFluid * BOND_CAP * 4 : 0);
+    return (size_t)h.n * 40 + 32 + (hasBonds ? (size_t)h.nFluid * BOND_CAP * 4 : 0) +
+           (scene_bodies(s) ? (size_t)h.n * 8 : 0);
   }
   bool ckpt_save(uint32_t s, sn_ckpt_pool* pool, uint64_t* handle) {
     SceneHost& h = sh[s];
     if (!h.loaded) return fail("checkpoint of a scene that is not loaded");
-    if (scene_bodies(s) != 0) return fail("checkpoints of scenes with rigid bodies are not supported");
     if (pool->device != device) return fail("checkpoint pool is on device %d, the engine on %d", pool->device, device);
     if (layoutDirty && !relayout()) return false;
     if (!pull_params()) return false;
@@ -1899,6 +1908,21 @@ struct World {
     if (ok && hasBonds)
       ok = cuda_ok(cudaMemcpyAsync(d + n * 40 + 32, b.bond + (size_t)h.slotBase * BOND_CAP,
                                    (size_t)h.nFluid * BOND_CAP * 4, cudaMemcpyDeviceToDevice, st), "ckpt");
+    r->nBodies = scene_bodies(s);
+    r->bodyRec.clear();
+    r->bodyDrv.clear();
+    if (ok && r->nBodies) {
+      const size_t restOff = n * 40 + 32 + (hasBonds ? (size_t)h.nFluid * BOND_CAP * 4 : 0);
+      ok = cuda_ok(cudaMemcpyAsync(d + restOff, b.rest + h.slotBase, n * 8, cudaMemcpyDeviceToDevice, st), "ckpt");
+      std::vector<int32_t> rec, drv;
+      ok = ok && read_records(rec, drv);
+      for (size_t i = 0; ok && i < bodies.size(); ++i) {
+        if (bodies[i].scene != s) continue;
+        r->bodyRec.insert(r->bodyRec.end(), rec.begin() + i * RG_BODY_WORDS, rec.begin() + (i + 1) * RG_BODY_WORDS);
+        r->bodyDrv.insert(r->bodyDrv.end(), drv.begin() + i * RG_DRIVER_WORDS,
+                          drv.begin() + (i + 1) * RG_DRIVER_WORDS);
+      }
+    }
     r->n = h.n;
     r->nFluid = h.nFluid;
     r->hasBonds = hasBonds ? 1u : 0u;
@@ -1935,8 +1959,14 @@ struct World {
                                    cudaMemcpyDeviceToDevice, st), "load");
     else if (ok)
       ok = cuda_ok(cudaMemsetAsync(bondRows, 0, (size_t)h.nFluid * BOND_CAP * 4, st), "load");
+    if (ok && r->nBodies) {
+      const size_t restOff = n * 40 + 32 + (r->hasBonds ? (size_t)h.nFluid * BOND_CAP * 4 : 0);
+      ok = cuda_ok(cudaMemcpyAsync(b.rest + h.slotBase, d + restOff, n * 8, cudaMemcpyDeviceToDevice, st), "load");
+    }
     cudaEventRecord(r->done, st);
     if (!ok) return false;
+    // the scene's bodies become the checkpoint's (none if it had none)
+    if ((r->nBodies || scene_bodies(s)) && !bodies_from_records(s, r->bodyRec, r->bodyDrv)) return false;
     h.substeps = r->substeps;
     hpar[s].formClock = (uint32_t)r->formClock;
     hpar[s].bondDirty = r->dirty;

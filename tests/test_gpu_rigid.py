@@ -266,3 +266,41 @@ def test_bodies_in_a_batch_match_each_scene_alone():
     assert bt.chain_hex(ic) == rc.chain_hex()
     assert np.array_equal(bt.read_bodies(ic), rc.read_bodies())
     bt.check_errors()
+
+
+def test_device_checkpoint_carries_bodies():
+    """A checkpoint of a scene with bodies (records, drivers, rest offsets)
+    rewinds it exactly: replaying from it repeats the chain and the body
+    records, also after the bodies were dissolved in between; a checkpoint
+    taken before the bodies existed removes them again."""
+    from sunaengine_gb300.checkpoints import CheckpointPool
+    from sunaengine_gb300.engine import Batch
+    a = scenes.rigid_tank(seed=0x3333)
+    bt = Batch(max_particles=a.n + 256, max_scenes=2)
+    ia = bt.add_scene(a)
+    pool = CheckpointPool(64 << 20)
+    h0 = bt.ckpt_save(ia, pool)                   # no bodies yet
+    bt.make_rigid_body(ia, a.meta['plank'])
+    cx, cy = a.meta['wheel_centre']
+    bt.make_axis_body(ia, a.meta['wheel'], cx, cy)
+    bt.set_body_driver(ia, 1, 32, [0, 0, 0, 0, 0, 30000, 0, 0, 0])
+    bt.step(15)
+    h1 = bt.ckpt_save(ia, pool)
+    bt.step(40)
+    want = (bt.chain_hex(ia), bt.read_bodies(ia).copy(), bt.read_rest_offsets(ia).copy())
+    bt.dissolve_all_bodies(ia)
+    bt.step(5)
+    bt.ckpt_load(ia, pool, h1)
+    assert bt.body_count(ia) == 2
+    bt.step(40)
+    assert bt.chain_hex(ia) == want[0]
+    assert np.array_equal(bt.read_bodies(ia), want[1])
+    assert np.array_equal(bt.read_rest_offsets(ia), want[2])
+    bt.ckpt_load(ia, pool, h0)
+    assert bt.body_count(ia) == 0
+    r = t.oracle(a, threads=16)
+    bt.step(10)
+    r.step(10)
+    assert bt.chain_hex(ia) == r.chain_hex()
+    bt.check_errors()
+    pool.close()
