@@ -337,15 +337,7 @@ __global__ void __launch_bounds__(256) k_predict_key(Bufs b) {
 
 // cellStart[k] = first sorted position whose key is >= k, for k in [0, K].
 __global__ void __launch_bounds__(256) k_cellstart(Bufs b) {
-  const uint32_t K = b.world->K, n = b.world->slotEnd;
-  for (uint32_t k = gtid(); k <= K; k += gstride()) {
-    uint32_t lo = 0, hi = n;
-    while (lo < hi) {
-      uint32_t mid = (lo + hi) >> 1;
-      if (b.skey[mid] < k) lo = mid + 1; else hi = mid;
-    }
-    b.cellStart[k] = lo;
-  }
+  cell_starts(b.skey, b.world->slotEnd, b.world->K, b.cellStart);
 }
 
 // Move the working set into sorted space.

@@ -161,15 +161,7 @@ __global__ void __launch_bounds__(256) k3_predict(Bufs3 b) {
 
 // cellStart[k] = first sorted index with key >= k, for k in [0, K].
 __global__ void __launch_bounds__(256) k3_cellstart(Bufs3 b) {
-  const uint32_t K = b.world->K, n = b.world->slotEnd;
-  for (uint32_t k = gtid3(); k <= K; k += gstride3()) {
-    uint32_t lo = 0, hi = n;
-    while (lo < hi) {
-      uint32_t mid = (lo + hi) >> 1;
-      if (b.skey[mid] < k) lo = mid + 1; else hi = mid;
-    }
-    b.cellStart[k] = lo;
-  }
+  cell_starts(b.skey, b.world->slotEnd, b.world->K, b.cellStart);
 }
 
 __global__ void __launch_bounds__(256) k3_gather(Bufs3 b) {

@@ -59,4 +59,35 @@ struct WorldPar {
   uint32_t nBodies;        // §20 body records (all scenes)
 };
 
+#ifdef __CUDACC__
+// cellStart[k] = first sorted position whose key is >= k, for k in [0, K],
+// over the n sorted keys. Each CTA (256 threads) first loads 256 pivots,
+// skey[j * n / 256], into shared memory; a key's answer lies between the last
+// pivot below it and the first at or above it, so the search takes 8 steps in
+// shared memory and about log2(n / 256) dependent global loads instead of
+// log2(n). Every thread of the CTA must call it.
+__device__ __forceinline__ void cell_starts(const uint32_t* __restrict__ skey, uint32_t n, uint32_t K,
+                                            uint32_t* __restrict__ cellStart) {
+  __shared__ uint32_t piv[256];
+  const uint32_t j = threadIdx.x;
+  const uint32_t pos = (uint32_t)(((uint64_t)j * n) >> 8);
+  piv[j] = n ? skey[pos] : 0xffffffffu;
+  __syncthreads();
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k <= K; k += gridDim.x * blockDim.x) {
+    uint32_t c = 0;  // pivots below k
+#pragma unroll
+    for (uint32_t step = 128; step; step >>= 1)
+      if (piv[c + step - 1] < k) c += step;
+    if (c == 255u && piv[255] < k) c = 256u;
+    uint32_t lo = c ? (uint32_t)(((uint64_t)(c - 1) * n) >> 8) + 1u : 0u;
+    uint32_t hi = c < 256u ? (uint32_t)(((uint64_t)c * n) >> 8) : n;
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (skey[mid] < k) lo = mid + 1; else hi = mid;
+    }
+    cellStart[k] = lo;
+  }
+}
+#endif
+
 }  // namespace sn
