@@ -2,6 +2,7 @@
 with world_size-2 gloo ranks on the CPU."""
 import json
 import os
+import re
 import socket
 import subprocess
 import sys
@@ -38,12 +39,14 @@ def test_max_over_ranks_and_barrier(tmp_path):
         ws, rank, local, dist = bench._dist()
         bench._barrier(dist)
         m = bench._max_over_ranks(dist, 10.0 + 5 * rank, local)
-        print(json.dumps({{"rank": rank, "ws": ws, "max": m, "backend": dist.get_backend()}}), flush=True)
+        sys.stdout.write(json.dumps({{"rank": rank, "ws": ws, "max": m, "backend": dist.get_backend()}}) + "\\n")
+        sys.stdout.flush()
         dist.destroy_process_group()
     '''))
     r = torchrun([str(script)])
     assert r.returncode == 0, r.stderr[-2000:]
-    lines = [json.loads(l) for l in r.stdout.splitlines() if l.startswith('{')]
+    # the two ranks share one stdout, so their lines may arrive run together
+    lines = [json.loads(x) for x in re.findall(r'\{[^{}]*\}', r.stdout)]
     assert sorted(l['rank'] for l in lines) == [0, 1]
     assert all(l['ws'] == 2 and l['max'] == 15.0 and l['backend'] == 'gloo' for l in lines)
 
