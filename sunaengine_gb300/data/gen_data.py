@@ -168,4 +168,6 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == '__main__':
-    main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference')
+    if len(sys.argv) != 2:
+        sys.exit('usage: python gen_data.py <path of a SunaEngine checkout>')
+    main(sys.argv[1])

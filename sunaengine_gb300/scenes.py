@@ -508,13 +508,20 @@ def batch_scenes(count: int = 256, seed: int = 0xba7c4, n_lo: int = 1024, n_hi: 
                  substeps: int = 1000):
     """Batched workload: ``count`` independent scenes, particle counts log-uniform
     in [n_lo, n_hi], aspect ratios uniform in [0.5, 2], each with its own stir
-    schedule. Returns (scenes, schedules)."""
+    schedule. Returns (scenes, schedules).
+
+    The scenes come from one seeded stream and each schedule from a stream of
+    its own (seeded by the workload seed and the scene index), so the scenes do
+    not depend on ``substeps`` and a shorter schedule is a prefix of a longer
+    one: scene ``i`` is the same scene in a 60-substep test and a 1000-substep
+    run.
+    """
     rng = np.random.Generator(np.random.PCG64(seed))
     scenes, sched = [], []
-    for _ in range(count):
+    for sid in range(count):
         n = int(round(math.exp(rng.uniform(math.log(n_lo), math.log(n_hi)))))
         aspect = float(rng.uniform(0.5, 2.0))
         sc = jittered_block(n, aspect, rng)
         scenes.append(sc)
-        sched.append(stir_schedule(sc, substeps, rng))
+        sched.append(stir_schedule(sc, substeps, np.random.Generator(np.random.PCG64([seed, sid]))))
     return scenes, sched
