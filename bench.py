@@ -43,6 +43,7 @@ sys.path.insert(0, str(ROOT))
 import numpy as np  # noqa: E402
 
 METRIC = 'particle-substeps/s'
+FULL_SUBSTEPS = 1000  # the stated length of the 2D workloads
 UNIT = 'particle-substeps/s'
 WORKLOAD = ('2D large scene: 1,048,576 fluid particles (1024x1024 lattice, 1 wu, +/-0.25 wu seeded jitter), '
             'WATER/OIL 64-column bands, temps U[10,90] deg, ITERS 4, H_slot every substep')
@@ -161,6 +162,30 @@ BYTES = {
 }
 
 
+# The oracle's recorded chains of the workloads at their full lengths
+# (tests/golden/make_config_vectors.py): a run's chain after substep k equals
+# the recorded one only if every digest up to k matched.
+VECTORS = ROOT / 'tests' / 'golden' / 'config_vectors'
+
+
+def recorded_chain(workload: str, k: int):
+    """The oracle's chain of `workload` after substep k, or None when k is not recorded."""
+    p = VECTORS / f'{workload}.json'
+    if not p.exists() or k <= 0:
+        return None
+    d = json.loads(p.read_text())
+    chain = d.get('chain')
+    if isinstance(chain, list):
+        return chain[k - 1] if k <= len(chain) else None
+    return None
+
+
+def parity_against(workload: str, k: int, got: str):
+    want = recorded_chain(workload, k)
+    return {'checked_at_substep': k, 'ok': (got == want) if want is not None else None,
+            'against': f'tests/golden/config_vectors/{workload}.json' if want is not None else 'not recorded'}
+
+
 # ncu summaries under profiles/ that carry the DRAM traffic of a dominant kernel
 PROFILE_OF = {'colour x4': 'k_colour_2d_large.md', 'solve+apply': 'k3_solve_3d_dam.md', 'density': 'k3_density_3d_dam.md'}
 
@@ -258,6 +283,7 @@ def workload_3d(steps: int, warmup: int, device: int, cpu_seconds: float = 6.0, 
     e.sync()
     ms, launches = e.last_timing()
     value = sc.n * steps / (ms / 1e3)
+    parity = parity_against('dam3d_64cubed', warmup + steps, e.chain_hex())
     names = ['predict', 'grid sort', 'cell ranges + gather', 'neighbour lists']
     names += ['density', 'solve+apply'] * e.iters + ['integrate+hash', 'fold']
     ph = e.profile_substep(max(3, min(steps, 10)))
@@ -290,7 +316,7 @@ def workload_3d(steps: int, warmup: int, device: int, cpu_seconds: float = 6.0, 
     wall = time.perf_counter() - t0
     e2.close()
     out = {'workload': WORKLOAD_3D, 'particles': sc.n, 'steps': steps, 'value': value, 'unit': UNIT,
-           'ms_per_step': ms / steps, 'gpu_launches': int(launches), 'roofline': roof,
+           'ms_per_step': ms / steps, 'gpu_launches': int(launches), 'roofline': roof, 'parity': parity,
            'e2e': {'value': sc.n * steps / wall, 'unit': UNIT, 'h2d_bytes_per_step': sc.n * 28 / steps,
                    'd2h_bytes_per_step': 32 + final.nbytes / steps}}
     if with_cpu:
@@ -354,6 +380,26 @@ def batched_workload(steps: int, warmup: int, device: int, plain_sample: int = 2
     b.check_errors()
     batched = nf * steps / (ms / 1e3)
     lanes_b = b.lanes()
+    # parity: advance (untimed) to the next substep the oracle's sample recorded
+    # and compare those scenes' chains
+    parity = {'ok': None, 'against': 'not recorded'}
+    vp = VECTORS / 'batch_256.json'
+    if vp.exists() and seed == 0xba7c4:
+        vec = json.loads(vp.read_text())
+        every = vec['every']
+        at = -(-(warmup + steps) // every) * every
+        if at <= vec['substeps']:
+            scs_full, sched_full = scenes.batch_scenes(count=256, seed=seed, substeps=at)
+            # the schedules drawn for `at` substeps extend the ones loaded (a prefix)
+            for sid, ev in enumerate(sched_full):
+                for (t_at, cx, cy, r, ix, iy) in ev:
+                    if t_at >= warmup + steps:
+                        b.schedule_impulse(sid, t_at, cx, cy, r, ix, iy)
+            b.step(at - (warmup + steps))
+            bad = [sid for sid, rec in vec['scenes'].items()
+                   if str(at) in rec['chain'] and b.chain_hex(int(sid)) != rec['chain'][str(at)]]
+            parity = {'checked_at_substep': at, 'ok': not bad, 'scenes_checked': len(vec['scenes']),
+                      'mismatched': bad, 'against': 'tests/golden/config_vectors/batch_256.json'}
     b.destroy()
     # plain path on a sample of the same scenes, one engine per scene, sequentially
     rng = np.random.Generator(np.random.PCG64(seed ^ 0x5a5a))
@@ -374,7 +420,7 @@ def batched_workload(steps: int, warmup: int, device: int, plain_sample: int = 2
     return {'scenes': len(scs), 'particles': int(nf), 'value': batched, 'unit': UNIT,
             'ms_per_step': ms / steps, 'gpu_launches_per_step': launches // max(1, steps),
             'plain_same_scenes': plain, 'plain_sample_scenes': int(len(pick)), 'lanes': lanes_b,
-            'batched_vs_plain': batched / plain}
+            'batched_vs_plain': batched / plain, 'parity': parity}
 
 
 def construction_workload(steps: int, warmup: int, device: int, with_cpu: bool = True, cpu_seconds: float = 4.0):
@@ -488,6 +534,7 @@ def ours(args):
     dev_ms, launches = e.last_timing()
     lanes_used = e.lanes()
     e.check_errors()
+    parity = parity_against('two_fluid_1024', args.warmup + args.steps, e.chain_hex())
     dev_ms = _max_over_ranks(dist, dev_ms, local)
     ms_step = dev_ms / args.steps
     value = ws * sc.nFluid * args.steps / (dev_ms / 1e3)
@@ -541,13 +588,35 @@ def ours(args):
     e2.destroy()
     e.destroy()
 
+    # The whole stated run: all FULL_SUBSTEPS substeps of the workload from its
+    # load, device-timed, and its chain against the oracle's at the last one.
+    full = None
+    if not args.no_full:
+        e3 = Engine(max_particles=sc.n, max_cells=1 << 20, device=local)
+        if lanes_pick is not None:
+            e3.set_lanes(lanes_pick)
+        e3.load_scene(sc)
+        e3.sync()
+        e3.step(FULL_SUBSTEPS)
+        e3.sync()
+        fms, _ = e3.last_timing()
+        e3.check_errors()
+        full = {'substeps': FULL_SUBSTEPS, 'value': sc.nFluid * FULL_SUBSTEPS / (fms / 1e3), 'unit': UNIT,
+                'ms_per_step': fms / FULL_SUBSTEPS,
+                'parity': parity_against('two_fluid_1024', FULL_SUBSTEPS, e3.chain_hex())}
+        e3.destroy()
+
     line = {
         'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': ws, 'steps': args.steps, 'warmup': args.warmup,
         'ms_per_step': ms_step, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
         'dtype': 'int32', 'data': 'synthetic',
         'config': {'workload': WORKLOAD, 'particles': sc.n, 'fluid_particles': sc.nFluid,
                    'parallelism': 'replicas' if ws > 1 else 'single', 'l2': 'working set > L2, no flush',
-                   'lanes': lanes_used, 'lanes_tuned_at_substep': tuned_at},
+                   'lanes': lanes_used, 'lanes_tuned_at_substep': tuned_at,
+                   'timed_substeps': [args.warmup, args.warmup + args.steps]},
+        'parity_ok': parity['ok'],
+        'parity': parity,
+        'full_config': full,
         'wall_ms_per_step': 1e3 * wall / args.steps,
         'gpu_launches': int(launches),
         'roofline': roof,
@@ -586,6 +655,7 @@ def main():
     ap.add_argument('--no-serving', action='store_true')
     ap.add_argument('--no-construction', action='store_true')
     ap.add_argument('--cpu-seconds', type=float, default=12.0)
+    ap.add_argument('--no-full', action='store_true', help='skip the full 1000-substep run of the headline workload')
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.impl == 'reference':

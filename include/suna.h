@@ -119,6 +119,21 @@ int sn_read_scratch(sn_engine* e, int32_t* out, size_t words);
 int sn_write_state(sn_engine* e, const int32_t* state, const int32_t* scratch, size_t n);
 /* Bond rows, nFluid*48 packed words (src/sim.wgsl:1594-1617). */
 int sn_read_bonds(sn_engine* e, uint32_t* out, size_t words);
+/* The last substep's per-slot fields that Engine.liveness (src/engine.js:
+ * 4490-4511) reads: the rho column of readDerived (:4290, Derived.rho,
+ * src/sim.wgsl:200) and the neighbour count of readNbrN (:4291; the count
+ * field only, without the reference's seal/congeal flag bits), n words each
+ * in slot order, 0 for wall slots; either pointer may be NULL. SN_E_INVALID
+ * when no substep has run since the particles last changed (load, spawn,
+ * erase, state write, checkpoint load). */
+int sn_read_fields(sn_engine* e, int32_t* rho, uint32_t* nbr_count, size_t n);
+/* Engine.readCellStart (src/engine.js:4292): cell_total + 1 words, entry k =
+ * the first sorted position of cell key k as of the last substep's grid.
+ * Keys are colour-major here (cell (cx, cy) of colour c = (cx&1)|(cy&1)<<1 is
+ * key keyOff[c] + (cy>>1)*ceil((gridW-(cx&1))/2) + (cx>>1)), not the
+ * reference's row-major index, so a cell's occupancy (entry k+1 - entry k)
+ * is the same multiset over all cells. Same refusal as sn_read_fields. */
+int sn_read_cell_start(sn_engine* e, uint32_t* out, size_t words);
 /* Engine.spawnFluid (src/engine.js:5901): append k fluid particles, relocate
  * the boundary block to the tail. *n_out = new n (unchanged when the capacity
  * refuses, as the reference silently does). `no_weld` holds the options bits:
@@ -334,20 +349,20 @@ int sn_batch_set_lanes(sn_batch* b, const uint32_t lanes[5]);
 
 /* ---- digest without device allocation ------------------------------------ */
 /* No counterpart in the reference. For callers that cannot allocate device
- * memory when they need a digest: code running while a stream is captured
- * into a CUDA graph (cudaMalloc is not allowed then), latency-bound loops that
- * cannot absorb cudaMalloc's device synchronisation, and embedding hosts that
- * own all device memory. The caller passes its own device buffers: d_state
- * (n*8 words, the Particle layout above), optionally d_bond (n_fluid*48 packed
- * bond words, or NULL for no bond fold), and d_out (8 words) that receives
- * H_set (0..3) || H_slot (4..7), exactly as sn_digest computes them. Work is
- * queued on `stream` (a cudaStream_t; NULL = the legacy default stream).
- * Scratch is a fixed 64 KiB array in the library's device image, so n is
- * limited to 16,777,216 particles (SN_E_CAPACITY above that, nothing launched).
- * The array is shared by all calls on a device: calls that overlap on the GPU
- * race and must be ordered by the caller. The first call on each device looks
- * up the array's device address; make that first call before any stream
- * capture starts. */
+ * memory when they need a digest: latency-bound loops that cannot absorb
+ * cudaMalloc's device synchronisation, and embedding hosts that own all device
+ * memory and forbid libraries from allocating. The caller passes its own
+ * device buffers: d_state (n*8 words, the Particle layout above), optionally
+ * d_bond (n_fluid*48 packed bond words, or NULL for no bond fold), and d_out
+ * (8 words) that receives H_set (0..3) || H_slot (4..7), exactly as sn_digest
+ * computes them. Work is queued on `stream` (a cudaStream_t; NULL = the legacy
+ * default stream). Scratch is a fixed 64 KiB array in the library's device
+ * image, so n is limited to 16,777,216 particles (SN_E_CAPACITY above that,
+ * nothing launched). The array is shared by all calls on a device: calls that
+ * overlap on the GPU race and must be ordered by the caller. The first call
+ * under each CUDA context (per device, and again after cudaDeviceReset or
+ * under a context the caller created) looks up the array's device address in
+ * that context. */
 #define SN_NOALLOC_MAX_PARTICLES 16777216u
 int sn_digest_device_noalloc(const int32_t* d_state, uint32_t n, uint32_t n_fluid, const uint32_t* d_bond,
                              uint32_t* d_out, void* stream);

@@ -81,6 +81,9 @@ def lib():
         l.sno_arm_fuse.restype = ctypes.c_int
         l.sno_arm_fuse.argtypes = [P]
         l.sno_weld_state.argtypes = [P, u32p]
+        for f in ('sno_read_nbr_counts', 'sno_read_cell_start'):
+            getattr(l, f).restype = ctypes.c_int
+            getattr(l, f).argtypes = [P, u32p, ctypes.c_size_t]
         l.sno_write_bonds.restype = ctypes.c_int
         l.sno_write_bonds.argtypes = [P, u32p, ctypes.c_size_t]
         l.sno_erase.restype = ctypes.c_int64
@@ -258,6 +261,17 @@ class OracleEngine:
     def read_derived(self):
         a = np.zeros(self.n * 16, np.int32)
         lib().sno_read_derived(self.h, a, a.size)
+        return a
+
+    def read_nbr_counts(self):
+        a = np.zeros(max(1, self.n), np.uint32)
+        lib().sno_read_nbr_counts(self.h, a, a.size)
+        return a[:self.n]
+
+    def read_cell_start(self, cell_total: int):
+        a = np.zeros(cell_total + 1, np.uint32)
+        if lib().sno_read_cell_start(self.h, a, a.size) != 0:
+            raise ValueError('oracle read_cell_start: wrong size')
         return a
 
     def read_bonds(self):

@@ -1874,6 +1874,17 @@ int sno_read_derived(SnoEngine* e, int32_t* out, size_t words) {
   std::memcpy(out, e->der.data(), (size_t)e->n * 64);
   return 0;
 }
+// readNbrN's count field (src/engine.js:4291) and readCellStart (:4292).
+int sno_read_nbr_counts(SnoEngine* e, uint32_t* out, size_t words) {
+  if (words < (size_t)e->n) return -1;
+  for (uint32_t i = 0; i < e->n; ++i) out[i] = e->nbrN[i] & ~(NBR_SEAL_BIT | NBR_EXT_SEAL_BIT | NBR_CONGEAL_BIT);
+  return 0;
+}
+int sno_read_cell_start(SnoEngine* e, uint32_t* out, size_t words) {
+  if (words < (size_t)e->cellTotal + 1) return -1;
+  std::memcpy(out, e->cellStart.data(), ((size_t)e->cellTotal + 1) * 4);
+  return 0;
+}
 int sno_read_bonds(SnoEngine* e, uint32_t* out, size_t words) {
   if (words < (size_t)e->nFluid * BOND_CAP) return -1;
   std::memcpy(out, e->bond.data(), (size_t)e->nFluid * BOND_CAP * 4);

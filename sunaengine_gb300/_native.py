@@ -132,6 +132,8 @@ SIGNATURES = {
     'sn_read_scratch': (ctypes.c_int, [P, P, sz]),
     'sn_write_state': (ctypes.c_int, [P, P, P, sz]),
     'sn_read_bonds': (ctypes.c_int, [P, P, sz]),
+    'sn_read_fields': (ctypes.c_int, [P, P, P, sz]),
+    'sn_read_cell_start': (ctypes.c_int, [P, P, sz]),
     'sn_spawn': (ctypes.c_int, [P, P, u32, u32, ctypes.POINTER(u32)]),
     'sn_impulse': (ctypes.c_int, [P, i32, i32, i32, i32, i32, u32, ctypes.POINTER(u32)]),
     'sn_debug_counters': (ctypes.c_int, [P, P]),

@@ -118,6 +118,20 @@ __global__ void __launch_bounds__(256) k_impulse_now(Bufs b, uint32_t s, Impulse
   if (threadIdx.x == 0) *hitsOut = h;
 }
 
+// The last substep's density (solveA's rho, the reference's Derived.rho,
+// src/sim.wgsl:200) and neighbour count (nbrN's count field) of each slot of
+// one scene, in slot order; wall slots read 0. Valid while the sorted-space
+// arrays still belong to the slots (no edit since the substep).
+__global__ void __launch_bounds__(256) k_slot_fields(Bufs b, uint32_t slotBase, uint32_t n, uint32_t nFluid,
+                                                     int32_t* __restrict__ rho, uint32_t* __restrict__ nbr) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint32_t p = b.inv[slotBase + i];
+    const bool fluid = i < nFluid;
+    rho[i] = fluid ? b.RX[p].x : 0;
+    nbr[i] = fluid ? (b.NBRN[p] & NBRN_COUNT) : 0u;
+  }
+}
+
 template <typename T>
 T* dalloc(size_t count, std::string& err) {
   if (count == 0) count = 1;
@@ -487,6 +501,7 @@ struct World {
   // loadScene packing (src/engine.js:3704-3951) into scene s.
   bool load(uint32_t s, const sn_scene* sc) {
     accFresh = false;
+    sortedFresh = false;
     SceneHost& h = sh[s];
     if (!validate_scene(sc, h.cap)) return false;
     // a scene load dissolves every body of the scene (src/engine.js:3811-3813)
@@ -937,6 +952,7 @@ struct World {
     lastLaunches = launchesPerSubstep * count;
     paramsStale = true;
     accFresh = chainOn;
+    sortedFresh = true;
     // step() (src/engine.js:3990-3997): an armed fusion outlives its gesture
     // only until the formation pass after release, i.e. this call.
     for (uint32_t s2 = 0; s2 < maxScenes; ++s2)
@@ -972,6 +988,7 @@ struct World {
         if (s2.used && s2.loaded) s2.substeps += 1;
       paramsStale = true;
       accFresh = chainOn;
+      sortedFresh = true;
     }
     for (auto& e : evs) cudaEventDestroy(e);
     uint32_t n = (uint32_t)std::max(0, used - 1);
@@ -990,6 +1007,10 @@ struct World {
   // digest of the current state, so digest() needs no hashing pass. Any call
   // that changes a scene's state outside a substep clears it.
   bool accFresh = false;
+  // sortedFresh: the sorted-space arrays (inv, RX, NBRN, cellStart) still
+  // describe the current slots: set by a substep, cleared by every call that
+  // changes which particle sits in which slot.
+  bool sortedFresh = false;
   bool digest(uint32_t s, uint32_t out[8]) {
     if (accFresh && !layoutDirty) {
       cudaMemcpyAsync(out, b.accLast + s * 8, 32, cudaMemcpyDeviceToHost, st);
@@ -1004,6 +1025,19 @@ struct World {
   bool read_words(const void* dsrc, void* out, size_t bytes) {
     cudaMemcpyAsync(out, dsrc, bytes, cudaMemcpyDeviceToHost, st);
     return cuda_ok(cudaStreamSynchronize(st), "read");
+  }
+
+  // readDerived's rho column and readNbrN's counts (src/engine.js:4290-4291)
+  // for scene s, slot order; either output may be null.
+  bool read_fields(uint32_t s, int32_t* rho, uint32_t* nbr) {
+    if (!sortedFresh || layoutDirty) return fail("no substep has run since the particles last changed");
+    const SceneHost& h = sh[s];
+    if (h.n == 0) return true;
+    k_slot_fields<<<grid_for(h.n), 256, 0, st>>>(b, h.slotBase, h.n, h.nFluid, reinterpret_cast<int32_t*>(tmpK),
+                                                 tmpV);
+    if (rho) cudaMemcpyAsync(rho, tmpK, (size_t)h.n * 4, cudaMemcpyDeviceToHost, st);
+    if (nbr) cudaMemcpyAsync(nbr, tmpV, (size_t)h.n * 4, cudaMemcpyDeviceToHost, st);
+    return cuda_ok(cudaStreamSynchronize(st), "readFields");
   }
 
   bool impulse_now(uint32_t s, int32_t cx, int32_t cy, int32_t r, int32_t ix, int32_t iy, uint32_t limit,
@@ -1021,6 +1055,7 @@ struct World {
   // spawnFluid (src/engine.js:5901-6020) for scene s.
   bool spawn(uint32_t s, const sn_particle* list, uint32_t k, bool noWeld, uint32_t* nOut, bool ownGroup = false) {
     accFresh = false;
+    sortedFresh = false;
     SceneHost& h = sh[s];
     if (!h.loaded) return fail("spawn before loadScene");
     if (k == 0) { if (nOut) *nOut = h.n; return true; }
@@ -1092,6 +1127,7 @@ struct World {
   // setWalls (src/engine.js:5262-5305).
   bool set_walls(uint32_t s, bool want, bool* onOut) {
     accFresh = false;
+    sortedFresh = false;
     SceneHost& h = sh[s];
     if (!h.loaded) return fail("setWalls before loadScene");
     const uint32_t nB = (uint32_t)(h.pos.size() / 2) - h.nFluid0;
@@ -1132,6 +1168,7 @@ struct World {
 
   bool write_state(uint32_t s, const int32_t* state, const int32_t* scratch, size_t n) {
     accFresh = false;
+    sortedFresh = false;
     SceneHost& h = sh[s];
     if (!h.loaded) return fail("write_state before loadScene");
     if (n != h.n) return fail("write_state: n = %zu but the loaded scene has %u", n, h.n);
@@ -1176,6 +1213,7 @@ struct World {
     if (!h.loaded) return fail("eraseWhere before loadScene");
     if (!keep || nkeep != h.nFluid) return fail("eraseWhere: need %u keep flags", h.nFluid);
     accFresh = false;
+    sortedFresh = false;
     const uint32_t oldF = h.nFluid, n = h.n, nB = n - oldF;
     std::vector<uint32_t> surv;
     for (uint32_t i = 0; i < oldF; ++i)
@@ -1375,6 +1413,7 @@ struct World {
     const SceneHost& h = sh[s];
     if (hi < lo) return true;
     accFresh = false;
+    sortedFresh = false;
     return cuda_ok(cudaMemcpyAsync(b.state + ((size_t)h.slotBase + lo) * 8, stw.data() + (size_t)lo * 8,
                                    ((size_t)hi - lo + 1) * 32, cudaMemcpyHostToDevice, st), "state") &&
            cuda_ok(cudaStreamSynchronize(st), "state");
@@ -1938,6 +1977,7 @@ struct World {
   }
   bool ckpt_load(uint32_t s, sn_ckpt_pool* pool, uint64_t handle) {
     accFresh = false;
+    sortedFresh = false;
     SceneHost& h = sh[s];
     if (!h.loaded) return fail("checkpoint load into a scene that is not loaded");
     sn_ckpt_pool::Rec* r = pool->find(handle);
@@ -2073,6 +2113,21 @@ int sn_read_bonds(sn_engine* e, uint32_t* out, size_t words) {
   SceneHost& h = e->w.sh[0];
   if (words < (size_t)h.nFluid * BOND_CAP) { e->w.err = "output buffer too small"; return SN_E_INVALID; }
   return rc_of(e->w, e->w.read_words(e->w.b.bond + (size_t)h.slotBase * BOND_CAP, out, (size_t)h.nFluid * BOND_CAP * 4));
+}
+int sn_read_fields(sn_engine* e, int32_t* rho, uint32_t* nbr_count, size_t n) {
+  if (!e) return SN_E_INVALID;
+  if (n < (size_t)e->w.sh[0].n) { e->w.err = "output buffer too small"; return SN_E_INVALID; }
+  return rc_of(e->w, e->w.read_fields(0, rho, nbr_count));
+}
+int sn_read_cell_start(sn_engine* e, uint32_t* out, size_t words) {
+  if (!e || !out) return SN_E_INVALID;
+  World& w = e->w;
+  if (!w.sortedFresh || w.layoutDirty) {
+    w.err = "no substep has run since the particles last changed";
+    return SN_E_INVALID;
+  }
+  if (words < (size_t)w.hw.K + 1) { w.err = "output buffer too small"; return SN_E_INVALID; }
+  return rc_of(w, w.read_words(w.b.cellStart, out, ((size_t)w.hw.K + 1) * 4));
 }
 int sn_spawn(sn_engine* e, const sn_particle* list, uint32_t k, uint32_t no_weld, uint32_t* n_out) {
   if (!e || (k && !list)) return SN_E_INVALID;

@@ -1,13 +1,12 @@
 // State digest of a caller-owned device buffer, with no device allocation.
 //
 // Who needs this: hosts that cannot call cudaMalloc at the moment they want
-// a digest. cudaMalloc is not a stream operation, so it is not allowed while
-// a stream is being captured into a CUDA graph; it can also synchronise the
-// device, which a latency-bound caller stepping other streams cannot afford;
-// and an embedding host that hands out device memory from its own fixed pool
-// may forbid libraries from allocating at all. Such a caller owns the state
-// buffer and the 8-word result buffer and only needs the engine's digest of
-// it (H_set || H_slot, the reference's statehash digest).
+// a digest. cudaMalloc can synchronise the device, which a latency-bound
+// caller stepping other streams cannot afford, and an embedding host that
+// hands out device memory from its own fixed pool may forbid libraries from
+// allocating at all. Such a caller owns the state buffer and the 8-word
+// result buffer and only needs the engine's digest of it (H_set || H_slot,
+// the reference's statehash digest).
 //
 // The per-block partial digests live in `g_partials`, a fixed array in this
 // library's device image: 2048 blocks x 8 words (64 KiB). Every GPU that
@@ -23,9 +22,13 @@
 //
 // Host code cannot pass `g_partials` itself to a kernel: in host code the
 // name denotes a host-side stand-in, not the device address. The device
-// address is fetched with cudaGetSymbolAddress once per device, with that
-// device current, by the first call on the device. That first call should
-// therefore come before any stream capture begins.
+// address is fetched with cudaGetSymbolAddress, with the caller's context
+// current, by the first call made under each CUDA context, and kept under
+// that context's process-unique id (cuCtxGetId). A context created later
+// (a second context on the same device, or the new primary context after
+// cudaDeviceReset) has a new id and gets its own lookup, so an address is
+// never reused outside the context it was fetched in.
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <cstdio>
 #include <mutex>
@@ -39,12 +42,18 @@ constexpr uint32_t NA_THREADS = 256;
 constexpr uint32_t NA_PER_BLOCK = 8192;  // particles one block digests
 constexpr uint32_t NA_MAX_BLOCKS = 2048;
 constexpr uint32_t NA_MAX_PARTICLES = NA_PER_BLOCK * NA_MAX_BLOCKS;  // 16,777,216
-constexpr int NA_MAX_DEVICES = 64;
+static_assert(NA_MAX_PARTICLES == SN_NOALLOC_MAX_PARTICLES, "suna.h states the same particle limit");
+constexpr int NA_CACHE = 32;  // contexts remembered; older entries are looked up again
 
 static __device__ __align__(256) uint32_t g_partials[NA_MAX_BLOCKS * 8];
 
+struct CtxAddr {
+  unsigned long long id;
+  uint32_t* addr;
+};
 std::mutex g_mu;
-uint32_t* g_addr[NA_MAX_DEVICES] = {nullptr};
+CtxAddr g_cache[NA_CACHE] = {};
+int g_used = 0, g_next = 0;
 
 // Pass 1: block b digests particles [b*8192, (b+1)*8192) and writes its 8
 // partial lane sums to partials[b]. u32 addition is commutative, so the split
@@ -99,23 +108,56 @@ __global__ void __launch_bounds__(NA_THREADS) k_na_final(const uint32_t* __restr
   }
 }
 
-// The device address of g_partials on the current device, looked up once.
-uint32_t* partials_on_current_device(int* dev_out) {
-  int dev = -1;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NA_MAX_DEVICES) return nullptr;
-  *dev_out = dev;
-  std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_addr[dev]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_partials);
-    if (e != cudaSuccess) {
-      fprintf(stderr, "[suna] sn_digest_device_noalloc: cudaGetSymbolAddress failed on device %d: %s\n", dev,
-              cudaGetErrorString(e));
-      return nullptr;
-    }
-    g_addr[dev] = static_cast<uint32_t*>(p);
+// The driver's process-unique id of the calling thread's current context, or
+// false when no context is current. The two driver calls are fetched through
+// the runtime, so the library needs no link against libcuda.
+using CtxGetCurrentFn = CUresult(CUDAAPI*)(CUcontext*);
+using CtxGetIdFn = CUresult(CUDAAPI*)(CUcontext, unsigned long long*);
+bool current_context_id(unsigned long long* id) {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  if (!get_current || !get_id) {
+    void* f1 = nullptr;
+    void* f2 = nullptr;
+    cudaDriverEntryPointQueryResult q1, q2;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+        q1 != cudaDriverEntryPointSuccess ||
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) != cudaSuccess ||
+        q2 != cudaDriverEntryPointSuccess)
+      return false;
+    get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+    get_id = reinterpret_cast<CtxGetIdFn>(f2);
   }
-  return g_addr[dev];
+  CUcontext ctx = nullptr;
+  if (get_current(&ctx) != CUDA_SUCCESS || !ctx) return false;
+  return get_id(ctx, id) == CUDA_SUCCESS;
+}
+
+// The device address of g_partials in the calling thread's current context.
+// The first call under a context looks it up; later calls under the same
+// context reuse it.
+uint32_t* partials_in_current_context() {
+  std::lock_guard<std::mutex> lock(g_mu);
+  unsigned long long id = 0;
+  const bool known = current_context_id(&id);
+  if (known)
+    for (int k = 0; k < g_used; ++k)
+      if (g_cache[k].id == id) return g_cache[k].addr;
+  // With no context current yet, this lookup is the runtime call that binds
+  // the device's primary context; the id is read after it.
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_partials);
+  if (e != cudaSuccess) {
+    int dev = -1;
+    cudaGetDevice(&dev);
+    fprintf(stderr, "[suna] sn_digest_device_noalloc: cudaGetSymbolAddress failed on device %d: %s\n", dev,
+            cudaGetErrorString(e));
+    return nullptr;
+  }
+  if (!known && !current_context_id(&id)) return static_cast<uint32_t*>(p);  // not cached: looked up next call
+  const int k = g_used < NA_CACHE ? g_used++ : (g_next++ % NA_CACHE);
+  g_cache[k] = CtxAddr{id, static_cast<uint32_t*>(p)};
+  return g_cache[k].addr;
 }
 
 }  // namespace
@@ -130,8 +172,7 @@ extern "C" int sn_digest_device_noalloc(const int32_t* d_state, uint32_t n, uint
             n, NA_MAX_PARTICLES, NA_MAX_BLOCKS, NA_PER_BLOCK);
     return SN_E_CAPACITY;
   }
-  int dev = -1;
-  uint32_t* partials = partials_on_current_device(&dev);
+  uint32_t* partials = partials_in_current_context();
   if (!partials) return SN_E_CUDA;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   uint32_t blocks = (n + NA_PER_BLOCK - 1) / NA_PER_BLOCK;

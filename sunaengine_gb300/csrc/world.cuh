@@ -69,9 +69,8 @@ struct WorldPar {
 __device__ __forceinline__ void cell_starts(const uint32_t* __restrict__ skey, uint32_t n, uint32_t K,
                                             uint32_t* __restrict__ cellStart) {
   __shared__ uint32_t piv[256];
-  const uint32_t j = threadIdx.x;
-  const uint32_t pos = (uint32_t)(((uint64_t)j * n) >> 8);
-  piv[j] = n ? skey[pos] : 0xffffffffu;
+  for (uint32_t j = threadIdx.x; j < 256u; j += blockDim.x)
+    piv[j] = n ? skey[(uint32_t)(((uint64_t)j * n) >> 8)] : 0xffffffffu;
   __syncthreads();
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k <= K; k += gridDim.x * blockDim.x) {
     uint32_t c = 0;  // pivots below k

@@ -154,6 +154,7 @@ class Engine:
         self._n, self._n_fluid = int(scene.n), int(scene.nFluid)
         self._substeps = 0
         self._scene = scene
+        self._initial_pos = np.ascontiguousarray(scene.pos, np.int32).reshape(-1).copy()
         return self
 
     def step(self, count: int = 1) -> int:
@@ -199,6 +200,37 @@ class Engine:
         if st.size != self.n * 8 or (sc is not None and sc.size != self.n * 2):
             raise EngineError('[aether] write_state: wrong buffer size')
         self._check(self._lib.sn_write_state(self._h, _ptr(st), _ptr(sc), self.n), 'writeState')
+
+    def read_fields(self):
+        """(rho, nbr_count) of the last substep per slot: readDerived's rho
+        column and readNbrN's counts (src/engine.js:4290-4291)."""
+        rho = np.zeros(max(1, self.n), np.int32)
+        nbr = np.zeros(max(1, self.n), np.uint32)
+        self._check(self._lib.sn_read_fields(self._h, _ptr(rho), _ptr(nbr), rho.size), 'readDerived')
+        return rho[:self.n], nbr[:self.n]
+
+    def read_cell_start(self) -> np.ndarray:
+        """readCellStart (src/engine.js:4292): cell_total + 1 words (colour-major keys)."""
+        a = np.zeros(self.info()['cell_total'] + 1, np.uint32)
+        self._check(self._lib.sn_read_cell_start(self._h, _ptr(a), a.size), 'readCellStart')
+        return a
+
+    def liveness(self, window: int = 0) -> dict:
+        """Engine.liveness (src/engine.js:4490-4511). With window > 0 the
+        positions are snapshotted and the simulation ADVANCES `window`
+        substeps, so movement over that recent interval is measured too."""
+        from .liveness import compute_liveness
+        recent = None
+        if window > 0:
+            before = self.read_state().reshape(-1, 8)
+            recent = np.ascontiguousarray(before[:self.n_fluid, :2]).reshape(-1)
+            self.step(window)
+        st = self.read_state()
+        rho, nbr = self.read_fields()
+        cs = self.read_cell_start()
+        sc = self._scene
+        return compute_liveness(st, self.n, self.n_fluid, int(sc.domW), int(sc.domH), rho=rho, nbr_count=nbr,
+                                cell_start=cs, initial_pos=self._initial_pos, recent_pos=recent)
 
     def read_bonds(self) -> np.ndarray:
         a = np.zeros(max(1, self.n_fluid * BOND_CAP), np.uint32)

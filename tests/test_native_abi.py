@@ -32,3 +32,15 @@ def test_library_exports_every_declared_symbol():
     assert not missing, f'not exported: {missing}'
     # and the python binding covers the same set
     assert set(_native.SIGNATURES) == set(declared_symbols())
+
+
+def test_noalloc_digest_refuses_oversize_without_a_launch():
+    """sn_digest_device_noalloc refuses a size past its fixed scratch on the
+    host, before any CUDA call, so host pointers are never dereferenced."""
+    import numpy as np
+    lib = _native.load()
+    one = np.zeros(8, np.int32)
+    out = np.zeros(8, np.uint32)
+    rc = lib.sn_digest_device_noalloc(one.ctypes.data_as(ctypes.c_void_p), (1 << 24) + 1, 0, None,
+                                      out.ctypes.data_as(ctypes.c_void_p), None)
+    assert rc == -2  # SN_E_CAPACITY

@@ -1,13 +1,16 @@
 """The no-allocation digest entry point against the engine's own digest.
 
 sn_digest_device_noalloc serves callers that cannot allocate device memory
-when they need a digest (inside a stream capture, in latency-bound loops, or
-under a host that owns all device memory). Its scratch is a fixed array in the
-library's device image. This test calls it through the C ABI on buffers the
-test owns and requires the 8 digest words to equal sn_digest's bit for bit,
-on two calls in a row over two different states, and checks that an
-over-limit size is refused. It is kept in its own file so that it runs last
-and runs the same alone or after the other tests.
+when they need a digest (latency-bound loops that cannot take cudaMalloc's
+device synchronisation, hosts that own all device memory). Its scratch is a
+fixed array in the library's device image. These tests call it through the C
+ABI on buffers the test owns and require the 8 digest words to equal
+sn_digest's bit for bit: on two calls in a row over two different states, and
+under a second CUDA context created on the same device, where the scratch
+array has a different device address than under the primary context. (The
+over-limit refusal is a host check; tests/test_native_abi.py covers it
+without a GPU.) They are kept in a file of their own so that they run last and
+run the same alone or after the other tests.
 """
 import ctypes
 
@@ -55,11 +58,76 @@ def test_noalloc_digest_matches_engine_digest_twice():
     assert np.array_equal(got, e2.digest().acc)
 
 
-def test_noalloc_digest_refuses_oversize():
+class _DriverContext:
+    """A context created with the driver API on device 0, made current on this
+    thread while the `with` block runs, with buffers allocated in it."""
+
+    def __init__(self):
+        self.cu = ctypes.CDLL('libcuda.so.1')
+        self.ctx = ctypes.c_void_p()
+        self.bufs = []
+
+    def _ok(self, rc, what):
+        assert rc == 0, f'{what} returned CUresult {rc}'
+
+    def __enter__(self):
+        dev = ctypes.c_int()
+        self._ok(self.cu.cuDeviceGet(ctypes.byref(dev), 0), 'cuDeviceGet')
+        # the new context is pushed current on this thread
+        if hasattr(self.cu, 'cuCtxCreate_v2'):
+            rc = self.cu.cuCtxCreate_v2(ctypes.byref(self.ctx), 0, dev)
+        else:
+            rc = self.cu.cuCtxCreate_v4(ctypes.byref(self.ctx), None, 0, dev)
+        self._ok(rc, 'cuCtxCreate')
+        return self
+
+    def to_device(self, arr: np.ndarray) -> int:
+        ptr = ctypes.c_uint64()
+        self._ok(self.cu.cuMemAlloc_v2(ctypes.byref(ptr), ctypes.c_size_t(max(arr.nbytes, 4))), 'cuMemAlloc')
+        self.bufs.append(ptr.value)
+        if arr.nbytes:
+            self._ok(self.cu.cuMemcpyHtoD_v2(ctypes.c_uint64(ptr.value), arr.ctypes.data_as(ctypes.c_void_p),
+                                             ctypes.c_size_t(arr.nbytes)), 'cuMemcpyHtoD')
+        return ptr.value
+
+    def to_host(self, ptr: int, arr: np.ndarray) -> np.ndarray:
+        self._ok(self.cu.cuCtxSynchronize(), 'cuCtxSynchronize')
+        self._ok(self.cu.cuMemcpyDtoH_v2(arr.ctypes.data_as(ctypes.c_void_p), ctypes.c_uint64(ptr),
+                                         ctypes.c_size_t(arr.nbytes)), 'cuMemcpyDtoH')
+        return arr
+
+    def __exit__(self, *exc):
+        for ptr in self.bufs:
+            self.cu.cuMemFree_v2(ctypes.c_uint64(ptr))
+        popped = ctypes.c_void_p()
+        self.cu.cuCtxPopCurrent_v2(ctypes.byref(popped))
+        self.cu.cuCtxDestroy_v2(self.ctx)
+        return False
+
+
+def test_noalloc_digest_under_a_second_context():
+    torch = pytest.importorskip('torch')
+    if not torch.cuda.is_available():
+        pytest.skip('needs a GPU')
     lib = _native.load()
-    one = np.zeros(8, np.int32)
-    out = np.zeros(8, np.uint32)
-    # refused on the host before any launch, so host pointers are never dereferenced
-    rc = lib.sn_digest_device_noalloc(one.ctypes.data_as(ctypes.c_void_p), (1 << 24) + 1, 0, None,
-                                      out.ctypes.data_as(ctypes.c_void_p), None)
-    assert rc == -2  # SN_E_CAPACITY
+    sc = scenes.make_scene('stretch_v1')
+    e = Engine(max_particles=sc.n + 64).load_scene(sc)
+    e.step(13)
+    want = e.digest().acc
+    state = np.ascontiguousarray(e.read_state().astype(np.int32))
+    bonds = np.ascontiguousarray(e.read_bonds().view(np.uint32))
+    # under the primary context first, so its address is cached before the new context exists
+    assert np.array_equal(_noalloc_digest(lib, torch, state, e.n, e.n_fluid, bonds), want)
+    for _ in range(2):  # two contexts in a row, each created, used and destroyed
+        with _DriverContext() as ctx:
+            d_state = ctx.to_device(state)
+            d_bond = ctx.to_device(bonds)
+            out = np.full(8, 0xffffffff, np.uint32)
+            d_out = ctx.to_device(out)
+            rc = lib.sn_digest_device_noalloc(ctypes.c_void_p(d_state), e.n, e.n_fluid, ctypes.c_void_p(d_bond),
+                                              ctypes.c_void_p(d_out), None)
+            assert rc == 0
+            got = ctx.to_host(d_out, out)
+            assert np.array_equal(got, want)
+    # and back under the primary context, where the cached address still holds
+    assert np.array_equal(_noalloc_digest(lib, torch, state, e.n, e.n_fluid, bonds), want)
