@@ -266,7 +266,8 @@ def reference_arm(args):
 BYTES_3D = {'predict': 52, 'grid sort': 24, 'cell ranges + gather': 0, 'neighbour lists': 16,
             'density': 24, 'solve+apply': 64, 'integrate+hash': 76, 'fold': 0}
 WORKLOAD_3D = ('3D dam break: 262,144 water particles (64^3 lattice at 1 wu, smix jitter) in the corner of a '
-               '48x40x48-cell (96x80x96 wu) walled box, ITERS 4, H_set||H_slot every substep')
+               '48x40x48-cell (96x80x96 wu) walled box, 4096 seeded bonds between lattice neighbours, ITERS 4, '
+               'H_set||H_slot every substep')
 
 
 def workload_3d(steps: int, warmup: int, device: int, cpu_seconds: float = 6.0, with_cpu: bool = True):
@@ -276,7 +277,9 @@ def workload_3d(steps: int, warmup: int, device: int, cpu_seconds: float = 6.0, 
     from sunaengine_gb300 import tables3d
     from sunaengine_gb300.engine3d import Engine3D
     sc = tables3d.dam3d_large()
+    rows = tables3d.bond_rows(sc, tables3d.dam3d_bonds(sc))
     e = Engine3D(max_particles=sc.n, iters=4, device=device).load_scene(sc)
+    e.write_bonds(rows, tables3d.DAM3D_BOND_K, tables3d.DAM3D_BOND_BRK)
     e.step(warmup)
     e.sync()
     e.step(steps)
@@ -309,6 +312,7 @@ def workload_3d(steps: int, warmup: int, device: int, cpu_seconds: float = 6.0, 
     e2.sync()
     t0 = time.perf_counter()
     e2.load_scene(sc)
+    e2.write_bonds(rows, tables3d.DAM3D_BOND_K, tables3d.DAM3D_BOND_BRK)
     for _ in range(steps):
         e2.step(1)
         e2.digest()
@@ -317,13 +321,16 @@ def workload_3d(steps: int, warmup: int, device: int, cpu_seconds: float = 6.0, 
     e2.close()
     out = {'workload': WORKLOAD_3D, 'particles': sc.n, 'steps': steps, 'value': value, 'unit': UNIT,
            'ms_per_step': ms / steps, 'gpu_launches': int(launches), 'roofline': roof, 'parity': parity,
-           'e2e': {'value': sc.n * steps / wall, 'unit': UNIT, 'h2d_bytes_per_step': sc.n * 28 / steps,
+           'e2e': {'value': sc.n * steps / wall, 'unit': UNIT, 'h2d_bytes_per_step': (sc.n * 28 + rows.nbytes) / steps,
                    'd2h_bytes_per_step': 32 + final.nbytes / steps}}
     if with_cpu:
         import oracle
         threads = os.cpu_count() or 1
         small = tables3d.column_fast(32, 32, 32, 48, 40, 48)
         o = oracle.Oracle3D(small.n, iters=4, threads=threads).load_scene(small)
+        # the same bond density: 512 seeded lattice bonds in the 32^3 block
+        o.write_bonds(tables3d.bond_rows(small, tables3d.lattice_bonds(32, 32, 32, 512, tables3d.DAM3D_BOND_SEED)),
+                      tables3d.DAM3D_BOND_K, tables3d.DAM3D_BOND_BRK)
         o.step(1)
         t0 = time.perf_counter()
         k = 0
@@ -332,7 +339,8 @@ def workload_3d(steps: int, warmup: int, device: int, cpu_seconds: float = 6.0, 
             k += 1
         dt = time.perf_counter() - t0
         out['cpu_baseline'] = {'value': small.n * k / dt, 'unit': UNIT, 'cores': threads, 'kind': 'port',
-                               'sample': f'{small.n}-particle 32^3 block of the same box, {k} substeps, {dt:.1f} s'}
+                               'sample': f'{small.n}-particle 32^3 block of the same box with 512 lattice bonds, '
+                                         f'{k} substeps, {dt:.1f} s'}
     return out
 
 
@@ -511,12 +519,12 @@ def ours(args):
         # best split changes with it (untimed; the measured engine only
         # receives the result).
         tuned_at = args.warmup + args.steps // 2
-        t = Engine(max_particles=sc.n, max_cells=1 << 20, device=local).load_scene(sc)
+        t = Engine(max_particles=sc.n, max_cells=1 << 20, device=local).set_staged(args.staged).load_scene(sc)
         t.step(tuned_at)
         t.autotune(3)
         lanes_pick = t.lanes()
         t.destroy()
-    e = Engine(max_particles=sc.n, max_cells=1 << 20, device=local)
+    e = Engine(max_particles=sc.n, max_cells=1 << 20, device=local).set_staged(args.staged)
     e.load_scene(sc)
     if lanes_pick is not None:
         e.set_lanes(lanes_pick)
@@ -565,7 +573,7 @@ def ours(args):
 
     # end to end through the public API: upload from host, H_slot read back every
     # substep, final state read back
-    e2 = Engine(max_particles=sc.n, max_cells=1 << 20, device=local)
+    e2 = Engine(max_particles=sc.n, max_cells=1 << 20, device=local).set_staged(args.staged)
     if lanes_pick is not None:
         e2.set_lanes(lanes_pick)
     e2.load_scene(sc)
@@ -592,7 +600,7 @@ def ours(args):
     # load, device-timed, and its chain against the oracle's at the last one.
     full = None
     if not args.no_full:
-        e3 = Engine(max_particles=sc.n, max_cells=1 << 20, device=local)
+        e3 = Engine(max_particles=sc.n, max_cells=1 << 20, device=local).set_staged(args.staged)
         if lanes_pick is not None:
             e3.set_lanes(lanes_pick)
         e3.load_scene(sc)
@@ -613,7 +621,8 @@ def ours(args):
         'config': {'workload': WORKLOAD, 'particles': sc.n, 'fluid_particles': sc.nFluid,
                    'parallelism': 'replicas' if ws > 1 else 'single', 'l2': 'working set > L2, no flush',
                    'lanes': lanes_used, 'lanes_tuned_at_substep': tuned_at,
-                   'timed_substeps': [args.warmup, args.warmup + args.steps]},
+                   'timed_substeps': [args.warmup, args.warmup + args.steps],
+                   'gathers': 'tile-staged (shared memory, bulk copies)' if args.staged else 'neighbour-list (global)'},
         'parity_ok': parity['ok'],
         'parity': parity,
         'full_config': full,
@@ -656,6 +665,8 @@ def main():
     ap.add_argument('--no-construction', action='store_true')
     ap.add_argument('--cpu-seconds', type=float, default=12.0)
     ap.add_argument('--no-full', action='store_true', help='skip the full 1000-substep run of the headline workload')
+    ap.add_argument('--staged', action='store_true',
+                    help='headline engines use the tile-staged gathers (sn_set_staged) instead of the list gathers')
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.impl == 'reference':

@@ -127,12 +127,12 @@ int sn_read_bonds(sn_engine* e, uint32_t* out, size_t words);
  * when no substep has run since the particles last changed (load, spawn,
  * erase, state write, checkpoint load). */
 int sn_read_fields(sn_engine* e, int32_t* rho, uint32_t* nbr_count, size_t n);
-/* Engine.readCellStart (src/engine.js:4292): cell_total + 1 words, entry k =
- * the first sorted position of cell key k as of the last substep's grid.
- * Keys are colour-major here (cell (cx, cy) of colour c = (cx&1)|(cy&1)<<1 is
- * key keyOff[c] + (cy>>1)*ceil((gridW-(cx&1))/2) + (cx>>1)), not the
- * reference's row-major index, so a cell's occupancy (entry k+1 - entry k)
- * is the same multiset over all cells. Same refusal as sn_read_fields. */
+/* Engine.readCellStart (src/engine.js:4292): cell_total + 1 words in the
+ * reference's layout, as of the last substep's grid: entry c (row-major cell
+ * index cy*gridW + cx) is the first position of cell c in a sort by cell
+ * index, entry cell_total the particle count. (This engine's own sorted order
+ * is tile-major; the entries are rebuilt from its per-cell occupancies.) Same
+ * refusal as sn_read_fields. */
 int sn_read_cell_start(sn_engine* e, uint32_t* out, size_t words);
 /* Engine.spawnFluid (src/engine.js:5901): append k fluid particles, relocate
  * the boundary block to the tail. *n_out = new n (unchanged when the capacity
@@ -346,6 +346,15 @@ int sn_batch_lanes(sn_batch* b, uint32_t out[5]);
  * neither the size rule nor sn_autotune changes them. */
 int sn_set_lanes(sn_engine* e, const uint32_t lanes[5]);
 int sn_batch_set_lanes(sn_batch* b, const uint32_t lanes[5]);
+/* (no counterpart) The sorted-space layout and gather kernels of solveA and
+ * the colour passes. 0 (the default): colour-major sorted space, neighbours
+ * gathered from global memory through the neighbour list. 1: tile-major sorted
+ * space (4 x 4-cell tiles), each tile's neighbourhood copied into shared memory
+ * with bulk copies and gathered there through 16-bit tile-local indices.
+ * Results are identical; only speed differs (the staged form measured slower
+ * on GB300). Takes effect at the next step. */
+int sn_set_staged(sn_engine* e, uint32_t on);
+int sn_batch_set_staged(sn_batch* b, uint32_t on);
 
 /* ---- digest without device allocation ------------------------------------ */
 /* No counterpart in the reference. For callers that cannot allocate device
@@ -439,6 +448,20 @@ int sn3_fnv(sn3_engine* e, uint32_t scene, uint32_t lanes[8]);
 int sn3_digest(sn3_engine* e, uint32_t scene, uint32_t acc[8]);
 int sn3_chain(sn3_engine* e, uint32_t scene, uint32_t chain[8]);
 int sn3_read_state(sn3_engine* e, uint32_t scene, int32_t* out, size_t words);
+/* (no counterpart: the reference's 3D page has no bonds) Build-defined bonds
+ * of a 3D scene, the 2D engine's bond distance constraint (src/sim.wgsl:
+ * 1594-1671, the bond gather of friction :1880-1934) restated over three axes.
+ * rows: n * 12 words, 6 entries per particle of {partner + 1, L0} (scene-local
+ * partner index plus one, 0 ending the row; rest length in ticks >> 5, 512..5120);
+ * a bond sits in both ends' rows. stiffness: Q16 in 0..65536; break_ratio: a
+ * bond breaks when |d|^2 > L0^2 * break_ratio / 2^16 (0: only the hard limit).
+ * Each solver iteration adds every bonded particle's correction, computed from
+ * the iteration's starting positions, to its density correction; a broken
+ * bond is tombstoned (bit 31 of its first word) in both rows. Replaces the
+ * scene's rows; a scene load clears them; checkpoints do not carry them. */
+int sn3_write_bonds(sn3_engine* e, uint32_t scene, const uint32_t* rows, size_t words, int32_t stiffness,
+                    int32_t break_ratio);
+int sn3_read_bonds(sn3_engine* e, uint32_t scene, uint32_t* out, size_t words);
 /* Keyframe restore: n particles' state words, the substep count and the chain
  * (NULL keeps the chain). */
 int sn3_write_state(sn3_engine* e, uint32_t scene, const int32_t* state, uint32_t n, uint64_t substeps,

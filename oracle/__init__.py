@@ -45,6 +45,7 @@ def lib():
         l.sno_create.restype = P
         l.sno_create.argtypes = [ctypes.c_uint32, i32p, i32p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int]
         l.sno_destroy.argtypes = [P]
+        l.sno_set_nbr_cut.argtypes = [P, ctypes.c_int]
         l.sno_load_scene.restype = ctypes.c_int
         l.sno_load_scene.argtypes = [P, ctypes.c_uint32, ctypes.c_uint32, i32p, i32p, u32p,
                                      P, P, P, ctypes.c_int32, ctypes.c_int32, ctypes.c_uint32]
@@ -140,6 +141,10 @@ def lib():
         l.sno3_write_state.argtypes = [P, i32p, ctypes.c_uint32, ctypes.c_uint64, P]
         l.sno3_step.restype = ctypes.c_int
         l.sno3_step.argtypes = [P, ctypes.c_uint32]
+        l.sno3_write_bonds.restype = ctypes.c_int
+        l.sno3_write_bonds.argtypes = [P, u32p, ctypes.c_size_t, ctypes.c_int32, ctypes.c_int32]
+        l.sno3_read_bonds.restype = ctypes.c_int
+        l.sno3_read_bonds.argtypes = [P, u32p, ctypes.c_size_t]
         for f in ('sno3_fnv', 'sno3_digest', 'sno3_chain', 'sno3_dbg'):
             getattr(l, f).argtypes = [P, u32p]
         l.sno3_read_state.restype = ctypes.c_int
@@ -262,6 +267,12 @@ class OracleEngine:
         a = np.zeros(self.n * 16, np.int32)
         lib().sno_read_derived(self.h, a, a.size)
         return a
+
+    def set_nbr_cut(self, on: bool = True):
+        """Stop a full neighbour list's scan when no flag bit can change (only
+        the overflow debug counter then differs from the full scan)."""
+        lib().sno_set_nbr_cut(self.h, 1 if on else 0)
+        return self
 
     def read_nbr_counts(self):
         a = np.zeros(max(1, self.n), np.uint32)
@@ -514,6 +525,18 @@ class Oracle3D:
         a = np.zeros(8 if f != 'sno3_dbg' else 16, np.uint32)
         getattr(lib(), f)(self.h, a)
         return a
+
+    def write_bonds(self, rows, stiffness: int, break_ratio: int):
+        """Build-defined 3D bonds (sno3_write_bonds): n * 12 words of rows."""
+        a = np.ascontiguousarray(np.asarray(rows, np.uint32).reshape(-1))
+        if lib().sno3_write_bonds(self.h, a, a.size, int(stiffness), int(break_ratio)) != 0:
+            raise ValueError('oracle 3D write_bonds: malformed rows')
+        return self
+
+    def read_bonds(self):
+        a = np.zeros(max(1, self.n * 12), np.uint32)
+        lib().sno3_read_bonds(self.h, a, a.size)
+        return a[:self.n * 12]
 
     def fnv_hex(self) -> str:
         return hex8(self._words('sno3_fnv'))

@@ -10,7 +10,10 @@
 // Build-defined additions (no reference counterpart): a per-substep chain of
 // the 2D engine's Murmur H_set/H_slot digest over each particle's 8 words
 // [p.x, p.y, p.z, mat, v.x, v.y, v.z, 0], so the 3D path can be checked every
-// substep like the 2D one; and a per-substep stir phase.
+// substep like the 2D one; a per-substep stir phase; and bonds, the 2D
+// engine's bond distance constraint (src/sim.wgsl:1594-1671, the bond gather
+// of friction at :1880-1934) restated over three axes and added to solveDp's
+// correction of each bonded particle (bond3 below).
 #include <cstdint>
 #include <cstring>
 #include <vector>
@@ -33,6 +36,11 @@ constexpr int32_t EPS_S = 524288;
 constexpr uint32_t GRAD_S = 16, S_ACC_S = 16, LAM_S = 24, DP_S = 20;
 constexpr int32_t S_TERM = 8388608;
 constexpr int32_t MARGIN = 32768;
+// bonds (build-defined): rows of 6 entries {partner + 1 | TOMB, L0}
+constexpr uint32_t BOND3_CAP = 6, BOND3_WORDS = 12, BOND3_TOMB = 0x80000000u, BOND3_J = 0x7fffffffu;
+constexpr uint32_t BOND3_PRE = 5;
+constexpr int32_t BOND3_L0_MIN = 512, BOND3_L0_MAX = 5120, BOND3_HARD_BREAK2 = 26214400, BOND3_D2_FLOOR = 262144;
+constexpr int32_t BOND3_TERM = 16777216, BOND3_DP_MAX = 16384;
 
 struct V3 { int32_t x, y, z; };
 
@@ -56,6 +64,8 @@ struct Sno3 {
   std::vector<int32_t> ballW, ballG;  // 1024 each, indexed by r2q >> 12
   std::vector<P3> ps;
   std::vector<uint32_t> cellOf, cellStart, cellCount, sorted, nbr, nbrN;
+  std::vector<uint32_t> bond;  // [maxN * BOND3_WORDS]
+  int32_t bondK = 0, bondBrk = 0;
   uint32_t dbg[16];
   uint32_t chain[8];
   uint64_t substeps = 0;
@@ -242,8 +252,52 @@ void density3(Sno3& e) {
   }
 }
 
+inline int32_t iabs3(int32_t x) { return x < 0 ? (int32_t)(0u - (uint32_t)x) : x; }
+
+// A bonded particle's correction from the iteration's starting positions,
+// its row walked in order. Per bond: d4 = (p_i - p_j) >> 5 (round half even);
+// a bond whose ends are too far apart is tombstoned in this end's row (the
+// test is symmetric, so the other end drops its copy in the same pass);
+// C = |d4|^2 - L0^2, q = C / (4 |d4|^2) in Q16 (the solver divide), and each
+// axis sums -clamp(d4 * (q * k >> 16) >> 3). The 2D constraint, src/sim.wgsl:
+// 1880-1934, with the material stiffness replaced by the scene's.
+V3 bond3(Sno3& e, uint32_t i, V3 pi, const Dbg& g) {
+  uint32_t* row = e.bond.data() + (size_t)i * BOND3_WORDS;
+  int32_t bx = 0, by = 0, bz = 0;
+  for (uint32_t k = 0; k < BOND3_CAP; ++k) {
+    const uint32_t w = row[2 * k];
+    if (w == 0u) break;
+    if (w & BOND3_TOMB) continue;
+    const int32_t L0 = (int32_t)row[2 * k + 1];
+    const int32_t L02 = wmul(L0, L0);
+    const V3& pj = e.ps[(w & BOND3_J) - 1u].pr;
+    const int32_t d4x = fp_shr_rne(fp_sub_sat(pi.x, pj.x, g), BOND3_PRE);
+    const int32_t d4y = fp_shr_rne(fp_sub_sat(pi.y, pj.y, g), BOND3_PRE);
+    const int32_t d4z = fp_shr_rne(fp_sub_sat(pi.z, pj.z, g), BOND3_PRE);
+    if (iabs3(d4x) > BOND3_L0_MAX || iabs3(d4y) > BOND3_L0_MAX || iabs3(d4z) > BOND3_L0_MAX) {
+      row[2 * k] = w | BOND3_TOMB;
+      continue;
+    }
+    const int32_t d2 = wadd(wadd(wmul(d4x, d4x), wmul(d4y, d4y)), wmul(d4z, d4z));
+    if (d2 >= BOND3_HARD_BREAK2 || (e.bondBrk != 0 && d2 > fp_mul_s(L02, e.bondBrk, 16u, g))) {
+      row[2 * k] = w | BOND3_TOMB;
+      continue;
+    }
+    if (d2 < BOND3_D2_FLOOR) continue;
+    const int32_t C = fp_sub_sat(d2, L02, g);
+    const int32_t q = fp_divshift(C, wmul(d2, 4), 16u, g);
+    const int32_t qk = fp_mul_s(q, e.bondK, 16u, g);
+    bx = wsub(bx, clampi(fp_mul_s(d4x, qk, 3u, g), -BOND3_TERM, BOND3_TERM));
+    by = wsub(by, clampi(fp_mul_s(d4y, qk, 3u, g), -BOND3_TERM, BOND3_TERM));
+    bz = wsub(bz, clampi(fp_mul_s(d4z, qk, 3u, g), -BOND3_TERM, BOND3_TERM));
+  }
+  return V3{clampi(fp_shr_rne(bx, 8u), -BOND3_DP_MAX, BOND3_DP_MAX), clampi(fp_shr_rne(by, 8u), -BOND3_DP_MAX, BOND3_DP_MAX),
+            clampi(fp_shr_rne(bz, 8u), -BOND3_DP_MAX, BOND3_DP_MAX)};
+}
+
 // solveDp + applyDp (3d/sim3d.wgsl:476-537): gather with a saturating running
-// sum in canonical neighbour order, then the walls, then apply.
+// sum in canonical neighbour order, then the walls, the ball and (build-
+// defined) the bonds, then apply.
 void solve3(Sno3& e) {
   PFOR3 for (int64_t ii = 0; ii < (int64_t)e.n; ++ii) {
     uint32_t i = (uint32_t)ii;
@@ -279,6 +333,10 @@ void solve3(Sno3& e) {
     if (bt.hit)
       acc = V3{fp_add_sat(acc.x, fp_mul_s(lami, bt.g.x, DP_S, g), g), fp_add_sat(acc.y, fp_mul_s(lami, bt.g.y, DP_S, g), g),
                fp_add_sat(acc.z, fp_mul_s(lami, bt.g.z, DP_S, g), g)};
+    if (!e.bond.empty() && e.bond[(size_t)i * BOND3_WORDS] != 0u) {
+      const V3 bd = bond3(e, i, pi, g);
+      acc = V3{fp_add_sat(acc.x, bd.x, g), fp_add_sat(acc.y, bd.y, g), fp_add_sat(acc.z, bd.z, g)};
+    }
     q.dp = acc;
   }
   PFOR3 for (int64_t ii = 0; ii < (int64_t)e.n; ++ii) {
@@ -359,6 +417,8 @@ int sno3_load(Sno3* e, uint32_t n, const int32_t* pos, const int32_t* vel, const
               uint32_t gy, uint32_t gz, int32_t stirAmp, uint32_t frame) {
   if (n > e->maxN || gx == 0 || gy == 0 || gz == 0) return -1;
   e->n = n; e->gx = gx; e->gy = gy; e->gz = gz; e->cellTotal = gx * gy * gz;
+  e->bond.clear();
+  e->bondK = e->bondBrk = 0;
   e->stirAmp = stirAmp;
   e->frame = frame;
   e->ps.assign(n, P3{});
@@ -457,6 +517,29 @@ void sno3_set_ball(Sno3* e, int on, int32_t x, int32_t y, int32_t z, int32_t rea
   e->ballG.assign(g1024, g1024 + 1024);
 }
 uint32_t sno3_n(Sno3* e) { return e->n; }
+// Build-defined bonds: n * 12 words of rows (see bond3), the scene's stiffness
+// (Q16) and break ratio; replaces all rows. -1 on a malformed row.
+int sno3_write_bonds(Sno3* e, const uint32_t* rows, size_t words, int32_t k, int32_t brk) {
+  if (words != (size_t)e->n * BOND3_WORDS || k < 0 || k > 65536 || brk < 0) return -1;
+  for (uint32_t i = 0; i < e->n; ++i)
+    for (uint32_t t = 0; t < BOND3_CAP; ++t) {
+      const uint32_t w = rows[(size_t)i * BOND3_WORDS + 2 * t], L0 = rows[(size_t)i * BOND3_WORDS + 2 * t + 1];
+      if (w == 0u) continue;
+      const uint32_t j = (w & BOND3_J) - 1u;
+      if (j >= e->n || j == i || (int32_t)L0 < BOND3_L0_MIN || (int32_t)L0 > BOND3_L0_MAX) return -1;
+    }
+  e->bond.assign((size_t)e->maxN * BOND3_WORDS, 0u);
+  std::memcpy(e->bond.data(), rows, words * 4);
+  e->bondK = k;
+  e->bondBrk = brk;
+  return 0;
+}
+int sno3_read_bonds(Sno3* e, uint32_t* out, size_t words) {
+  if (words < (size_t)e->n * BOND3_WORDS) return -1;
+  if (e->bond.empty()) std::memset(out, 0, (size_t)e->n * BOND3_WORDS * 4);
+  else std::memcpy(out, e->bond.data(), (size_t)e->n * BOND3_WORDS * 4);
+  return 0;
+}
 int sno3_write_state(Sno3* e, const int32_t* words, uint32_t n, uint64_t substeps, const uint32_t* chain) {
   if (n > e->maxN) return -1;
   e->ps.assign(n, P3{});

@@ -111,6 +111,7 @@ struct SnoEngine {
   uint32_t matCount = 0, authoredCount = 0;
   int32_t gravQ = 65536;                 // setGravityScale (src/engine.js:4843), Q16
   int threads = 1;
+  bool nbrCut = false;  // stop a full list's scan when no flag can change (pass_buildNbr)
   // params
   uint32_t n = 0, nFluid = 0, gridW = 1, gridH = 1, cellTotal = 1, cellShift = 18;
   int32_t originX = 0, originY = 0, domW = 0, domH = 0, vmax = VMAX;
@@ -325,8 +326,17 @@ void pass_grid(E& e) {
   }
 }
 
-// src/sim.wgsl:1190-1254
+// src/sim.wgsl:1190-1254. With e.nbrCut set (sno_set_nbr_cut) the scan of a
+// particle's cells stops once its list holds MAXNBR entries, when no live fluid
+// particle carries FLAG_SEAL or FLAG_CONGEAL: every later candidate could only
+// be truncated away, so the list, its count and its flag bits are what the full
+// scan gives; only the overflow counter (debug flag 6) stops counting. The full
+// scan is O(occupancy^2) in a crowded cell.
 void pass_buildNbr(E& e, const std::vector<Particle>& in) {
+  bool flagsLive = false;
+  for (uint32_t j = 0; j < e.nFluid && !flagsLive; ++j)
+    flagsLive = !(in[j].flags & FLAG_DEAD) && (in[j].flags & (FLAG_SEAL | FLAG_CONGEAL));
+  const bool cut = e.nbrCut && !flagsLive;
   PFOR for (int64_t ii = 0; ii < (int64_t)e.n; ++ii) {
     uint32_t i = (uint32_t)ii;
     Dbg g = e.D();
@@ -357,9 +367,11 @@ void pass_buildNbr(E& e, const std::vector<Particle>& in) {
           if (cnt >= MAXNBR) { g.flag(6); continue; }
           e.nbr[base + cnt] = j;
           cnt++;
+          if (cut && cnt >= MAXNBR) goto listed;
         }
       }
     }
+  listed:
     e.nbrN[i] = cnt | (sealSeen ? NBR_SEAL_BIT : 0u) | (extSeen ? NBR_EXT_SEAL_BIT : 0u) |
                 (congealSeen ? NBR_CONGEAL_BIT : 0u);
   }
@@ -1727,6 +1739,7 @@ SnoEngine* sno_create(uint32_t maxParticles, const int32_t* luts, const int32_t*
 }
 
 void sno_destroy(SnoEngine* e) { delete e; }
+void sno_set_nbr_cut(SnoEngine* e, int on) { e->nbrCut = on != 0; }
 
 // setJets (src/engine.js:4740-4770): the first JET_MAX = 8 jets, [x, y, r, fx, fy] each.
 uint32_t sno_set_jets(SnoEngine* e, const int32_t* q, uint32_t k) {

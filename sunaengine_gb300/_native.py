@@ -175,6 +175,8 @@ SIGNATURES = {
     'sn3_digest': (ctypes.c_int, [P, u32, P]),
     'sn3_chain': (ctypes.c_int, [P, u32, P]),
     'sn3_read_state': (ctypes.c_int, [P, u32, P, ctypes.c_size_t]),
+    'sn3_write_bonds': (ctypes.c_int, [P, u32, P, ctypes.c_size_t, i32, i32]),
+    'sn3_read_bonds': (ctypes.c_int, [P, u32, P, ctypes.c_size_t]),
     'sn3_write_state': (ctypes.c_int, [P, u32, P, u32, u64, P]),
     'sn3_debug_counters': (ctypes.c_int, [P, P]),
     'sn3_sync': (ctypes.c_int, [P]),
@@ -224,6 +226,8 @@ SIGNATURES = {
     'sn_write_body': (ctypes.c_int, [P, P, u32, u32, P, u32, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(u32)]),
     'sn_autotune': (ctypes.c_int, [P, u32, ctypes.POINTER(u32)]),
     'sn_batch_autotune': (ctypes.c_int, [P, u32, ctypes.POINTER(u32)]),
+    'sn_set_staged': (ctypes.c_int, [P, u32]),
+    'sn_batch_set_staged': (ctypes.c_int, [P, u32]),
     'sn_lanes': (ctypes.c_int, [P, P]),
     'sn_batch_lanes': (ctypes.c_int, [P, P]),
     'sn_ckpt_pool_create': (ctypes.c_int, [ctypes.c_size_t, ctypes.c_int32, ctypes.POINTER(P)]),

@@ -188,6 +188,7 @@ struct World {
   Bufs b{};
   uint32_t *tmpK = nullptr, *tmpV = nullptr, *hist = nullptr, *hits = nullptr;
   uint32_t* accTmp = nullptr;
+  BoxChunk* boxChunks = nullptr;  // [capSlots / CELL_CHUNK + capSlots / CELL_BIG + 1] (k_cellbox)
   ImpulseEv* devEv = nullptr;
   size_t devEvCap = 0;
   EvPar* devEp = nullptr;
@@ -222,10 +223,11 @@ struct World {
     if (gexec) cudaGraphExecDestroy(gexec);
     if (graph) cudaGraphDestroy(graph);
     void* ptrs[] = {b.state, b.stacc, b.predSlot, b.sceneOf, b.keys, b.inv, b.bond, b.bondCand, b.skey,
-                    b.sslot, b.cellStart, b.PL, b.PL2, b.RX, b.NQ, b.POS, b.SCN, b.DP, b.HEAT, b.CORR, b.NBR, b.NBRN,
+                    b.sslot, b.cellStart, b.PL, b.PL2, b.RX, b.NQ, b.POS, b.SCN, b.DP, b.HEAT, b.CORR, b.NBR,
+                    b.NBRL, b.NBRN, (void*)b.tiles, b.TR, b.OVF, b.CB,
                     (void*)b.luts, (void*)b.WG, (void*)b.CA, (void*)b.mats, (void*)b.rcp,
                     b.scenes, b.world, b.acc, b.accLast, b.chain, b.dbg, b.err, b.work, tmpK, tmpV, hist,
-                    hits, accTmp, devEv, devEp};
+                    hits, accTmp, devEv, devEp, boxChunks};
     for (void* p : ptrs)
       if (p) cudaFree(p);
     if (ev0) cudaEventDestroy(ev0);
@@ -283,7 +285,6 @@ struct World {
     b.bondCand = dalloc<uint32_t>(C * BOND_CAP, err);
     b.skey = dalloc<uint32_t>(C, err);
     b.sslot = dalloc<uint32_t>(C, err);
-    b.cellStart = dalloc<uint32_t>((size_t)maxCells + 1, err);
     b.PL = dalloc<int4>(C, err);
     b.PL2 = dalloc<int4>(C, err);
     b.RX = dalloc<int4>(C, err);
@@ -294,6 +295,7 @@ struct World {
     b.HEAT = dalloc<int32_t>(C, err);
     b.CORR = dalloc<int32_t>(C, err);
     b.NBR = dalloc<uint32_t>(C * MAXNBR, err);
+    b.NBRL = dalloc<uint16_t>(C * MAXNBR, err);
     b.NBRN = dalloc<uint32_t>(C, err);
     b.nbrStride = (uint32_t)C;
     uint16_t* drcp = dalloc<uint16_t>(32768, err);
@@ -314,6 +316,7 @@ struct World {
     hist = dalloc<uint32_t>(radix::hist_words((uint32_t)C), err);
     hits = dalloc<uint32_t>(1, err);
     accTmp = dalloc<uint32_t>((size_t)scenesCap * 8, err);
+    boxChunks = dalloc<BoxChunk>(C / CELL_CHUNK + C / CELL_BIG + 1, err);
     devEp = dalloc<EvPar>(scenesCap, err);
     b.rbody = dalloc<int32_t>((size_t)RG_MAX_BODIES * RG_BODY_WORDS, err);
     b.rdrv = dalloc<int32_t>((size_t)RG_MAX_BODIES * RG_DRIVER_WORDS, err);
@@ -420,35 +423,77 @@ struct World {
 
   bool relayout() {
     if (!merge_device_clocks()) return false;
-    uint32_t counts[4] = {0, 0, 0, 0};
     uint32_t slotEnd = 0, nAct = 0, numScenes = 0;
+    uint64_t cells = 0;
     for (uint32_t s = 0; s < maxScenes; ++s) {
       SceneHost& h = sh[s];
-      ScenePar& p = hpar[s];
-      if (!h.used) { p.active = 0; continue; }
-      numScenes = s + 1;
+      if (!h.used) continue;
       slotEnd = std::max(slotEnd, h.slotBase + h.cap);
-      if (!h.loaded) { p.active = 0; continue; }
-      nAct += h.n;
-      for (int c = 0; c < 4; ++c) {
-        uint32_t nA = (h.gridW + 1 - (c & 1)) / 2;
-        uint32_t nB = (h.gridH + 1 - (c >> 1)) / 2;
-        p.keyOff[c] = counts[c];  // relative for now
-        p.nA[c] = nA;
-        counts[c] += nA * nB;
+      if (h.loaded) {
+        nAct += h.n;
+        cells += (uint64_t)h.gridW * h.gridH;
       }
     }
-    uint64_t K = (uint64_t)counts[0] + counts[1] + counts[2] + counts[3];
-    if (K > maxCells) return fail("total grid cells %llu exceed max_cells %u", (unsigned long long)K, maxCells);
-    uint32_t base[5];
-    base[0] = 0;
-    for (int c = 0; c < 4; ++c) base[c + 1] = base[c] + counts[c];
-    for (uint32_t s = 0; s < maxScenes; ++s)
-      if (sh[s].used && sh[s].loaded)
-        for (int c = 0; c < 4; ++c) hpar[s].keyOff[c] += base[c];
+    if (cells > maxCells) return fail("total grid cells %llu exceed max_cells %u", (unsigned long long)cells, maxCells);
+    uint64_t K = 0, tiles = 0;
+    tileHost.clear();
+    if (!staged) {
+      // colour-major layout: every scene's colour-c cells, colour by colour
+      uint32_t counts[4] = {0, 0, 0, 0};
+      for (uint32_t s = 0; s < maxScenes; ++s) {
+        SceneHost& h = sh[s];
+        ScenePar& p = hpar[s];
+        if (!h.used) { p.active = 0; continue; }
+        numScenes = s + 1;
+        if (!h.loaded) { p.active = 0; continue; }
+        p.tileShift = 0;
+        for (int c = 0; c < 4; ++c) {
+          const uint32_t nA = (h.gridW + 1 - (c & 1)) / 2;
+          const uint32_t nB = (h.gridH + 1 - (c >> 1)) / 2;
+          p.keyOff[c] = counts[c];  // relative for now
+          p.nA[c] = nA;
+          counts[c] += nA * nB;
+        }
+      }
+      uint32_t base[5];
+      base[0] = 0;
+      for (int c = 0; c < 4; ++c) base[c + 1] = base[c] + counts[c];
+      for (uint32_t s = 0; s < maxScenes; ++s)
+        if (sh[s].used && sh[s].loaded)
+          for (int c = 0; c < 4; ++c) hpar[s].keyOff[c] += base[c];
+      for (int c = 0; c < 5; ++c) hw.colourBase[c] = base[c];
+      K = base[4];
+    } else {
+      // tile-major layout, tiles of 4 x 4 cells: at the densities the solver
+      // reaches (16 to ~30 particles per 4 wu cell) a tile's neighbourhood of
+      // 36 cells stays inside the staging capacity, where 8 x 8 tiles
+      // (100 cells) overflow it
+      const uint32_t ts = tileShiftPinned ? tileShiftPinned : 2u, T = 1u << ts;
+      for (uint32_t s = 0; s < maxScenes; ++s) {
+        SceneHost& h = sh[s];
+        ScenePar& p = hpar[s];
+        if (!h.used) { p.active = 0; continue; }
+        numScenes = s + 1;
+        if (!h.loaded) { p.active = 0; continue; }
+        p.tileShift = ts;
+        p.tilesX = (h.gridW + T - 1) >> ts;
+        p.tilesY = (h.gridH + T - 1) >> ts;
+        p.keyBase = (uint32_t)K;
+        p.tileBase = (uint32_t)tiles;
+        for (uint32_t ty = 0; ty < p.tilesY; ++ty)
+          for (uint32_t tx = 0; tx < p.tilesX; ++tx)
+            tileHost.push_back(TileInfo{s, tx, ty, (uint32_t)(K + (((uint64_t)ty * p.tilesX + tx) << (2u * ts)))});
+        K += ((uint64_t)p.tilesX * p.tilesY) << (2u * ts);
+        tiles += (uint64_t)p.tilesX * p.tilesY;
+      }
+      for (int c = 0; c < 5; ++c) hw.colourBase[c] = 0;
+    }
+    if (K >= 0xffffffffull) return fail("grid keys overflow");
+    if (!ensure_tile_buffers((uint32_t)K, (uint32_t)tiles)) return false;
     hw.numScenes = numScenes;
     hw.K = (uint32_t)K;
-    for (int c = 0; c < 5; ++c) hw.colourBase[c] = base[c];
+    hw.nTiles = (uint32_t)tiles;
+    hw.stageCap = STAGE_MAX;
     hw.slotEnd = slotEnd;
     hw.nAct = nAct;
     update_features();
@@ -461,6 +506,41 @@ struct World {
               cuda_ok(cudaMemcpyAsync(b.scenes, hpar.data(), sizeof(ScenePar) * maxScenes,
                                       cudaMemcpyHostToDevice, st), "scenes");
     return ok && cuda_ok(cudaStreamSynchronize(st), "relayout");
+  }
+
+  // Grow the key- and tile-sized buffers to the layout's needs (cell starts
+  // of every key, the tile table and the per-substep run table), and upload
+  // the tile table.
+  std::vector<TileInfo> tileHost;
+  uint32_t keyCap = 0, tileCap = 0;
+  uint32_t tileShiftPinned = 0;
+  // the tile-major layout with shared-memory staged gathers (sn_set_staged);
+  // off by default: measured slower than the list gathers it replaces
+  bool staged = false;
+  bool ensure_tile_buffers(uint32_t K, uint32_t tiles) {
+    if (K + 1 > keyCap) {
+      if (b.cellStart) cudaFree(b.cellStart);
+      if (b.CB) cudaFree(b.CB);
+      keyCap = std::max<uint32_t>(K + 1, keyCap + keyCap / 2);
+      b.cellStart = dalloc<uint32_t>(keyCap, err);
+      b.CB = dalloc<int4>(keyCap, err);
+      if (!b.cellStart || !b.CB) return false;
+    }
+    if (tiles > tileCap || !b.tiles) {
+      if (b.tiles) cudaFree(const_cast<TileInfo*>(b.tiles));
+      if (b.TR) cudaFree(b.TR);
+      if (b.OVF) cudaFree(b.OVF);
+      tileCap = std::max<uint32_t>(std::max<uint32_t>(tiles, 1u), tileCap + tileCap / 2);
+      b.tiles = dalloc<TileInfo>(tileCap, err);
+      b.TR = dalloc<uint32_t>((size_t)tileCap * TR_STRIDE, err);
+      b.OVF = dalloc<uint32_t>(tileCap, err);
+      if (!b.tiles || !b.TR || !b.OVF) return false;
+    }
+    if (!tileHost.empty() &&
+        !cuda_ok(cudaMemcpyAsync(const_cast<TileInfo*>(b.tiles), tileHost.data(), sizeof(TileInfo) * tileHost.size(),
+                                 cudaMemcpyHostToDevice, st), "tiles"))
+      return false;
+    return true;
   }
 
   // Fetch the device-side scene parameters (clocks move on the device).
@@ -640,12 +720,34 @@ struct World {
   bool autoLanes = true, lanesTuned = false, setLanes = false;
   uint32_t tunedAtN = 0;
 
+  // The tile-staged kernels: one CTA per tile, at most as many CTAs as fit
+  // on the GPU at once (grid-stride over the tiles beyond that).
+  size_t stage_bytes() const { return (size_t)hw.stageCap * sizeof(int4); }
+  int grid_tiles(const void* fn) {
+    int per = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 256, stage_bytes());
+    const uint64_t cap = (uint64_t)numSMs * (uint64_t)std::max(per, 1);
+    // at least two CTAs per SM, for the tiles too large to stage, which the
+    // whole grid shares
+    return (int)std::min<uint64_t>(cap, std::max<uint64_t>(hw.nTiles, 2ull * numSMs));
+  }
   template <bool DBG, int L>
   void launch_solveA(int lastIter) {
-    k_solveA<DBG, L><<<grid_occ((const void*)k_solveA<DBG, L>, (uint64_t)hw.nAct * L), 256, 0, st>>>(b, lastIter);
+    if (staged)
+      k_solveA_tiled<DBG, L><<<grid_tiles((const void*)k_solveA_tiled<DBG, L>), 256, stage_bytes(), st>>>(b, lastIter);
+    else
+      k_solveA<DBG, L><<<grid_occ((const void*)k_solveA<DBG, L>, (uint64_t)hw.nAct * L), 256, 0, st>>>(b, lastIter);
   }
   template <bool DBG, int L>
   void launch_colours() {
+    if (staged) {
+      const int g = grid_tiles((const void*)k_colour_tiled<DBG, L, false>);
+      k_colour_tiled<DBG, L, true><<<g, 256, stage_bytes(), st>>>(b, 0, b.PL, b.PL2);
+      k_colour_tiled<DBG, L, false><<<g, 256, stage_bytes(), st>>>(b, 1, b.PL2, b.PL);
+      k_colour_tiled<DBG, L, false><<<g, 256, stage_bytes(), st>>>(b, 2, b.PL, b.PL2);
+      k_colour_tiled<DBG, L, false><<<g, 256, stage_bytes(), st>>>(b, 3, b.PL2, b.PL);
+      return;
+    }
     const int g = grid_occ((const void*)k_colour<DBG, L>, (uint64_t)hw.nAct * L / 4 + 256);
     for (int c = 0; c < 4; ++c) {
       const int4* src = (c & 1) ? b.PL2 : b.PL;
@@ -665,7 +767,10 @@ struct World {
   }
   template <bool DBG, int L>
   void launch_nbr() {
-    k_nbr<DBG, L><<<grid_occ((const void*)k_nbr<DBG, L>, (uint64_t)hw.nAct * L), 256, 0, st>>>(b);
+    if (staged)
+      k_nbr<DBG, L, true><<<grid_occ((const void*)k_nbr<DBG, L, true>, (uint64_t)hw.nAct * L), 256, 0, st>>>(b);
+    else
+      k_nbr<DBG, L, false><<<grid_occ((const void*)k_nbr<DBG, L, false>, (uint64_t)hw.nAct * L), 256, 0, st>>>(b);
   }
   template <bool DBG, int L>
   void launch_post1() {
@@ -712,10 +817,15 @@ struct World {
     mark();
     k_cellstart<<<grid_for((uint64_t)hw.K + 1), 256, 0, st>>>(b);
     k_gather<<<ga, 256, 0, st>>>(b);
+    if (staged) k_tiles<<<grid_for((uint64_t)hw.nTiles * 32), 256, 0, st>>>(b);
+    if (!DBG) {
+      k_cellbox<<<grid_for((uint64_t)hw.K * 32), 256, 0, st>>>(b, boxChunks);
+      k_cellbox_chunks<<<numSMs * 2, 256, 0, st>>>(b, boxChunks);
+    }
     mark();
     SN_LANES(lc.n, (launch_nbr<DBG, L_>()));
     mark();
-    Lc += 3;
+    Lc += 3 + (staged ? 1 : 0) + (DBG ? 0 : 2);
     for (uint32_t it = 0; it < iters; ++it) {
       const int last = it + 1 == iters ? 1 : 0;
       SN_LANES(lc.a, (launch_solveA<DBG, L_>(last)));
@@ -1188,6 +1298,8 @@ struct World {
       return fail("a transition produced a seal-class row (containment is not built); results past it are not "
                   "the reference's");
     if (e[0] & ERR_BOND_PARTNER) return fail("a bond partner slot exceeds the 17-bit bond word");
+    if (e[0] & ERR_STAGE_TIMEOUT)
+      return fail("a tile's staged copy did not complete within the bounded wait; results past it are not valid");
     return true;
   }
 
@@ -2126,8 +2238,26 @@ int sn_read_cell_start(sn_engine* e, uint32_t* out, size_t words) {
     w.err = "no substep has run since the particles last changed";
     return SN_E_INVALID;
   }
-  if (words < (size_t)w.hw.K + 1) { w.err = "output buffer too small"; return SN_E_INVALID; }
-  return rc_of(w, w.read_words(w.b.cellStart, out, ((size_t)w.hw.K + 1) * 4));
+  const SceneHost& h = w.sh[0];
+  const ScenePar& S = w.hpar[0];
+  if (words < (size_t)h.cellTotal + 1) { w.err = "output buffer too small"; return SN_E_INVALID; }
+  std::vector<uint32_t> dev((size_t)w.hw.K + 1);
+  if (!w.read_words(w.b.cellStart, dev.data(), dev.size() * 4)) return rc_of(w, false);
+  // the reference's layout: row-major cells, each cell's first position in a
+  // sort by cell index (a prefix sum of the cells' occupancies)
+  const uint32_t ts = S.tileShift, T = 1u << ts;
+  uint32_t run = 0;
+  for (uint32_t cy = 0; cy < h.gridH; ++cy)
+    for (uint32_t cx = 0; cx < h.gridW; ++cx) {
+      const uint32_t lx = cx & (T - 1u), ly = cy & (T - 1u), c = (lx & 1u) | ((ly & 1u) << 1);
+      const uint32_t key = ts == 0u ? S.keyOff[(cx & 1u) | ((cy & 1u) << 1)] + (cy >> 1) * S.nA[(cx & 1u) | ((cy & 1u) << 1)] + (cx >> 1)
+                                    : S.keyBase + ((((cy >> ts) * S.tilesX) + (cx >> ts)) << (2u * ts)) +
+                                          (c << (2u * ts - 2u)) + (ly >> 1) * (T >> 1) + (lx >> 1);
+      out[(size_t)cy * h.gridW + cx] = run;
+      run += dev[key + 1] - dev[key];
+    }
+  out[h.cellTotal] = run;
+  return SN_OK;
 }
 int sn_spawn(sn_engine* e, const sn_particle* list, uint32_t k, uint32_t no_weld, uint32_t* n_out) {
   if (!e || (k && !list)) return SN_E_INVALID;
@@ -2345,6 +2475,18 @@ int sn_autotune(sn_engine* e, uint32_t reps, uint32_t* substeps_run) {
 int sn_batch_autotune(sn_batch* b, uint32_t reps, uint32_t* substeps_run) {
   if (!b) return SN_E_INVALID;
   return rc_of(b->w, b->w.autotune(reps, substeps_run));
+}
+int sn_set_staged(sn_engine* e, uint32_t on) {
+  if (!e) return SN_E_INVALID;
+  e->w.staged = on != 0;
+  e->w.layoutDirty = true;
+  return SN_OK;
+}
+int sn_batch_set_staged(sn_batch* b, uint32_t on) {
+  if (!b) return SN_E_INVALID;
+  b->w.staged = on != 0;
+  b->w.layoutDirty = true;
+  return SN_OK;
 }
 int sn_lanes(sn_engine* e, uint32_t out[5]) {
   if (!e || !out) return SN_E_INVALID;

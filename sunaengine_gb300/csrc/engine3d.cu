@@ -60,6 +60,8 @@ struct Scene3Host {
   int32_t ball[3] = {0, 0, 0};
   double ballR = -1.0;
   int32_t reach = 0;
+  int32_t bondK = 0, bondBrk = 0;  // build-defined bonds (sn3_write_bonds)
+  bool bonds = false;              // some slot of the scene has a bond row
 };
 
 struct Engine3 {
@@ -101,7 +103,7 @@ struct Engine3 {
   ~Engine3() {
     if (gexec) cudaGraphExecDestroy(gexec);
     if (graph) cudaGraphDestroy(graph);
-    void* ptrs[] = {b.state, b.sceneOf, b.PRS, b.keys, b.skey, b.sslot, b.cellStart, b.PW, b.PW2, b.PL, b.NBR,
+    void* ptrs[] = {b.state, b.sceneOf, b.bond, b.bflag, b.inv, b.PRS, b.keys, b.skey, b.sslot, b.cellStart, b.PW, b.PW2, b.PL, b.NBR,
                     b.NBRN, (void*)b.WG, (void*)b.PG, (void*)b.mats, (void*)b.rcp, b.scenes, b.world, b.acc,
                     b.accLast, b.chain, b.dbg, tmpK, tmpV, hist, accTmp, fnvBuf, ballDev};
     for (void* p : ptrs)
@@ -143,6 +145,9 @@ struct Engine3 {
     size_t C = capSlots;
     b.state = dalloc3<int32_t>(C * 8, err);
     b.sceneOf = dalloc3<uint32_t>(C, err);
+    b.bond = dalloc3<uint32_t>(C * BOND3_WORDS, err);
+    b.bflag = dalloc3<uint32_t>(C, err);
+    b.inv = dalloc3<uint32_t>(C, err);
     b.PRS = dalloc3<int4>(C, err);
     b.keys = dalloc3<uint32_t>(C, err);
     b.skey = dalloc3<uint32_t>(C, err);
@@ -274,6 +279,8 @@ struct Engine3 {
         p.ball[1] = h.ball[1];
         p.ball[2] = h.ball[2];
         p.reach = h.reach;
+        p.bondK = h.bondK;
+        p.bondBrk = h.bondBrk;
         p.active = 1;
         K += p.cellTotal;
         nAct += h.n;
@@ -497,6 +504,7 @@ struct Engine3 {
                                            0xa4093822u, 0x299f31d0u, 0x082efa98u, 0xec4e6c89u};
     cudaMemcpyAsync(b.chain + (size_t)s * 8, CHAIN_INIT, 32, cudaMemcpyHostToDevice, st);
     cudaMemsetAsync(b.acc + (size_t)s * 8, 0, 32, st);
+    if (!clear_bonds(s)) return false;
     h.n = sc->n;
     h.gx = sc->gx;
     h.gy = sc->gy;
@@ -509,8 +517,70 @@ struct Engine3 {
     return cuda_ok(cudaStreamSynchronize(st), "load");
   }
 
+  bool clear_bonds(uint32_t s) {
+    Scene3Host& h = sh[s];
+    h.bonds = false;
+    h.bondK = h.bondBrk = 0;
+    return cuda_ok(cudaMemsetAsync(b.bond + (size_t)h.slotBase * BOND3_WORDS, 0, (size_t)h.cap * BOND3_WORDS * 4, st),
+                   "bonds") &&
+           cuda_ok(cudaMemsetAsync(b.bflag + h.slotBase, 0, (size_t)h.cap * 4, st), "bonds");
+  }
+
+  // Bond rows of scene s (BOND3_CAP entries of {partner + 1, L0} per particle,
+  // scene-local partner indices, each bond in both ends' rows), with the
+  // scene's stiffness and break ratio. Build-defined: the reference's 3D page
+  // has no bonds.
+  bool write_bonds(uint32_t s, const uint32_t* rows, size_t words, int32_t k, int32_t brk) {
+    accFresh = false;
+    if (!check_scene(s)) return false;
+    Scene3Host& h = sh[s];
+    if (!rows || words != (size_t)h.n * BOND3_WORDS) return fail("bond rows need n * %u words", BOND3_WORDS);
+    if (k < 0 || k > 65536) return fail("bond stiffness %d outside 0..65536", k);
+    if (brk < 0) return fail("bond break ratio must be >= 0");
+    std::vector<uint32_t> flag(h.n, 0u);
+    bool any = false;
+    for (uint32_t i = 0; i < h.n; ++i) {
+      const uint32_t* r = rows + (size_t)i * BOND3_WORDS;
+      bool ended = false;
+      for (uint32_t e = 0; e < BOND3_CAP; ++e) {
+        const uint32_t w = r[2 * e], L0 = r[2 * e + 1];
+        if (w == 0u) {
+          ended = true;
+          if (L0 != 0u) return fail("bond row %u: an empty entry carries a rest length", i);
+          continue;
+        }
+        if (ended) return fail("bond row %u: an entry follows the end of the row", i);
+        const uint32_t j = (w & BOND3_J) - 1u;
+        if (j >= h.n || j == i) return fail("bond row %u names partner %u", i, j);
+        if ((int32_t)L0 < BOND3_L0_MIN || (int32_t)L0 > BOND3_L0_MAX)
+          return fail("bond row %u: rest length %u outside %d..%d", i, L0, BOND3_L0_MIN, BOND3_L0_MAX);
+        flag[i] = 1u;
+        any = true;
+      }
+    }
+    if (!clear_bonds(s)) return false;
+    if (h.n) {
+      cudaMemcpyAsync(b.bond + (size_t)h.slotBase * BOND3_WORDS, rows, words * 4, cudaMemcpyHostToDevice, st);
+      cudaMemcpyAsync(b.bflag + h.slotBase, flag.data(), (size_t)h.n * 4, cudaMemcpyHostToDevice, st);
+    }
+    h.bonds = any;
+    h.bondK = k;
+    h.bondBrk = brk;
+    layoutDirty = true;
+    return cuda_ok(cudaStreamSynchronize(st), "write_bonds");
+  }
+
+  bool read_bonds(uint32_t s, uint32_t* out, size_t words) {
+    if (!check_scene(s)) return false;
+    const size_t need = (size_t)sh[s].n * BOND3_WORDS;
+    if (!out || words < need) return fail("read_bonds needs %zu words", need);
+    cudaMemcpyAsync(out, b.bond + (size_t)sh[s].slotBase * BOND3_WORDS, need * 4, cudaMemcpyDeviceToHost, st);
+    return cuda_ok(cudaStreamSynchronize(st), "read_bonds");
+  }
+
   bool remove(uint32_t s) {
     if (!check_scene(s, false)) return false;
+    if (!clear_bonds(s) || !cuda_ok(cudaStreamSynchronize(st), "remove")) return false;
     sh[s] = Scene3Host{};
     layoutDirty = true;
     return true;
@@ -773,6 +843,15 @@ int sn3_digest(sn3_engine* e, uint32_t scene, uint32_t acc[8]) {
 int sn3_chain(sn3_engine* e, uint32_t scene, uint32_t chain[8]) {
   if (!e || !chain) return SN_E_INVALID;
   return rc3(e->w, e->w.chain(scene, chain));
+}
+int sn3_write_bonds(sn3_engine* e, uint32_t scene, const uint32_t* rows, size_t words, int32_t stiffness,
+                    int32_t break_ratio) {
+  if (!e) return SN_E_INVALID;
+  return rc3(e->w, e->w.write_bonds(scene, rows, words, stiffness, break_ratio));
+}
+int sn3_read_bonds(sn3_engine* e, uint32_t scene, uint32_t* out, size_t words) {
+  if (!e) return SN_E_INVALID;
+  return rc3(e->w, e->w.read_bonds(scene, out, words));
 }
 int sn3_read_state(sn3_engine* e, uint32_t scene, int32_t* out, size_t words) {
   if (!e) return SN_E_INVALID;

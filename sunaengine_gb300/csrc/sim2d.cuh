@@ -37,6 +37,7 @@
 #pragma once
 #include <cstdint>
 #include "fixed.cuh"
+#include "stage.cuh"
 #include "statehash.cuh"
 #include "world.cuh"
 
@@ -129,9 +130,12 @@ struct Bufs {
   int2* DP;
   int32_t* HEAT;
   int32_t* CORR;
-  uint32_t* NBR;        // [MAXNBR][nbrStride]
+  uint32_t* NBR;        // [MAXNBR][nbrStride] sorted indices | NBR_BOUNDARY
+  uint16_t* NBRL;       // [MAXNBR][nbrStride] the same neighbours as tile-local indices | NBRL_BOUNDARY
   uint32_t* NBRN;
   uint32_t nbrStride;
+  const TileInfo* tiles;  // [nTiles]
+  uint32_t* TR;           // [nTiles][TR_STRIDE] run table of each tile's neighbourhood
   // tables and per-scene data
   const int32_t* luts;  // 5*TN, reference layout
   const int2* WG;       // [TN] {W, G}
@@ -145,7 +149,12 @@ struct Bufs {
   uint32_t* chain;      // [S * 8]
   uint32_t* dbg;        // [16]
   uint32_t* err;        // [4]
-  uint32_t* work;       // [4] per-substep flags: [0] = some particle has a friction/bond row
+  uint32_t* work;       // [4] per-substep flags: [0] = some particle has a friction/bond row,
+                        // [1] = some live fluid particle carries INFO_SEAL or INFO_CONGEAL,
+                        // [2] = tiles too large to stage (entries of OVF),
+                        // [3] = chunks of crowded cells for k_cellbox_chunks
+  uint32_t* OVF;        // [nTiles] the tiles of this substep whose neighbourhood exceeds stageCap
+  int4* CB;             // [K] pred bounding box of each cell above CELL_BIG particles (k_cellbox)
   // §20 rigid bodies
   int32_t* rbody;       // [bodies * 32] body records (the reference's RB_* words; word 29 = scene)
   int32_t* rdrv;        // [bodies * 10] driver sidecars (RD_* words)
@@ -154,7 +163,7 @@ struct Bufs {
   uint32_t* rmark;      // [cap] rigidMember's leave marks, slot space
 };
 
-enum : uint32_t { ERR_UNSUPPORTED_ROW = 1u, ERR_BOND_PARTNER = 2u };
+enum : uint32_t { ERR_UNSUPPORTED_ROW = 1u, ERR_BOND_PARTNER = 2u, ERR_STAGE_TIMEOUT = 4u };
 
 __device__ __forceinline__ int32_t matw(const Bufs& b, uint32_t m, int w) { return __ldg(b.mats + m * MAT_WORDS + w); }
 
@@ -199,9 +208,38 @@ __device__ __forceinline__ int32_t sym_k(int32_t ri, int32_t rj, const uint16_t*
   int32_t den = max(RHO_FLOOR_K, add_sat(ri, rj, f));
   return clampi(divshift<16>(TWO_RHO0, den, rcp, f), 0, RINV_MAX);
 }
+// The grid key of cell (cx, cy) (both inside the scene's grid). Colour-major
+// layout (tileShift 0): the scene's colour-c cells in (cy/2, cx/2) row-major
+// order from keyOff[c]. Tile-major layout: tile, then colour, then the
+// colour's cells row-major inside the tile.
 __device__ __forceinline__ uint32_t key_of(const ScenePar& S, int32_t cx, int32_t cy) {
-  uint32_t c = (uint32_t)(cx & 1) | ((uint32_t)(cy & 1) << 1);
-  return S.keyOff[c] + (uint32_t)(cy >> 1) * S.nA[c] + (uint32_t)(cx >> 1);
+  if (S.tileShift == 0u) {
+    const uint32_t c = (uint32_t)(cx & 1) | ((uint32_t)(cy & 1) << 1);
+    return S.keyOff[c] + (uint32_t)(cy >> 1) * S.nA[c] + (uint32_t)(cx >> 1);
+  }
+  const uint32_t ts = S.tileShift, T = 1u << ts;
+  const uint32_t tx = (uint32_t)cx >> ts, ty = (uint32_t)cy >> ts;
+  const uint32_t lx = (uint32_t)cx & (T - 1u), ly = (uint32_t)cy & (T - 1u);
+  const uint32_t c = (lx & 1u) | ((ly & 1u) << 1);
+  return S.keyBase + ((ty * S.tilesX + tx) << (2u * ts)) + (c << (2u * ts - 2u)) + (ly >> 1) * (T >> 1) +
+         (lx >> 1);
+}
+// Index of the tile (world-wide) holding cell (cx, cy).
+__device__ __forceinline__ uint32_t tile_of(const ScenePar& S, int32_t cx, int32_t cy) {
+  return S.tileBase + ((uint32_t)cy >> S.tileShift) * S.tilesX + ((uint32_t)cx >> S.tileShift);
+}
+__device__ __forceinline__ uint32_t tile_runs(uint32_t tileShift) { return 9u + (2u << tileShift); }
+// Which run of tile (tx, ty)'s neighbourhood holds cell (gx, gy), a cell of
+// the tile or of the one-cell ring around it: 0 = the tile, 1-2 = the halo row
+// below (by x parity), 3-4 = the row above, then the left column's T + 2
+// cells bottom to top, then the right column's.
+__device__ __forceinline__ uint32_t halo_run(uint32_t tileShift, uint32_t tx, uint32_t ty, int32_t gx, int32_t gy) {
+  const int32_t T = 1 << tileShift;
+  const int32_t lx = gx - (int32_t)(tx << tileShift), ly = gy - (int32_t)(ty << tileShift);
+  const bool inx = lx >= 0 && lx < T, iny = ly >= 0 && ly < T;
+  if (inx && iny) return 0u;
+  if (inx) return (ly < 0 ? 1u : 3u) + (uint32_t)(gx & 1);
+  return 5u + (lx < 0 ? 0u : (uint32_t)T + 2u) + (uint32_t)(ly + 1);
 }
 __device__ __forceinline__ int2 cell_coord(const ScenePar& S, int2 p) {
   int32_t cx = p.x >> S.cellShift;
@@ -305,7 +343,12 @@ template <bool DBG>
 __global__ void __launch_bounds__(256) k_predict_key(Bufs b) {
   Flags<DBG> f{b.dbg};
   const uint32_t K = b.world->K, slotEnd = b.world->slotEnd;
-  if (gtid() == 0) b.work[0] = 0u;  // set again by k_gather
+  if (gtid() == 0) {  // per-substep flags, set again by k_gather, k_tiles and k_cellbox
+    b.work[0] = 0u;
+    b.work[1] = 0u;
+    b.work[2] = 0u;
+    b.work[3] = 0u;
+  }
   for (uint32_t slot = gtid(); slot < slotEnd; slot += gstride()) {
     uint32_t s = b.sceneOf[slot];
     const ScenePar& S = b.scenes[s];
@@ -364,6 +407,179 @@ __global__ void __launch_bounds__(256) k_gather(Bufs b) {
     const unsigned bal = __ballot_sync(__activemask(), fr);
     if (fr && (threadIdx.x & 31u) == (unsigned)(__ffs(bal) - 1) && *(volatile uint32_t*)b.work == 0u)
       atomicOr(b.work, 1u);
+    // a live fluid particle a neighbour-list flag can see (buildNbr's sealSeen / congealSeen)
+    const bool fl = !((uint32_t)rec.w & (INFO_BOUNDARY | INFO_DEAD)) && ((uint32_t)rec.w & (INFO_SEAL | INFO_CONGEAL));
+    const unsigned bfl = __ballot_sync(__activemask(), fl);
+    if (fl && (threadIdx.x & 31u) == (unsigned)(__ffs(bfl) - 1) && *(volatile uint32_t*)(b.work + 1) == 0u)
+      atomicOr(b.work + 1, 1u);
+  }
+}
+
+// Cells holding more than CELL_BIG particles get a bounding box of their
+// preds each substep (k_cellbox / k_cellbox_chunks); the list build skips such
+// a cell when even the box's nearest point fails lut_index's test, since every
+// candidate in it would then be rejected. Wall clamping can pile 10^5
+// particles into one edge cell, and a particle beside the pile would otherwise
+// test every one of them.
+constexpr uint32_t CELL_BIG = 64;
+constexpr uint32_t CELL_CHUNK = 4096;  // a larger cell is reduced in chunks of this many, one CTA each
+// lut_index's rejection is monotone in |d.x| and |d.y|: if the box's nearest
+// point (per axis) is rejected, so is every candidate in the box.
+__device__ __forceinline__ bool box_reaches(int4 box, int2 pi) {
+  const int64_t gx = max(max((int64_t)box.x - pi.x, (int64_t)pi.x - box.z), (int64_t)0);
+  const int64_t gy = max(max((int64_t)box.y - pi.y, (int64_t)pi.y - box.w), (int64_t)0);
+  if (gx >= REJECT_D || gy >= REJECT_D) return false;
+  const int32_t ax = ((int32_t)gx + 8) >> 4, ay = ((int32_t)gy + 8) >> 4;
+  return ax * ax + ay * ay < H2S;
+}
+struct BoxChunk {
+  uint32_t key, lo, hi, pad;
+};
+// One warp per cell (grid-stride over the keys): the pred box of every cell
+// above CELL_BIG particles, reduced by the warp itself up to CELL_CHUNK
+// particles; a larger cell gets an empty box here and one chunk entry per
+// CELL_CHUNK particles in `chunks` (count in work[3]) for k_cellbox_chunks.
+__global__ void __launch_bounds__(256) k_cellbox(Bufs b, BoxChunk* __restrict__ chunks) {
+  const uint32_t K = b.world->K, lane = threadIdx.x & 31u, warps = gstride() >> 5;
+  for (uint32_t k = gtid() >> 5; k < K; k += warps) {
+    const uint32_t lo = b.cellStart[k], hi = b.cellStart[k + 1];
+    if (hi - lo <= CELL_BIG) continue;
+    if (hi - lo > CELL_CHUNK) {
+      const uint32_t n = (hi - lo + CELL_CHUNK - 1) / CELL_CHUNK;
+      uint32_t base = 0;
+      if (lane == 0) {
+        b.CB[k] = make_int4(INT32_MAX, INT32_MAX, INT32_MIN, INT32_MIN);
+        base = atomicAdd(b.work + 3, n);
+      }
+      base = __shfl_sync(0xffffffffu, base, 0);
+      for (uint32_t c = lane; c < n; c += 32)
+        chunks[base + c] = BoxChunk{k, lo + c * CELL_CHUNK, min(hi, lo + (c + 1) * CELL_CHUNK), 0u};
+      continue;
+    }
+    int32_t x0 = INT32_MAX, y0 = INT32_MAX, x1 = INT32_MIN, y1 = INT32_MIN;
+    for (uint32_t q = lo + lane; q < hi; q += 32) {
+      const int2 pq = ld_pred(b.PL, q);
+      x0 = min(x0, pq.x);
+      y0 = min(y0, pq.y);
+      x1 = max(x1, pq.x);
+      y1 = max(y1, pq.y);
+    }
+    x0 = __reduce_min_sync(0xffffffffu, x0);
+    y0 = __reduce_min_sync(0xffffffffu, y0);
+    x1 = __reduce_max_sync(0xffffffffu, x1);
+    y1 = __reduce_max_sync(0xffffffffu, y1);
+    if (lane == 0) b.CB[k] = make_int4(x0, y0, x1, y1);
+  }
+}
+// One CTA per chunk of a crowded cell: the chunk's box, merged into the
+// cell's with four atomics (min/max are order-free).
+__global__ void __launch_bounds__(256) k_cellbox_chunks(Bufs b, const BoxChunk* __restrict__ chunks) {
+  __shared__ int32_t red[4][8];
+  const uint32_t n = b.work[3], lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  for (uint32_t c = blockIdx.x; c < n; c += gridDim.x) {
+    const BoxChunk ch = chunks[c];
+    int32_t x0 = INT32_MAX, y0 = INT32_MAX, x1 = INT32_MIN, y1 = INT32_MIN;
+    for (uint32_t q = ch.lo + threadIdx.x; q < ch.hi; q += blockDim.x) {
+      const int2 pq = ld_pred(b.PL, q);
+      x0 = min(x0, pq.x);
+      y0 = min(y0, pq.y);
+      x1 = max(x1, pq.x);
+      y1 = max(y1, pq.y);
+    }
+    x0 = __reduce_min_sync(0xffffffffu, x0);
+    y0 = __reduce_min_sync(0xffffffffu, y0);
+    x1 = __reduce_max_sync(0xffffffffu, x1);
+    y1 = __reduce_max_sync(0xffffffffu, y1);
+    if (lane == 0) {
+      red[0][warp] = x0;
+      red[1][warp] = y0;
+      red[2][warp] = x1;
+      red[3][warp] = y1;
+    }
+    __syncthreads();
+    if (threadIdx.x < 4) {
+      int32_t v = red[threadIdx.x][0];
+      for (int w = 1; w < 8; ++w) v = threadIdx.x < 2 ? min(v, red[threadIdx.x][w]) : max(v, red[threadIdx.x][w]);
+      int32_t* box = reinterpret_cast<int32_t*>(b.CB + ch.key);
+      if (threadIdx.x < 2) atomicMin(box + threadIdx.x, v);
+      else atomicMax(box + threadIdx.x, v);
+    }
+    __syncthreads();
+  }
+}
+
+// The run table of every tile's neighbourhood for this substep (one warp per
+// tile): run r's first sorted position in TR[t][r], its offset in the tile's
+// staged copy in TR[t][TR_BASE + r], and the copy's length in
+// TR[t][TR_BASE + runs]. Runs outside the scene's grid are empty.
+__global__ void __launch_bounds__(256) k_tiles(Bufs b) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t nT = b.world->nTiles;
+  const uint32_t warps = gstride() >> 5;
+  for (uint32_t t = gtid() >> 5; t < nT; t += warps) {
+    const TileInfo ti = b.tiles[t];
+    const ScenePar& S = b.scenes[ti.scene];
+    const uint32_t ts = S.tileShift, T = 1u << ts, H = T >> 1, runs = tile_runs(ts);
+    uint32_t* tr = b.TR + (size_t)t * TR_STRIDE;
+    uint32_t carry = 0, own = 0;
+    for (uint32_t r0 = 0; r0 < runs; r0 += 32) {
+      const uint32_t r = r0 + lane;
+      uint32_t start = 0, len = 0;
+      if (r < runs && S.active) {
+        uint32_t k0 = 0, kn = 0;
+        bool any = false;
+        if (r == 0) {
+          k0 = ti.key0;
+          kn = T * T;
+          any = true;
+        } else if (r <= 4) {
+          // a colour's cells in one halo row: H consecutive keys of the tile above or below
+          const int32_t gy = (int32_t)(ti.ty * T) + (r <= 2 ? -1 : (int32_t)T);
+          const uint32_t xpar = (r - 1u) & 1u;
+          if (gy >= 0 && gy < (int32_t)S.gridH) {
+            const uint32_t ty2 = (uint32_t)gy >> ts, ly = (uint32_t)gy & (T - 1u);
+            const uint32_t c = xpar | ((ly & 1u) << 1);
+            k0 = S.keyBase + ((ty2 * S.tilesX + ti.tx) << (2u * ts)) + (c << (2u * ts - 2u)) + (ly >> 1) * H;
+            kn = H;
+            any = true;
+          }
+        } else {
+          const uint32_t j = r - 5u;
+          const bool right = j >= T + 2u;
+          const int32_t gx = (int32_t)(ti.tx * T) + (right ? (int32_t)T : -1);
+          const int32_t gy = (int32_t)(ti.ty * T) - 1 + (int32_t)(right ? j - (T + 2u) : j);
+          if (gx >= 0 && gx < (int32_t)S.gridW && gy >= 0 && gy < (int32_t)S.gridH) {
+            k0 = key_of(S, gx, gy);
+            kn = 1;
+            any = true;
+          }
+        }
+        if (any) {
+          start = b.cellStart[k0];
+          len = b.cellStart[k0 + kn] - start;
+        }
+      }
+      // exclusive prefix of the lengths in run order
+      uint32_t inc = len;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= (uint32_t)o) inc += v;
+      }
+      if (r < runs) {
+        tr[r] = start;
+        tr[TR_BASE + r] = carry + inc - len;
+      }
+      if (r0 == 0) own = __shfl_sync(0xffffffffu, len, 0);
+      carry += __shfl_sync(0xffffffffu, inc, 31);
+    }
+    if (lane == 0) {
+      tr[TR_BASE + runs] = carry;
+      // a tile with particles whose neighbourhood cannot be staged is gathered
+      // from global memory by every CTA (list order does not matter: each
+      // particle's result depends only on its inputs)
+      if (own && carry > b.world->stageCap) b.OVF[atomicAdd(b.work + 2, 1u)] = t;
+    }
   }
 }
 
@@ -376,8 +592,14 @@ __global__ void __launch_bounds__(256) k_gather(Bufs b) {
 // L lanes share one particle: they test L consecutive candidates of a cell at
 // once and place the hits with a ballot prefix, so the list keeps exactly the
 // sequential order (and the same MAXNBR cut) whatever L is.
-template <bool DBG, int L>
-__global__ void __launch_bounds__(256) k_nbr(Bufs b) {
+template <bool DBG, int L, bool TILED>
+__global__ void __launch_bounds__(256, TILED ? 6 : 8) k_nbr(Bufs b) {
+  // Once a list is full, a later candidate can only raise a flag bit or the
+  // overflow counter. With no live SEAL/CONGEAL fluid particle in the world
+  // and no counters kept, nothing it could change remains, so the scan stops:
+  // the list, its count and its flags are the full scan's. (A cell crowded by
+  // wall clamping can hold 10^5 particles, where the full scan is quadratic.)
+  const bool cut = !DBG && b.work[1] == 0u;
   if constexpr (L == 1) {
     Flags<DBG> f{b.dbg};
     const uint32_t nAct = b.world->nAct, stride = b.nbrStride;
@@ -393,6 +615,11 @@ __global__ void __launch_bounds__(256) k_nbr(Bufs b) {
       uint32_t cnt = 0;
       bool congeal = false, sealSeen = false;
       uint32_t* out = b.NBR + p;
+      // the tile-local list: offsets into this particle's tile's staged neighbourhood
+      const uint32_t ts = S.tileShift, tx = (uint32_t)cc.x >> ts, ty = (uint32_t)cc.y >> ts;
+      const uint32_t* tr = TILED ? b.TR + (size_t)tile_of(S, cc.x, cc.y) * TR_STRIDE : b.TR;
+      const bool local = TILED && !bnd && tr[TR_BASE + tile_runs(ts)] <= b.world->stageCap;
+      uint16_t* outl = b.NBRL + p;
       for (int dy = -1; dy <= 1; ++dy) {
         int32_t gy = cc.y + dy;
         if (gy < 0 || gy >= (int32_t)S.gridH) continue;
@@ -403,6 +630,8 @@ __global__ void __launch_bounds__(256) k_nbr(Bufs b) {
           if ((dx < 0 && (skip & SKIP_LEFT)) || (dx > 0 && (skip & SKIP_RIGHT))) continue;
           uint32_t key = key_of(S, gx, gy);
           uint32_t lo = b.cellStart[key], hi = b.cellStart[key + 1];
+          if (!DBG && hi - lo > CELL_BIG && !box_reaches(b.CB[key], pi)) continue;
+          const uint32_t delta = local ? tr[TR_BASE + halo_run(ts, tx, ty, gx, gy)] - tr[halo_run(ts, tx, ty, gx, gy)] : 0u;
           for (uint32_t q = lo; q < hi; ++q) {
             if (q == p) continue;
             int4 o = b.PL[q];
@@ -413,10 +642,14 @@ __global__ void __launch_bounds__(256) k_nbr(Bufs b) {
             if (!(iq & INFO_BOUNDARY) && (iq & INFO_SEAL)) sealSeen = true;
             if (cnt >= (uint32_t)MAXNBR) { f.flag(6); continue; }
             if (!bnd) out[(size_t)cnt * stride] = q | (iq & INFO_BOUNDARY);
+            if (TILED && local)
+              outl[(size_t)cnt * stride] = (uint16_t)((q + delta) | ((iq & INFO_BOUNDARY) ? NBRL_BOUNDARY : 0u));
             cnt++;
+            if (cut && cnt >= (uint32_t)MAXNBR) goto listed;
           }
         }
       }
+    listed:
       b.NBRN[p] = bnd ? 0u : (cnt | (congeal ? NBRN_CONGEAL : 0u) | (sealSeen ? NBRN_SEAL : 0u));
     }
     return;
@@ -441,23 +674,35 @@ __global__ void __launch_bounds__(256) k_nbr(Bufs b) {
     uint32_t cnt = 0;
     bool congeal = false, sealSeen = false;
     uint32_t* out = b.NBR + p;
+    const uint32_t ts = S.tileShift, tx = (uint32_t)cc.x >> ts, ty = (uint32_t)cc.y >> ts;
+    const uint32_t* tr = (TILED && work) ? b.TR + (size_t)tile_of(S, cc.x, cc.y) * TR_STRIDE : b.TR;
+    const bool local = TILED && work && !bnd && tr[TR_BASE + tile_runs(ts)] <= b.world->stageCap;
     for (int dy = -1; dy <= 1; ++dy) {
       for (int dx = -1; dx <= 1; ++dx) {
         const int32_t gy = cc.y + dy, gx = cc.x + dx;
-        uint32_t lo = 0, len = 0;
+        uint32_t lo = 0, len = 0, delta = 0;
         const bool far = (dy < 0 && (skip & SKIP_DOWN)) || (dy > 0 && (skip & SKIP_UP)) ||
                          (dx < 0 && (skip & SKIP_LEFT)) || (dx > 0 && (skip & SKIP_RIGHT));
-        if (work && !far && gy >= 0 && gy < (int32_t)S.gridH && gx >= 0 && gx < (int32_t)S.gridW) {
+        const bool full = cut && cnt >= (uint32_t)MAXNBR;  // uniform over the particle's lanes
+        if (work && !far && !full && gy >= 0 && gy < (int32_t)S.gridH && gx >= 0 && gx < (int32_t)S.gridW) {
           const uint32_t key = key_of(S, gx, gy);
           lo = b.cellStart[key];
           len = b.cellStart[key + 1] - lo;
+          if (!DBG && len > CELL_BIG && !box_reaches(b.CB[key], pi)) len = 0;
+          if (TILED && local) {
+            const uint32_t run = halo_run(ts, tx, ty, gx, gy);
+            delta = tr[TR_BASE + run] - tr[run];
+          }
         }
-        const uint32_t maxLen = L == 1 ? len : __reduce_max_sync(0xffffffffu, len);
-        for (uint32_t t = sub; t - sub < maxLen; t += L) {
+        for (uint32_t t = sub;; t += L) {
+          // the warp walks on while any of its particles has candidates left
+          // in this cell and room (or a reason) to keep them
+          const bool more = t < len && !(cut && cnt >= (uint32_t)MAXNBR);
+          if (!__any_sync(0xffffffffu, more)) break;
           const uint32_t q = lo + t;
           bool hit = false;
           uint32_t iq = 0;
-          if (t < len && q != p) {
+          if (more && q != p) {
             const int4 o = b.PL[q];
             iq = (uint32_t)o.w;
             hit = !(iq & INFO_DEAD) && lut_index(pdelta(pi, xy(o), f), f) >= 0;
@@ -472,7 +717,12 @@ __global__ void __launch_bounds__(256) k_nbr(Bufs b) {
             if (!(iq & INFO_BOUNDARY) && (iq & INFO_CONGEAL)) congeal = true;
             if (!(iq & INFO_BOUNDARY) && (iq & INFO_SEAL)) sealSeen = true;
             if (pos >= (uint32_t)MAXNBR) f.flag(6);
-            else if (!bnd) out[(size_t)pos * stride] = q | (iq & INFO_BOUNDARY);
+            else if (!bnd) {
+              out[(size_t)pos * stride] = q | (iq & INFO_BOUNDARY);
+              if (TILED && local)
+                b.NBRL[(size_t)pos * stride + p] =
+                    (uint16_t)((q + delta) | ((iq & INFO_BOUNDARY) ? NBRL_BOUNDARY : 0u));
+            }
           }
           cnt += nhit;
         }
@@ -489,61 +739,192 @@ __global__ void __launch_bounds__(256) k_nbr(Bufs b) {
   }
 }
 
-// solveA (src/sim.wgsl:1270-1318): density, |grad C|^2, lambda. On the last
-// iteration it also stores rinv (finalize's, src/sim.wgsl:2261-2262), which
-// depends only on this rho.
-template <bool DBG, int L>
-__global__ void __launch_bounds__(256) k_solveA(Bufs b, int lastIter) {
-  Flags<DBG> f{b.dbg};
-  const uint32_t nAct = b.world->nAct, stride = b.nbrStride;
+// ---- tile-staged gathers ------------------------------------------------------
+//
+// solveA and the colour passes run one CTA per tile (grid-stride over the
+// world's tiles). The CTA copies its tile's neighbourhood runs from PL into
+// shared memory with bulk copies (stage_tile) and reads every neighbour record
+// there through the tile-local list NBRL. A tile whose neighbourhood exceeds
+// the staging capacity reads neighbours from global memory through the
+// sorted-index list NBR instead; both give the same sums.
+
+// Neighbour access for the staged path: records in shared memory, entries of
+// the tile-local list.
+struct NbrStaged {
+  const int4* sm;
+  const uint16_t* nl;
+  uint32_t stride;
+  __device__ __forceinline__ uint32_t entry(uint32_t p, uint32_t k) const { return nl[(size_t)k * stride + p]; }
+  __device__ __forceinline__ int4 rec(uint32_t e) const { return sm[e & NBRL_INDEX]; }
+  __device__ __forceinline__ int2 pred(uint32_t e) const {
+    return *reinterpret_cast<const int2*>(sm + (e & NBRL_INDEX));
+  }
+  __device__ __forceinline__ bool wall(uint32_t e) const { return (e & NBRL_BOUNDARY) != 0u; }
+};
+// Neighbour access from global memory: records in PL, sorted-index entries.
+struct NbrGlobal {
+  const int4* g;
+  const uint32_t* nl;
+  uint32_t stride;
+  __device__ __forceinline__ uint32_t entry(uint32_t p, uint32_t k) const { return nl[(size_t)k * stride + p]; }
+  __device__ __forceinline__ int4 rec(uint32_t e) const { return g[e & ~NBR_BOUNDARY]; }
+  __device__ __forceinline__ int2 pred(uint32_t e) const { return ld_pred(g, e & ~NBR_BOUNDARY); }
+  __device__ __forceinline__ bool wall(uint32_t e) const { return (e & NBR_BOUNDARY) != 0u; }
+};
+
+// Copy tile t's neighbourhood (`total` records in `runs` runs) from `from`
+// (PL or PL2) into `stg`. Every thread of the CTA calls it; warp 0 arms the barrier and issues
+// one bulk copy per non-empty run. Returns false for the whole CTA when the
+// copies did not land within the bounded wait (ERR_STAGE_TIMEOUT is raised).
+__device__ __forceinline__ bool stage_tile(const Bufs& b, const int4* from, const uint32_t* tr, uint32_t runs,
+                                           uint32_t total, int4* stg, uint64_t* bar, uint32_t parity, uint32_t* okS) {
+  if (threadIdx.x < 32) {
+    // the previous tile's reads of stg (ordered by the CTA barrier that ended
+    // it) come before these async writes
+    stage::fence_proxy_async_smem();
+    if (threadIdx.x == 0) stage::mbar_arrive_expect_tx(bar, total * 16u);
+    __syncwarp();
+    for (uint32_t r = threadIdx.x; r < runs; r += 32) {
+      const uint32_t off = tr[TR_BASE + r], len = tr[TR_BASE + r + 1] - off;
+      if (len) stage::bulk_g2s(stg + off, from + tr[r], len * 16u, bar);
+    }
+    if (threadIdx.x == 0) {
+      bool ok = stage::mbar_wait_bounded(bar, parity);
+      if (!ok) {
+        atomicOr(b.err, ERR_STAGE_TIMEOUT);
+        stage::mbar_wait_bounded(bar, parity);  // let copies in flight land before the CTA exits
+      }
+      *okS = ok ? 1u : 0u;
+    }
+  }
+  __syncthreads();
+  return *okS != 0u;
+}
+
+// solveA's neighbour sums for one particle (L lanes share its list).
+template <bool DBG, int L, class NB>
+__device__ __forceinline__ void solveA_sums(const Bufs& b, const NB& nb, uint32_t p, uint32_t cnt, uint32_t sub,
+                                            int2 pi, const Flags<DBG>& f, int32_t& rho, int32_t& S, int32_t& sgx,
+                                            int32_t& sgy) {
+  // one neighbour ahead: its entry and position are in flight while the
+  // current pair is computed
+  uint32_t en = sub < cnt ? nb.entry(p, sub) : 0u;
+  int2 pn = nb.pred(en);
+  uint32_t en2 = sub + L < cnt ? nb.entry(p, sub + L) : 0u;
+  for (uint32_t k = sub; k < cnt; k += L) {
+    const int2 pj = pn;
+    if (k + L < cnt) pn = nb.pred(en2);
+    if (k + 2 * L < cnt) en2 = nb.entry(p, k + 2 * L);
+    const int2 d = pdelta(pi, pj, f);
+    const int id = lut_index(d, f);
+    if (id < 0) continue;
+    const int2 wg = __ldg(b.WG + id);
+    rho = wadd(rho, wg.x);
+    const int32_t gx = mulf<26>(wg.y, d.x, f), gy = mulf<26>(wg.y, d.y, f);
+    sgx = wadd(sgx, gx);
+    sgy = wadd(sgy, gy);
+    S = wadd(S, wadd(mulfc<11>(gx, gx, 0, S_TERM, f), mulfc<11>(gy, gy, 0, S_TERM, f)));
+  }
+  if (L > 1) {
+    rho = gsum<L>(rho);
+    S = gsum<L>(S);
+    sgx = gsum<L>(sgx);
+    sgy = gsum<L>(sgy);
+  }
+}
+
+// solveA (src/sim.wgsl:1270-1318) for particles [p0, p0 + n) of one tile,
+// `me_of(i)` giving particle p0 + i's own record: density, |grad C|^2,
+// lambda. On the last iteration it also stores rinv (finalize's,
+// src/sim.wgsl:2261-2262), which depends only on this rho.
+template <bool DBG, int L, bool BOTH, class NB, class ME>
+__device__ __forceinline__ void solveA_tile(const Bufs& b, const NB& nb, ME me_of, uint32_t p0, uint32_t n,
+                                            int lastIter, const Flags<DBG>& f) {
   const int32_t W0 = __ldg(b.luts);
-  const uint32_t sub = threadIdx.x & (L - 1), G = gstride() / L;
-  for (uint32_t p = gtid() / L;; p += G) {
-    if (__shfl_sync(0xffffffffu, p, 0) >= nAct) break;  // warp-uniform exit
-    const bool valid = p < nAct;
-    int4 me = valid ? b.PL[p] : make_int4(0, 0, 0, (int32_t)INFO_BOUNDARY);
-    uint32_t info = (uint32_t)me.w;
-    const bool act = !(info & INFO_BOUNDARY);
-    int2 pi = xy(me);
-    uint32_t cnt = act ? (b.NBRN[p] & NBRN_COUNT) : 0u;
+  const uint32_t sub = threadIdx.x & (L - 1);
+  for (uint32_t i = threadIdx.x / L;; i += blockDim.x / L) {
+    if (__shfl_sync(0xffffffffu, i, 0) >= n) break;  // warp-uniform exit
+    const bool valid = i < n;
+    const uint32_t p = p0 + (valid ? i : 0u);
+    const int4 me = valid ? me_of(i) : make_int4(0, 0, 0, (int32_t)INFO_BOUNDARY);
+    const uint32_t info = (uint32_t)me.w;
+    const bool act = valid && !(info & INFO_BOUNDARY);
+    const uint32_t cnt = act ? (b.NBRN[p] & NBRN_COUNT) : 0u;
     int32_t rho = 0, S = 0, sgx = 0, sgy = 0;
-    const uint32_t* np = b.NBR + (act ? p : 0u);
-    // one neighbour ahead: its index and position are in flight while the
-    // current pair is computed
-    uint32_t qn = sub < cnt ? (np[(size_t)sub * stride] & ~NBR_BOUNDARY) : 0u;
-    int2 pn = ld_pred(b.PL, qn);
-    uint32_t qn2 = sub + L < cnt ? (np[(size_t)(sub + L) * stride] & ~NBR_BOUNDARY) : 0u;
-    for (uint32_t k = sub; k < cnt; k += L) {
-      int2 pj = pn;
-      if (k + L < cnt) pn = ld_pred(b.PL, qn2);
-      if (k + 2 * L < cnt) qn2 = np[(size_t)(k + 2 * L) * stride] & ~NBR_BOUNDARY;
-      int2 d = pdelta(pi, pj, f);
-      int id = lut_index(d, f);
-      if (id < 0) continue;
-      int2 wg = __ldg(b.WG + id);
-      rho = wadd(rho, wg.x);
-      int32_t gx = mulf<26>(wg.y, d.x, f), gy = mulf<26>(wg.y, d.y, f);
-      sgx = wadd(sgx, gx);
-      sgy = wadd(sgy, gy);
-      S = wadd(S, wadd(mulfc<11>(gx, gx, 0, S_TERM, f), mulfc<11>(gy, gy, 0, S_TERM, f)));
-    }
-    if (L > 1) {
-      rho = gsum<L>(rho);
-      S = gsum<L>(S);
-      sgx = gsum<L>(sgx);
-      sgy = gsum<L>(sgy);
-    }
+    solveA_sums<DBG, L>(b, nb, p, cnt, sub, xy(me), f, rho, S, sgx, sgy);
     if (!act || sub != 0) continue;
     rho = wadd(rho, W0);
     S = wadd(S, wadd(clampi(mul<11>(sgx, sgx, f), 0, S_TERM), clampi(mul<11>(sgy, sgy, f), 0, S_TERM)));
-    int32_t Cq = clampi(shr_rne<4>(wsub(rho, RHO0)), 0, C_MAX);
-    int32_t eps = matw(b, info & INFO_MAT, M_eps);
-    int32_t lam = clampi(neg_sat(divshift<25>(Cq, wadd(S, eps), b.rcp, f), f), -LAM_MAX, LAM_MAX);
+    const int32_t Cq = clampi(shr_rne<4>(wsub(rho, RHO0)), 0, C_MAX);
+    const int32_t eps = matw(b, info & INFO_MAT, M_eps);
+    const int32_t lam = clampi(neg_sat(divshift<25>(Cq, wadd(S, eps), b.rcp, f), f), -LAM_MAX, LAM_MAX);
     b.PL[p].z = lam;
-    b.PL2[p].z = lam;
+    if constexpr (BOTH) b.PL2[p].z = lam;
     int4& rx = b.RX[p];
     rx.x = rho;
     if (lastIter) rx.y = clampi(divshift<16>(RHO0, max(rho, RHO_FLOOR_RINV), b.rcp, f), 0, RINV_MAX);
+  }
+}
+
+// solveA over the sorted particles, the grid striding over them (colour-major
+// layout). lam goes to both buffers of the colour sweep, which copies only
+// preds between them.
+template <bool DBG, int L>
+__global__ void __launch_bounds__(256) k_solveA(Bufs b, int lastIter) {
+  Flags<DBG> f{b.dbg};
+  const uint32_t nAct = b.world->nAct;
+  const int4* PL = b.PL;
+  const uint32_t chunk = blockDim.x / L;
+  for (uint32_t i0 = blockIdx.x * chunk; i0 < nAct; i0 += gridDim.x * chunk)
+    solveA_tile<DBG, L, true>(b, NbrGlobal{PL, b.NBR, b.nbrStride}, [&](uint32_t i) { return PL[i0 + i]; }, i0,
+                              min(nAct - i0, chunk), lastIter, f);
+}
+
+// solveA over every tile. Only lam (PL.z) is written in PL, and no particle
+// reads a neighbour's lam here, so other CTAs may stage records of a tile
+// whose lam this pass is writing. Tiles that fit are staged, one CTA per tile;
+// then every CTA works through the tiles too large to stage (the OVF list),
+// all threads of the grid striding over each one's particles.
+template <bool DBG, int L>
+__global__ void __launch_bounds__(256, 4) k_solveA_tiled(Bufs b, int lastIter) {
+  extern __shared__ int4 stg[];
+  __shared__ uint64_t bar;
+  __shared__ uint32_t okS;
+  Flags<DBG> f{b.dbg};
+  if (threadIdx.x == 0) {
+    stage::mbar_init(&bar, 1);
+    stage::fence_mbar_init();
+  }
+  __syncthreads();
+  uint32_t parity = 0;
+  const uint32_t nT = b.world->nTiles, stride = b.nbrStride, cap = b.world->stageCap;
+  for (uint32_t t = blockIdx.x; t < nT; t += gridDim.x) {
+    const TileInfo ti = b.tiles[t];
+    if (!b.scenes[ti.scene].active) continue;
+    const uint32_t runs = tile_runs(b.scenes[ti.scene].tileShift);
+    const uint32_t* tr = b.TR + (size_t)t * TR_STRIDE;
+    const uint32_t p0 = tr[0], n = tr[TR_BASE + 1], total = tr[TR_BASE + runs];
+    if (n == 0 || total > cap) continue;
+    if (!stage_tile(b, b.PL, tr, runs, total, stg, &bar, parity, &okS)) return;
+    parity ^= 1u;
+    solveA_tile<DBG, L, false>(b, NbrStaged{stg, b.NBRL, stride}, [&](uint32_t i) { return stg[i]; }, p0, n,
+                               lastIter, f);
+    __syncthreads();  // stg is read before the next tile's copy lands
+  }
+  const uint32_t nOvf = b.work[2];
+  const int4* PL = b.PL;
+  for (uint32_t k = 0; k < nOvf; ++k) {
+    const uint32_t* tr = b.TR + (size_t)b.OVF[k] * TR_STRIDE;
+    const uint32_t p0 = tr[0], n = tr[TR_BASE + 1];
+    // the grid strides over the tile's particles: shift p0 by this CTA's share
+    const uint32_t first = blockIdx.x * (blockDim.x / L);
+    if (first >= n) continue;
+    const uint32_t per = gridDim.x * (blockDim.x / L);
+    for (uint32_t i0 = first; i0 < n; i0 += per) {
+      const uint32_t m = min(n - i0, blockDim.x / L);
+      solveA_tile<DBG, L, false>(b, NbrGlobal{PL, b.NBR, stride}, [&](uint32_t i) { return PL[p0 + i0 + i]; },
+                                 p0 + i0, m, lastIter, f);
+    }
   }
 }
 
@@ -552,35 +933,33 @@ __global__ void __launch_bounds__(256) k_solveA(Bufs b, int lastIter) {
 // build drops its term; debug builds still read it.
 // RIG: the warp holds a rigid member, whose own correction skips the members
 // of its body (src/sim.wgsl:1355-1358).
-template <bool DBG, int L, bool RIG = false>
-__device__ __forceinline__ int2 solveB_dp(const Bufs& b, const int4* __restrict__ src, uint32_t p, uint32_t cnt,
-                                          uint32_t sub, int2 pi, int32_t li, const Flags<DBG>& f,
-                                          uint32_t infoI = 0u) {
-  const uint32_t stride = b.nbrStride;
+template <bool DBG, int L, bool RIG, class NB>
+__device__ __forceinline__ int2 solveB_dp(const Bufs& b, const NB& nb, uint32_t p, uint32_t cnt, uint32_t sub,
+                                          int2 pi, int32_t li, const Flags<DBG>& f, uint32_t infoI = 0u) {
   int32_t dpx = 0, dpy = 0;
-  const uint32_t* np = b.NBR + p;
-  uint32_t en = sub < cnt ? np[(size_t)sub * stride] : 0u;
-  int4 on = src[en & ~NBR_BOUNDARY];
-  uint32_t en2 = sub + L < cnt ? np[(size_t)(sub + L) * stride] : 0u;
+  uint32_t en = sub < cnt ? nb.entry(p, sub) : 0u;
+  int4 on = nb.rec(en);
+  uint32_t en2 = sub + L < cnt ? nb.entry(p, sub + L) : 0u;
   for (uint32_t k = sub; k < cnt; k += L) {
-    uint32_t e = en;
-    int4 o = on;
+    const uint32_t e = en;
+    const int4 o = on;
     if (k + L < cnt) {
       en = en2;
-      on = src[en & ~NBR_BOUNDARY];
+      on = nb.rec(en);
     }
-    if (k + 2 * L < cnt) en2 = np[(size_t)(k + 2 * L) * stride];
+    if (k + 2 * L < cnt) en2 = nb.entry(p, k + 2 * L);
+    const bool wall = nb.wall(e);
     if constexpr (RIG) {
-      if (!(e & NBR_BOUNDARY) && same_body(infoI, (uint32_t)o.w)) continue;
+      if (!wall && same_body(infoI, (uint32_t)o.w)) continue;
     }
-    int2 d = pdelta(pi, xy(o), f);
-    int id = lut_index(d, f);
+    const int2 d = pdelta(pi, xy(o), f);
+    const int id = lut_index(d, f);
     if (id < 0) continue;
-    int32_t lj = (e & NBR_BOUNDARY) ? li : o.z;
+    const int32_t lj = wall ? li : o.z;
     int32_t co;
     if constexpr (DBG) co = add_sat(add_sat(li, lj, f), __ldg(b.luts + 4 * TN + id), f);
     else co = li + lj;
-    int32_t gt = __ldg(b.WG + id).y;
+    const int32_t gt = __ldg(b.WG + id).y;
     dpx = wadd(dpx, mulfc<12>(co, mulf<26>(gt, d.x, f), -DP_TERM, DP_TERM, f));
     dpy = wadd(dpy, mulfc<12>(co, mulf<26>(gt, d.y, f), -DP_TERM, DP_TERM, f));
   }
@@ -601,15 +980,43 @@ __device__ __forceinline__ int2 apply_dp(const Bufs& b, const ScenePar& S, uint3
   return wall_clamp(S, make_int2(add_sat(pr.x, dx, f), add_sat(pr.y, dy, f)));
 }
 
-// One colour of the block Gauss-Seidel sweep: solveB_cK + applyDp_cK fused.
-// The pass reads every pred from `src` and writes its colour's corrected preds
-// to `dst`, so a particle never reads a value written in the same pass: that
-// is the Jacobi-within-a-colour rule the reference gets from its separate
-// solveB/applyDp dispatches (src/sim.wgsl:1323-1332). `dst` must leave the
-// pass complete, so the pass also copies the two colours that are stale in it:
-// the sweep alternates A->B, B->A, A->B, B->A, colour c is written in phase c
-// and read again four phases later, so phase c copies colours c+1 and c-1.
-// After phase 3 buffer A is complete again.
+// The colour class's particles [lo, lo + n) of one tile: dp of each from the
+// pre-pass records, then `out(p, me, dp)` stores the result. `me_of(p)` gives
+// particle p's own pre-pass record. Walls are not passed to `out`.
+template <bool DBG, int L, class NB, class ME, class OUT>
+__device__ __forceinline__ void colour_tile(const Bufs& b, const NB& nb, ME me_of, OUT out, uint32_t lo, uint32_t n,
+                                            const Flags<DBG>& f) {
+  const uint32_t sub = threadIdx.x & (L - 1);
+  for (uint32_t i = threadIdx.x / L;; i += blockDim.x / L) {
+    if (__shfl_sync(0xffffffffu, i, 0) >= n) break;  // warp-uniform exit
+    const bool mine = i < n;
+    const uint32_t p = lo + (mine ? i : 0u);
+    const int4 me = mine ? me_of(p) : make_int4(0, 0, 0, (int32_t)INFO_BOUNDARY);
+    const uint32_t info = (uint32_t)me.w;
+    const bool act = mine && !(info & INFO_BOUNDARY);
+    const uint32_t cnt = act ? (b.NBRN[p] & NBRN_COUNT) : 0u;
+    const bool rigidI = act && (info & INFO_RIGID);
+    int2 dp;
+    if (__any_sync(0xffffffffu, rigidI))
+      dp = solveB_dp<DBG, L, true>(b, nb, p, cnt, sub, xy(me), me.z, f, rigidI ? info : 0u);
+    else
+      dp = solveB_dp<DBG, L, false>(b, nb, p, cnt, sub, xy(me), me.z, f);
+    if (sub != 0 || !act) continue;
+    out(p, me, dp);
+  }
+}
+
+// One colour of the block Gauss-Seidel sweep (colour-major layout):
+// solveB_cK + applyDp_cK fused. The pass reads every pred from `src` and
+// writes its colour's corrected preds to `dst`, so a particle never reads a
+// value written in the same pass: that is the Jacobi-within-a-colour rule the
+// reference gets from its separate solveB/applyDp dispatches
+// (src/sim.wgsl:1323-1332). `dst` must leave the pass complete, so the pass
+// also copies the two colours that are stale in it: the sweep alternates
+// A->B, B->A, A->B, B->A, colour c is written in phase c and read again four
+// phases later, so phase c copies colours c+1 and c-1. After phase 3 buffer A
+// is complete again. A rigid member's dp is not applied: rigidSolve folds it
+// into its body at the end of the iteration (src/sim.wgsl:1418-1429).
 template <bool DBG, int L>
 __global__ void __launch_bounds__(256, 8) k_colour(Bufs b, int colour, const int4* __restrict__ src,
                                                 int4* __restrict__ dst) {
@@ -621,37 +1028,118 @@ __global__ void __launch_bounds__(256, 8) k_colour(Bufs b, int colour, const int
   const uint32_t lo3 = b.cellStart[cb[c3]], hi3 = b.cellStart[cb[c3 + 1]];
   // The grid covers this colour's range only (the launch is sized to the
   // resident capacity); the copies of the neighbouring colours follow.
-  const uint32_t nC = hi - lo;
-  const uint32_t sub = threadIdx.x & (L - 1), G = gstride() / L;
-  for (uint32_t i = gtid() / L;; i += G) {
-    if (__shfl_sync(0xffffffffu, i, 0) >= nC) break;  // warp-uniform exit
-    const uint32_t p = lo + i;
-    const bool mine = i < nC;
-    int4 me = mine ? src[p] : make_int4(0, 0, 0, (int32_t)INFO_BOUNDARY);
-    const uint32_t info = (uint32_t)me.w;
-    const bool act = mine && !(info & INFO_BOUNDARY);  // walls are identical in both buffers
-    const uint32_t cnt = act ? (b.NBRN[p] & NBRN_COUNT) : 0u;
-    const bool rigidI = act && (info & INFO_RIGID);
-    int2 dp;
-    if (__any_sync(0xffffffffu, rigidI))
-      dp = solveB_dp<DBG, L, true>(b, src, act ? p : 0u, cnt, sub, xy(me), me.z, f, rigidI ? info : 0u);
-    else
-      dp = solveB_dp<DBG, L>(b, src, act ? p : 0u, cnt, sub, xy(me), me.z, f);
-    if (sub != 0 || !act) continue;
-    int2 pr = xy(me);
-    // a rigid member's dp is not applied: rigidSolve folds it into its body
-    // at the end of the iteration (src/sim.wgsl:1418-1429)
-    if (rigidI) b.DP[p] = dp;
-    if (!(info & INFO_PINNED)) {
-      const ScenePar& S = b.scenes[b.SCN[p]];
-      pr = apply_dp(b, S, info & INFO_MAT, pr, dp, f);
-    }
-    *reinterpret_cast<int2*>(dst + p) = pr;
-  }
+  const uint32_t chunk = blockDim.x / L;
+  const NbrGlobal nb{src, b.NBR, b.nbrStride};
+  for (uint32_t i0 = blockIdx.x * chunk; i0 < hi - lo; i0 += gridDim.x * chunk)
+    colour_tile<DBG, L>(
+        b, nb, [&](uint32_t p) { return src[p]; },
+        [&](uint32_t p, int4 me, int2 dp) {
+          const uint32_t info = (uint32_t)me.w;
+          int2 pr = xy(me);
+          if (info & INFO_RIGID) b.DP[p] = dp;
+          if (!(info & INFO_PINNED)) pr = apply_dp(b, b.scenes[b.SCN[p]], info & INFO_MAT, pr, dp, f);
+          *reinterpret_cast<int2*>(dst + p) = pr;
+        },
+        lo + i0, min(hi - lo - i0, chunk), f);
   const uint32_t n1 = hi1 - lo1, n13 = n1 + (hi3 - lo3);
   for (uint32_t i = gtid(); i < n13; i += gstride()) {
     const uint32_t p = i < n1 ? lo1 + i : lo3 + (i - n1);
     *reinterpret_cast<int2*>(dst + p) = *reinterpret_cast<const int2*>(src + p);
+  }
+}
+
+// One colour of the sweep in the tile-major layout, with staged gathers.
+// The pass reads every record from `src` and writes every record to `dst`
+// (colour c's with their corrected preds, the rest unchanged), so a particle
+// never reads a value written in the same pass: that is the Jacobi-within-a-
+// colour rule the reference gets from its separate solveB/applyDp dispatches
+// (src/sim.wgsl:1323-1332). The sweep alternates A->B, B->A, A->B, B->A, so
+// after the fourth colour A is current again. The first pass of an iteration
+// (FULL) writes whole records, since B's lam is one iteration old; the others
+// write only the preds.
+//
+// Tiles that fit are staged from `src`, one CTA per tile, which writes its
+// whole tile to `dst` from the staged copy; then every CTA works through the
+// tiles too large to stage, the grid striding over each one's particles.
+// A rigid member's dp is not applied: rigidSolve folds it into its body at the
+// end of the iteration (src/sim.wgsl:1418-1429).
+template <bool DBG, int L, bool FULL>
+__global__ void __launch_bounds__(256, 6) k_colour_tiled(Bufs b, int colour, const int4* __restrict__ src,
+                                                      int4* __restrict__ dst) {
+  extern __shared__ int4 stg[];
+  __shared__ uint64_t bar;
+  __shared__ uint32_t okS;
+  Flags<DBG> f{b.dbg};
+  if (threadIdx.x == 0) {
+    stage::mbar_init(&bar, 1);
+    stage::fence_mbar_init();
+  }
+  __syncthreads();
+  auto put = [&](uint32_t p, int4 rec) {
+    if constexpr (FULL) dst[p] = rec;
+    else *reinterpret_cast<int2*>(dst + p) = xy(rec);
+  };
+  // the corrected record of an active colour-c particle
+  auto moved = [&](const ScenePar& S, uint32_t p, int4 me, int2 dp) {
+    const uint32_t info = (uint32_t)me.w;
+    if (info & INFO_RIGID) b.DP[p] = dp;
+    if (!(info & INFO_PINNED)) {
+      const int2 pr = apply_dp(b, S, info & INFO_MAT, xy(me), dp, f);
+      me.x = pr.x;
+      me.y = pr.y;
+    }
+    put(p, me);
+  };
+  uint32_t parity = 0;
+  const uint32_t nT = b.world->nTiles, stride = b.nbrStride, cap = b.world->stageCap;
+  for (uint32_t t = blockIdx.x; t < nT; t += gridDim.x) {
+    const TileInfo ti = b.tiles[t];
+    const ScenePar& S = b.scenes[ti.scene];
+    if (!S.active) continue;
+    const uint32_t ts = S.tileShift, runs = tile_runs(ts);
+    const uint32_t* tr = b.TR + (size_t)t * TR_STRIDE;
+    const uint32_t p0 = tr[0], n0 = tr[TR_BASE + 1], total = tr[TR_BASE + runs];
+    if (n0 == 0 || total > cap) continue;
+    const uint32_t Q = 1u << (2u * ts - 2u);
+    const uint32_t lo = b.cellStart[ti.key0 + colour * Q], n = b.cellStart[ti.key0 + (colour + 1) * Q] - lo;
+    if (!stage_tile(b, src, tr, runs, total, stg, &bar, parity, &okS)) return;
+    parity ^= 1u;
+    colour_tile<DBG, L>(
+        b, NbrStaged{stg, b.NBRL, stride}, [&](uint32_t p) { return stg[p - p0]; },
+        [&](uint32_t p, int4 me, int2 dp) { moved(S, p, me, dp); }, lo, n, f);
+    // the rest of the tile (other colours and walls) unchanged
+    for (uint32_t i = threadIdx.x; i < n0; i += blockDim.x) {
+      const uint32_t p = p0 + i;
+      const int4 me = stg[i];
+      if (p - lo < n && !((uint32_t)me.w & INFO_BOUNDARY)) continue;  // written above
+      put(p, me);
+    }
+    __syncthreads();  // stg is read before the next tile's copy lands
+  }
+  const uint32_t nOvf = b.work[2];
+  for (uint32_t k = 0; k < nOvf; ++k) {
+    const uint32_t tIdx = b.OVF[k];
+    const TileInfo ti = b.tiles[tIdx];
+    const ScenePar& S = b.scenes[ti.scene];
+    const uint32_t* tr = b.TR + (size_t)tIdx * TR_STRIDE;
+    const uint32_t p0 = tr[0], n0 = tr[TR_BASE + 1];
+    const uint32_t Q = 1u << (2u * S.tileShift - 2u);
+    const uint32_t lo = b.cellStart[ti.key0 + colour * Q], n = b.cellStart[ti.key0 + (colour + 1) * Q] - lo;
+    // colour c: the grid strides over the class with L lanes per particle
+    const uint32_t first = blockIdx.x * (blockDim.x / L), per = gridDim.x * (blockDim.x / L);
+    for (uint32_t i0 = first; i0 < n; i0 += per) {
+      const uint32_t m = min(n - i0, blockDim.x / L);
+      colour_tile<DBG, L>(
+          b, NbrGlobal{src, b.NBR, stride}, [&](uint32_t p) { return src[p]; },
+          [&](uint32_t p, int4 me, int2 dp) { moved(S, p, me, dp); }, lo + i0, m, f);
+    }
+    // every other record of the tile, and the class's walls, copied
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n0; i += gridDim.x * blockDim.x) {
+      const uint32_t p = p0 + i;
+      const int4 me = src[p];
+      if (p - lo < n && !((uint32_t)me.w & INFO_BOUNDARY)) continue;
+      put(p, me);
+    }
   }
 }
 

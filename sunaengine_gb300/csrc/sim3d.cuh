@@ -50,6 +50,24 @@ constexpr int LUT_WORDS = 2 * LUT_N + 2 * PLANE_N;
 constexpr int32_t RHO0 = 1048576, C_MAX = 1048576, LAM_MAX = 4194304, EPS_S = 524288;
 constexpr int32_t S_TERM = 8388608, MARGIN = 32768, BALL_R2MAX = 4194304;
 constexpr uint32_t TAG_W = 0xfffu, TAG_SHIFT = 12;
+constexpr uint32_t TAG_BONDED = 0x80000000u;  // the particle's slot has a bond row
+constexpr uint32_t TAG_SCENE = 0x7ffffu;      // (tag >> TAG_SHIFT) & TAG_SCENE = scene
+__device__ __forceinline__ uint32_t scene_of_tag(uint32_t tag) { return (tag >> TAG_SHIFT) & TAG_SCENE; }
+
+// Bonds (build-defined; the reference's 3D page has none): the 2D engine's
+// bond distance constraint (src/sim.wgsl:1594-1671, the bond gather of
+// friction at :1880-1934) restated over three axes. Each slot has a row of
+// BOND3_CAP entries of two words, {partner + 1 | BOND3_TOMB, L0}: the partner's
+// scene-local index plus one (0 ends the row), and the rest length in ticks
+// >> 5. A bond is stored in both ends' rows.
+constexpr uint32_t BOND3_CAP = 6, BOND3_WORDS = 2 * BOND3_CAP;
+constexpr uint32_t BOND3_TOMB = 0x80000000u, BOND3_J = 0x7fffffffu;
+constexpr int BOND3_PRE = 5;               // d4 = d >> 5 (round half even)
+constexpr int32_t BOND3_L0_MIN = 512, BOND3_L0_MAX = 5120;
+constexpr int32_t BOND3_HARD_BREAK2 = 26214400;  // L0_MAX^2
+constexpr int32_t BOND3_D2_FLOOR = 262144;
+constexpr int32_t BOND3_TERM = 16777216;
+constexpr int32_t BOND3_DP_MAX = 16384;    // a bond moves a particle at most 1/4 wu per iteration
 constexpr uint32_t NO_SCENE = 0xffffffffu;
 constexpr uint32_t MAX_AXIS_CELLS = 52;  // keeps the reference's wrapping r2q of any in-world pair non-negative
 
@@ -64,7 +82,9 @@ struct Scene3 {
   uint32_t active;
   uint32_t substep;  // this scene's substep counter (low 32 bits), advanced by k3_fold
   uint32_t frame;    // 0: stir phase fixed per step call; F > 0: fixed per frame of F substeps
-  uint32_t pad;
+  int32_t bondK;     // bond stiffness, Q16 (0..65536)
+  int32_t bondBrk;   // a bond breaks when d^2 > L0^2 * bondBrk / 2^16 (0: never, by ratio)
+  uint32_t pad[3];
 };
 
 struct World3 {
@@ -74,6 +94,9 @@ struct World3 {
 struct Bufs3 {
   int32_t* state;
   uint32_t* sceneOf;
+  uint32_t* bond;     // [cap * BOND3_WORDS] bond rows, slot order
+  uint32_t* bflag;    // [cap] 1 when the slot's row holds an entry
+  uint32_t* inv;      // [cap] slot -> sorted position (this substep)
   int4* PRS;
   uint32_t *keys, *skey, *sslot, *cellStart;
   int4 *PW, *PW2, *PL;
@@ -153,7 +176,8 @@ __global__ void __launch_bounds__(256) k3_predict(Bufs3 b) {
     vy = mul<16>(vy, damp, f);
     vz = mul<16>(vz, damp, f);
     int3 pr = clamp_world(S, add_sat(p.x, vx, f), add_sat(p.y, vy, f), add_sat(p.z, vz, f));
-    b.PRS[slot] = make_int4(pr.x, pr.y, pr.z, (int32_t)((uint32_t)(256 + rhoW) | (sc << TAG_SHIFT)));
+    const uint32_t bonded = b.bflag[slot] ? TAG_BONDED : 0u;
+    b.PRS[slot] = make_int4(pr.x, pr.y, pr.z, (int32_t)((uint32_t)(256 + rhoW) | (sc << TAG_SHIFT) | bonded));
     uint32_t cx = (uint32_t)pr.x >> HSHIFT, cy = (uint32_t)pr.y >> HSHIFT, cz = (uint32_t)pr.z >> HSHIFT;
     b.keys[slot] = S.keyOff + (cz * S.gy + cy) * S.gx + cx;
   }
@@ -166,7 +190,11 @@ __global__ void __launch_bounds__(256) k3_cellstart(Bufs3 b) {
 
 __global__ void __launch_bounds__(256) k3_gather(Bufs3 b) {
   const uint32_t nAct = b.world->nAct;
-  for (uint32_t s = gtid3(); s < nAct; s += gstride3()) b.PW[s] = b.PRS[b.sslot[s]];
+  for (uint32_t s = gtid3(); s < nAct; s += gstride3()) {
+    const uint32_t slot = b.sslot[s];
+    b.PW[s] = b.PRS[slot];
+    b.inv[slot] = s;
+  }
 }
 
 // buildNbr (3d/sim3d.wgsl:341-390): dz, dy, dx, ascending id; MAXNBR cut
@@ -180,7 +208,7 @@ __global__ void __launch_bounds__(256) k3_nbr(Bufs3 b) {
     Flags<DBG> f{b.dbg};
     for (uint32_t s = gtid3(); s < nAct; s += gstride3()) {
       const int4 me = b.PW[s];
-      const uint32_t sc = (uint32_t)me.w >> TAG_SHIFT;
+      const uint32_t sc = scene_of_tag((uint32_t)me.w);
       const Scene3& S = b.scenes[sc];
       const int32_t cx = me.x >> HSHIFT, cy = me.y >> HSHIFT, cz = me.z >> HSHIFT;
       const int32_t x0 = max(cx - 1, 0), x1 = min(cx + 1, (int32_t)S.gx - 1);
@@ -220,7 +248,7 @@ __global__ void __launch_bounds__(256) k3_nbr(Bufs3 b) {
     if (__shfl_sync(0xffffffffu, s, 0) >= nAct) break;  // warp-uniform exit
     const bool valid = s < nAct;
     const int4 me = valid ? b.PW[s] : make_int4(0, 0, 0, 0);
-    const uint32_t sc = (uint32_t)me.w >> TAG_SHIFT;
+    const uint32_t sc = scene_of_tag((uint32_t)me.w);
     const Scene3& S = b.scenes[sc];
     const int32_t cx = me.x >> HSHIFT, cy = me.y >> HSHIFT, cz = me.z >> HSHIFT;
     const int32_t x0 = max(cx - 1, 0), x1 = min(cx + 1, (int32_t)S.gx - 1);
@@ -327,7 +355,7 @@ __global__ void __launch_bounds__(256) k3_density(Bufs3 b, const int4* __restric
       sgz = gsum3<L>(sgz);
     }
     if (!valid || sub != 0) continue;
-    const uint32_t sc = (uint32_t)me.w >> TAG_SHIFT;
+    const uint32_t sc = scene_of_tag((uint32_t)me.w);
     const Scene3& S = b.scenes[sc];
     rho = wadd(rho, wmul(W0, (int32_t)((uint32_t)me.w & TAG_W)) >> 8);
 #pragma unroll
@@ -372,6 +400,50 @@ __device__ __forceinline__ bool dp_term(const Bufs3& b, const int4& me, const in
   ty = mulf<20>(lsum, mulf<16>(gt, dy, f), f);
   tz = mulf<20>(lsum, mulf<16>(gt, dz, f), f);
   return true;
+}
+
+// The bond correction of one bonded particle from the iteration's starting
+// positions (PL), its row walked in order; a bond whose ends have parted too
+// far is tombstoned in this end's row (the test is symmetric, so the other end
+// tombstones its copy in the same pass). Per bond, as the 2D constraint:
+// d4 = (p_i - p_j) >> 5, C = |d4|^2 - L0^2, q = C / (4 |d4|^2) (Q16), and
+// each axis sums -clamp(d4 * q * k >> 3); the sum moves the particle by
+// clamp(sum >> 8 (round half even), +-BOND3_DP_MAX).
+template <bool DBG>
+__device__ __forceinline__ int3 bond_dp(const Bufs3& b, const Scene3& S, uint32_t slot, const int4& me,
+                                        const Flags<DBG>& f) {
+  uint32_t* row = b.bond + (size_t)slot * BOND3_WORDS;
+  int32_t bx = 0, by = 0, bz = 0;
+  for (uint32_t k = 0; k < BOND3_CAP; ++k) {
+    const uint32_t w = row[2 * k];
+    if (w == 0u) break;
+    if (w & BOND3_TOMB) continue;
+    const int32_t L0 = (int32_t)row[2 * k + 1];
+    const int32_t L02 = wmul(L0, L0);
+    const int4 o = b.PL[b.inv[S.slotBase + (w & BOND3_J) - 1u]];
+    const int32_t d4x = shr_rne<BOND3_PRE>(sub_sat(me.x, o.x, f));
+    const int32_t d4y = shr_rne<BOND3_PRE>(sub_sat(me.y, o.y, f));
+    const int32_t d4z = shr_rne<BOND3_PRE>(sub_sat(me.z, o.z, f));
+    if (abs(d4x) > BOND3_L0_MAX || abs(d4y) > BOND3_L0_MAX || abs(d4z) > BOND3_L0_MAX) {
+      row[2 * k] = w | BOND3_TOMB;
+      continue;
+    }
+    const int32_t d2 = wadd(wadd(wmul(d4x, d4x), wmul(d4y, d4y)), wmul(d4z, d4z));
+    if (d2 >= BOND3_HARD_BREAK2 || (S.bondBrk != 0 && d2 > mul<16>(L02, S.bondBrk, f))) {
+      row[2 * k] = w | BOND3_TOMB;
+      continue;
+    }
+    if (d2 < BOND3_D2_FLOOR) continue;
+    const int32_t C = sub_sat(d2, L02, f);
+    const int32_t qv = divshift<16>(C, wmul(d2, 4), b.rcp, f);
+    const int32_t qk = mul<16>(qv, S.bondK, f);
+    bx = wsub(bx, clampi(mul<3>(d4x, qk, f), -BOND3_TERM, BOND3_TERM));
+    by = wsub(by, clampi(mul<3>(d4y, qk, f), -BOND3_TERM, BOND3_TERM));
+    bz = wsub(bz, clampi(mul<3>(d4z, qk, f), -BOND3_TERM, BOND3_TERM));
+  }
+  return make_int3(clampi(shr_rne<8>(bx), -BOND3_DP_MAX, BOND3_DP_MAX),
+                   clampi(shr_rne<8>(by), -BOND3_DP_MAX, BOND3_DP_MAX),
+                   clampi(shr_rne<8>(bz), -BOND3_DP_MAX, BOND3_DP_MAX));
 }
 
 // solveDp + applyDp (3d/sim3d.wgsl:476-537), fused over a double buffer:
@@ -439,7 +511,7 @@ __global__ void __launch_bounds__(256) k3_solve(Bufs3 b, const int4* __restrict_
       }
     }
     const int32_t tag = PWin[s].w;
-    const uint32_t sc = (uint32_t)tag >> TAG_SHIFT;
+    const uint32_t sc = scene_of_tag((uint32_t)tag);
     const Scene3& S = b.scenes[sc];
     const int32_t lami = me.w;
 #pragma unroll
@@ -460,6 +532,12 @@ __global__ void __launch_bounds__(256) k3_solve(Bufs3 b, const int4* __restrict_
       ax = add_sat(ax, mul<20>(lami, bg.x, f), f);
       ay = add_sat(ay, mul<20>(lami, bg.y, f), f);
       az = add_sat(az, mul<20>(lami, bg.z, f), f);
+    }
+    if ((uint32_t)tag & TAG_BONDED) {
+      const int3 bd = bond_dp(b, S, b.sslot[s], me, f);
+      ax = add_sat(ax, bd.x, f);
+      ay = add_sat(ay, bd.y, f);
+      az = add_sat(az, bd.z, f);
     }
     int3 pr = clamp_world(S, add_sat(me.x, ax, f), add_sat(me.y, ay, f), add_sat(me.z, az, f));
     PWout[s] = make_int4(pr.x, pr.y, pr.z, tag);
@@ -482,7 +560,7 @@ __global__ void __launch_bounds__(256) k3_integrate(Bufs3 b, const int4* __restr
     if (valid) {
       uint32_t slot = b.sslot[s];
       int4 pr = PW[s];
-      sc = (uint32_t)pr.w >> TAG_SHIFT;
+      sc = scene_of_tag((uint32_t)pr.w);
       local = slot - b.scenes[sc].slotBase;
       int4* w4 = reinterpret_cast<int4*>(b.state + (size_t)slot * 8);
       int4 p = w4[0];

@@ -5,13 +5,27 @@
 //   * SLOT space: each scene owns a contiguous slot range [slotBase, slotBase+cap).
 //     Slot i - slotBase is the reference's particle index (fluid first, then the
 //     boundary block), so hashed state words, stAcc and bond rows live here.
-//   * SORTED space: every active particle of every scene, ordered by grid key.
-//     Keys are colour-major: all scenes' colour-0 cells, then colour-1, ...; a
-//     scene's cells of one colour are in (cy/2, cx/2) row-major order; inside
-//     a cell, particles are in ascending slot order (the reference's canonical
-//     order, src/sim.wgsl:1126-1168). One colour class is therefore one
-//     contiguous sorted range, and every solver gather reads neighbours from a
-//     few nearby ranges.
+//   * SORTED space: every active particle of every scene, ordered by grid key,
+//     in one of two layouts chosen per world.
+//     Colour-major (the default): all scenes' colour-0 cells, then colour-1,
+//     ...; a scene's cells of one colour are in (cy/2, cx/2) row-major order.
+//     One colour class is one contiguous sorted range.
+//     Tile-major (the staged gathers): each scene's grid is cut into square
+//     tiles of T x T cells (T = 2^tileShift), tiles in row-major order, and
+//     inside a tile the four colour classes one after another, each colour's
+//     cells in (ly/2, lx/2) row-major order. A tile's particles are one
+//     contiguous sorted range, and so is each colour class inside it.
+//     In both layouts the particles of a cell are in ascending slot order (the
+//     reference's canonical order, src/sim.wgsl:1126-1168).
+//
+// In the tile-major layout a tile's neighbourhood (the tile plus a one-cell
+// ring around it) is 9 + 2T contiguous runs of sorted space: the tile itself,
+// the two colour runs of the halo row below and of the row above (a colour's
+// cells in one tile row are consecutive keys), and the T + 2 single cells of
+// the halo column on each side. The per-substep run table (TR) lists each
+// run's first sorted position and its offset in the tile's staged copy; the
+// staged kernels copy the runs into shared memory with bulk copies and read
+// neighbours there through 16-bit tile-local indices.
 #pragma once
 #include <cstdint>
 
@@ -24,6 +38,17 @@ constexpr int MAT_MAX = 64;
 constexpr int TN = 3202;
 constexpr int LUT_WORDS = 5 * TN;
 constexpr uint32_t NBR_BOUNDARY = 0x80000000u;  // set in a neighbour entry when it is a wall particle
+constexpr uint16_t NBRL_BOUNDARY = 0x8000u;     // the same flag in a tile-local (16-bit) entry
+constexpr uint16_t NBRL_INDEX = 0x7fffu;
+
+// Tiles: side 2^tileShift cells, tileShift in [TILE_SHIFT_MIN, TILE_SHIFT_MAX].
+constexpr uint32_t TILE_SHIFT_MIN = 2, TILE_SHIFT_MAX = 4;
+constexpr uint32_t TR_RUNS_MAX = 9 + 2 * (1u << TILE_SHIFT_MAX);  // 41
+constexpr uint32_t TR_STRIDE = 96;   // words per tile: [0, 48) run starts, [48, 96) run offsets (+ total)
+constexpr uint32_t TR_BASE = 48;
+// A tile whose neighbourhood holds more records than the staged kernels'
+// shared-memory copy is gathered from global memory instead.
+constexpr uint32_t STAGE_MAX = 2048;
 
 // Per-scene parameters (the reference's Params uniform, src/sim.wgsl:225-300,
 // plus this layout's key offsets).
@@ -34,8 +59,12 @@ struct ScenePar {
   uint32_t gridW, gridH, cellShift, cellTotal;
   int32_t domW, domH, vmax;
   uint32_t weldHold;   // the weld tag a gesture holds open (0: none)
-  uint32_t keyOff[4];  // global key of this scene's first colour-c cell
-  uint32_t nA[4];      // colour-c cells per grid row: (gridW + 1 - (c & 1)) / 2
+  uint32_t keyOff[4];  // colour-major layout: global key of this scene's first colour-c cell
+  uint32_t nA[4];      // colour-major layout: colour-c cells per grid row, (gridW + 1 - (c & 1)) / 2
+  uint32_t tileShift;  // 0: colour-major layout; else tile-major, tile side = 2^tileShift cells
+  uint32_t keyBase;    // tile-major layout: global key of this scene's first cell (its first tile)
+  uint32_t tileBase;   // tile-major layout: global index of this scene's first tile
+  uint32_t tilesX, tilesY;
   uint32_t formClock;  // formation clock (the engine's `_substep`), advanced on device
   uint32_t bondDirty;  // run formation on the next substep regardless of the clock
   uint32_t formNow;    // formation runs in the substep in flight (set by predict)
@@ -50,13 +79,20 @@ struct ScenePar {
 // World-level totals, written by the host when the scene set changes.
 struct WorldPar {
   uint32_t numScenes;
-  uint32_t K;              // total grid cells over all scenes = sentinel key
-  uint32_t colourBase[5];  // first global key of each colour class; [4] = K
+  uint32_t K;              // total grid keys over all scenes = sentinel key
+  uint32_t colourBase[5];  // colour-major layout: first key of each colour class; [4] = K
+  uint32_t nTiles;         // tile-major layout: tiles over all scenes (0 in the colour-major layout)
+  uint32_t stageCap;       // records a staged kernel copies per tile at most (its shared-memory copy)
   uint32_t slotEnd;        // 1 + last slot that can be active
   uint32_t nAct;           // active particles (sorted-space length)
   uint32_t hasFriction;    // some material has fric != 0 or bondK != 0
   uint32_t hasBonds;       // some material has bondK != 0
   uint32_t nBodies;        // §20 body records (all scenes)
+};
+
+// One tile of the world: its scene, its tile coordinates and its first key.
+struct TileInfo {
+  uint32_t scene, tx, ty, key0;
 };
 
 #ifdef __CUDACC__

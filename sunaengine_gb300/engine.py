@@ -526,6 +526,12 @@ class Engine:
         a = np.array([lanes[k] for k in ('solveA', 'colours', 'post1', 'post2', 'nbr')], np.uint32)
         self._check(self._lib.sn_set_lanes(self._h, _ptr(a)), 'setLanes')
 
+    def set_staged(self, on: bool = True):
+        """Tile-major sorted space with shared-memory staged gathers for solveA
+        and the colour passes (same results; see sn_set_staged)."""
+        self._check(self._lib.sn_set_staged(self._h, 1 if on else 0), 'setStaged')
+        return self
+
     def profile_substep(self, reps: int = 3) -> np.ndarray:
         """Mean device ms per kernel phase over `reps` real substeps (profileSubstep)."""
         out = np.zeros(64, np.float32)
@@ -772,6 +778,11 @@ class Batch:
     def set_lanes(self, lanes: dict):
         a = np.array([lanes[k] for k in ('solveA', 'colours', 'post1', 'post2', 'nbr')], np.uint32)
         self._check(self._lib.sn_batch_set_lanes(self._h, _ptr(a)), 'setLanes')
+
+    def set_staged(self, on: bool = True):
+        """Tile-major sorted space with shared-memory staged gathers (sn_batch_set_staged)."""
+        self._check(self._lib.sn_batch_set_staged(self._h, 1 if on else 0), 'setStaged')
+        return self
 
     # device keyframes (sn_batch_ckpt_*): see checkpoints.CheckpointPool
     def ckpt_bytes(self, sid: int) -> int:

@@ -170,6 +170,19 @@ class Engine3D:
         self._check(self._lib.sn3_read_state(self.h, int(scene), _ptr(a), a.size), 'read_state')
         return a
 
+    def write_bonds(self, rows, stiffness: int, break_ratio: int, scene: int = 0):
+        """Build-defined bonds of a scene (sn3_write_bonds): rows of
+        tables3d.BOND3_WORDS words per particle (tables3d.bond_rows)."""
+        a = np.ascontiguousarray(np.asarray(rows, np.uint32).reshape(-1))
+        self._check(self._lib.sn3_write_bonds(self.h, int(scene), _ptr(a), a.size, int(stiffness), int(break_ratio)),
+                    'write_bonds')
+
+    def read_bonds(self, scene: int = 0) -> np.ndarray:
+        n = self.info(scene)['n']
+        a = np.zeros(max(1, n * tables3d.BOND3_WORDS), np.uint32)
+        self._check(self._lib.sn3_read_bonds(self.h, int(scene), _ptr(a), a.size), 'read_bonds')
+        return a[:n * tables3d.BOND3_WORDS]
+
     def write_state(self, state, substeps: int, chain_words=None, scene: int = 0):
         st = np.ascontiguousarray(np.asarray(state).reshape(-1), dtype=np.int32)
         if st.size % 8:

@@ -269,3 +269,80 @@ class SpawnSeed:
             out[i] = (js_round((cx + dx * rad) * ONE), js_round((cy + dy * rad) * ONE),
                       js_round((cz + dz * rad) * ONE))
         return out
+
+
+# ---- build-defined 3D bonds -------------------------------------------------------
+# The reference's 3D page has no bonds; the 3D dam-break workload asks for
+# 4096 seeded bonds between lattice neighbours. They use the 2D engine's bond
+# distance constraint restated over three axes (the engine's sn3_write_bonds):
+# a row of BOND3_CAP entries {partner + 1, L0} per particle, L0 the rest
+# length in ticks >> 5.
+BOND3_CAP = 6
+BOND3_WORDS = 2 * BOND3_CAP
+BOND3_L0_MIN, BOND3_L0_MAX = 512, 5120
+DAM3D_BONDS = 4096
+DAM3D_BOND_SEED = 0xb0d3
+DAM3D_BOND_K = 32768          # stiffness 0.5 (Q16)
+DAM3D_BOND_BRK = 4 * 65536    # breaks past twice its rest length
+
+
+def lattice_index(bx: int, by: int, bz: int, i: int, j: int, k: int) -> int:
+    """Particle index of lattice site (i, j, k) in a ``column_fast`` block:
+    x fastest, then z, then y."""
+    return (j * bz + k) * bx + i
+
+
+def lattice_bonds(bx: int, by: int, bz: int, count: int, seed: int) -> np.ndarray:
+    """``count`` distinct bonds between face-adjacent lattice sites of a
+    bx x by x bz block, drawn from a seeded stream: a site and an axis (+x,
+    +y, +z), redrawn when the neighbour is outside the block or the pair is
+    already bonded. Returns (count, 2) particle indices, first < second, in
+    draw order."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    seen, out = set(), []
+    while len(out) < count:
+        i, j, k = (int(v) for v in rng.integers(0, (bx, by, bz)))
+        axis = int(rng.integers(0, 3))
+        i2, j2, k2 = i + (axis == 0), j + (axis == 1), k + (axis == 2)
+        if i2 >= bx or j2 >= by or k2 >= bz:
+            continue
+        a, b = lattice_index(bx, by, bz, i, j, k), lattice_index(bx, by, bz, i2, j2, k2)
+        if (a, b) in seen:
+            continue
+        seen.add((a, b))
+        out.append((a, b))
+    return np.array(out, np.int64)
+
+
+def dam3d_bonds(sc: 'Scene3D') -> np.ndarray:
+    """The 3D dam break's 4096 seeded lattice-neighbour bonds."""
+    assert sc.n == 64 * 64 * 64
+    return lattice_bonds(64, 64, 64, DAM3D_BONDS, DAM3D_BOND_SEED)
+
+
+def _shr_rne(x: np.ndarray, s: int) -> np.ndarray:
+    """Arithmetic shift right by s, rounding half to even (the engine's shr_rne)."""
+    x = np.asarray(x, np.int64)
+    q = x >> s
+    r = x - (q << s)
+    half = 1 << (s - 1)
+    return q + ((r > half) | ((r == half) & (q & 1 == 1))).astype(np.int64)
+
+
+def bond_rows(sc: 'Scene3D', bonds: np.ndarray) -> np.ndarray:
+    """Rows for sn3_write_bonds: each bond (a, b) appended to both ends' rows
+    in bond order, with rest length L0 = floor(sqrt(|d4|^2)) of the scene's
+    starting positions (d4 = (p_a - p_b) >> 5, rounded half to even), clamped
+    to [512, 5120]."""
+    rows = np.zeros((sc.n, BOND3_CAP, 2), np.uint32)
+    fill = np.zeros(sc.n, np.int64)
+    pos = np.asarray(sc.pos, np.int64)
+    for a, b in np.asarray(bonds, np.int64):
+        d4 = _shr_rne(pos[a] - pos[b], 5)
+        L0 = min(max(math.isqrt(int((d4 * d4).sum())), BOND3_L0_MIN), BOND3_L0_MAX)
+        for u, v in ((a, b), (b, a)):
+            if fill[u] >= BOND3_CAP:
+                raise ValueError(f'particle {u} has more than {BOND3_CAP} bonds')
+            rows[u, fill[u]] = (v + 1, L0)
+            fill[u] += 1
+    return rows.reshape(-1)

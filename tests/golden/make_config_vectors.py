@@ -60,7 +60,10 @@ def _scene2d(name):
 def record_2d(name: str, threads: int):
     import oracle
     sc, total = _scene2d(name)
-    e = oracle.OracleEngine(sc.n + 64, threads=threads).load_scene(sc)
+    # the neighbour-list cut changes no state word, list or flag (only the
+    # overflow debug counter); without it the crowded corner cell these scenes
+    # build (up to 10^5 particles) makes each substep O(occupancy^2)
+    e = oracle.OracleEngine(sc.n + 64, threads=threads).load_scene(sc).set_nbr_cut(True)
     chain, digest = [], {}
     t0 = time.time()
     for k in range(1, total + 1):
@@ -103,7 +106,7 @@ def _batch_one(args):
     from sunaengine_gb300 import scenes
     scs, sched = scenes.batch_scenes(count=256, seed=0xba7c4, substeps=total)
     sc, ev = scs[sid], sched[sid]
-    e = oracle.OracleEngine(sc.n + 8, threads=1).load_scene(sc)
+    e = oracle.OracleEngine(sc.n + 8, threads=1).load_scene(sc).set_nbr_cut(True)
     at = {}
     for (s, cx, cy, r, ix, iy) in ev:
         at.setdefault(s, []).append((cx, cy, r, ix, iy))

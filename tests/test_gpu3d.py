@@ -164,3 +164,39 @@ def test_lane_split_gathers_are_exact(lanes, name, n):
     same(g, r)
     if lanes == 2:
         assert np.array_equal(g.debug_counters(), r.debug_counters())
+
+
+@pytest.mark.parametrize('debug,brk', [(False, 4 * 65536), (True, 4 * 65536), (False, 70000)])
+def test_bonds_match_oracle(debug, brk):
+    """Build-defined 3D bonds on the GPU against the oracle: chain, state,
+    bond rows (tombstones included: brk 70000 breaks some) and, in the debug
+    build, the fixed-point event counters."""
+    sc = tables3d.column_fast(16, 16, 16, 20, 20, 20)
+    rows = tables3d.bond_rows(sc, tables3d.lattice_bonds(16, 16, 16, 600, 7))
+    g, r = both(sc, iters=4, debug=debug)
+    g.write_bonds(rows, 32768, brk)
+    r.write_bonds(rows, 32768, brk)
+    for k in (1, 5, 20, 14):
+        g.step(k)
+        r.step(k)
+        same(g, r)
+    assert np.array_equal(g.read_bonds(), r.read_bonds())
+    if debug:
+        assert np.array_equal(g.debug_counters(), r.debug_counters())
+
+
+def test_bonds_refused_and_cleared():
+    from sunaengine_gb300.engine import EngineError
+    sc = tables3d.column_fast(8, 8, 8, 12, 12, 12)
+    rows = tables3d.bond_rows(sc, tables3d.lattice_bonds(8, 8, 8, 40, 3)).reshape(-1, 6, 2)
+    g = Engine3D(max_particles=sc.n).load_scene(sc)
+    bad = rows.copy()
+    bad[0, 0, 1] = 100  # rest length below the minimum
+    with pytest.raises(EngineError):
+        g.write_bonds(bad, 32768, 0)
+    with pytest.raises(EngineError):
+        g.write_bonds(rows, 70000, 0)  # stiffness above 1.0
+    g.write_bonds(rows, 32768, 0)
+    assert (g.read_bonds().reshape(-1, 6, 2)[:, :, 0] != 0).sum() == 80
+    g.load_scene(sc)  # a load clears the scene's bonds
+    assert not g.read_bonds().any()

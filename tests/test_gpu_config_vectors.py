@@ -69,7 +69,7 @@ def test_dam3d_64cubed_full_length():
     for k, want in enumerate(vec['chain'], start=1):
         e.step(1)
         assert e.chain_hex() == want, f'chain differs at substep {k}'
-    assert e.fnv() == vec['fnv']
+    assert e.fnv_hex() == vec["fnv"]
     e.close()
 
 

@@ -26,11 +26,8 @@ def test_fields_match_the_oracle():
     assert np.array_equal(rho[:sc.nFluid], r.read_derived().reshape(-1, 16)[:sc.nFluid, 10])
     assert np.array_equal(nbr[:sc.nFluid], r.read_nbr_counts()[:sc.nFluid])
     assert not rho[sc.nFluid:].any() and not nbr[sc.nFluid:].any()
-    cs = g.read_cell_start()
     ct = g.info()['cell_total']
-    occ_g = np.sort(np.diff(cs.astype(np.int64)))
-    occ_r = np.sort(np.diff(r.read_cell_start(ct).astype(np.int64)))
-    assert np.array_equal(occ_g, occ_r)
+    assert np.array_equal(g.read_cell_start(), r.read_cell_start(ct))  # the reference's row-major layout
     # an edit that changes slots invalidates them until the next substep
     g.spawn_fluid([{'x': 40 * 65536, 'y': 40 * 65536, 'mat': 0}])
     with pytest.raises(EngineError):

@@ -102,3 +102,21 @@ def test_oracle_one_tick_control(oracle_mod):
     a.step(20)
     b.step(20)
     assert a.digest() != b.digest()
+
+
+def test_neighbour_cut_changes_no_state(oracle_mod):
+    """The oracle's neighbour-list cut (stop a full list's scan when no fluid
+    particle carries a seal or congeal flag) leaves every state word, chain
+    and neighbour count as the full scan gives them; only the overflow debug
+    counter stops counting. The overdense scene overflows its lists."""
+    import numpy as np
+    sc = scenes.make_scene('overdense_v1')
+    a = oracle_mod.OracleEngine(sc.n + 64, threads=4).load_scene(sc)
+    b = oracle_mod.OracleEngine(sc.n + 64, threads=4).load_scene(sc).set_nbr_cut(True)
+    for _ in range(4):
+        a.step(5)
+        b.step(5)
+        assert a.chain_hex() == b.chain_hex()
+        assert np.array_equal(a.read_state(), b.read_state())
+        assert np.array_equal(a.read_nbr_counts(), b.read_nbr_counts())
+    assert a.debug_counters()[6] > 0 and b.debug_counters()[6] < a.debug_counters()[6]

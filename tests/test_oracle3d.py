@@ -128,3 +128,48 @@ def test_spawn_and_ball_inputs():
     assert o.n == 3100 and not np.array_equal(before, after[:3100])
     # the spawned particles start at rest where they were put, then move
     assert not np.array_equal(after[3000:, :3], pos) and np.all(after[3000:, 3] == 3)
+
+
+def test_bonds_hold_pairs_and_break_symmetrically():
+    """Build-defined 3D bonds (the 2D bond constraint over three axes): bonded
+    lattice neighbours stay near their rest length while unbonded ones drift;
+    a bond breaks in both ends' rows in the same pass; the rows refuse bad
+    input."""
+    sc = tables3d.column_fast(16, 16, 16, 20, 20, 20)
+    bonds = tables3d.lattice_bonds(16, 16, 16, 600, 7)
+    rows = tables3d.bond_rows(sc, bonds)
+    free = oracle3(sc.n, iters=4, threads=4).load_scene(sc)
+    held = oracle3(sc.n, iters=4, threads=4).load_scene(sc).write_bonds(rows, 32768, 4 * 65536)
+    free.step(60)
+    held.step(60)
+    assert free.chain_hex() != held.chain_hex()
+    pf = free.read_state().reshape(-1, 8)[:, :3].astype(np.int64)
+    ph = held.read_state().reshape(-1, 8)[:, :3].astype(np.int64)
+    dist = lambda p: np.sqrt(((p[bonds[:, 0]] - p[bonds[:, 1]]) ** 2).sum(1)) / 65536
+    assert dist(ph).max() < 1.2 < dist(pf).max()
+    # a tight break ratio: bonds break, always in both rows
+    tight = oracle3(sc.n, iters=4, threads=4).load_scene(sc).write_bonds(rows, 32768, 70000)
+    tight.step(40)
+    r = tight.read_bonds().reshape(-1, 6, 2)
+    broken = 0
+    for a, b in bonds:
+        ta = [bool(w >> 31) for w, _ in r[a] if w and (w & 0x7fffffff) - 1 == b]
+        tb = [bool(w >> 31) for w, _ in r[b] if w and (w & 0x7fffffff) - 1 == a]
+        assert ta == tb
+        broken += ta[0]
+    assert 0 < broken < len(bonds)
+    with pytest.raises(ValueError):
+        bad = rows.copy().reshape(-1, 6, 2)
+        bad[0, 0, 0] = sc.n + 5  # partner outside the scene
+        oracle3(sc.n).load_scene(sc).write_bonds(bad, 32768, 0)
+
+
+def test_dam3d_bond_layout():
+    sc = tables3d.dam3d_large()
+    bonds = tables3d.dam3d_bonds(sc)
+    assert len(bonds) == 4096 and len({tuple(b) for b in bonds}) == 4096
+    d = np.abs(sc.pos[bonds[:, 0]].astype(np.int64) - sc.pos[bonds[:, 1]].astype(np.int64))
+    # lattice neighbours: one axis about 1 wu apart, the others within the jitter
+    assert ((d.max(1) > 40000) & (d.max(1) < 80000)).all()
+    rows = tables3d.bond_rows(sc, bonds).reshape(-1, 6, 2)
+    assert (rows[:, :, 0] != 0).sum() == 2 * 4096
