@@ -10,20 +10,26 @@ alternating 64-column bands, per-particle temperatures uniform in
 on. One step = one substep of that scene. The working set (~0.5 GB) is far
 larger than the 129 MB L2, so no L2 flush is needed between substeps.
 
-Printed: one JSON line with the device-timed value, the end-to-end value
-through the public API (scene upload from host memory, a digest read back
-after every substep, final state read back), the per-phase roofline of the
-dominant kernel, the CPU baseline, the batched workload (256 scenes of
-1k-64k particles with stir impulses) against the same scenes stepped one at a
-time on the plain path, the 3D dam break, the serving stream, the
+Printed: one JSON line with the device-timed value over substeps
+[warmup, warmup + steps) (`config.timed_substeps`), the chain at the window's
+end against the oracle's record (`parity_ok`), the whole stated run of 1000
+substeps (`full_config`, with its own parity), the end-to-end value through
+the public API (scene upload from host memory, a digest read back after every
+substep, final state read back), the per-phase roofline of the dominant
+kernel, the CPU baseline, the batched workload (256 scenes of 1k-64k
+particles with stir impulses, also over its full 1000 substeps) against the
+same scenes stepped one at a time on the plain path, the 3D dam break (with
+its 4096 bonds; also over its full 500 substeps), the serving stream, the
 construction site (rigid bodies and containment at scale, with and without
 its bodies) and GPU clock samples.
 
 --impl reference times the reference's algorithm on the host cores: the
 reference itself is JavaScript + WGSL for WebGPU and cannot run here (no JS
 runtime, no WebGPU), so its CPU restatement (oracle/, pinned bit-exact to the
-reference's golden chain) is timed instead, with all host threads, on a
-65,536-particle sample of the same workload.
+reference's golden chain) is timed instead, with all host threads, on the
+same scene and the same substep window as the GPU arm (a 256 x 256 slice when
+the window is longer than 60 substeps). The CPU baseline in the GPU arm's
+line is the same measurement.
 """
 from __future__ import annotations
 
@@ -43,7 +49,8 @@ sys.path.insert(0, str(ROOT))
 import numpy as np  # noqa: E402
 
 METRIC = 'particle-substeps/s'
-FULL_SUBSTEPS = 1000  # the stated length of the 2D workloads
+FULL_SUBSTEPS = 1000    # the stated length of the 2D workloads
+FULL_SUBSTEPS_3D = 500  # and of the 3D dam break
 UNIT = 'particle-substeps/s'
 WORKLOAD = ('2D large scene: 1,048,576 fluid particles (1024x1024 lattice, 1 wu, +/-0.25 wu seeded jitter), '
             'WATER/OIL 64-column bands, temps U[10,90] deg, ITERS 4, H_slot every substep')
@@ -187,7 +194,7 @@ def parity_against(workload: str, k: int, got: str):
 
 
 # ncu summaries under profiles/ that carry the DRAM traffic of a dominant kernel
-PROFILE_OF = {'colour x4': 'k_colour_2d_large.md', 'solve+apply': 'k3_solve_3d_dam.md', 'density': 'k3_density_3d_dam.md'}
+PROFILE_OF = {'colour x4': 'k_colour_2d_large.md', 'solve+apply': 'k3_solve_3d_dam.md', 'density': 'kernels_3d_dam.md'}
 
 
 def profiled_traffic(phase: str):
@@ -210,53 +217,48 @@ def phase_names(iters: int):
     return names
 
 
-def run_cpu_baseline(sample_side: int = 256, seconds: float = 12.0, threads: int = 0):
-    """The oracle (CPU restatement of the reference substep) on a bounded sample."""
+def run_cpu_baseline(warmup: int, steps: int, threads: int = 0, side: int = 1024):
+    """The oracle (CPU restatement of the reference substep) on the same scene
+    and the same substep window as the GPU's timed region: `warmup` untimed
+    substeps from the load, then `steps` timed ones, all host threads. The
+    1 M-particle scene takes about a second per substep on 16 cores, so the
+    default window (5 + 20 substeps) is about half a minute of CPU work; past
+    60 substeps the window runs on a side x side slice of the scene instead."""
     import oracle
     from sunaengine_gb300 import scenes
     threads = threads or os.cpu_count() or 1
-    sc = scenes.large_two_fluid(side=sample_side)
+    if warmup + steps > 60:
+        side = 256
+    sc = scenes.large_two_fluid(side=side)
     e = oracle.OracleEngine(sc.n + 64, threads=threads).load_scene(sc)
-    e.step(1)
+    e.step(warmup)
     t0 = time.perf_counter()
-    k = 0
-    while True:
-        e.step(1)
-        k += 1
-        if time.perf_counter() - t0 >= seconds:
-            break
+    e.step(steps)
     dt = time.perf_counter() - t0
-    return {'value': sc.nFluid * k / dt, 'unit': UNIT, 'cores': threads, 'kind': 'port',
-            'sample': f'{sc.nFluid} fluid particles ({sample_side}x{sample_side} slice of the same workload), '
-                      f'{k} substeps, {dt:.1f} s'}
+    return {'value': sc.nFluid * steps / dt, 'unit': UNIT, 'cores': threads, 'kind': 'port',
+            'sample': f'{sc.nFluid} fluid particles ({side}x{side} lattice of the same workload), substeps '
+                      f'[{warmup}, {warmup + steps}) timed, {dt:.1f} s'}
 
 
 def reference_arm(args):
     ws, rank, local, dist = _dist()
     if rank != 0:
         return 0
-    import oracle
-    from sunaengine_gb300 import scenes
-    threads = os.cpu_count() or 1
-    side = 256
-    sc = scenes.large_two_fluid(side=side)
-    e = oracle.OracleEngine(sc.n + 64, threads=threads).load_scene(sc)
-    e.step(args.warmup)
-    t0 = time.perf_counter()
-    e.step(args.steps)
-    dt = time.perf_counter() - t0
-    v = sc.nFluid * args.steps / dt
+    cb = run_cpu_baseline(args.warmup, args.steps)
+    v = cb['value']
     line = {
         'impl': 'reference', 'metric': METRIC, 'value': v, 'unit': UNIT, 'n_gpus': args.gpus,
-        'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': 1e3 * dt / args.steps,
+        'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': None,
         'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'int32', 'data': 'synthetic',
-        'config': {'workload': WORKLOAD, 'sample': f'{sc.nFluid}-particle {side}x{side} slice', 'parallelism': 'cpu'},
-        'cpu_baseline': {'value': v, 'unit': UNIT, 'cores': threads, 'kind': 'port',
-                         'sample': f'{sc.nFluid} fluid particles, {args.steps} substeps'},
+        'config': {'workload': WORKLOAD, 'sample': cb['sample'], 'parallelism': 'cpu',
+                   'timed_substeps': [args.warmup, args.warmup + args.steps]},
+        'cpu_baseline': cb,
         'e2e': {'value': v, 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
         'note': 'the reference is JS+WGSL for WebGPU (no JS runtime or WebGPU here); its CPU restatement, '
-                'pinned bit-exact to the reference golden chain, is timed',
+                'pinned bit-exact to the reference golden chain, is timed on the same window of the same scene',
     }
+    n = int(cb['sample'].split()[0])
+    line['ms_per_step'] = 1e3 * n / v
     print(json.dumps(line), flush=True)
     return 0
 
@@ -306,6 +308,17 @@ def workload_3d(steps: int, warmup: int, device: int, cpu_seconds: float = 6.0, 
             'algorithmic_bytes_per_launch': bpl, 'launch_ms': per_launch,
             'phases_ms_per_substep': {k: v[0] for k, v in agg.items()}}
     e.close()
+    # the whole stated run (500 substeps), device-timed, chain against the oracle's at the end
+    ef = Engine3D(max_particles=sc.n, iters=4, device=device).load_scene(sc)
+    ef.write_bonds(rows, tables3d.DAM3D_BOND_K, tables3d.DAM3D_BOND_BRK)
+    ef.sync()
+    ef.step(FULL_SUBSTEPS_3D)
+    ef.sync()
+    fms, _ = ef.last_timing()
+    full = {'substeps': FULL_SUBSTEPS_3D, 'value': sc.n * FULL_SUBSTEPS_3D / (fms / 1e3), 'unit': UNIT,
+            'ms_per_step': fms / FULL_SUBSTEPS_3D,
+            'parity': parity_against('dam3d_64cubed', FULL_SUBSTEPS_3D, ef.chain_hex())}
+    ef.close()
     # end to end: upload the scene, step(1) + digest() per substep, read the state back
     e2 = Engine3D(max_particles=sc.n, iters=4, device=device).load_scene(sc)
     e2.step(1)
@@ -321,6 +334,7 @@ def workload_3d(steps: int, warmup: int, device: int, cpu_seconds: float = 6.0, 
     e2.close()
     out = {'workload': WORKLOAD_3D, 'particles': sc.n, 'steps': steps, 'value': value, 'unit': UNIT,
            'ms_per_step': ms / steps, 'gpu_launches': int(launches), 'roofline': roof, 'parity': parity,
+           'full_config': full,
            'e2e': {'value': sc.n * steps / wall, 'unit': UNIT, 'h2d_bytes_per_step': (sc.n * 28 + rows.nbytes) / steps,
                    'd2h_bytes_per_step': 32 + final.nbytes / steps}}
     if with_cpu:
@@ -358,7 +372,8 @@ def serving_workload(device: int, count: int = 40, rate_hz: float = 4.0, budget_
     return stats
 
 
-def batched_workload(steps: int, warmup: int, device: int, plain_sample: int = 24, seed: int = 0xba7c4):
+def batched_workload(steps: int, warmup: int, device: int, plain_sample: int = 24, seed: int = 0xba7c4,
+                     full_run: bool = True):
     """256 scenes (1k-64k particles, log-uniform) with stir schedules: batched
     vs the same scenes stepped one at a time on the plain path."""
     from sunaengine_gb300 import scenes
@@ -409,6 +424,39 @@ def batched_workload(steps: int, warmup: int, device: int, plain_sample: int = 2
             parity = {'checked_at_substep': at, 'ok': not bad, 'scenes_checked': len(vec['scenes']),
                       'mismatched': bad, 'against': 'tests/golden/config_vectors/batch_256.json'}
     b.destroy()
+    # the whole stated run: FULL_SUBSTEPS substeps of every scene with its
+    # full stir schedule, device-timed in chunks of 100 substeps, the sampled
+    # scenes' chains checked against the oracle's record after every chunk
+    full = None
+    if full_run:
+        scs_f, sched_f = scenes.batch_scenes(count=256, seed=seed, substeps=FULL_SUBSTEPS)
+        bf = Batch(max_particles=total + 16, max_scenes=len(scs_f), max_cells=1 << 22, device=device)
+        for sid, (s_, ev) in enumerate(zip(scs_f, sched_f)):
+            assert bf.add_scene(s_) == sid
+            for (at, cx, cy, r, ix, iy) in ev:
+                bf.schedule_impulse(sid, at, cx, cy, r, ix, iy)
+        bf.set_lanes(lanes_b)
+        vec = json.loads(vp.read_text()) if vp.exists() and seed == 0xba7c4 else None
+        fms, bad, checked = 0.0, [], 0
+        for k in range(100, FULL_SUBSTEPS + 1, 100):
+            bf.step(100)
+            bf.sync()
+            fms += bf.last_timing()[0]
+            if vec is not None:
+                for sid, rec in vec['scenes'].items():
+                    want = rec['chain'].get(str(k))
+                    if want is not None:
+                        checked += 1
+                        if bf.chain_hex(int(sid)) != want:
+                            bad.append((int(sid), k))
+        bf.check_errors()
+        bf.destroy()
+        full = {'substeps': FULL_SUBSTEPS, 'value': nf * FULL_SUBSTEPS / (fms / 1e3), 'unit': UNIT,
+                'ms_per_step': fms / FULL_SUBSTEPS,
+                'parity': {'ok': (not bad) if vec is not None else None, 'chains_checked': checked,
+                           'mismatched': bad[:8],
+                           'against': 'tests/golden/config_vectors/batch_256.json' if vec is not None
+                           else 'not recorded'}}
     # plain path on a sample of the same scenes, one engine per scene, sequentially
     rng = np.random.Generator(np.random.PCG64(seed ^ 0x5a5a))
     pick = rng.choice(len(scs), size=min(plain_sample, len(scs)), replace=False)
@@ -428,7 +476,7 @@ def batched_workload(steps: int, warmup: int, device: int, plain_sample: int = 2
     return {'scenes': len(scs), 'particles': int(nf), 'value': batched, 'unit': UNIT,
             'ms_per_step': ms / steps, 'gpu_launches_per_step': launches // max(1, steps),
             'plain_same_scenes': plain, 'plain_sample_scenes': int(len(pick)), 'lanes': lanes_b,
-            'batched_vs_plain': batched / plain, 'parity': parity}
+            'batched_vs_plain': batched / plain, 'parity': parity, 'full_config': full}
 
 
 def construction_workload(steps: int, warmup: int, device: int, with_cpu: bool = True, cpu_seconds: float = 4.0):
@@ -489,7 +537,7 @@ def sections_only(args):
     line = {'metric': METRIC, 'value': None, 'unit': UNIT, 'n_gpus': ws, 'steps': args.steps,
             'warmup': args.warmup, 'note': 'headline section skipped (--no-2d)'}
     if rank == 0 and not args.no_batched:
-        line['batched'] = batched_workload(args.steps, args.warmup, local)
+        line['batched'] = batched_workload(args.steps, args.warmup, local, full_run=not args.no_full)
     if rank == 0 and not args.no_3d:
         line['cfg3_3d'] = workload_3d(args.steps, args.warmup, local, with_cpu=not args.no_cpu)
     if rank == 0 and not args.no_serving:
@@ -633,7 +681,7 @@ def ours(args):
         'clocks': clk.summary(),
     }
     if rank == 0 and not args.no_batched:
-        line['batched'] = batched_workload(args.steps, args.warmup, local)
+        line['batched'] = batched_workload(args.steps, args.warmup, local, full_run=not args.no_full)
     if rank == 0 and not args.no_3d:
         line['cfg3_3d'] = workload_3d(args.steps, args.warmup, local, with_cpu=not args.no_cpu)
     if rank == 0 and not args.no_serving:
@@ -641,7 +689,7 @@ def ours(args):
     if rank == 0 and not args.no_construction:
         line['construction'] = construction_workload(args.steps, args.warmup, local, with_cpu=not args.no_cpu)
     if rank == 0 and not args.no_cpu:
-        line['cpu_baseline'] = run_cpu_baseline(seconds=args.cpu_seconds)
+        line['cpu_baseline'] = run_cpu_baseline(args.warmup, args.steps)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:
@@ -663,7 +711,6 @@ def main():
                     help='keep the rule-based lanes (profiling runs: a tuner under ncu sees serialised timings)')
     ap.add_argument('--no-serving', action='store_true')
     ap.add_argument('--no-construction', action='store_true')
-    ap.add_argument('--cpu-seconds', type=float, default=12.0)
     ap.add_argument('--no-full', action='store_true', help='skip the full 1000-substep run of the headline workload')
     ap.add_argument('--staged', action='store_true',
                     help='headline engines use the tile-staged gathers (sn_set_staged) instead of the list gathers')

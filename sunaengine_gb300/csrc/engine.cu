@@ -57,11 +57,11 @@ __device__ __forceinline__ bool in_disc(int32_t px, int32_t py, const ImpulseEv&
 }
 
 __device__ uint32_t apply_event(Bufs b, const ScenePar& S, const ImpulseEv& ev) {
-  __shared__ uint32_t wsum[8];
+  __shared__ uint32_t wsum[32];
   __shared__ uint32_t total;
   uint32_t hits = 0;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  for (uint32_t base = 0; base < S.nFluid && hits < ev.limit; base += 256) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = (int)(blockDim.x >> 5);
+  for (uint32_t base = 0; base < S.nFluid && hits < ev.limit; base += blockDim.x) {
     uint32_t i = base + tid;
     bool in = false;
     int32_t* w = nullptr;
@@ -73,7 +73,7 @@ __device__ uint32_t apply_event(Bufs b, const ScenePar& S, const ImpulseEv& ev) 
     if (lane == 0) wsum[warp] = __popc(bal);
     __syncthreads();
     uint32_t before = 0, all = 0;
-    for (int k = 0; k < 8; ++k) {
+    for (int k = 0; k < nw; ++k) {
       if (k < warp) before += wsum[k];
       all += wsum[k];
     }
@@ -93,7 +93,10 @@ __device__ uint32_t apply_event(Bufs b, const ScenePar& S, const ImpulseEv& ev) 
   return hits;
 }
 
-__global__ void __launch_bounds__(256) k_impulse_sched(Bufs b, const ImpulseEv* __restrict__ evs,
+// One CTA of IMPULSE_THREADS per scene: the disc test covers the scene's
+// particles IMPULSE_THREADS at a time, in slot order (the hit ranks).
+constexpr int IMPULSE_THREADS = 1024;
+__global__ void __launch_bounds__(IMPULSE_THREADS) k_impulse_sched(Bufs b, const ImpulseEv* __restrict__ evs,
                                                        EvPar* __restrict__ ep) {
   uint32_t s = blockIdx.x;
   if (s >= b.world->numScenes) return;
@@ -796,7 +799,7 @@ struct World {
     const int ga = grid_for(hw.nAct);
     uint64_t Lc = 0;
     if (anyEvents) {
-      k_impulse_sched<<<hw.numScenes, 256, 0, st>>>(b, devEv, devEp);
+      k_impulse_sched<<<hw.numScenes, IMPULSE_THREADS, 0, st>>>(b, devEv, devEp);
       ++Lc;
     }
     mark();

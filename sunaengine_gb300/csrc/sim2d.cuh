@@ -634,7 +634,7 @@ __global__ void __launch_bounds__(256, TILED ? 6 : 8) k_nbr(Bufs b) {
           const uint32_t delta = local ? tr[TR_BASE + halo_run(ts, tx, ty, gx, gy)] - tr[halo_run(ts, tx, ty, gx, gy)] : 0u;
           for (uint32_t q = lo; q < hi; ++q) {
             if (q == p) continue;
-            int4 o = b.PL[q];
+            const int4 o = b.PL[q];
             uint32_t iq = (uint32_t)o.w;
             if (iq & INFO_DEAD) continue;
             if (lut_index(pdelta(pi, xy(o), f), f) < 0) continue;
