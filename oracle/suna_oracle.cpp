@@ -25,6 +25,9 @@
 #include <vector>
 #include <algorithm>
 #include "fixed_ref.h"
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 using namespace ofx;
 
@@ -122,6 +125,18 @@ struct SnoEngine {
   std::vector<Derived> der;
   std::vector<uint32_t> cellCount, cellStart, cellOf, sortedIds, nbr, nbrN, bond, bondCand;
   uint32_t dbg[16];
+  // Per-thread counters, merged into dbg at the end of every substep and
+  // before any read: a counter that fires on many pairs would otherwise be an
+  // atomic on one shared line for every thread. Counts are order-free sums.
+  static constexpr int DBG_THREADS = 256;
+  alignas(64) uint32_t dbgT[DBG_THREADS][16] = {};
+  void merge_dbg() {
+    for (int t = 0; t < DBG_THREADS; ++t)
+      for (int k = 0; k < 16; ++k) {
+        dbg[k] += dbgT[t][k];
+        dbgT[t][k] = 0;
+      }
+  }
   uint32_t chain[8];
   uint32_t acc[8];
   int parity = 0;
@@ -150,7 +165,14 @@ struct SnoEngine {
   uint32_t sceneNFluid = 0;
   bool sceneHasTemp = false, sceneHasFuel = false;
 
-  Dbg D() { return Dbg{dbg}; }
+  Dbg D() {
+#ifdef _OPENMP
+    const int t = omp_get_thread_num();
+    return Dbg{t < DBG_THREADS ? dbgT[t] : dbg};
+#else
+    return Dbg{dbgT[0]};
+#endif
+  }
   const int32_t* M(uint32_t m) const { return mats[m]; }
 };
 
@@ -1714,6 +1736,7 @@ void substep(E& e) {
   fold_chain(e.chain, e.acc);
   e.parity = 1 - e.parity;
   e.substepCount++;
+  e.merge_dbg();
 }
 
 }  // namespace
@@ -1734,6 +1757,7 @@ SnoEngine* sno_create(uint32_t maxParticles, const int32_t* luts, const int32_t*
   std::memcpy(e->matsAuth, e->mats, sizeof(e->mats));
   e->matCount = e->authoredCount = matCount;
   std::memset(e->dbg, 0, sizeof(e->dbg));
+  std::memset(e->dbgT, 0, sizeof(e->dbgT));
   build_cos_table(e->cosT);
   return e;
 }
@@ -1797,6 +1821,7 @@ int sno_load_scene(SnoEngine* e, uint32_t n, uint32_t nFluid, const int32_t* pos
   e->bond.assign((size_t)cap * BOND_CAP, 0);
   e->bondCand.assign((size_t)cap * BOND_CAP, 0);
   std::memset(e->dbg, 0, sizeof(e->dbg));
+  std::memset(e->dbgT, 0, sizeof(e->dbgT));
   for (uint32_t i = 0; i < n; ++i) {
     uint32_t m = matId[i];
     const int32_t* row = e->mats[m];
@@ -1871,7 +1896,10 @@ void sno_weld_state(SnoEngine* e, uint32_t out[4]) {
 void sno_digest(SnoEngine* e, uint32_t acc[8]) { digest(*e, e->st[e->parity], acc); }
 void sno_chain(SnoEngine* e, uint32_t chain[8]) { std::memcpy(chain, e->chain, sizeof(e->chain)); }
 void sno_reset_chain(SnoEngine* e) { std::memcpy(e->chain, CHAIN_INIT, sizeof(e->chain)); }
-void sno_dbg(SnoEngine* e, uint32_t out[16]) { std::memcpy(out, e->dbg, sizeof(e->dbg)); }
+void sno_dbg(SnoEngine* e, uint32_t out[16]) {
+  e->merge_dbg();
+  std::memcpy(out, e->dbg, sizeof(e->dbg));
+}
 uint32_t sno_n(SnoEngine* e) { return e->n; }
 uint32_t sno_nfluid(SnoEngine* e) { return e->nFluid; }
 uint64_t sno_substeps(SnoEngine* e) { return e->substepCount; }

@@ -135,6 +135,10 @@ __global__ void __launch_bounds__(256) k_slot_fields(Bufs b, uint32_t slotBase, 
   }
 }
 
+__global__ void __launch_bounds__(256) k_fill_u32(uint32_t* __restrict__ out, uint32_t n, uint32_t v) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = v;
+}
+
 template <typename T>
 T* dalloc(size_t count, std::string& err) {
   if (count == 0) count = 1;
@@ -158,9 +162,10 @@ struct SceneHost {
   uint32_t gridW = 1, gridH = 1, cellShift = 18, cellTotal = 1;
   int32_t domW = 0, domH = 0;
   uint64_t substeps = 0;
-  // the loaded scene's arrays: spawnFluid re-packs the boundary block from them
-  std::vector<int32_t> pos, temp, fuel;
-  std::vector<uint32_t> mat;
+  // the loaded scene's boundary block: spawnFluid and setWalls re-pack it
+  std::vector<int32_t> bpos, btemp, bfuel;
+  std::vector<uint32_t> bmat;
+  uint64_t matSeen = 0;  // the material rows any particle of the scene has worn (loaded or spawned)
   uint32_t nFluid0 = 0;
   bool hasTemp = false, hasFuel = false;
   uint32_t weldSeq = 1;                   // _weldSeq: the loaded scene holds tag sequence 1
@@ -235,6 +240,8 @@ struct World {
       if (p) cudaFree(p);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
+    if (st) cudaStreamSynchronize(st);
+    if (pin) cudaFreeHost(pin);
     if (st) cudaStreamDestroy(st);
   }
 
@@ -374,8 +381,8 @@ struct World {
     std::vector<uint32_t> stack;
     for (auto& s : sh) {
       if (!s.used) continue;
-      for (uint32_t m : s.mat)
-        if (m < matCount && !seen[m]) { seen[m] = true; stack.push_back(m); }
+      for (uint32_t m = 0; m < matCount; ++m)
+        if (((s.matSeen >> m) & 1ull) && !seen[m]) { seen[m] = true; stack.push_back(m); }
     }
     // spawns may add any row: be conservative once a scene exists
     while (!stack.empty()) {
@@ -511,6 +518,24 @@ struct World {
     return ok && cuda_ok(cudaStreamSynchronize(st), "relayout");
   }
 
+  // A pinned host staging buffer, grown on demand and kept: scene uploads are
+  // packed straight into it (a pageable source would be copied through the
+  // driver's own staging first).
+  void* pin = nullptr;
+  size_t pinCap = 0;
+  void* pinned(size_t bytes) {
+    if (bytes <= pinCap && pin) return pin;
+    if (pin) {
+      cudaStreamSynchronize(st);  // no copy from the old buffer is in flight
+      cudaFreeHost(pin);
+      pin = nullptr;
+      pinCap = 0;
+    }
+    if (!cuda_ok(cudaHostAlloc(&pin, std::max<size_t>(bytes, 1), cudaHostAllocDefault), "cudaHostAlloc")) return nullptr;
+    pinCap = bytes;
+    return pin;
+  }
+
   // Grow the key- and tile-sized buffers to the layout's needs (cell starts
   // of every key, the tile table and the per-substep run table), and upload
   // the tile table.
@@ -602,46 +627,60 @@ struct World {
     h.domH = sc->dom_h;
     h.substeps = 0;
     h.nFluid0 = sc->n_fluid;
-    h.pos.assign(sc->pos, sc->pos + 2 * (size_t)sc->n);
-    h.mat.assign(sc->mat_id, sc->mat_id + sc->n);
+    const size_t nf = sc->n_fluid, nn = sc->n;
+    h.bpos.assign(sc->pos + 2 * nf, sc->pos + 2 * nn);
+    h.bmat.assign(sc->mat_id + nf, sc->mat_id + nn);
     h.hasTemp = sc->temp != nullptr;
     h.hasFuel = sc->fuel != nullptr;
-    h.temp.assign(sc->n, 0);
-    h.fuel.assign(sc->n, 0);
-    if (sc->temp) h.temp.assign(sc->temp, sc->temp + sc->n);
-    if (sc->fuel) h.fuel.assign(sc->fuel, sc->fuel + sc->n);
+    h.btemp.assign(nn - nf, 0);
+    h.bfuel.assign(nn - nf, 0);
+    if (sc->temp) h.btemp.assign(sc->temp + nf, sc->temp + nn);
+    if (sc->fuel) h.bfuel.assign(sc->fuel + nf, sc->fuel + nn);
     h.weldSeq = 1;
     h.weldHold = h.weldHoldSeq = h.fuseTag = h.lastWeldTag = 0;
     h.wallsOn = true;
     h.events.clear();
     h.consumed = 0;
     eventsDirty = true;
-    std::vector<int32_t> stw((size_t)h.cap * 8, 0);
-    for (uint32_t i = 0; i < sc->n; ++i) {
-      uint32_t m = sc->mat_id[i];
+    // per-row words of the packing, looked up once
+    uint32_t fluidFl[MAT_MAX], wallFl[MAT_MAX];
+    int32_t fuel0[MAT_MAX];
+    for (uint32_t m = 0; m < matCount; ++m) {
       const int32_t* r = row(m);
-      uint32_t want = r[M_phantom] != 0 ? FLAG_DEAD : 0u;
-      uint32_t given = sc->flags ? sc->flags[i] : 0u;
-      uint32_t tag = (i < sc->n_fluid && spawn_welds(m)) ? (1u << 8) : 0u;
-      int32_t* w = &stw[(size_t)i * 8];
+      wallFl[m] = (r[M_phantom] != 0 ? FLAG_DEAD : 0u) | (seal_row(m) ? FLAG_SEAL : 0u);
+      fluidFl[m] = wallFl[m] | (spawn_welds(m) ? (1u << 8) : 0u);
+      fuel0[m] = r[M_fuel0];
+    }
+    // packed straight into pinned host memory, one copy to the device
+    int32_t* stw = static_cast<int32_t*>(pinned((size_t)h.cap * 32));
+    if (!stw) return false;
+    uint64_t seenMask = 0;
+    for (uint32_t i = 0; i < sc->n; ++i) {
+      const uint32_t m = sc->mat_id[i];
+      seenMask |= 1ull << m;
+      const uint32_t given = sc->flags ? sc->flags[i] : 0u;
+      int32_t* w = stw + (size_t)i * 8;
       w[0] = sc->pos[2 * i];
       w[1] = sc->pos[2 * i + 1];
       w[2] = sc->vel[2 * i];
       w[3] = sc->vel[2 * i + 1];
       w[4] = (int32_t)m;
-      w[5] = (int32_t)(given | want | (seal_row(m) ? FLAG_SEAL : 0u) | tag);
+      w[5] = (int32_t)(given | (i < sc->n_fluid ? fluidFl[m] : wallFl[m]));
       w[6] = sc->temp ? sc->temp[i] : AMBIENT;
-      w[7] = sc->fuel ? sc->fuel[i] : r[M_fuel0];
+      w[7] = sc->fuel ? sc->fuel[i] : fuel0[m];
     }
-    std::vector<uint32_t> so(h.cap, s);
-    bool ok = cuda_ok(cudaMemcpyAsync(b.state + (size_t)h.slotBase * 8, stw.data(), stw.size() * 4,
+    std::memset(stw + (size_t)sc->n * 8, 0, (size_t)(h.cap - sc->n) * 32);
+    h.matSeen = seenMask;
+    bool ok = cuda_ok(cudaMemcpyAsync(b.state + (size_t)h.slotBase * 8, stw, (size_t)h.cap * 32,
                                       cudaMemcpyHostToDevice, st), "state") &&
               cuda_ok(cudaMemsetAsync(b.stacc + h.slotBase, 0, sizeof(int2) * h.cap, st), "stacc") &&
               cuda_ok(cudaMemsetAsync(b.bond + (size_t)h.slotBase * BOND_CAP, 0, 4ull * BOND_CAP * h.cap, st), "bond") &&
               cuda_ok(cudaMemsetAsync(b.bondCand + (size_t)h.slotBase * BOND_CAP, 0, 4ull * BOND_CAP * h.cap, st),
-                      "bondCand") &&
-              cuda_ok(cudaMemcpyAsync(b.sceneOf + h.slotBase, so.data(), 4ull * h.cap, cudaMemcpyHostToDevice, st),
-                      "sceneOf");
+                      "bondCand");
+    if (ok) {
+      k_fill_u32<<<grid_for(h.cap), 256, 0, st>>>(b.sceneOf + h.slotBase, h.cap, s);
+      ok = cuda_ok(cudaGetLastError(), "sceneOf");
+    }
     if (!ok) return false;
     ScenePar& p = hpar[s];
     p = ScenePar{};
@@ -1205,13 +1244,12 @@ struct World {
       w[7] = std::max(0, q.has_fuel ? q.fuel : r[M_fuel0]);
     }
     for (uint32_t bb = 0; bb < nB; ++bb) {
-      uint32_t src = h.nFluid0 + bb;
       int32_t* w = &stw[(size_t)(k + bb) * 8];
-      w[0] = h.pos[2 * src];
-      w[1] = h.pos[2 * src + 1];
-      w[4] = (int32_t)h.mat[src];
-      w[6] = h.hasTemp ? h.temp[src] : AMBIENT;
-      w[7] = h.hasFuel ? h.fuel[src] : row(h.mat[src])[M_fuel0];
+      w[0] = h.bpos[2 * bb];
+      w[1] = h.bpos[2 * bb + 1];
+      w[4] = (int32_t)h.bmat[bb];
+      w[6] = h.hasTemp ? h.btemp[bb] : AMBIENT;
+      w[7] = h.hasFuel ? h.bfuel[bb] : row(h.bmat[bb])[M_fuel0];
     }
     size_t off = (size_t)h.slotBase + h.nFluid;
     bool ok = cuda_ok(cudaMemcpyAsync(b.state + off * 8, stw.data(), stw.size() * 4, cudaMemcpyHostToDevice, st),
@@ -1222,7 +1260,8 @@ struct World {
     if (!ok || !pull_params()) return false;
     h.n = newN;
     h.nFluid = newFluid;
-    for (uint32_t i = 0; i < k; ++i) h.mat.push_back((uint32_t)std::max(0, list[i].mat));
+    for (uint32_t i = 0; i < k; ++i)
+      h.matSeen |= 1ull << (uint32_t)std::min<int32_t>((int32_t)matCount - 1, std::max<int32_t>(0, list[i].mat));
     hpar[s].n = newN;
     hpar[s].nFluid = newFluid;
     hpar[s].bondDirty = 1;
@@ -1243,7 +1282,7 @@ struct World {
     sortedFresh = false;
     SceneHost& h = sh[s];
     if (!h.loaded) return fail("setWalls before loadScene");
-    const uint32_t nB = (uint32_t)(h.pos.size() / 2) - h.nFluid0;
+    const uint32_t nB = (uint32_t)h.bmat.size();
     bool cur = h.wallsOn;
     if (nB == 0) { h.wallsOn = want; if (onOut) *onOut = want; return true; }
     if (want == cur) { if (onOut) *onOut = cur; return true; }
@@ -1255,13 +1294,12 @@ struct World {
       if (h.nFluid + nB > h.cap) { if (onOut) *onOut = cur; return true; }
       std::vector<int32_t> stw((size_t)nB * 8, 0);
       for (uint32_t bb = 0; bb < nB; ++bb) {
-        uint32_t src = h.nFluid0 + bb;
         int32_t* w = &stw[(size_t)bb * 8];
-        w[0] = h.pos[2 * src];
-        w[1] = h.pos[2 * src + 1];
-        w[4] = (int32_t)h.mat[src];
-        w[6] = h.hasTemp ? h.temp[src] : AMBIENT;
-        w[7] = h.hasFuel ? h.fuel[src] : row(h.mat[src])[M_fuel0];
+        w[0] = h.bpos[2 * bb];
+        w[1] = h.bpos[2 * bb + 1];
+        w[4] = (int32_t)h.bmat[bb];
+        w[6] = h.hasTemp ? h.btemp[bb] : AMBIENT;
+        w[7] = h.hasFuel ? h.bfuel[bb] : row(h.bmat[bb])[M_fuel0];
       }
       size_t off = (size_t)h.slotBase + h.nFluid;
       if (!cuda_ok(cudaMemcpyAsync(b.state + off * 8, stw.data(), stw.size() * 4, cudaMemcpyHostToDevice, st), "walls") ||

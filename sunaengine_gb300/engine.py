@@ -185,7 +185,7 @@ class Engine:
         self._check(self._lib.sn_reset_chain(self._h), 'resetChain')
 
     def read_state(self) -> np.ndarray:
-        a = np.zeros(self.n * 8, np.int32)
+        a = np.empty(self.n * 8, np.int32)
         self._check(self._lib.sn_read_state(self._h, _ptr(a), a.size), 'readState')
         return a
 
@@ -670,7 +670,7 @@ class Batch:
 
     def read_state(self, sid: int) -> np.ndarray:
         n = self.info(sid)['n']
-        a = np.zeros(n * 8, np.int32)
+        a = np.empty(n * 8, np.int32)
         self._check(self._lib.sn_batch_read_state(self._h, int(sid), _ptr(a), a.size), 'read_state')
         return a
 

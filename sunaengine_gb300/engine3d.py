@@ -166,7 +166,7 @@ class Engine3D:
 
     def read_state(self, scene: int = 0) -> np.ndarray:
         n = self.info(scene)['n']
-        a = np.zeros(n * 8, np.int32)
+        a = np.empty(n * 8, np.int32)
         self._check(self._lib.sn3_read_state(self.h, int(scene), _ptr(a), a.size), 'read_state')
         return a
 
