@@ -135,6 +135,67 @@ __global__ void __launch_bounds__(256) k_slot_fields(Bufs b, uint32_t slotBase, 
   }
 }
 
+// Per material row, the words loadScene derives (src/engine.js:3855-3880):
+// the flag bits a fluid / wall particle of that row gets (FLAG_DEAD for a
+// phantom row, FLAG_SEAL for a seal-class row, the scene weld tag for a fluid
+// particle of a welding row) and the row's fuel0.
+struct LoadTables {
+  uint32_t fluidFl[MAT_MAX], wallFl[MAT_MAX];
+  int32_t fuel0[MAT_MAX];
+};
+// The uploaded arrays (SoA, see upload_scene): pos 2n, vel 2n, mat n, flags n,
+// temp n, fuel n; `present` bit 0/1/2: flags/temp/fuel given.
+// loadScene's per-particle checks (the same tests, in the same order, as the
+// host's validate_particle): res[0] = the first failing particle, res[1..2] =
+// the mask of material rows present.
+__global__ void __launch_bounds__(256) k_load_check(const int32_t* __restrict__ raw, uint32_t n, uint32_t nFluid,
+                                                    uint32_t matCount, uint32_t present, LoadTables T,
+                                                    uint32_t* __restrict__ res) {
+  uint64_t seen = 0;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint32_t m = (uint32_t)raw[4 * (size_t)n + i];
+    const int32_t px = raw[2 * (size_t)i], py = raw[2 * (size_t)i + 1];
+    const int32_t lo = i < nFluid ? 0 : -MAX_POS;
+    const uint32_t fl = (present & 1u) ? (uint32_t)raw[5 * (size_t)n + i] : 0u;
+    bool bad = m >= matCount || px < lo || px > MAX_POS || py < lo || py > MAX_POS || (fl & ~FLAG_MASK);
+    if (!bad && (present & 2u)) {
+      const int32_t t = raw[6 * (size_t)n + i];
+      bad = t < TEMP_MIN || t > TEMP_MAX;
+    }
+    if (!bad && (present & 4u)) bad = raw[7 * (size_t)n + i] < 0;
+    if (!bad && (fl & FLAG_DEAD) && !(T.wallFl[m] & FLAG_DEAD)) bad = true;
+    if (bad) atomicMin(res, i);
+    else seen |= 1ull << m;
+  }
+  const uint32_t lo32 = __reduce_or_sync(0xffffffffu, (uint32_t)seen);
+  const uint32_t hi32 = __reduce_or_sync(0xffffffffu, (uint32_t)(seen >> 32));
+  if ((threadIdx.x & 31u) == 0u) {
+    if (lo32) atomicOr(res + 1, lo32);
+    if (hi32) atomicOr(res + 2, hi32);
+  }
+}
+// loadScene's packing (src/engine.js:3855-3880) of the checked arrays into the
+// scene's cap slots of state words; slots past n are zero.
+__global__ void __launch_bounds__(256) k_load_pack(const int32_t* __restrict__ raw, uint32_t n, uint32_t nFluid,
+                                                   uint32_t cap, uint32_t present, LoadTables T,
+                                                   int32_t* __restrict__ state) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += gridDim.x * blockDim.x) {
+    int4 a = make_int4(0, 0, 0, 0), c = make_int4(0, 0, 0, 0);
+    if (i < n) {
+      const uint32_t m = (uint32_t)raw[4 * (size_t)n + i];
+      const uint32_t given = (present & 1u) ? (uint32_t)raw[5 * (size_t)n + i] : 0u;
+      a = make_int4(raw[2 * (size_t)i], raw[2 * (size_t)i + 1], raw[2 * (size_t)n + 2 * (size_t)i],
+                    raw[2 * (size_t)n + 2 * (size_t)i + 1]);
+      c = make_int4((int32_t)m, (int32_t)(given | (i < nFluid ? T.fluidFl[m] : T.wallFl[m])),
+                    (present & 2u) ? raw[6 * (size_t)n + i] : AMBIENT,
+                    (present & 4u) ? raw[7 * (size_t)n + i] : T.fuel0[m]);
+    }
+    int4* w4 = reinterpret_cast<int4*>(state + (size_t)i * 8);
+    w4[0] = a;
+    w4[1] = c;
+  }
+}
+
 __global__ void __launch_bounds__(256) k_fill_u32(uint32_t* __restrict__ out, uint32_t n, uint32_t v) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = v;
 }
@@ -235,13 +296,11 @@ struct World {
                     b.NBRL, b.NBRN, (void*)b.tiles, b.TR, b.OVF, b.CB,
                     (void*)b.luts, (void*)b.WG, (void*)b.CA, (void*)b.mats, (void*)b.rcp,
                     b.scenes, b.world, b.acc, b.accLast, b.chain, b.dbg, b.err, b.work, tmpK, tmpV, hist,
-                    hits, accTmp, devEv, devEp, boxChunks};
+                    hits, accTmp, devEv, devEp, boxChunks, upl, uplRes};
     for (void* p : ptrs)
       if (p) cudaFree(p);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
-    if (st) cudaStreamSynchronize(st);
-    if (pin) cudaFreeHost(pin);
     if (st) cudaStreamDestroy(st);
   }
 
@@ -518,24 +577,6 @@ struct World {
     return ok && cuda_ok(cudaStreamSynchronize(st), "relayout");
   }
 
-  // A pinned host staging buffer, grown on demand and kept: scene uploads are
-  // packed straight into it (a pageable source would be copied through the
-  // driver's own staging first).
-  void* pin = nullptr;
-  size_t pinCap = 0;
-  void* pinned(size_t bytes) {
-    if (bytes <= pinCap && pin) return pin;
-    if (pin) {
-      cudaStreamSynchronize(st);  // no copy from the old buffer is in flight
-      cudaFreeHost(pin);
-      pin = nullptr;
-      pinCap = 0;
-    }
-    if (!cuda_ok(cudaHostAlloc(&pin, std::max<size_t>(bytes, 1), cudaHostAllocDefault), "cudaHostAlloc")) return nullptr;
-    pinCap = bytes;
-    return pin;
-  }
-
   // Grow the key- and tile-sized buffers to the layout's needs (cell starts
   // of every key, the tile table and the per-substep run table), and upload
   // the tile table.
@@ -584,25 +625,67 @@ struct World {
     return cuda_ok(cudaMemcpyAsync(b.scenes + s, &hpar[s], sizeof(ScenePar), cudaMemcpyHostToDevice, st), "push");
   }
 
-  bool validate_scene(const sn_scene* sc, uint32_t cap) {
+  bool validate_header(const sn_scene* sc, uint32_t cap) {
     if (!sc) return fail("scene is NULL");
     if (sc->n_fluid > sc->n) return fail("scene.nFluid out of range");
     if (sc->n > cap) return fail("scene.n = %u exceeds maxParticles = %u", sc->n, cap);
     if (sc->n > 0 && (!sc->pos || !sc->vel || !sc->mat_id)) return fail("scene arrays missing");
-    for (uint32_t i = 0; i < sc->n; ++i) {
-      if (sc->mat_id[i] >= matCount) return fail("matId[%u] = %u >= matCount %u", i, sc->mat_id[i], matCount);
-      int32_t lo = i < sc->n_fluid ? 0 : -MAX_POS;
-      if (sc->pos[2 * i] < lo || sc->pos[2 * i] > MAX_POS || sc->pos[2 * i + 1] < lo || sc->pos[2 * i + 1] > MAX_POS)
-        return fail("pos[%u] outside [%d, 2^27]", i, lo);
-      if (sc->flags && (sc->flags[i] & ~FLAG_MASK)) return fail("flags[%u] sets a reserved bit", i);
-      if (sc->temp && (sc->temp[i] < TEMP_MIN || sc->temp[i] > TEMP_MAX)) return fail("temp[%u] out of range", i);
-      if (sc->fuel && sc->fuel[i] < 0) return fail("fuel[%u] < 0", i);
-      uint32_t want = row(sc->mat_id[i])[M_phantom] != 0 ? FLAG_DEAD : 0u;
-      if (sc->flags && (sc->flags[i] & FLAG_DEAD) && !want) return fail("flags[%u] sets FLAG_DEAD on a live row", i);
-    }
     if (sc->cell_shift < 1 || sc->cell_shift > 27) return fail("cellShift outside 1..27");
     if ((1u << sc->cell_shift) < (uint32_t)KERNEL_H) return fail("cells smaller than the kernel radius");
     if (sc->dom_w < 2 * 32768 || sc->dom_h < 2 * 32768) return fail("domain smaller than the wall margin");
+    return true;
+  }
+  // The per-particle checks of loadScene (src/engine.js:3704-3760), in this
+  // order, for particle i; false with the message of the first that fails.
+  // k_load_check applies the same tests to every particle on the device.
+  bool validate_particle(const sn_scene* sc, uint32_t i) {
+    if (sc->mat_id[i] >= matCount) return fail("matId[%u] = %u >= matCount %u", i, sc->mat_id[i], matCount);
+    int32_t lo = i < sc->n_fluid ? 0 : -MAX_POS;
+    if (sc->pos[2 * i] < lo || sc->pos[2 * i] > MAX_POS || sc->pos[2 * i + 1] < lo || sc->pos[2 * i + 1] > MAX_POS)
+      return fail("pos[%u] outside [%d, 2^27]", i, lo);
+    if (sc->flags && (sc->flags[i] & ~FLAG_MASK)) return fail("flags[%u] sets a reserved bit", i);
+    if (sc->temp && (sc->temp[i] < TEMP_MIN || sc->temp[i] > TEMP_MAX)) return fail("temp[%u] out of range", i);
+    if (sc->fuel && sc->fuel[i] < 0) return fail("fuel[%u] < 0", i);
+    uint32_t want = row(sc->mat_id[i])[M_phantom] != 0 ? FLAG_DEAD : 0u;
+    if (sc->flags && (sc->flags[i] & FLAG_DEAD) && !want) return fail("flags[%u] sets FLAG_DEAD on a live row", i);
+    return true;
+  }
+
+  // The scene's arrays uploaded as they are (SoA, 8 words per particle:
+  // pos 2n, vel 2n, mat n, flags n, temp n, fuel n), checked and packed on
+  // the device: a host loop over a 10^6-particle scene costs milliseconds.
+  int32_t* upl = nullptr;
+  uint32_t* uplRes = nullptr;  // [4]: first failing index, material mask (2 words)
+  bool upload_scene(const sn_scene* sc, LoadTables& T, uint64_t* seen) {
+    const size_t n = sc->n;
+    if (!upl) {
+      upl = dalloc<int32_t>((size_t)capSlots * 8, err);
+      uplRes = dalloc<uint32_t>(4, err);
+      if (!upl || !uplRes) return false;
+    }
+    bool ok = true;
+    auto up = [&](size_t off, const void* src, size_t words) {
+      if (src && words) ok = ok && cuda_ok(cudaMemcpyAsync(upl + off, src, words * 4, cudaMemcpyHostToDevice, st), "upload");
+    };
+    up(0, sc->pos, 2 * n);
+    up(2 * n, sc->vel, 2 * n);
+    up(4 * n, sc->mat_id, n);
+    up(5 * n, sc->flags, n);
+    up(6 * n, sc->temp, n);
+    up(7 * n, sc->fuel, n);
+    const uint32_t init[4] = {0xffffffffu, 0u, 0u, 0u};
+    ok = ok && cuda_ok(cudaMemcpyAsync(uplRes, init, 16, cudaMemcpyHostToDevice, st), "upload");
+    if (!ok) return false;
+    const uint32_t present = (sc->flags ? 1u : 0u) | (sc->temp ? 2u : 0u) | (sc->fuel ? 4u : 0u);
+    if (n) k_load_check<<<grid_for(n), 256, 0, st>>>(upl, sc->n, sc->n_fluid, matCount, present, T, uplRes);
+    uint32_t res[4];
+    cudaMemcpyAsync(res, uplRes, 16, cudaMemcpyDeviceToHost, st);
+    if (!cuda_ok(cudaStreamSynchronize(st), "load check")) return false;
+    if (res[0] != 0xffffffffu) {
+      if (!validate_particle(sc, res[0])) return false;
+      return fail("particle %u failed the device check but passes the host check", res[0]);
+    }
+    *seen = (uint64_t)res[1] | ((uint64_t)res[2] << 32);
     return true;
   }
 
@@ -611,7 +694,17 @@ struct World {
     accFresh = false;
     sortedFresh = false;
     SceneHost& h = sh[s];
-    if (!validate_scene(sc, h.cap)) return false;
+    if (!validate_header(sc, h.cap)) return false;
+    LoadTables T;
+    for (uint32_t m = 0; m < MAT_MAX; ++m) {
+      if (m >= matCount) { T.fluidFl[m] = T.wallFl[m] = 0u; T.fuel0[m] = 0; continue; }
+      const int32_t* r = row(m);
+      T.wallFl[m] = (r[M_phantom] != 0 ? FLAG_DEAD : 0u) | (seal_row(m) ? FLAG_SEAL : 0u);
+      T.fluidFl[m] = T.wallFl[m] | (spawn_welds(m) ? (1u << 8) : 0u);
+      T.fuel0[m] = r[M_fuel0];
+    }
+    uint64_t seenMask = 0;
+    if (!upload_scene(sc, T, &seenMask)) return false;
     // a scene load dissolves every body of the scene (src/engine.js:3811-3813)
     if (!drop_scene_bodies(s)) return false;
     uint32_t cs = 1u << sc->cell_shift;
@@ -642,37 +735,11 @@ struct World {
     h.events.clear();
     h.consumed = 0;
     eventsDirty = true;
-    // per-row words of the packing, looked up once
-    uint32_t fluidFl[MAT_MAX], wallFl[MAT_MAX];
-    int32_t fuel0[MAT_MAX];
-    for (uint32_t m = 0; m < matCount; ++m) {
-      const int32_t* r = row(m);
-      wallFl[m] = (r[M_phantom] != 0 ? FLAG_DEAD : 0u) | (seal_row(m) ? FLAG_SEAL : 0u);
-      fluidFl[m] = wallFl[m] | (spawn_welds(m) ? (1u << 8) : 0u);
-      fuel0[m] = r[M_fuel0];
-    }
-    // packed straight into pinned host memory, one copy to the device
-    int32_t* stw = static_cast<int32_t*>(pinned((size_t)h.cap * 32));
-    if (!stw) return false;
-    uint64_t seenMask = 0;
-    for (uint32_t i = 0; i < sc->n; ++i) {
-      const uint32_t m = sc->mat_id[i];
-      seenMask |= 1ull << m;
-      const uint32_t given = sc->flags ? sc->flags[i] : 0u;
-      int32_t* w = stw + (size_t)i * 8;
-      w[0] = sc->pos[2 * i];
-      w[1] = sc->pos[2 * i + 1];
-      w[2] = sc->vel[2 * i];
-      w[3] = sc->vel[2 * i + 1];
-      w[4] = (int32_t)m;
-      w[5] = (int32_t)(given | (i < sc->n_fluid ? fluidFl[m] : wallFl[m]));
-      w[6] = sc->temp ? sc->temp[i] : AMBIENT;
-      w[7] = sc->fuel ? sc->fuel[i] : fuel0[m];
-    }
-    std::memset(stw + (size_t)sc->n * 8, 0, (size_t)(h.cap - sc->n) * 32);
     h.matSeen = seenMask;
-    bool ok = cuda_ok(cudaMemcpyAsync(b.state + (size_t)h.slotBase * 8, stw, (size_t)h.cap * 32,
-                                      cudaMemcpyHostToDevice, st), "state") &&
+    k_load_pack<<<grid_for(h.cap), 256, 0, st>>>(upl, sc->n, sc->n_fluid, h.cap,
+                                                  (sc->flags ? 1u : 0u) | (sc->temp ? 2u : 0u) | (sc->fuel ? 4u : 0u), T,
+                                                  b.state + (size_t)h.slotBase * 8);
+    bool ok = cuda_ok(cudaGetLastError(), "pack") &&
               cuda_ok(cudaMemsetAsync(b.stacc + h.slotBase, 0, sizeof(int2) * h.cap, st), "stacc") &&
               cuda_ok(cudaMemsetAsync(b.bond + (size_t)h.slotBase * BOND_CAP, 0, 4ull * BOND_CAP * h.cap, st), "bond") &&
               cuda_ok(cudaMemsetAsync(b.bondCand + (size_t)h.slotBase * BOND_CAP, 0, 4ull * BOND_CAP * h.cap, st),

@@ -291,3 +291,29 @@ def test_refuses_bad_input():
     big = scenes.make_scene('dambreak_v1')
     with pytest.raises(EngineError):
         e.load_scene(big)  # n > maxParticles
+
+
+def test_load_checks_report_the_first_bad_particle():
+    """loadScene's per-particle checks run on the device; the refusal names the
+    first failing particle and its first failing rule, as the host rules read,
+    and a refused load leaves the loaded scene as it was."""
+    sc = _pool('WATER', 20, 8)
+    e = Engine(max_particles=sc.n + 64).load_scene(sc)
+    e.step(3)
+    before = e.read_state().copy()
+    cases = []
+    b1 = sc.copy(); b1.pos = b1.pos.copy(); b1.pos[7, 0] = -5; b1.matId = b1.matId.copy(); b1.matId[40] = 99
+    cases.append((b1, 'pos[7]'))
+    b2 = sc.copy(); b2.temp = np.full(sc.n, 65536 * 20, np.int32); b2.temp[30] = 1 << 30; b2.fuel = np.zeros(sc.n, np.int32)
+    b2.fuel[12] = -1
+    cases.append((b2, 'fuel[12]'))
+    b3 = sc.copy(); b3.flags = np.zeros(sc.n, np.uint32); b3.flags[5] = 2  # FLAG_DEAD on a WATER (live) row
+    cases.append((b3, 'flags[5] sets FLAG_DEAD'))
+    for bad, want in cases:
+        with pytest.raises(EngineError) as ex:
+            e.load_scene(bad)
+        assert want in str(ex.value), str(ex.value)
+        assert np.array_equal(e.read_state(), before)
+    e.load_scene(sc)  # a good load after refused ones
+    e.step(3)
+    assert np.array_equal(e.read_state(), before)
