@@ -403,6 +403,22 @@ def batched_workload(steps: int, warmup: int, device: int, plain_sample: int = 2
     b.check_errors()
     batched = nf * steps / (ms / 1e3)
     lanes_b = b.lanes()
+    # the same window with the solver iterations as one persistent kernel per
+    # substep (sn_batch_set_persistent), for comparison with the graph of
+    # per-phase launches
+    bp = make()
+    bp.set_lanes(lanes_b)
+    bp.set_persistent(True)
+    bp.step(warmup)
+    bp.sync()
+    bp.step(steps)
+    pms, plaunch = bp.last_timing()
+    bp.check_errors()
+    same = all(bp.chain_hex(i) == b.chain_hex(i) for i in range(len(scs)))
+    bp.destroy()
+    persistent = {'value': nf * steps / (pms / 1e3), 'ms_per_step': pms / steps,
+                  'gpu_launches_per_step': plaunch // max(1, steps), 'vs_graph': (nf * steps / (pms / 1e3)) / batched,
+                  'chains_equal_to_graph': same}
     # parity: advance (untimed) to the next substep the oracle's sample recorded
     # and compare those scenes' chains
     parity = {'ok': None, 'against': 'not recorded'}
@@ -476,7 +492,8 @@ def batched_workload(steps: int, warmup: int, device: int, plain_sample: int = 2
     return {'scenes': len(scs), 'particles': int(nf), 'value': batched, 'unit': UNIT,
             'ms_per_step': ms / steps, 'gpu_launches_per_step': launches // max(1, steps),
             'plain_same_scenes': plain, 'plain_sample_scenes': int(len(pick)), 'lanes': lanes_b,
-            'batched_vs_plain': batched / plain, 'parity': parity, 'full_config': full}
+            'batched_vs_plain': batched / plain, 'parity': parity, 'full_config': full,
+            'persistent_loop': persistent}
 
 
 def construction_workload(steps: int, warmup: int, device: int, with_cpu: bool = True, cpu_seconds: float = 4.0):

@@ -355,6 +355,15 @@ int sn_batch_set_lanes(sn_batch* b, const uint32_t lanes[5]);
  * on GB300). Takes effect at the next step. */
 int sn_set_staged(sn_engine* e, uint32_t on);
 int sn_batch_set_staged(sn_batch* b, uint32_t on);
+/* (no counterpart) Run the solver iterations (solveA, the four colour
+ * passes and friction/applyFric, ITERS times) as one persistent cooperative
+ * kernel with grid barriers between the phases, instead of one launch per
+ * phase. Applies to worlds with no rigid body in the default layout; others
+ * keep the per-phase launches. Results are identical (measured slower
+ * on GB300 than the captured per-phase graph; off by default). A barrier that
+ * waits past its bound raises an error that sn_check_errors reports. */
+int sn_set_persistent(sn_engine* e, uint32_t on);
+int sn_batch_set_persistent(sn_batch* b, uint32_t on);
 
 /* ---- digest without device allocation ------------------------------------ */
 /* No counterpart in the reference. For callers that cannot allocate device

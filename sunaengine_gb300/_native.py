@@ -228,6 +228,8 @@ SIGNATURES = {
     'sn_batch_autotune': (ctypes.c_int, [P, u32, ctypes.POINTER(u32)]),
     'sn_set_staged': (ctypes.c_int, [P, u32]),
     'sn_batch_set_staged': (ctypes.c_int, [P, u32]),
+    'sn_set_persistent': (ctypes.c_int, [P, u32]),
+    'sn_batch_set_persistent': (ctypes.c_int, [P, u32]),
     'sn_lanes': (ctypes.c_int, [P, P]),
     'sn_batch_lanes': (ctypes.c_int, [P, P]),
     'sn_ckpt_pool_create': (ctypes.c_int, [ctypes.c_size_t, ctypes.c_int32, ctypes.POINTER(P)]),

@@ -296,7 +296,7 @@ struct World {
                     b.NBRL, b.NBRN, (void*)b.tiles, b.TR, b.OVF, b.CB,
                     (void*)b.luts, (void*)b.WG, (void*)b.CA, (void*)b.mats, (void*)b.rcp,
                     b.scenes, b.world, b.acc, b.accLast, b.chain, b.dbg, b.err, b.work, tmpK, tmpV, hist,
-                    hits, accTmp, devEv, devEp, boxChunks, upl, uplRes};
+                    hits, accTmp, devEv, devEp, boxChunks, upl, uplRes, barBuf};
     for (void* p : ptrs)
       if (p) cudaFree(p);
     if (ev0) cudaEventDestroy(ev0);
@@ -380,6 +380,7 @@ struct World {
     b.dbg = dalloc<uint32_t>(16, err);
     b.err = dalloc<uint32_t>(4, err);
     b.work = dalloc<uint32_t>(4, err);
+    barBuf = dalloc<uint32_t>(2, err);
     tmpK = dalloc<uint32_t>(C, err);
     tmpV = dalloc<uint32_t>(C, err);
     hist = dalloc<uint32_t>(radix::hist_words((uint32_t)C), err);
@@ -586,6 +587,8 @@ struct World {
   // the tile-major layout with shared-memory staged gathers (sn_set_staged);
   // off by default: measured slower than the list gathers it replaces
   bool staged = false;
+  // the solver iterations as one persistent cooperative kernel (sn_set_persistent); off by default
+  bool persistent = false;
   bool ensure_tile_buffers(uint32_t K, uint32_t tiles) {
     if (K + 1 > keyCap) {
       if (b.cellStart) cudaFree(b.cellStart);
@@ -864,6 +867,28 @@ struct World {
       k_colour<DBG, L><<<g, 256, 0, st>>>(b, c, src, dst);
     }
   }
+  // One cooperative launch of every solver iteration (k_iters_persistent):
+  // the grid is exactly the resident capacity, which the cooperative launch
+  // guarantees to run at once (its grid barriers need every CTA resident).
+  uint32_t* barBuf = nullptr;
+  template <bool DBG, int L>
+  void launch_persistent() {
+    const void* fn = (const void*)k_iters_persistent<DBG, L>;
+    int per = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 256, 0);
+    cudaMemsetAsync(barBuf, 0, 8, st);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(std::max(per, 1) * numSMs));
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k_iters_persistent<DBG, L>, b, iters, barBuf);
+  }
   template <bool DBG, int L>
   void launch_contain_stress() {
     k_contain_stress<DBG, L>
@@ -935,7 +960,15 @@ struct World {
     SN_LANES(lc.n, (launch_nbr<DBG, L_>()));
     mark();
     Lc += 3 + (staged ? 1 : 0) + (DBG ? 0 : 2);
-    for (uint32_t it = 0; it < iters; ++it) {
+    // the persistent form of the iteration loop (sn_set_persistent): worlds
+    // with no rigid body, in the colour-major layout, and not while
+    // profile_substep times the phases one by one
+    const bool persist = persistent && !staged && nB == 0 && pev == nullptr;
+    if (persist) {
+      SN_LANES(lc.c, (launch_persistent<DBG, L_>()));
+      Lc += 1;
+    }
+    for (uint32_t it = 0; it < (persist ? 0u : iters); ++it) {
       const int last = it + 1 == iters ? 1 : 0;
       SN_LANES(lc.a, (launch_solveA<DBG, L_>(last)));
       mark();
@@ -1406,6 +1439,8 @@ struct World {
       return fail("a transition produced a seal-class row (containment is not built); results past it are not "
                   "the reference's");
     if (e[0] & ERR_BOND_PARTNER) return fail("a bond partner slot exceeds the 17-bit bond word");
+    if (e[0] & ERR_BARRIER)
+      return fail("a grid barrier of the persistent solver loop timed out; results past it are not valid");
     if (e[0] & ERR_STAGE_TIMEOUT)
       return fail("a tile's staged copy did not complete within the bounded wait; results past it are not valid");
     return true;
@@ -2594,6 +2629,18 @@ int sn_batch_set_staged(sn_batch* b, uint32_t on) {
   if (!b) return SN_E_INVALID;
   b->w.staged = on != 0;
   b->w.layoutDirty = true;
+  return SN_OK;
+}
+int sn_set_persistent(sn_engine* e, uint32_t on) {
+  if (!e) return SN_E_INVALID;
+  e->w.persistent = on != 0;
+  e->w.graphValid = false;
+  return SN_OK;
+}
+int sn_batch_set_persistent(sn_batch* b, uint32_t on) {
+  if (!b) return SN_E_INVALID;
+  b->w.persistent = on != 0;
+  b->w.graphValid = false;
   return SN_OK;
 }
 int sn_lanes(sn_engine* e, uint32_t out[5]) {

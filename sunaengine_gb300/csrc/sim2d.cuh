@@ -163,7 +163,7 @@ struct Bufs {
   uint32_t* rmark;      // [cap] rigidMember's leave marks, slot space
 };
 
-enum : uint32_t { ERR_UNSUPPORTED_ROW = 1u, ERR_BOND_PARTNER = 2u, ERR_STAGE_TIMEOUT = 4u };
+enum : uint32_t { ERR_UNSUPPORTED_ROW = 1u, ERR_BOND_PARTNER = 2u, ERR_STAGE_TIMEOUT = 4u, ERR_BARRIER = 8u };
 
 __device__ __forceinline__ int32_t matw(const Bufs& b, uint32_t m, int w) { return __ldg(b.mats + m * MAT_WORDS + w); }
 
@@ -870,14 +870,18 @@ __device__ __forceinline__ void solveA_tile(const Bufs& b, const NB& nb, ME me_o
 // layout). lam goes to both buffers of the colour sweep, which copies only
 // preds between them.
 template <bool DBG, int L>
-__global__ void __launch_bounds__(256) k_solveA(Bufs b, int lastIter) {
-  Flags<DBG> f{b.dbg};
+__device__ __forceinline__ void solveA_all(const Bufs& b, int lastIter, const Flags<DBG>& f) {
   const uint32_t nAct = b.world->nAct;
   const int4* PL = b.PL;
   const uint32_t chunk = blockDim.x / L;
   for (uint32_t i0 = blockIdx.x * chunk; i0 < nAct; i0 += gridDim.x * chunk)
     solveA_tile<DBG, L, true>(b, NbrGlobal{PL, b.NBR, b.nbrStride}, [&](uint32_t i) { return PL[i0 + i]; }, i0,
                               min(nAct - i0, chunk), lastIter, f);
+}
+template <bool DBG, int L>
+__global__ void __launch_bounds__(256) k_solveA(Bufs b, int lastIter) {
+  Flags<DBG> f{b.dbg};
+  solveA_all<DBG, L>(b, lastIter, f);
 }
 
 // solveA over every tile. Only lam (PL.z) is written in PL, and no particle
@@ -1017,10 +1021,11 @@ __device__ __forceinline__ void colour_tile(const Bufs& b, const NB& nb, ME me_o
 // phases later, so phase c copies colours c+1 and c-1. After phase 3 buffer A
 // is complete again. A rigid member's dp is not applied: rigidSolve folds it
 // into its body at the end of the iteration (src/sim.wgsl:1418-1429).
+// (No __restrict__ here: the persistent kernel reads buffers that its own
+// earlier phases wrote, which must not go through the non-coherent load path.)
 template <bool DBG, int L>
-__global__ void __launch_bounds__(256, 8) k_colour(Bufs b, int colour, const int4* __restrict__ src,
-                                                int4* __restrict__ dst) {
-  Flags<DBG> f{b.dbg};
+__device__ __forceinline__ void colour_all(const Bufs& b, int colour, const int4* src, int4* dst,
+                                           const Flags<DBG>& f) {
   const uint32_t* cb = b.world->colourBase;
   const uint32_t lo = b.cellStart[cb[colour]], hi = b.cellStart[cb[colour + 1]];
   const int c1 = (colour + 1) & 3, c3 = (colour + 3) & 3;
@@ -1046,6 +1051,12 @@ __global__ void __launch_bounds__(256, 8) k_colour(Bufs b, int colour, const int
     const uint32_t p = i < n1 ? lo1 + i : lo3 + (i - n1);
     *reinterpret_cast<int2*>(dst + p) = *reinterpret_cast<const int2*>(src + p);
   }
+}
+template <bool DBG, int L>
+__global__ void __launch_bounds__(256, 8) k_colour(Bufs b, int colour, const int4* __restrict__ src,
+                                                int4* __restrict__ dst) {
+  Flags<DBG> f{b.dbg};
+  colour_all<DBG, L>(b, colour, src, dst, f);
 }
 
 // One colour of the sweep in the tile-major layout, with staged gathers.
@@ -1156,9 +1167,7 @@ __device__ __forceinline__ bool friction_row(const Bufs& b, uint32_t m) {
 // gathers, which the split shortens L-fold. The bond gather stays on the
 // particle's first lane.
 template <bool DBG, int L>
-__global__ void __launch_bounds__(256) k_friction(Bufs b) {
-  if (*b.work == 0u) return;  // no particle has a friction or bond row this substep
-  Flags<DBG> f{b.dbg};
+__device__ __forceinline__ void friction_all(const Bufs& b, const Flags<DBG>& f) {
   const uint32_t nAct = b.world->nAct, stride = b.nbrStride;
   const uint32_t sub = threadIdx.x & (L - 1), G = gstride() / L;
   for (uint32_t p = gtid() / L;; p += G) {
@@ -1278,10 +1287,15 @@ __global__ void __launch_bounds__(256) k_friction(Bufs b) {
   }
 }
 
-template <bool DBG>
-__global__ void __launch_bounds__(256) k_apply_fric(Bufs b) {
-  if (*b.work == 0u) return;
+template <bool DBG, int L>
+__global__ void __launch_bounds__(256) k_friction(Bufs b) {
+  if (*b.work == 0u) return;  // no particle has a friction or bond row this substep
   Flags<DBG> f{b.dbg};
+  friction_all<DBG, L>(b, f);
+}
+
+template <bool DBG>
+__device__ __forceinline__ void apply_fric_all(const Bufs& b, const Flags<DBG>& f) {
   const uint32_t nAct = b.world->nAct;
   for (uint32_t p = gtid(); p < nAct; p += gstride()) {
     int4 me = b.PL[p];
@@ -1295,6 +1309,71 @@ __global__ void __launch_bounds__(256) k_apply_fric(Bufs b) {
     *reinterpret_cast<int2*>(b.PL2 + p) = np;
   }
 }
+template <bool DBG>
+__global__ void __launch_bounds__(256) k_apply_fric(Bufs b) {
+  if (*b.work == 0u) return;
+  Flags<DBG> f{b.dbg};
+  apply_fric_all<DBG>(b, f);
+}
+
+// ---- the persistent form of the solver loop (opt-in, sn_set_persistent) ----
+//
+// One cooperative launch runs all `iters` iterations of solveA, the four
+// colour passes and (when some particle has a friction or bond row this
+// substep) friction and applyFric, for worlds with no rigid body (rigidSolve
+// keeps the per-phase launches), the phases separated by grid barriers
+// instead of kernel boundaries. The barrier counts arrivals monotonically in bar[0] (zeroed
+// before each launch) and releases generation g by writing g + 1 to bar[1];
+// a CTA that waits longer than BARRIER_WAIT_CYCLES raises ERR_BARRIER and the
+// kernel returns (its results are then not valid; sn_check_errors reports it).
+constexpr long long BARRIER_WAIT_CYCLES = 1ll << 31;  // about a second
+__device__ __forceinline__ bool grid_barrier(uint32_t* bar, uint32_t* err, uint32_t& gen) {
+  __shared__ uint32_t okS;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    okS = 1u;
+    __threadfence();
+    const uint32_t target = gridDim.x * (gen + 1u);
+    if (atomicAdd(bar, 1u) + 1u == target) {
+      atomicExch(bar + 1, gen + 1u);
+    } else {
+      const long long t0 = clock64();
+      while (*(volatile uint32_t*)(bar + 1) <= gen) {
+        if (clock64() - t0 > BARRIER_WAIT_CYCLES) {
+          atomicOr(err, ERR_BARRIER);
+          okS = 0u;
+          break;
+        }
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  gen += 1u;
+  return okS != 0u;
+}
+template <bool DBG, int L>
+__global__ void __launch_bounds__(256, 8) k_iters_persistent(Bufs b, uint32_t iters, uint32_t* bar) {
+  Flags<DBG> f{b.dbg};
+  uint32_t gen = 0;
+  for (uint32_t it = 0; it < iters; ++it) {
+    solveA_all<DBG, L>(b, it + 1 == iters ? 1 : 0, f);
+    for (int c = 0; c < 4; ++c) {
+      if (!grid_barrier(bar, b.err, gen)) return;
+      colour_all<DBG, L>(b, c, (c & 1) ? b.PL2 : b.PL, (c & 1) ? b.PL : b.PL2, f);
+    }
+    // friction and applyFric, when some particle has a friction or bond row
+    // this substep (the flag is the same for every CTA)
+    if (*(volatile uint32_t*)b.work != 0u) {
+      if (!grid_barrier(bar, b.err, gen)) return;
+      friction_all<DBG, L>(b, f);
+      if (!grid_barrier(bar, b.err, gen)) return;
+      apply_fric_all<DBG>(b, f);
+    }
+    if (it + 1 < iters && !grid_barrier(bar, b.err, gen)) return;
+  }
+}
+
 
 // finalize + xsph + normals + conduct (src/sim.wgsl:2245-2582) in one sweep
 // over the neighbour list. vtmp_j = clamp(pred_j - pos_j) is finalize's

@@ -532,6 +532,12 @@ class Engine:
         self._check(self._lib.sn_set_staged(self._h, 1 if on else 0), 'setStaged')
         return self
 
+    def set_persistent(self, on: bool = True):
+        """The solver iterations as one persistent cooperative kernel (same
+        results; see sn_set_persistent)."""
+        self._check(self._lib.sn_set_persistent(self._h, 1 if on else 0), 'setPersistent')
+        return self
+
     def profile_substep(self, reps: int = 3) -> np.ndarray:
         """Mean device ms per kernel phase over `reps` real substeps (profileSubstep)."""
         out = np.zeros(64, np.float32)
@@ -782,6 +788,11 @@ class Batch:
     def set_staged(self, on: bool = True):
         """Tile-major sorted space with shared-memory staged gathers (sn_batch_set_staged)."""
         self._check(self._lib.sn_batch_set_staged(self._h, 1 if on else 0), 'setStaged')
+        return self
+
+    def set_persistent(self, on: bool = True):
+        """The solver iterations as one persistent cooperative kernel (sn_batch_set_persistent)."""
+        self._check(self._lib.sn_batch_set_persistent(self._h, 1 if on else 0), 'setPersistent')
         return self
 
     # device keyframes (sn_batch_ckpt_*): see checkpoints.CheckpointPool
