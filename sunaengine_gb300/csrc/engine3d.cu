@@ -24,6 +24,56 @@ namespace radix = sn::radix;
 
 namespace {
 
+// Scene upload (pos 3n, vel 3n, mat n as uploaded): res[0] = the first
+// particle whose material is outside the table.
+__global__ void __launch_bounds__(256) k3_load_check(const int32_t* __restrict__ raw, uint32_t n, uint32_t matCount,
+                                                     uint32_t* __restrict__ res) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    if ((uint32_t)raw[6 * (size_t)n + i] >= matCount) atomicMin(res, i);
+}
+// ... and its packing into state words {p.xyz, mat, v.xyz, 0}.
+__global__ void __launch_bounds__(256) k3_load_pack(const int32_t* __restrict__ raw, uint32_t n, uint32_t hasVel,
+                                                    int32_t* __restrict__ state) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int32_t* pp = raw + 3 * (size_t)i;
+    const int32_t* vv = raw + 3 * (size_t)n + 3 * (size_t)i;
+    int4* w4 = reinterpret_cast<int4*>(state + (size_t)i * 8);
+    w4[0] = make_int4(pp[0], pp[1], pp[2], raw[6 * (size_t)n + i]);
+    w4[1] = hasVel ? make_int4(vv[0], vv[1], vv[2], 0) : make_int4(0, 0, 0, 0);
+  }
+}
+// Bond rows as uploaded: res[0] = the first malformed row (an entry after the
+// row's end, a rest length on an empty entry, a partner outside the scene or
+// itself, a rest length outside [BOND3_L0_MIN, BOND3_L0_MAX]); res[1] != 0 when
+// any row holds an entry.
+__global__ void __launch_bounds__(256) k3_bonds_check(const uint32_t* __restrict__ rows, uint32_t n,
+                                                      uint32_t* __restrict__ res) {
+  bool anyRow = false;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint32_t* r = rows + (size_t)i * BOND3_WORDS;
+    bool ended = false, bad = false;
+    for (uint32_t e = 0; e < BOND3_CAP; ++e) {
+      const uint32_t w = r[2 * e], L0 = r[2 * e + 1];
+      if (w == 0u) {
+        ended = true;
+        bad |= L0 != 0u;
+        continue;
+      }
+      const uint32_t j = (w & BOND3_J) - 1u;
+      bad |= ended || j >= n || j == i || (int32_t)L0 < BOND3_L0_MIN || (int32_t)L0 > BOND3_L0_MAX;
+      anyRow = true;
+    }
+    if (bad) atomicMin(res, i);
+  }
+  if (__any_sync(0xffffffffu, anyRow) && (threadIdx.x & 31u) == 0u) atomicOr(res + 1, 1u);
+}
+// bflag[i] = 1 when row i holds an entry.
+__global__ void __launch_bounds__(256) k3_bond_flags(const uint32_t* __restrict__ rows, uint32_t n,
+                                                     uint32_t* __restrict__ flag) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    flag[i] = rows[(size_t)i * BOND3_WORDS] != 0u ? 1u : 0u;
+}
+
 template <typename T>
 T* dalloc3(size_t count, std::string& err) {
   if (count == 0) count = 1;
@@ -105,7 +155,7 @@ struct Engine3 {
     if (graph) cudaGraphDestroy(graph);
     void* ptrs[] = {b.state, b.sceneOf, b.bond, b.bflag, b.inv, b.PRS, b.keys, b.skey, b.sslot, b.cellStart, b.PW, b.PW2, b.PL, b.NBR,
                     b.NBRN, (void*)b.WG, (void*)b.PG, (void*)b.mats, (void*)b.rcp, b.scenes, b.world, b.acc,
-                    b.accLast, b.chain, b.dbg, tmpK, tmpV, hist, accTmp, fnvBuf, ballDev};
+                    b.accLast, b.chain, b.dbg, tmpK, tmpV, hist, accTmp, fnvBuf, ballDev, upl, uplRes};
     for (void* p : ptrs)
       if (p) cudaFree(p);
     if (ev0) cudaEventDestroy(ev0);
@@ -483,23 +533,26 @@ struct Engine3 {
     if (sc->n > 0 && (!sc->pos || !sc->mat)) return fail("pos and mat are required");
     for (uint32_t a : {sc->gx, sc->gy, sc->gz})
       if (a < 1 || a > MAX_AXIS_CELLS) return fail("grid dims must be 1..%u cells per axis", MAX_AXIS_CELLS);
-    for (uint32_t i = 0; i < sc->n; ++i)
-      if (sc->mat[i] >= matCount) return fail("mat[%u] = %u outside the material table", i, sc->mat[i]);
-    std::vector<int32_t> words((size_t)sc->n * 8, 0);
-    for (uint32_t i = 0; i < sc->n; ++i) {
-      int32_t* w = words.data() + (size_t)i * 8;
-      w[0] = sc->pos[3 * i];
-      w[1] = sc->pos[3 * i + 1];
-      w[2] = sc->pos[3 * i + 2];
-      w[3] = (int32_t)sc->mat[i];
-      if (sc->vel) {
-        w[4] = sc->vel[3 * i];
-        w[5] = sc->vel[3 * i + 1];
-        w[6] = sc->vel[3 * i + 2];
-      }
+    // the arrays go up as they are (pos 3n, vel 3n, mat n), are checked on the
+    // device (the first bad material index) and packed there; a refused load
+    // leaves the scene's state as it was
+    if (sc->n) {
+      if (!ensure_upload()) return false;
+      const size_t n = sc->n;
+      bool ok = cuda_ok(cudaMemcpyAsync(upl, sc->pos, n * 12, cudaMemcpyHostToDevice, st), "upload") &&
+                (!sc->vel || cuda_ok(cudaMemcpyAsync(upl + 3 * n, sc->vel, n * 12, cudaMemcpyHostToDevice, st), "upload")) &&
+                cuda_ok(cudaMemcpyAsync(upl + 6 * n, sc->mat, n * 4, cudaMemcpyHostToDevice, st), "upload");
+      const uint32_t none = 0xffffffffu;
+      ok = ok && cuda_ok(cudaMemcpyAsync(uplRes, &none, 4, cudaMemcpyHostToDevice, st), "upload");
+      if (!ok) return false;
+      k3_load_check<<<grid_for(sc->n), 256, 0, st>>>(upl, sc->n, matCount, uplRes);
+      uint32_t bad = 0;
+      cudaMemcpyAsync(&bad, uplRes, 4, cudaMemcpyDeviceToHost, st);
+      if (!cuda_ok(cudaStreamSynchronize(st), "load check")) return false;
+      if (bad != none) return fail("mat[%u] = %u outside the material table", bad, sc->mat[bad]);
+      k3_load_pack<<<grid_for(sc->n), 256, 0, st>>>(upl, sc->n, sc->vel ? 1u : 0u, b.state + (size_t)h.slotBase * 8);
+      if (!cuda_ok(cudaGetLastError(), "pack")) return false;
     }
-    if (!words.empty())
-      cudaMemcpyAsync(b.state + (size_t)h.slotBase * 8, words.data(), words.size() * 4, cudaMemcpyHostToDevice, st);
     static const uint32_t CHAIN_INIT[8] = {0x243f6a88u, 0x85a308d3u, 0x13198a2eu, 0x03707344u,
                                            0xa4093822u, 0x299f31d0u, 0x082efa98u, 0xec4e6c89u};
     cudaMemcpyAsync(b.chain + (size_t)s * 8, CHAIN_INIT, 32, cudaMemcpyHostToDevice, st);
@@ -515,6 +568,17 @@ struct Engine3 {
     h.loaded = true;
     layoutDirty = true;
     return cuda_ok(cudaStreamSynchronize(st), "load");
+  }
+
+  // A device buffer the scene loads and bond writes upload into before their
+  // device-side checks (capSlots x BOND3_WORDS words: fits either).
+  int32_t* upl = nullptr;
+  uint32_t* uplRes = nullptr;
+  bool ensure_upload() {
+    if (upl) return true;
+    upl = dalloc3<int32_t>((size_t)capSlots * BOND3_WORDS, err);
+    uplRes = dalloc3<uint32_t>(2, err);
+    return upl && uplRes;
   }
 
   bool clear_bonds(uint32_t s) {
@@ -537,9 +601,20 @@ struct Engine3 {
     if (!rows || words != (size_t)h.n * BOND3_WORDS) return fail("bond rows need n * %u words", BOND3_WORDS);
     if (k < 0 || k > 65536) return fail("bond stiffness %d outside 0..65536", k);
     if (brk < 0) return fail("bond break ratio must be >= 0");
-    std::vector<uint32_t> flag(h.n, 0u);
-    bool any = false;
-    for (uint32_t i = 0; i < h.n; ++i) {
+    // the rows go up as they are and are checked on the device (the first bad
+    // row is then named by the same host rules); a refused write leaves the
+    // scene's rows as they were
+    if (!ensure_upload()) return false;
+    const uint32_t none[2] = {0xffffffffu, 0u};
+    bool ok = cuda_ok(cudaMemcpyAsync(upl, rows, words * 4, cudaMemcpyHostToDevice, st), "upload") &&
+              cuda_ok(cudaMemcpyAsync(uplRes, none, 8, cudaMemcpyHostToDevice, st), "upload");
+    if (!ok) return false;
+    if (h.n) k3_bonds_check<<<grid_for(h.n), 256, 0, st>>>(reinterpret_cast<const uint32_t*>(upl), h.n, uplRes);
+    uint32_t res[2];
+    cudaMemcpyAsync(res, uplRes, 8, cudaMemcpyDeviceToHost, st);
+    if (!cuda_ok(cudaStreamSynchronize(st), "bond check")) return false;
+    if (res[0] != 0xffffffffu) {
+      const uint32_t i = res[0];
       const uint32_t* r = rows + (size_t)i * BOND3_WORDS;
       bool ended = false;
       for (uint32_t e = 0; e < BOND3_CAP; ++e) {
@@ -554,14 +629,15 @@ struct Engine3 {
         if (j >= h.n || j == i) return fail("bond row %u names partner %u", i, j);
         if ((int32_t)L0 < BOND3_L0_MIN || (int32_t)L0 > BOND3_L0_MAX)
           return fail("bond row %u: rest length %u outside %d..%d", i, L0, BOND3_L0_MIN, BOND3_L0_MAX);
-        flag[i] = 1u;
-        any = true;
       }
+      return fail("bond row %u failed the device check but passes the host check", i);
     }
+    const bool any = res[1] != 0u;
     if (!clear_bonds(s)) return false;
     if (h.n) {
-      cudaMemcpyAsync(b.bond + (size_t)h.slotBase * BOND3_WORDS, rows, words * 4, cudaMemcpyHostToDevice, st);
-      cudaMemcpyAsync(b.bflag + h.slotBase, flag.data(), (size_t)h.n * 4, cudaMemcpyHostToDevice, st);
+      cudaMemcpyAsync(b.bond + (size_t)h.slotBase * BOND3_WORDS, upl, words * 4, cudaMemcpyDeviceToDevice, st);
+      k3_bond_flags<<<grid_for(h.n), 256, 0, st>>>(b.bond + (size_t)h.slotBase * BOND3_WORDS, h.n,
+                                                     b.bflag + h.slotBase);
     }
     h.bonds = any;
     h.bondK = k;
