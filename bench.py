@@ -235,9 +235,20 @@ def run_cpu_baseline(warmup: int, steps: int, threads: int = 0, side: int = 1024
     t0 = time.perf_counter()
     e.step(steps)
     dt = time.perf_counter() - t0
-    return {'value': sc.nFluid * steps / dt, 'unit': UNIT, 'cores': threads, 'kind': 'port',
-            'sample': f'{sc.nFluid} fluid particles ({side}x{side} lattice of the same workload), substeps '
-                      f'[{warmup}, {warmup + steps}) timed, {dt:.1f} s'}
+    out = {'value': sc.nFluid * steps / dt, 'unit': UNIT, 'cores': threads, 'kind': 'port',
+           'sample': f'{sc.nFluid} fluid particles ({side}x{side} lattice of the same workload), substeps '
+                     f'[{warmup}, {warmup + steps}) timed, {dt:.1f} s'}
+    # one thread, on a 256 x 256 slice of the scene, the same window
+    small = scenes.large_two_fluid(side=256)
+    e1 = oracle.OracleEngine(small.n + 64, threads=1).load_scene(small)
+    e1.step(warmup)
+    t0 = time.perf_counter()
+    e1.step(min(steps, 10))
+    dt1 = time.perf_counter() - t0
+    out['single_thread'] = {'value': small.nFluid * min(steps, 10) / dt1, 'unit': UNIT, 'cores': 1,
+                            'sample': f'{small.nFluid} fluid particles (256x256 slice), substeps '
+                                      f'[{warmup}, {warmup + min(steps, 10)}), {dt1:.1f} s'}
+    return out
 
 
 def reference_arm(args):
@@ -677,6 +688,12 @@ def ours(args):
         full = {'substeps': FULL_SUBSTEPS, 'value': sc.nFluid * FULL_SUBSTEPS / (fms / 1e3), 'unit': UNIT,
                 'ms_per_step': fms / FULL_SUBSTEPS,
                 'parity': parity_against('two_fluid_1024', FULL_SUBSTEPS, e3.chain_hex())}
+        # where the settled substep's time goes: the per-phase profile of the
+        # three substeps after the run (the compressed column, crowded edge cell)
+        late = {}
+        for nm, t in zip(phase_names(e3.iters), e3.profile_substep(3)):
+            late[nm] = late.get(nm, 0.0) + float(t)
+        full['phases_ms_per_substep_after'] = late
         e3.destroy()
 
     line = {

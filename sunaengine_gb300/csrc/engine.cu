@@ -56,41 +56,63 @@ __device__ __forceinline__ bool in_disc(int32_t px, int32_t py, const ImpulseEv&
   return !(s > __dmul_rn(r, r));
 }
 
-__device__ uint32_t apply_event(Bufs b, const ScenePar& S, const ImpulseEv& ev) {
+// Exclusive block-wide prefix sum of v (every thread of the CTA calls it);
+// *total receives the block's sum.
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* total) {
   __shared__ uint32_t wsum[32];
-  __shared__ uint32_t total;
-  uint32_t hits = 0;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = (int)(blockDim.x >> 5);
-  for (uint32_t base = 0; base < S.nFluid && hits < ev.limit; base += blockDim.x) {
-    uint32_t i = base + tid;
-    bool in = false;
-    int32_t* w = nullptr;
-    if (i < S.nFluid) {
-      w = b.state + (size_t)(S.slotBase + i) * 8;
-      in = in_disc(w[0], w[1], ev);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (int)(blockDim.x >> 5);
+  uint32_t inc = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += t;
+  }
+  if (lane == 31) wsum[warp] = inc;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = lane < nw ? wsum[lane] : 0u;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += t;
     }
-    uint32_t bal = __ballot_sync(0xffffffffu, in);
-    if (lane == 0) wsum[warp] = __popc(bal);
-    __syncthreads();
-    uint32_t before = 0, all = 0;
-    for (int k = 0; k < nw; ++k) {
-      if (k < warp) before += wsum[k];
-      all += wsum[k];
-    }
-    uint32_t rank = hits + before + __popc(bal & ((1u << lane) - 1u));
-    if (in && rank < ev.limit) {
+    wsum[lane] = w;  // inclusive over warps
+  }
+  __syncthreads();
+  const uint32_t before = warp ? wsum[warp - 1] : 0u;
+  *total = wsum[nw - 1];
+  __syncthreads();  // wsum is reused by the next call
+  return before + inc - v;
+}
+
+// One disc impulse over scene S's fluid particles (every thread of the CTA
+// calls it). The hits are ranked in slot order: each thread owns a
+// contiguous slot range, counts its hits, and a block scan gives each hit its
+// rank; the first `limit` hits get the impulse. Returns min(hits, limit).
+__device__ uint32_t apply_event(Bufs b, const ScenePar& S, const ImpulseEv& ev) {
+  const uint32_t n = S.nFluid, T = blockDim.x;
+  const uint32_t per = (n + T - 1) / T;
+  const uint32_t lo = min(n, threadIdx.x * per), hi = min(n, lo + per);
+  uint32_t cnt = 0;
+  for (uint32_t i = lo; i < hi; ++i) {
+    const int32_t* w = b.state + (size_t)(S.slotBase + i) * 8;
+    cnt += in_disc(w[0], w[1], ev) ? 1u : 0u;
+  }
+  uint32_t total = 0;
+  uint32_t rank = block_exclusive_scan(cnt, &total);
+  if (cnt && rank < ev.limit)
+    for (uint32_t i = lo; i < hi && rank < ev.limit; ++i) {
+      int32_t* w = b.state + (size_t)(S.slotBase + i) * 8;
+      if (!in_disc(w[0], w[1], ev)) continue;
       int64_t vx = (int64_t)w[2] + ev.ix, vy = (int64_t)w[3] + ev.iy;
       vx = vx < -VMAX ? -VMAX : (vx > VMAX ? VMAX : vx);
       vy = vy < -VMAX ? -VMAX : (vy > VMAX ? VMAX : vy);
       w[2] = (int32_t)vx;
       w[3] = (int32_t)vy;
+      ++rank;
     }
-    if (tid == 0) total = hits + all;
-    __syncthreads();
-    hits = min(total, ev.limit);
-    __syncthreads();
-  }
-  return hits;
+  __syncthreads();  // the next event of the scene reads these velocities
+  return min(total, ev.limit);
 }
 
 // One CTA of IMPULSE_THREADS per scene: the disc test covers the scene's
