@@ -45,15 +45,33 @@ struct EvPar {
 };
 
 // Device impulse: one CTA per scene; due events apply in queue order, hits
-// counted in slot order with a block-wide ballot scan, first `limit` hits
-// only. The disc test is the reference's JS arithmetic: IEEE doubles, each
-// product and the sum rounded to nearest, no fused multiply-add.
-__device__ __forceinline__ bool in_disc(int32_t px, int32_t py, const ImpulseEv& ev) {
+// counted in slot order with a block-wide scan, first `limit` hits only.
+// The disc test is the reference's JS arithmetic: IEEE doubles, each product
+// and the sum rounded to nearest, no fused multiply-add, then !(s > r*r).
+__device__ __forceinline__ bool in_disc_f64(int32_t px, int32_t py, const ImpulseEv& ev) {
   double dx = (double)px - (double)ev.cx;
   double dy = (double)py - (double)ev.cy;
   double r = (double)ev.r;
   double s = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
   return !(s > __dmul_rn(r, r));
+}
+// The same decision, taken in exact 64-bit integers wherever the doubles'
+// rounding cannot change it (a filtered exact predicate). With X = dx^2 + dy^2
+// and R = r^2 exact, each rounding to nearest moves a value by at most 2^-53
+// of itself, so s lies within X * 3 * 2^-53 of X and r*r within R * 2^-53 of
+// R; a gap |X - R| above (X >> 50) + (R >> 50) + 2 exceeds both, and the
+// exact comparison gives the doubles' answer. Near-ties (and |dx| or |dy| at
+// or above 2^31, where X could leave u64) take the double path.
+__device__ __forceinline__ bool in_disc(int32_t px, int32_t py, const ImpulseEv& ev) {
+  const int64_t dx = (int64_t)px - ev.cx, dy = (int64_t)py - ev.cy;
+  const uint64_t ax = (uint64_t)(dx < 0 ? -dx : dx), ay = (uint64_t)(dy < 0 ? -dy : dy);
+  if ((ax | ay) >> 31) return in_disc_f64(px, py, ev);
+  const uint64_t X = ax * ax + ay * ay;
+  const uint64_t R = (uint64_t)((int64_t)ev.r * ev.r);
+  const uint64_t m = (X >> 50) + (R >> 50) + 2u;
+  if (X > R + m) return false;
+  if (X + m < R) return true;
+  return in_disc_f64(px, py, ev);
 }
 
 // Exclusive block-wide prefix sum of v (every thread of the CTA calls it);
@@ -87,30 +105,59 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* t
 
 // One disc impulse over scene S's fluid particles (every thread of the CTA
 // calls it). The hits are ranked in slot order: each thread owns a
-// contiguous slot range, counts its hits, and a block scan gives each hit its
-// rank; the first `limit` hits get the impulse. Returns min(hits, limit).
+// contiguous slot range, tests it (positions read eight at a time, the hits
+// kept as a bit mask when the range is at most 64 slots), and a block scan
+// gives each thread the rank of its first hit; the first `limit` hits get the
+// impulse. Returns min(hits, limit).
 __device__ uint32_t apply_event(Bufs b, const ScenePar& S, const ImpulseEv& ev) {
   const uint32_t n = S.nFluid, T = blockDim.x;
   const uint32_t per = (n + T - 1) / T;
   const uint32_t lo = min(n, threadIdx.x * per), hi = min(n, lo + per);
+  int32_t* base = b.state + (size_t)S.slotBase * 8;
+  auto pos = [&](uint32_t i) { return *reinterpret_cast<const int2*>(base + (size_t)i * 8); };
   uint32_t cnt = 0;
-  for (uint32_t i = lo; i < hi; ++i) {
-    const int32_t* w = b.state + (size_t)(S.slotBase + i) * 8;
-    cnt += in_disc(w[0], w[1], ev) ? 1u : 0u;
+  uint64_t mask = 0;
+  const bool masked = per <= 64u;
+  uint32_t i = lo;
+  for (; i + 8 <= hi; i += 8) {
+    int2 q[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) q[j] = pos(i + j);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const bool h = in_disc(q[j].x, q[j].y, ev);
+      cnt += h ? 1u : 0u;
+      if (masked && h) mask |= 1ull << (i + j - lo);
+    }
+  }
+  for (; i < hi; ++i) {
+    const int2 q = pos(i);
+    const bool h = in_disc(q.x, q.y, ev);
+    cnt += h ? 1u : 0u;
+    if (masked && h) mask |= 1ull << (i - lo);
   }
   uint32_t total = 0;
   uint32_t rank = block_exclusive_scan(cnt, &total);
-  if (cnt && rank < ev.limit)
-    for (uint32_t i = lo; i < hi && rank < ev.limit; ++i) {
-      int32_t* w = b.state + (size_t)(S.slotBase + i) * 8;
-      if (!in_disc(w[0], w[1], ev)) continue;
-      int64_t vx = (int64_t)w[2] + ev.ix, vy = (int64_t)w[3] + ev.iy;
-      vx = vx < -VMAX ? -VMAX : (vx > VMAX ? VMAX : vx);
-      vy = vy < -VMAX ? -VMAX : (vy > VMAX ? VMAX : vy);
-      w[2] = (int32_t)vx;
-      w[3] = (int32_t)vy;
-      ++rank;
+  auto kick = [&](uint32_t k) {
+    int32_t* w = base + (size_t)k * 8;
+    int64_t vx = (int64_t)w[2] + ev.ix, vy = (int64_t)w[3] + ev.iy;
+    vx = vx < -VMAX ? -VMAX : (vx > VMAX ? VMAX : vx);
+    vy = vy < -VMAX ? -VMAX : (vy > VMAX ? VMAX : vy);
+    w[2] = (int32_t)vx;
+    w[3] = (int32_t)vy;
+  };
+  if (cnt && rank < ev.limit) {
+    if (masked) {
+      for (; mask && rank < ev.limit; mask &= mask - 1u, ++rank) kick(lo + (uint32_t)(__ffsll((long long)mask) - 1));
+    } else {
+      for (uint32_t k = lo; k < hi && rank < ev.limit; ++k) {
+        const int2 q = pos(k);
+        if (!in_disc(q.x, q.y, ev)) continue;
+        kick(k);
+        ++rank;
+      }
     }
+  }
   __syncthreads();  // the next event of the scene reads these velocities
   return min(total, ev.limit);
 }

@@ -199,6 +199,14 @@ __device__ __forceinline__ int lut_index(int2 d, const Flags<DBG>& f) {
   if (r2 >= H2S) return -1;
   return r2 >> 15;
 }
+// lut_index(d) >= 0 without the index, branch-free (release builds): an axis
+// above HS is clamped to HS + 1, whose square alone already exceeds H2S, so
+// the sum rejects exactly when lut_index does (and cannot wrap).
+__device__ __forceinline__ bool in_kernel(int2 d) {
+  static_assert((int64_t)(HS + 1) * (HS + 1) >= H2S && 2 * (int64_t)(HS + 1) * (HS + 1) < INT32_MAX, "clamp");
+  const int32_t ax = min((abs(d.x) + 8) >> 4, HS + 1), ay = min((abs(d.y) + 8) >> 4, HS + 1);
+  return ax * ax + ay * ay < H2S;
+}
 __device__ __forceinline__ int2 wall_clamp(const ScenePar& S, int2 p) {
   return make_int2(clampi(p.x, WALL, S.domW - WALL), clampi(p.y, WALL, S.domH - WALL));
 }
@@ -631,6 +639,22 @@ __global__ void __launch_bounds__(256, TILED ? 6 : 8) k_nbr(Bufs b) {
           uint32_t key = key_of(S, gx, gy);
           uint32_t lo = b.cellStart[key], hi = b.cellStart[key + 1];
           if (!DBG && hi - lo > CELL_BIG && !box_reaches(b.CB[key], pi)) continue;
+          if (!TILED && cut) {
+            // The stopping scan: no live fluid particle carries SEAL or
+            // CONGEAL (so neither flag can be raised) and the list ends at
+            // MAXNBR (so nothing overflows); the next record is loaded one
+            // candidate ahead.
+            int4 nx = lo < hi ? b.PL[lo] : make_int4(0, 0, 0, 0);
+            for (uint32_t q = lo; q < hi; ++q) {
+              const int4 o = nx;
+              if (q + 1 < hi) nx = b.PL[q + 1];
+              const uint32_t iq = (uint32_t)o.w;
+              if (q == p || (iq & INFO_DEAD) || !in_kernel(pdelta(pi, xy(o), f))) continue;
+              out[(size_t)cnt * stride] = q | (iq & INFO_BOUNDARY);
+              if (++cnt >= (uint32_t)MAXNBR) goto listed;
+            }
+            continue;
+          }
           const uint32_t delta = local ? tr[TR_BASE + halo_run(ts, tx, ty, gx, gy)] - tr[halo_run(ts, tx, ty, gx, gy)] : 0u;
           for (uint32_t q = lo; q < hi; ++q) {
             if (q == p) continue;

@@ -188,6 +188,36 @@ def test_spawn_and_impulse_match_oracle(oracle_mod):
     assert gpu.chain_hex() == ref.chain_hex()
 
 
+def test_impulse_disc_near_ties_match_oracle(oracle_mod):
+    """applyImpulse's disc test (src/engine.js:6077-6098) where the reference's
+    double rounding decides: particles at |dx| = r ~ 2^27 with dy = 0..11, so
+    dx^2 + dy^2 - r^2 = dy^2 (at dy = 1 the exact sum is outside the disc and
+    the doubles put it inside), beside particles far inside and far outside."""
+    sc = _pool('WATER', 30, 10)
+    gpu, ref = _pair(sc)
+    st = gpu.read_state().reshape(-1, 8).copy()
+    nf = sc.nFluid
+    half = nf // 2
+    cy = 1000
+    for k, r in enumerate([(1 << 27) - 1, (1 << 27) - 37, 3 * (1 << 25) + 5]):
+        s = st.copy()
+        for i in range(half):
+            # two in three on the rim (dx = r, dy = 0..11); the rest at dx = 0,
+            # dy ~ 2^27 - 1000 (well inside or well outside, by r)
+            rim = (i + k) % 3 != 0
+            s[i, 0] = r if rim else 0
+            s[i, 1] = cy + (i % 12) if rim else (1 << 27) - (i % 5)
+        gpu.write_state_keep_scratch(s.reshape(-1))
+        ref.write_state(s.reshape(-1))
+        for cx, lim in [(0, 3000), (0, 5), (2 * r, 3000)]:  # cx = 2r: the rim at dx = -r
+            assert gpu.apply_impulse(cx, cy, r, 777, -555, lim) == ref.impulse(cx, cy, r, 777, -555, lim)
+            assert np.array_equal(gpu.read_state(), ref.read_state()), (r, cx, lim)
+        # a disc around the untouched pool: the exact integer decision alone
+        args = (20 * ONE, 5 * ONE, 8 * ONE, -300, 900)
+        assert gpu.apply_impulse(*args) == ref.impulse(*args)
+        assert np.array_equal(gpu.read_state(), ref.read_state())
+
+
 def test_spawn_refused_at_capacity():
     sc = _pool('WATER', 10, 5)
     e = Engine(max_particles=sc.n + 2).load_scene(sc)
