@@ -58,6 +58,17 @@ def _ptr(a: Optional[np.ndarray]):
     return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
 
 
+def _out_words(out: Optional[np.ndarray], words: int) -> np.ndarray:
+    """A fresh int32 array of `words`, or the first `words` of a caller's buffer."""
+    if out is None:
+        return np.empty(words, np.int32)
+    if not isinstance(out, np.ndarray) or out.dtype != np.int32 or out.ndim != 1 or \
+            not out.flags.c_contiguous or not out.flags.writeable or out.size < words:
+        raise EngineError(f'[aether] read_state: out must be a writeable contiguous 1-D int32 array of at least '
+                          f'{words} words')
+    return out[:words]
+
+
 def _opts(max_particles, max_cells, iters, debug, chain, device, luts, mats, lanes=0):
     luts = np.ascontiguousarray(data.luts() if luts is None else luts, dtype=np.int32)
     if luts.size != data.LUT_WORDS or data.table_hash(luts) != data.TABLE_HASH:
@@ -184,8 +195,11 @@ class Engine:
     def reset_chain(self):
         self._check(self._lib.sn_reset_chain(self._h), 'resetChain')
 
-    def read_state(self) -> np.ndarray:
-        a = np.empty(self.n * 8, np.int32)
+    def read_state(self, out: Optional[np.ndarray] = None) -> np.ndarray:
+        """readState: the scene's state words (8 per slot). `out`, when given, is
+        a caller-owned contiguous int32 array of at least n * 8 words that
+        receives them (and is returned), so repeated reads reuse one buffer."""
+        a = _out_words(out, self.n * 8)
         self._check(self._lib.sn_read_state(self._h, _ptr(a), a.size), 'readState')
         return a
 
@@ -674,9 +688,8 @@ class Batch:
         self._check(self._lib.sn_batch_get_info(self._h, int(sid), ctypes.byref(i)), 'info')
         return {k: getattr(i, k) for k, _ in i._fields_}
 
-    def read_state(self, sid: int) -> np.ndarray:
-        n = self.info(sid)['n']
-        a = np.empty(n * 8, np.int32)
+    def read_state(self, sid: int, out: Optional[np.ndarray] = None) -> np.ndarray:
+        a = _out_words(out, self.info(sid)['n'] * 8)
         self._check(self._lib.sn_batch_read_state(self._h, int(sid), _ptr(a), a.size), 'read_state')
         return a
 

@@ -17,7 +17,7 @@ from typing import Optional
 import numpy as np
 
 from . import _native, tables3d
-from .engine import Digest, EngineError
+from .engine import Digest, EngineError, _out_words
 
 SUBSTEPS_PER_FRAME = 2   # CFG.substeps (3d/app.js:20)
 ITERS = 3                # CFG.iters (3d/app.js:21)
@@ -164,9 +164,8 @@ class Engine3D:
     def chain_hex(self, scene: int = 0) -> str:
         return ''.join(f'{int(w):08x}' for w in self._words(self._lib.sn3_chain, scene))
 
-    def read_state(self, scene: int = 0) -> np.ndarray:
-        n = self.info(scene)['n']
-        a = np.empty(n * 8, np.int32)
+    def read_state(self, scene: int = 0, out: Optional[np.ndarray] = None) -> np.ndarray:
+        a = _out_words(out, self.info(scene)['n'] * 8)
         self._check(self._lib.sn3_read_state(self.h, int(scene), _ptr(a), a.size), 'read_state')
         return a
 

@@ -218,6 +218,16 @@ def test_impulse_disc_near_ties_match_oracle(oracle_mod):
         assert np.array_equal(gpu.read_state(), ref.read_state())
 
 
+def test_read_state_into_caller_buffer():
+    sc = _pool('WATER', 20, 8)
+    e = Engine(max_particles=sc.n + 64).load_scene(sc)
+    e.step(3)
+    buf = np.full(sc.n * 8 + 5, -1, np.int32)
+    got = e.read_state(out=buf)
+    assert got.base is buf and np.array_equal(got, e.read_state())
+    assert (buf[sc.n * 8:] == -1).all()
+
+
 def test_spawn_refused_at_capacity():
     sc = _pool('WATER', 10, 5)
     e = Engine(max_particles=sc.n + 2).load_scene(sc)

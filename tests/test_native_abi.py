@@ -44,3 +44,23 @@ def test_noalloc_digest_refuses_oversize_without_a_launch():
     rc = lib.sn_digest_device_noalloc(one.ctypes.data_as(ctypes.c_void_p), (1 << 24) + 1, 0, None,
                                       out.ctypes.data_as(ctypes.c_void_p), None)
     assert rc == -2  # SN_E_CAPACITY
+
+
+def test_read_state_out_buffer_rules():
+    """read_state(out=...) takes a caller's writeable contiguous 1-D int32
+    array of at least the needed words and returns its leading view."""
+    import numpy as np
+    import pytest as _pt
+    from sunaengine_gb300.engine import EngineError, _out_words
+    buf = np.zeros(100, np.int32)
+    v = _out_words(buf, 64)
+    assert v.size == 64 and v.base is buf
+    assert _out_words(None, 8).size == 8
+    for bad in (np.zeros(63, np.int32), np.zeros(64, np.int64), np.zeros((8, 8), np.int32),
+                np.zeros(128, np.int32)[::2]):
+        with _pt.raises(EngineError):
+            _out_words(bad, 64)
+    ro = np.zeros(64, np.int32)
+    ro.flags.writeable = False
+    with _pt.raises(EngineError):
+        _out_words(ro, 64)
