@@ -11,6 +11,10 @@ equal chains at every recorded substep mean every digest matched:
   of 500;
 * the 256-scene batch (stir impulses on each scene's own clock): the sampled
   scenes' chains every 100 substeps of 1000, all 256 scenes stepped together.
+
+The 2D workloads replay in each mode of the substep: the default per-phase
+graph, the tile-staged shared-memory gathers (sn_set_staged) and the
+persistent solver loop (sn_set_persistent).
 """
 import json
 from pathlib import Path
@@ -29,10 +33,21 @@ def _vector(name):
     return json.loads(p.read_text())
 
 
-def _replay_2d(sc, vec, max_cells=0):
+MODES = ['graph', 'staged', 'persistent']
+
+
+def _mode(x, mode):
+    if mode == 'staged':
+        x.set_staged(True)
+    elif mode == 'persistent':
+        x.set_persistent(True)
+    return x
+
+
+def _replay_2d(sc, vec, mode, max_cells=0):
     from sunaengine_gb300.engine import Engine
     assert sc.n == vec['particles'] and sc.nFluid == vec['fluid_particles']
-    e = Engine(max_particles=sc.n, max_cells=max_cells, iters=vec['iters']).load_scene(sc)
+    e = _mode(Engine(max_particles=sc.n, max_cells=max_cells, iters=vec['iters']), mode).load_scene(sc)
     for k, want in enumerate(vec['chain'], start=1):
         e.step(1)
         got = e.chain_hex()
@@ -45,16 +60,18 @@ def _replay_2d(sc, vec, max_cells=0):
     e.destroy()
 
 
-def test_dambreak_64x64_full_length():
+@pytest.mark.parametrize('mode', MODES)
+def test_dambreak_64x64_full_length(mode):
     from sunaengine_gb300 import scenes
     vec = _vector('dambreak_64x64')
-    _replay_2d(scenes.lattice_dambreak(), vec)
+    _replay_2d(scenes.lattice_dambreak(), vec, mode)
 
 
-def test_two_fluid_1024_full_length():
+@pytest.mark.parametrize('mode', MODES)
+def test_two_fluid_1024_full_length(mode):
     from sunaengine_gb300 import scenes
     vec = _vector('two_fluid_1024')
-    _replay_2d(scenes.large_two_fluid(side=1024), vec, max_cells=1 << 20)
+    _replay_2d(scenes.large_two_fluid(side=1024), vec, mode, max_cells=1 << 20)
 
 
 def test_dam3d_64cubed_full_length():
@@ -73,13 +90,14 @@ def test_dam3d_64cubed_full_length():
     e.close()
 
 
-def test_batch_256_full_length():
+@pytest.mark.parametrize('mode', MODES)
+def test_batch_256_full_length(mode):
     from sunaengine_gb300 import scenes
     from sunaengine_gb300.engine import Batch
     vec = _vector('batch_256')
     total = vec['substeps']
     scs, sched = scenes.batch_scenes(count=vec['scenes_total'], seed=vec['seed'], substeps=total)
-    b = Batch(max_particles=sum(s.n for s in scs) + 16, max_scenes=len(scs), max_cells=1 << 22)
+    b = _mode(Batch(max_particles=sum(s.n for s in scs) + 16, max_scenes=len(scs), max_cells=1 << 22), mode)
     for sid, (s, ev) in enumerate(zip(scs, sched)):
         assert b.add_scene(s) == sid
         for (at, cx, cy, r, ix, iy) in ev:
