@@ -504,6 +504,11 @@ int sn_ckpt_pool_usage(const sn_ckpt_pool* p, size_t* used, size_t* capacity);
 /* Release a checkpoint (waits for copies in flight that touch it). */
 int sn_ckpt_free(sn_ckpt_pool* p, uint64_t handle);
 /* Bytes a checkpoint of this scene takes now (before 256-byte rounding). */
+int sn_ckpt_bytes(sn_engine* e, size_t* bytes);
+/* The single-scene engine's keyframe on the device: WaterDemo.snapshot() /
+ * restore() (src/demo_boot.js:286-320) without a host round trip. */
+int sn_ckpt_save(sn_engine* e, sn_ckpt_pool* p, uint64_t* handle);
+int sn_ckpt_load(sn_engine* e, sn_ckpt_pool* p, uint64_t handle);
 int sn_batch_ckpt_bytes(sn_batch* b, uint32_t id, size_t* bytes);
 int sn_batch_ckpt_save(sn_batch* b, uint32_t id, sn_ckpt_pool* p, uint64_t* handle);
 int sn_batch_ckpt_load(sn_batch* b, uint32_t id, sn_ckpt_pool* p, uint64_t handle);

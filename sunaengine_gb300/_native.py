@@ -237,6 +237,9 @@ SIGNATURES = {
     'sn_ckpt_pool_last_error': (ctypes.c_char_p, [P]),
     'sn_ckpt_pool_usage': (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)]),
     'sn_ckpt_free': (ctypes.c_int, [P, u64]),
+    'sn_ckpt_bytes': (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_size_t)]),
+    'sn_ckpt_save': (ctypes.c_int, [P, P, ctypes.POINTER(u64)]),
+    'sn_ckpt_load': (ctypes.c_int, [P, P, u64]),
     'sn_batch_ckpt_bytes': (ctypes.c_int, [P, u32, ctypes.POINTER(ctypes.c_size_t)]),
     'sn_batch_ckpt_save': (ctypes.c_int, [P, u32, P, ctypes.POINTER(u64)]),
     'sn_batch_ckpt_load': (ctypes.c_int, [P, u32, P, u64]),

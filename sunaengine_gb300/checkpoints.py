@@ -1,7 +1,8 @@
 """Device checkpoint pool (``sn_ckpt_pool`` in include/suna.h).
 
-A pool is one device allocation. ``Batch.ckpt_save`` / ``Engine3D.ckpt_save``
-copy a scene's keyframe into it on the engine's stream (no host round trip)
+A pool is one device allocation. ``Engine.ckpt_save`` / ``Batch.ckpt_save`` /
+``Engine3D.ckpt_save`` copy a scene's keyframe into it on the engine's stream
+(no host round trip)
 and return a handle; ``ckpt_load`` restores the scene to exactly that point.
 """
 from __future__ import annotations

@@ -2761,6 +2761,20 @@ int sn_ckpt_free(sn_ckpt_pool* p, uint64_t handle) {
   if (!p) return SN_E_INVALID;
   return p->free_rec(handle) ? SN_OK : SN_E_INVALID;
 }
+int sn_ckpt_bytes(sn_engine* e, size_t* bytes) {
+  if (!e || !bytes || !e->w.sh[0].loaded) return SN_E_INVALID;
+  *bytes = e->w.ckpt_bytes(0);
+  return SN_OK;
+}
+int sn_ckpt_save(sn_engine* e, sn_ckpt_pool* p, uint64_t* handle) {
+  if (!e || !p || !handle) return SN_E_INVALID;
+  if (e->w.ckpt_save(0, p, handle)) return SN_OK;
+  return e->w.err.rfind("checkpoint pool full", 0) == 0 ? SN_E_CAPACITY : rc_of(e->w, false);
+}
+int sn_ckpt_load(sn_engine* e, sn_ckpt_pool* p, uint64_t handle) {
+  if (!e || !p) return SN_E_INVALID;
+  return rc_of(e->w, e->w.ckpt_load(0, p, handle));
+}
 int sn_batch_ckpt_bytes(sn_batch* b, uint32_t id, size_t* bytes) {
   if (!b || !bytes || id >= b->w.maxScenes || !b->w.sh[id].loaded) return SN_E_INVALID;
   *bytes = b->w.ckpt_bytes(id);

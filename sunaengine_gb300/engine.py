@@ -540,6 +540,25 @@ class Engine:
         a = np.array([lanes[k] for k in ('solveA', 'colours', 'post1', 'post2', 'nbr')], np.uint32)
         self._check(self._lib.sn_set_lanes(self._h, _ptr(a)), 'setLanes')
 
+    # device keyframes (sn_ckpt_*): see checkpoints.CheckpointPool
+    def ckpt_bytes(self) -> int:
+        out = ctypes.c_size_t()
+        self._check(self._lib.sn_ckpt_bytes(self._h, ctypes.byref(out)), 'ckpt_bytes')
+        return int(out.value)
+
+    def ckpt_save(self, pool) -> int:
+        """Save the scene (state, stAcc, chain, bond rows, bodies, clocks) into
+        `pool` on the device; returns the checkpoint's handle."""
+        out = ctypes.c_uint64()
+        self._check(self._lib.sn_ckpt_save(self._h, pool.h, ctypes.byref(out)), 'ckpt_save')
+        return int(out.value)
+
+    def ckpt_load(self, pool, handle: int):
+        """Restore the scene to the checkpoint exactly (same n and n_fluid)."""
+        self._check(self._lib.sn_ckpt_load(self._h, pool.h, int(handle)), 'ckpt_load')
+        self._substeps = int(self.info()['substep_count'])
+        return self
+
     def set_staged(self, on: bool = True):
         """Tile-major sorted space with shared-memory staged gathers for solveA
         and the colour passes (same results; see sn_set_staged)."""

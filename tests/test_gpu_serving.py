@@ -102,3 +102,41 @@ def test_adding_a_scene_keeps_the_others_clocks():
     mix.remove_scene(sb)
     mix.step(18)
     assert (mix.digest(sa).hex, mix.chain_hex(sa)) == want
+
+
+@pytest.mark.parametrize('kind', ['bonds', 'bodies'])
+def test_engine_device_checkpoints_restore_exactly(kind):
+    """sn_ckpt_save / sn_ckpt_load on the single-scene engine: after a load,
+    the next substeps repeat the ones that followed the save bit for bit
+    (state, chain, bond rows, body records, rest offsets, clocks)."""
+    from sunaengine_gb300 import scenes
+    from sunaengine_gb300.engine import Engine
+    pool = CheckpointPool(64 << 20)
+    if kind == 'bonds':
+        sc = scenes.make_scene('stretch_v1')
+        e = Engine(max_particles=sc.n + 64).load_scene(sc)
+    else:
+        sc = scenes.rigid_tank()
+        e = Engine(max_particles=sc.n + 256).load_scene(sc)
+        cx, cy = sc.meta['wheel_centre']
+        assert e.make_rigid_body(sc.meta['plank']) == 0
+        assert e.make_axis_body(sc.meta['wheel'], cx + 2 * 65536, cy) == 1
+    e.step(9)
+    assert e.ckpt_bytes() > sc.n * 40
+    h = e.ckpt_save(pool)
+
+    def now():
+        out = [e.digest().hex, e.chain_hex(), e.read_state().tobytes(), e.read_bonds().tobytes()]
+        if kind == 'bodies':
+            out += [e.read_bodies().tobytes(), e.read_rest_offsets().tobytes()]
+        return out
+
+    e.step(23)
+    ahead = now()
+    e.ckpt_load(pool, h)
+    assert e.substep_count == 9 and e.info()['substep_count'] == 9
+    e.step(23)
+    assert now() == ahead
+    e.check_errors()
+    pool.free(h)
+    e.destroy()
