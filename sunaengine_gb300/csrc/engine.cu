@@ -448,7 +448,7 @@ struct World {
     b.chain = dalloc<uint32_t>((size_t)scenesCap * 8, err);
     b.dbg = dalloc<uint32_t>(16, err);
     b.err = dalloc<uint32_t>(4, err);
-    b.work = dalloc<uint32_t>(4, err);
+    b.work = dalloc<uint32_t>(8, err);
     barBuf = dalloc<uint32_t>(2, err);
     tmpK = dalloc<uint32_t>(C, err);
     tmpV = dalloc<uint32_t>(C, err);
@@ -1515,6 +1515,10 @@ struct World {
     return true;
   }
 
+  // Bond rows written by the host (or a checkpoint) may be non-empty: from
+  // here on the digest pass reads every row (work[4] is never cleared).
+  void mark_bonds_live() { cudaMemsetAsync(b.work + 4, 0xff, 4, st); }
+
   // Bond rows of scene s from the host (the write half of the reference's
   // readBond/writeBuffer(bond) pair that replaceWhere and sliceBonds use).
   bool write_bonds(uint32_t s, const uint32_t* in, size_t words) {
@@ -1524,6 +1528,7 @@ struct World {
     accFresh = false;
     cudaMemcpyAsync(b.bond + (size_t)h.slotBase * BOND_CAP, in, (size_t)h.nFluid * BOND_CAP * 4,
                     cudaMemcpyHostToDevice, st);
+    mark_bonds_live();
     return cuda_ok(cudaStreamSynchronize(st), "writeBonds");
   }
 
@@ -1577,8 +1582,10 @@ struct World {
     if (!repair_bodies_after_erase(s, surv, stOut)) return false;
     cudaMemcpyAsync(b.state + (size_t)h.slotBase * 8, stOut.data(), stOut.size() * 4, cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(b.stacc + h.slotBase, scOut.data(), scOut.size() * 4, cudaMemcpyHostToDevice, st);
-    if (oldF)
+    if (oldF) {
       cudaMemcpyAsync(b.bond + (size_t)h.slotBase * BOND_CAP, bOut.data(), bOut.size() * 4, cudaMemcpyHostToDevice, st);
+      mark_bonds_live();
+    }
     if (!cuda_ok(cudaStreamSynchronize(st), "erase write")) return false;
     if (!pull_params()) return false;
     h.n = newN;
@@ -2318,9 +2325,11 @@ struct World {
               cuda_ok(cudaMemcpyAsync(b.stacc + h.slotBase, d + n * 32, n * 8, cudaMemcpyDeviceToDevice, st), "load") &&
               cuda_ok(cudaMemcpyAsync(b.chain + (size_t)s * 8, d + n * 40, 32, cudaMemcpyDeviceToDevice, st), "load");
     uint32_t* bondRows = b.bond + (size_t)h.slotBase * BOND_CAP;
-    if (ok && r->hasBonds)
+    if (ok && r->hasBonds) {
       ok = cuda_ok(cudaMemcpyAsync(bondRows, d + n * 40 + 32, (size_t)h.nFluid * BOND_CAP * 4,
                                    cudaMemcpyDeviceToDevice, st), "load");
+      mark_bonds_live();
+    }
     else if (ok)
       ok = cuda_ok(cudaMemsetAsync(bondRows, 0, (size_t)h.nFluid * BOND_CAP * 4, st), "load");
     if (ok && r->nBodies) {

@@ -149,10 +149,13 @@ struct Bufs {
   uint32_t* chain;      // [S * 8]
   uint32_t* dbg;        // [16]
   uint32_t* err;        // [4]
-  uint32_t* work;       // [4] per-substep flags: [0] = some particle has a friction/bond row,
+  uint32_t* work;       // [8] per-substep flags: [0] = some particle has a friction/bond row,
                         // [1] = some live fluid particle carries INFO_SEAL or INFO_CONGEAL,
                         // [2] = tiles too large to stage (entries of OVF),
-                        // [3] = chunks of crowded cells for k_cellbox_chunks
+                        // [3] = chunks of crowded cells for k_cellbox_chunks;
+                        // and, never reset: [4] = some bond row of the world may be
+                        // non-empty (set by bond formation and by every host write of
+                        // bond rows)
   uint32_t* OVF;        // [nTiles] the tiles of this substep whose neighbourhood exceeds stageCap
   int4* CB;             // [K] pred bounding box of each cell above CELL_BIG particles (k_cellbox)
   // §20 rigid bodies
@@ -2015,10 +2018,14 @@ template <bool HASH>
 __global__ void __launch_bounds__(256) k_form2(Bufs b, uint32_t* __restrict__ acc) {
   __shared__ uint32_t dsacc[8], dsscene;
   if (HASH) digest_block_begin(dsacc, &dsscene);
+  // While no bond row of the world has ever been non-empty (work[4] clear),
+  // the digest needs no row reads: an empty row folds nothing. A row this
+  // launch forms is read by the thread that formed it.
+  const bool rowsLive = b.work[4] != 0u;
   const uint32_t slotEnd = b.world->slotEnd;
   const uint32_t nIter = HASH ? (slotEnd + gstride() - 1) / gstride() * gstride() : slotEnd;
   for (uint32_t slot = gtid(); slot < nIter; slot += gstride()) {
-    bool valid = false;
+    bool valid = false, formed = false;
     uint32_t s = 0;
     uint32_t h[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     if (slot < slotEnd) {
@@ -2045,6 +2052,10 @@ __global__ void __launch_bounds__(256) k_form2(Bufs b, uint32_t* __restrict__ ac
         // bond rows are dense too: an empty row stays as it is
         if (nn != 0u || row[0] != 0u)
           for (int k = nn; k < BOND_CAP; ++k) row[k] = 0;
+        if (nn != 0u) {
+          formed = true;
+          if (!rowsLive) b.work[4] = 1u;
+        }
         int32_t* w = b.state + (size_t)slot * 8;
         uint32_t fo = (uint32_t)w[5] & ~FLAG_CONGEAL;
         if (!(fo & FLAG_RIGID) && (fo & WELD_TAG_MASK) != S.weldHold) fo &= ~WELD_TAG_MASK;
@@ -2052,7 +2063,8 @@ __global__ void __launch_bounds__(256) k_form2(Bufs b, uint32_t* __restrict__ ac
       }
       if (HASH) {
         valid = S.active && i < S.n;
-        if (valid) particle_digest(b.state + (size_t)slot * 8, i, i < S.nFluid ? row : nullptr, h);
+        if (valid)
+          particle_digest(b.state + (size_t)slot * 8, i, (i < S.nFluid && (rowsLive || formed)) ? row : nullptr, h);
       }
     }
     if (HASH) digest_add_block(acc, dsacc, &dsscene, valid, s, h);
