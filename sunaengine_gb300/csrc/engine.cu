@@ -204,6 +204,64 @@ __global__ void __launch_bounds__(256) k_slot_fields(Bufs b, uint32_t slotBase, 
   }
 }
 
+// eraseWhere (src/engine.js:6460-6650) on the device, for a scene without
+// bodies. k_erase_rank: one CTA; each thread takes a contiguous range of the
+// keep flags, and a block scan gives every survivor its new index in slot
+// order (oldToNew[i], -1 for an erased particle; *kept = the survivors).
+__global__ void __launch_bounds__(1024) k_erase_rank(const uint8_t* __restrict__ keep, uint32_t n,
+                                                     int32_t* __restrict__ oldToNew, uint32_t* __restrict__ kept) {
+  const uint32_t T = blockDim.x, per = (n + T - 1) / T;
+  const uint32_t lo = min(n, threadIdx.x * per), hi = min(n, lo + per);
+  uint32_t cnt = 0;
+  for (uint32_t i = lo; i < hi; ++i) cnt += keep[i] ? 1u : 0u;
+  uint32_t total = 0;
+  uint32_t r = block_exclusive_scan(cnt, &total);
+  for (uint32_t i = lo; i < hi; ++i) oldToNew[i] = keep[i] ? (int32_t)r++ : -1;
+  if (threadIdx.x == 0) *kept = total;
+}
+// The survivors' state words and stAcc, then the boundary block after them,
+// written at their new slots into scratch; newToOld[k] = survivor k's old slot.
+__global__ void __launch_bounds__(256) k_erase_move(const int32_t* __restrict__ state, const int2* __restrict__ stacc,
+                                                    const int32_t* __restrict__ oldToNew, uint32_t n, uint32_t oldF,
+                                                    uint32_t newF, int4* __restrict__ outState,
+                                                    int2* __restrict__ outStacc, uint32_t* __restrict__ newToOld) {
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    const int32_t d = j < oldF ? oldToNew[j] : (int32_t)(newF + (j - oldF));
+    if (d < 0) continue;
+    const int4* src = reinterpret_cast<const int4*>(state + (size_t)j * 8);
+    outState[2 * (size_t)d] = src[0];
+    outState[2 * (size_t)d + 1] = src[1];
+    outStacc[d] = stacc[j];
+    if (j < oldF) newToOld[d] = j;
+  }
+}
+// Survivor k's bond row from its old row: tombstones and bonds to erased
+// particles dropped, partners renumbered (a partner index past the old fluid
+// count is dropped too); rows from the survivor count up to the old fluid
+// count come out empty.
+__global__ void __launch_bounds__(256) k_erase_bonds(const uint32_t* __restrict__ bond,
+                                                     const int32_t* __restrict__ oldToNew,
+                                                     const uint32_t* __restrict__ newToOld, uint32_t oldF,
+                                                     uint32_t newF, uint32_t* __restrict__ out) {
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < oldF; k += gridDim.x * blockDim.x) {
+    uint32_t* o = out + (size_t)k * BOND_CAP;
+    uint32_t c = 0;
+    if (k < newF) {
+      const uint32_t* row = bond + (size_t)newToOld[k] * BOND_CAP;
+      for (int q = 0; q < BOND_CAP; ++q) {
+        const uint32_t w = row[q];
+        if (w == 0u) break;
+        if (w & BOND_TOMB) continue;
+        const uint32_t j = w & BOND_J_MASK;
+        const int32_t nj = j < oldF ? oldToNew[j] : -1;
+        if (nj < 0) continue;
+        o[c++] = (w & BOND_L0_MASK) | (uint32_t)nj;
+      }
+    }
+    for (; c < (uint32_t)BOND_CAP; ++c) o[c] = 0u;
+  }
+}
+
 // Per material row, the words loadScene derives (src/engine.js:3855-3880):
 // the flag bits a fluid / wall particle of that row gets (FLAG_DEAD for a
 // phantom row, FLAG_SEAL for a seal-class row, the scene weld tag for a fluid
@@ -365,7 +423,7 @@ struct World {
                     b.NBRL, b.NBRN, (void*)b.tiles, b.TR, b.OVF, b.CB,
                     (void*)b.luts, (void*)b.WG, (void*)b.CA, (void*)b.mats, (void*)b.rcp,
                     b.scenes, b.world, b.acc, b.accLast, b.chain, b.dbg, b.err, b.work, tmpK, tmpV, hist,
-                    hits, accTmp, devEv, devEp, boxChunks, upl, uplRes, barBuf};
+                    hits, accTmp, devEv, devEp, boxChunks, upl, uplRes, barBuf, eraseBuf};
     for (void* p : ptrs)
       if (p) cudaFree(p);
     if (ev0) cudaEventDestroy(ev0);
@@ -1550,6 +1608,76 @@ struct World {
     const uint32_t newF = (uint32_t)surv.size();
     if (removedOut) *removedOut = oldF - newF;
     if (newF == oldF) return true;
+    const uint32_t newN = newF + nB;
+    if (scene_bodies(s) == 0) {
+      if (!erase_device(s, keep, oldF, newF)) return false;
+    } else if (!erase_host(s, surv)) {
+      return false;
+    }
+    if (!pull_params()) return false;
+    h.n = newN;
+    h.nFluid = newF;
+    hpar[s].n = newN;
+    hpar[s].nFluid = newF;
+    hpar[s].bondDirty = 1;
+    layoutDirty = true;
+    eventsDirty = true;
+    return push_scene(s) && cuda_ok(cudaStreamSynchronize(st), "erase");
+  }
+
+  // eraseWhere's compaction on the device (a scene without bodies): survivor
+  // ranks, state and stAcc moved through scratch, bond rows renumbered into
+  // the scene's candidate rows (free until the formation that the erase
+  // schedules rewrites them) and copied back.
+  char* eraseBuf = nullptr;
+  size_t eraseCap = 0;
+  bool erase_device(uint32_t s, const uint8_t* keep, uint32_t oldF, uint32_t newF) {
+    const SceneHost& h = sh[s];
+    const size_t n = h.n, cap = capSlots;
+    const size_t offStacc = cap * 32, offO2N = offStacc + cap * 8, offN2O = offO2N + cap * 4, offKeep = offN2O + cap * 4;
+    const size_t bytes = offKeep + ((cap + 255) & ~(size_t)255) + 256;
+    if (eraseCap < bytes) {
+      if (eraseBuf) cudaFree(eraseBuf);
+      eraseBuf = dalloc<char>(bytes, err);
+      eraseCap = eraseBuf ? bytes : 0;
+      if (!eraseBuf) return false;
+    }
+    int4* tState = reinterpret_cast<int4*>(eraseBuf);
+    int2* tStacc = reinterpret_cast<int2*>(eraseBuf + offStacc);
+    int32_t* o2n = reinterpret_cast<int32_t*>(eraseBuf + offO2N);
+    uint32_t* n2o = reinterpret_cast<uint32_t*>(eraseBuf + offN2O);
+    uint8_t* dKeep = reinterpret_cast<uint8_t*>(eraseBuf + offKeep);
+    uint32_t* dKept = reinterpret_cast<uint32_t*>(eraseBuf + bytes - 256);
+    const size_t base = h.slotBase, newN = newF + (n - oldF);
+    uint32_t* bondRows = b.bond + base * BOND_CAP;
+    uint32_t* scratchRows = b.bondCand + base * BOND_CAP;
+    bool ok = cuda_ok(cudaMemcpyAsync(dKeep, keep, oldF, cudaMemcpyHostToDevice, st), "erase keep");
+    if (!ok) return false;
+    k_erase_rank<<<1, 1024, 0, st>>>(dKeep, oldF, o2n, dKept);
+    k_erase_move<<<grid_for(n), 256, 0, st>>>(b.state + base * 8, b.stacc + base, o2n, (uint32_t)n, oldF, newF,
+                                              tState, tStacc, n2o);
+    if (oldF) k_erase_bonds<<<grid_for(oldF), 256, 0, st>>>(bondRows, o2n, n2o, oldF, newF, scratchRows);
+    ok = cuda_ok(cudaMemcpyAsync(b.state + base * 8, tState, newN * 32, cudaMemcpyDeviceToDevice, st), "erase state") &&
+         cuda_ok(cudaMemcpyAsync(b.stacc + base, tStacc, newN * 8, cudaMemcpyDeviceToDevice, st), "erase stAcc");
+    if (ok && oldF) {
+      ok = cuda_ok(cudaMemcpyAsync(bondRows, scratchRows, (size_t)oldF * BOND_CAP * 4, cudaMemcpyDeviceToDevice, st),
+                   "erase bonds") &&
+           cuda_ok(cudaMemsetAsync(scratchRows, 0, (size_t)oldF * BOND_CAP * 4, st), "erase cand");
+      mark_bonds_live();
+    }
+    uint32_t kept = 0;
+    ok = ok && cuda_ok(cudaMemcpyAsync(&kept, dKept, 4, cudaMemcpyDeviceToHost, st), "erase") &&
+         cuda_ok(cudaStreamSynchronize(st), "erase");
+    if (!ok) return false;
+    if (kept != newF) return fail("erase: the device kept %u particles, the host %u", kept, newF);
+    return true;
+  }
+
+  // The same compaction on the host, for a scene with bodies (their repair
+  // reads the compacted state).
+  bool erase_host(uint32_t s, const std::vector<uint32_t>& surv) {
+    SceneHost& h = sh[s];
+    const uint32_t oldF = h.nFluid, n = h.n, nB = n - oldF, newF = (uint32_t)surv.size();
     std::vector<int32_t> stIn((size_t)n * 8), scIn((size_t)n * 2);
     std::vector<uint32_t> bIn((size_t)oldF * BOND_CAP);
     cudaMemcpyAsync(stIn.data(), b.state + (size_t)h.slotBase * 8, stIn.size() * 4, cudaMemcpyDeviceToHost, st);
@@ -1574,7 +1702,8 @@ struct World {
         const uint32_t w = bIn[(size_t)surv[k] * BOND_CAP + q];
         if (w == 0u) break;
         if (w & BOND_TOMB) continue;
-        const int32_t nj = oldToNew[w & BOND_J_MASK];
+        const uint32_t j = w & BOND_J_MASK;
+        const int32_t nj = j < oldF ? oldToNew[j] : -1;
         if (nj < 0) continue;
         bOut[(size_t)k * BOND_CAP + c++] = (w & BOND_L0_MASK) | (uint32_t)nj;
       }
@@ -1586,16 +1715,7 @@ struct World {
       cudaMemcpyAsync(b.bond + (size_t)h.slotBase * BOND_CAP, bOut.data(), bOut.size() * 4, cudaMemcpyHostToDevice, st);
       mark_bonds_live();
     }
-    if (!cuda_ok(cudaStreamSynchronize(st), "erase write")) return false;
-    if (!pull_params()) return false;
-    h.n = newN;
-    h.nFluid = newF;
-    hpar[s].n = newN;
-    hpar[s].nFluid = newF;
-    hpar[s].bondDirty = 1;
-    layoutDirty = true;
-    eventsDirty = true;
-    return push_scene(s) && cuda_ok(cudaStreamSynchronize(st), "erase");
+    return cuda_ok(cudaStreamSynchronize(st), "erase write");
   }
 
   // ---- §20 rigid bodies: host side (src/engine.js:2050-2150, 5452-5811) ----------

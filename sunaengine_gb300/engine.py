@@ -707,6 +707,18 @@ class Batch:
         self._check(self._lib.sn_batch_get_info(self._h, int(sid), ctypes.byref(i)), 'info')
         return {k: getattr(i, k) for k, _ in i._fields_}
 
+    def erase(self, sid: int, keep) -> int:
+        """eraseWhere's compaction on scene ``sid``: one keep flag per fluid slot;
+        returns the number erased. The other scenes are untouched."""
+        k = np.ascontiguousarray(np.asarray(keep, dtype=bool).astype(np.uint8))
+        out = ctypes.c_uint32()
+        self._check(self._lib.sn_batch_erase(self._h, int(sid), _ptr(k), k.size, ctypes.byref(out)), 'eraseWhere')
+        return int(out.value)
+
+    def write_bonds(self, sid: int, bonds: np.ndarray):
+        b = np.ascontiguousarray(bonds, dtype=np.uint32).reshape(-1)
+        self._check(self._lib.sn_batch_write_bonds(self._h, int(sid), _ptr(b), b.size), 'writeBonds')
+
     def read_state(self, sid: int, out: Optional[np.ndarray] = None) -> np.ndarray:
         a = _out_words(out, self.info(sid)['n'] * 8)
         self._check(self._lib.sn_batch_read_state(self._h, int(sid), _ptr(a), a.size), 'read_state')

@@ -78,3 +78,58 @@ def test_weld_gestures_and_fusion_match_oracle():
     steps(5)
     assert np.array_equal(g.read_bonds(), r.read_bonds())
     assert list(g.debug_counters()) == list(r.debug_counters())
+
+
+def test_device_erase_at_size_matches_oracle():
+    """eraseWhere's device compaction on a 65,536-particle two-fluid scene
+    (two in three particles of a horizontal band erased): state and counts
+    equal to the oracle's right after, chains equal after more substeps."""
+    from sunaengine_gb300 import scenes
+    sc = scenes.large_two_fluid(side=256)
+    g = Engine(max_particles=sc.n + 64).load_scene(sc)
+    r = t.oracle(sc)
+    for x in (g, r):
+        x.step(3)
+    st = r.read_state().reshape(-1, 8)
+    nf = r.n_fluid
+    ys = st[:nf, 1]
+    lo, hi = np.percentile(ys, 40), np.percentile(ys, 60)
+    keep = ~((ys > lo) & (ys < hi) & (np.arange(nf) % 3 != 0))
+    assert g.erase(keep) == r.erase(keep) == int((~keep).sum())
+    assert g.n == r.n and g.n_fluid == r.n_fluid
+    assert np.array_equal(g.read_state(), r.read_state())
+    for x in (g, r):
+        x.step(5)
+    assert g.chain_hex() == r.chain_hex()
+    g.check_errors()
+
+
+def test_batch_erase_leaves_the_other_scenes_alone():
+    """sn_batch_erase on the middle scene of three: the erased scene equals the
+    oracle's, the others equal a twin batch that erased nothing."""
+    from sunaengine_gb300 import scenes
+    from sunaengine_gb300.engine import Batch
+    scs = [t.gel(), scenes.make_scene('pool_v1', w=40, h=12), scenes.make_scene('stretch_v1')]
+    twins = []
+    for _ in range(2):
+        b = Batch(max_particles=sum(s.n for s in scs) + 256, max_scenes=3)
+        for s in scs:
+            b.add_scene(s)
+        b.step(4)
+        twins.append(b)
+    a, b = twins
+    r = t.oracle(scs[1])
+    r.step(4)
+    st = r.read_state().reshape(-1, 8)
+    keep = st[:r.n_fluid, 0] < np.median(st[:r.n_fluid, 0])
+    assert b.erase(1, keep) == r.erase(keep)
+    assert np.array_equal(b.read_state(1), r.read_state())
+    for x in (a, b, r):
+        x.step(6)
+    assert b.chain_hex(1) == r.chain_hex()
+    for sid in (0, 2):
+        assert b.chain_hex(sid) == a.chain_hex(sid)
+        assert np.array_equal(b.read_state(sid), a.read_state(sid))
+    for x in (a, b):
+        x.check_errors()
+        x.destroy()
