@@ -451,6 +451,12 @@ def batched_workload(steps: int, warmup: int, device: int, plain_sample: int = 2
                    if str(at) in rec['chain'] and b.chain_hex(int(sid)) != rec['chain'][str(at)]]
             parity = {'checked_at_substep': at, 'ok': not bad, 'scenes_checked': len(vec['scenes']),
                       'mismatched': bad, 'against': 'tests/golden/config_vectors/batch_256.json'}
+    # where a batched substep's time goes: CUDA events between the phases over
+    # three substeps after the parity check (the stir impulses run before the
+    # first phase and are not in it)
+    phases = {}
+    for nm, t_ in zip(phase_names(4), b.profile_substep(3)):
+        phases[nm] = phases.get(nm, 0.0) + float(t_)
     b.destroy()
     # the whole stated run: FULL_SUBSTEPS substeps of every scene with its
     # full stir schedule, device-timed in chunks of 100 substeps, the sampled
@@ -505,7 +511,7 @@ def batched_workload(steps: int, warmup: int, device: int, plain_sample: int = 2
             'ms_per_step': ms / steps, 'gpu_launches_per_step': launches // max(1, steps),
             'plain_same_scenes': plain, 'plain_sample_scenes': int(len(pick)), 'lanes': lanes_b,
             'batched_vs_plain': batched / plain, 'parity': parity, 'full_config': full,
-            'persistent_loop': persistent}
+            'persistent_loop': persistent, 'phases_ms_per_substep': phases}
 
 
 def construction_workload(steps: int, warmup: int, device: int, with_cpu: bool = True, cpu_seconds: float = 4.0):
