@@ -400,13 +400,21 @@ def batched_workload(steps: int, warmup: int, device: int, plain_sample: int = 2
             for (at, cx, cy, r, ix, iy) in ev:
                 bb.schedule_impulse(sid, at, cx, cy, r, ix, iy)
         return bb
-    # lanes tuned on a separate run advanced to the middle of the timed window
+    # layout, then lanes, tuned on a separate run advanced to the middle of the
+    # timed window
     t = make()
     t.step(warmup + steps // 2)
+    layout = t.autotune_layout(1)
     t.autotune(2)
     pick = t.lanes()
     t.destroy()
-    b = make()
+
+    def with_layout(x):
+        if layout['layout']:
+            x.set_staged(True).set_tile_shape(layout['layout'])
+        return x
+
+    b = with_layout(make())
     b.set_lanes(pick)
     b.step(warmup)
     b.sync()
@@ -418,7 +426,7 @@ def batched_workload(steps: int, warmup: int, device: int, plain_sample: int = 2
     # the same window with the solver iterations as one persistent kernel per
     # substep (sn_batch_set_persistent), for comparison with the graph of
     # per-phase launches
-    bp = make()
+    bp = with_layout(make())
     bp.set_lanes(lanes_b)
     bp.set_persistent(True)
     bp.step(warmup)
@@ -469,7 +477,7 @@ def batched_workload(steps: int, warmup: int, device: int, plain_sample: int = 2
             assert bf.add_scene(s_) == sid
             for (at, cx, cy, r, ix, iy) in ev:
                 bf.schedule_impulse(sid, at, cx, cy, r, ix, iy)
-        bf.set_lanes(lanes_b)
+        with_layout(bf).set_lanes(lanes_b)
         vec = json.loads(vp.read_text()) if vp.exists() and seed == 0xba7c4 else None
         fms, bad, checked = 0.0, [], 0
         for k in range(100, FULL_SUBSTEPS + 1, 100):
@@ -511,7 +519,7 @@ def batched_workload(steps: int, warmup: int, device: int, plain_sample: int = 2
             'ms_per_step': ms / steps, 'gpu_launches_per_step': launches // max(1, steps),
             'plain_same_scenes': plain, 'plain_sample_scenes': int(len(pick)), 'lanes': lanes_b,
             'batched_vs_plain': batched / plain, 'parity': parity, 'full_config': full,
-            'persistent_loop': persistent, 'phases_ms_per_substep': phases}
+            'persistent_loop': persistent, 'phases_ms_per_substep': phases, 'layout_tuning': layout}
 
 
 def construction_workload(steps: int, warmup: int, device: int, with_cpu: bool = True, cpu_seconds: float = 4.0):
@@ -595,19 +603,29 @@ def ours(args):
     sc = scenes.large_two_fluid(side=1024)
     tuned_at = None
     lanes_pick = None
+    layout = {'layout': 2 if args.staged else 0, 'tuned': False}
     if not args.no_autotune:
-        # The lane split per gather class is tuned on a separate run of the
-        # same scene, advanced to the middle of the timed window: the lattice
-        # the scene starts from settles within a few hundred substeps and the
-        # best split changes with it (untimed; the measured engine only
-        # receives the result).
+        # The layout (list gathers, or staged gathers and their tile shape)
+        # and then the lane split per gather class are tuned on a separate run
+        # of the same scene, advanced to the middle of the timed window: the
+        # lattice the scene starts from settles within a few hundred substeps
+        # and the best choice changes with it (untimed; the measured engines
+        # only receive the result). --staged pins the staged layout.
         tuned_at = args.warmup + args.steps // 2
         t = Engine(max_particles=sc.n, max_cells=1 << 20, device=local).set_staged(args.staged).load_scene(sc)
         t.step(tuned_at)
+        if not args.staged:
+            layout = dict(t.autotune_layout(2), tuned=True)
         t.autotune(3)
         lanes_pick = t.lanes()
         t.destroy()
-    e = Engine(max_particles=sc.n, max_cells=1 << 20, device=local).set_staged(args.staged)
+
+    def with_layout(x):
+        if layout['layout']:
+            x.set_staged(True).set_tile_shape(layout['layout'])
+        return x
+
+    e = with_layout(Engine(max_particles=sc.n, max_cells=1 << 20, device=local))
     e.load_scene(sc)
     if lanes_pick is not None:
         e.set_lanes(lanes_pick)
@@ -656,7 +674,7 @@ def ours(args):
 
     # end to end through the public API: upload from host, H_slot read back every
     # substep, final state read back
-    e2 = Engine(max_particles=sc.n, max_cells=1 << 20, device=local).set_staged(args.staged)
+    e2 = with_layout(Engine(max_particles=sc.n, max_cells=1 << 20, device=local))
     if lanes_pick is not None:
         e2.set_lanes(lanes_pick)
     e2.load_scene(sc)
@@ -689,7 +707,7 @@ def ours(args):
     # load, device-timed, and its chain against the oracle's at the last one.
     full = None
     if not args.no_full:
-        e3 = Engine(max_particles=sc.n, max_cells=1 << 20, device=local).set_staged(args.staged)
+        e3 = with_layout(Engine(max_particles=sc.n, max_cells=1 << 20, device=local))
         if lanes_pick is not None:
             e3.set_lanes(lanes_pick)
         e3.load_scene(sc)
@@ -717,7 +735,9 @@ def ours(args):
                    'parallelism': 'replicas' if ws > 1 else 'single', 'l2': 'working set > L2, no flush',
                    'lanes': lanes_used, 'lanes_tuned_at_substep': tuned_at,
                    'timed_substeps': [args.warmup, args.warmup + args.steps],
-                   'gathers': 'tile-staged (shared memory, bulk copies)' if args.staged else 'neighbour-list (global)'},
+                   'gathers': (f"tile-staged (shared memory, bulk copies), tiles of {1 << layout['layout']} cells"
+                               if layout['layout'] else 'neighbour-list (global)'),
+                   'layout_tuning': layout},
         'parity_ok': parity['ok'],
         'parity': parity,
         'full_config': full,

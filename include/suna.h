@@ -355,6 +355,19 @@ int sn_batch_set_lanes(sn_batch* b, const uint32_t lanes[5]);
  * on GB300). Takes effect at the next step. */
 int sn_set_staged(sn_engine* e, uint32_t on);
 int sn_batch_set_staged(sn_batch* b, uint32_t on);
+/* (no counterpart) The staged layout's tiles: 2^shift cells a side, shift 2,
+ * 3 or 4 (default 2). Takes effect at the next step. */
+int sn_set_tile_shape(sn_engine* e, uint32_t shift);
+int sn_batch_set_tile_shape(sn_batch* b, uint32_t shift);
+/* (no counterpart) Layout tuning: runs reps + 1 REAL substeps (the first
+ * untimed) under each of the list gathers and the staged gathers with tiles
+ * of 4, 8 and 16 cells, and keeps the fastest. *substeps_run receives the
+ * substeps it ran, *layout the pick (0 = list gathers, else the tile side's
+ * log2), ms_per_substep[4] (may be null) the device ms per substep of each
+ * candidate in that order. Results are identical under every layout. */
+int sn_autotune_layout(sn_engine* e, uint32_t reps, uint32_t* substeps_run, uint32_t* layout, float* ms_per_substep);
+int sn_batch_autotune_layout(sn_batch* b, uint32_t reps, uint32_t* substeps_run, uint32_t* layout,
+                             float* ms_per_substep);
 /* (no counterpart) Run the solver iterations (solveA, the four colour
  * passes and friction/applyFric, ITERS times) as one persistent cooperative
  * kernel with grid barriers between the phases, instead of one launch per

@@ -227,6 +227,12 @@ SIGNATURES = {
     'sn_autotune': (ctypes.c_int, [P, u32, ctypes.POINTER(u32)]),
     'sn_batch_autotune': (ctypes.c_int, [P, u32, ctypes.POINTER(u32)]),
     'sn_set_staged': (ctypes.c_int, [P, u32]),
+    'sn_set_tile_shape': (ctypes.c_int, [P, u32]),
+    'sn_batch_set_tile_shape': (ctypes.c_int, [P, u32]),
+    'sn_autotune_layout': (ctypes.c_int, [P, u32, ctypes.POINTER(u32), ctypes.POINTER(u32),
+                                          ctypes.POINTER(ctypes.c_float)]),
+    'sn_batch_autotune_layout': (ctypes.c_int, [P, u32, ctypes.POINTER(u32), ctypes.POINTER(u32),
+                                                ctypes.POINTER(ctypes.c_float)]),
     'sn_batch_set_staged': (ctypes.c_int, [P, u32]),
     'sn_set_persistent': (ctypes.c_int, [P, u32]),
     'sn_batch_set_persistent': (ctypes.c_int, [P, u32]),

@@ -710,7 +710,7 @@ struct World {
   // the tile table.
   std::vector<TileInfo> tileHost;
   uint32_t keyCap = 0, tileCap = 0;
-  uint32_t tileShiftPinned = 0;
+  uint32_t tileShiftPinned = 0;  // the staged layout's tile side, log2 (0: 2, tiles of 4 x 4 cells)
   // the tile-major layout with shared-memory staged gathers (sn_set_staged);
   // off by default: measured slower than the list gathers it replaces
   bool staged = false;
@@ -1200,6 +1200,43 @@ struct World {
     if (layoutDirty && !relayout()) return false;
     if (eventsDirty && !upload_events()) return false;
     return tune_lanes(std::max(1u, per), used);
+  }
+
+  // Layout tuning: the list gathers (colour-major keys) and the tile-staged
+  // gathers with tiles of 4, 8 and 16 cells, each run for one untimed
+  // substep (it re-lays out and re-captures) and `per` timed ones; the
+  // fastest stays. Every layout gives the same results, so these are the
+  // scenes' real substeps. ms[k] = device ms per substep of candidate k.
+  bool autotune_layout(uint32_t per, uint32_t* used, uint32_t* pick, float* ms) {
+    static const uint32_t cand[4] = {0u, 2u, 3u, 4u};
+    if (used) *used = 0;
+    bool any = false;
+    for (auto& s2 : sh) any |= (s2.used && s2.loaded);
+    if (!any) return fail("autotune before loadScene()");
+    per = std::max(1u, per);
+    float best = 0.f;
+    uint32_t bestC = 0, n = 0;
+    for (int ci = 0; ci < 4; ++ci) {
+      staged = cand[ci] != 0u;
+      if (staged) tileShiftPinned = cand[ci];
+      layoutDirty = true;
+      if (!step(1) || !step(per)) return false;
+      n += per + 1;
+      float t = 0.f;
+      if (!timing(&t)) return false;
+      t /= (float)per;
+      if (ms) ms[ci] = t;
+      if (ci == 0 || t < best) {
+        best = t;
+        bestC = cand[ci];
+      }
+    }
+    staged = bestC != 0u;
+    if (staged) tileShiftPinned = bestC;
+    layoutDirty = true;
+    if (used) *used = n;
+    if (pick) *pick = bestC;
+    return true;
   }
 
   bool tune_lanes(uint32_t per, uint32_t* used) {
@@ -2816,6 +2853,27 @@ int sn_autotune(sn_engine* e, uint32_t reps, uint32_t* substeps_run) {
 int sn_batch_autotune(sn_batch* b, uint32_t reps, uint32_t* substeps_run) {
   if (!b) return SN_E_INVALID;
   return rc_of(b->w, b->w.autotune(reps, substeps_run));
+}
+int sn_autotune_layout(sn_engine* e, uint32_t reps, uint32_t* substeps_run, uint32_t* layout, float* ms_per_substep) {
+  if (!e) return SN_E_INVALID;
+  return rc_of(e->w, e->w.autotune_layout(reps, substeps_run, layout, ms_per_substep));
+}
+int sn_batch_autotune_layout(sn_batch* b, uint32_t reps, uint32_t* substeps_run, uint32_t* layout,
+                             float* ms_per_substep) {
+  if (!b) return SN_E_INVALID;
+  return rc_of(b->w, b->w.autotune_layout(reps, substeps_run, layout, ms_per_substep));
+}
+int sn_set_tile_shape(sn_engine* e, uint32_t shift) {
+  if (!e || shift < TILE_SHIFT_MIN || shift > TILE_SHIFT_MAX) return SN_E_INVALID;
+  e->w.tileShiftPinned = shift;
+  e->w.layoutDirty = true;
+  return SN_OK;
+}
+int sn_batch_set_tile_shape(sn_batch* b, uint32_t shift) {
+  if (!b || shift < TILE_SHIFT_MIN || shift > TILE_SHIFT_MAX) return SN_E_INVALID;
+  b->w.tileShiftPinned = shift;
+  b->w.layoutDirty = true;
+  return SN_OK;
 }
 int sn_set_staged(sn_engine* e, uint32_t on) {
   if (!e) return SN_E_INVALID;

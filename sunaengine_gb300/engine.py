@@ -559,6 +559,24 @@ class Engine:
         self._substeps = int(self.info()['substep_count'])
         return self
 
+    def set_tile_shape(self, shift: int):
+        """The staged layout's tiles: 2**shift cells a side (2, 3 or 4)."""
+        self._check(self._lib.sn_set_tile_shape(self._h, int(shift)), 'setTileShape')
+        return self
+
+    def autotune_layout(self, reps: int = 2) -> dict:
+        """Time real substeps under the list gathers and the staged gathers at
+        each tile shape (sn_autotune_layout) and keep the fastest. Returns the
+        pick (0 = list gathers, else the tile side's log2) and the measured
+        ms per substep of each candidate."""
+        used, pick = ctypes.c_uint32(), ctypes.c_uint32()
+        ms = (ctypes.c_float * 4)()
+        self._check(self._lib.sn_autotune_layout(self._h, int(reps), ctypes.byref(used), ctypes.byref(pick), ms),
+                    'autotuneLayout')
+        self._substeps += int(used.value)
+        return {'layout': int(pick.value), 'substeps': int(used.value),
+                'ms_per_substep': dict(zip(('list', 'tiles4', 'tiles8', 'tiles16'), (float(x) for x in ms)))}
+
     def set_staged(self, on: bool = True):
         """Tile-major sorted space with shared-memory staged gathers for solveA
         and the colour passes (same results; see sn_set_staged)."""
@@ -828,6 +846,21 @@ class Batch:
     def set_lanes(self, lanes: dict):
         a = np.array([lanes[k] for k in ('solveA', 'colours', 'post1', 'post2', 'nbr')], np.uint32)
         self._check(self._lib.sn_batch_set_lanes(self._h, _ptr(a)), 'setLanes')
+
+    def set_tile_shape(self, shift: int):
+        """The staged layout's tiles: 2**shift cells a side (2, 3 or 4)."""
+        self._check(self._lib.sn_batch_set_tile_shape(self._h, int(shift)), 'setTileShape')
+        return self
+
+    def autotune_layout(self, reps: int = 2) -> dict:
+        """sn_batch_autotune_layout: the fastest of the list and staged layouts
+        on real substeps of every scene (see Engine.autotune_layout)."""
+        used, pick = ctypes.c_uint32(), ctypes.c_uint32()
+        ms = (ctypes.c_float * 4)()
+        self._check(self._lib.sn_batch_autotune_layout(self._h, int(reps), ctypes.byref(used), ctypes.byref(pick),
+                                                       ms), 'autotuneLayout')
+        return {'layout': int(pick.value), 'substeps': int(used.value),
+                'ms_per_substep': dict(zip(('list', 'tiles4', 'tiles8', 'tiles16'), (float(x) for x in ms)))}
 
     def set_staged(self, on: bool = True):
         """Tile-major sorted space with shared-memory staged gathers (sn_batch_set_staged)."""
