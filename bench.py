@@ -552,6 +552,7 @@ def construction_workload(steps: int, warmup: int, device: int, with_cpu: bool =
         if bodies:
             out['bodies_live'] = int((e.read_bodies()[:, 0] == 1).sum())
             out['chain'] = e.chain_hex()
+            out['parity'] = parity_against('construction_site', warmup + steps, e.chain_hex())
         e.destroy()
     out['rigid_share'] = 1.0 - out['without_bodies']['ms_per_step'] / out['with_bodies']['ms_per_step']
     if with_cpu:

@@ -8,6 +8,10 @@ The workloads (sizes and inputs as the benchmark builds them):
   jitter and temperatures, 1000 substeps;
 * ``dam3d_64cubed``: the 262,144-particle 3D dam break with its 4096 seeded
   lattice-neighbour bonds, 4 iterations, 500 substeps;
+* ``construction_site``: the 74,384-particle construction site (24 bays of a
+  METAL plank made a free rigid body, a WOOD disc made an axis body and a
+  held STONE rail, over a WATER pool), its 48 bodies made in the order the
+  benchmark makes them, 500 substeps;
 * ``batch_256``: the 256 seeded scenes of 1 k-64 k particles with their stir
   schedules, 1000 substeps; a sample of scenes spanning the size range (every
   ``--stride``-th scene by size, plus the smallest and largest), each stepped
@@ -22,7 +26,7 @@ The chain after substep k pins every digest up to k: a GPU run whose chain
 equals the recorded one at its last substep matched the oracle on every
 substep before it.
 
-    python tests/golden/make_config_vectors.py dambreak_64x64 two_fluid_1024
+    python tests/golden/make_config_vectors.py dambreak_64x64 two_fluid_1024 construction_site
     python tests/golden/make_config_vectors.py batch_256 --stride 4 --procs 8
 
 Outputs go to tests/golden/config_vectors/<workload>.json. Each run takes
@@ -75,6 +79,28 @@ def record_2d(name: str, threads: int):
             print(f'{name}: {k}/{total} substeps, {time.time() - t0:.0f} s', flush=True)
     return {'workload': name, 'particles': int(sc.n), 'fluid_particles': int(sc.nFluid), 'iters': 4,
             'substeps': total, 'chain': chain, 'digest': digest}
+
+
+def record_construction(threads: int, total: int = 500):
+    import oracle
+    from sunaengine_gb300 import scenes
+    sc = scenes.construction_site()
+    # no neighbour-list cut: the held rail is seal-class, so flags can still change
+    e = oracle.OracleEngine(sc.n, threads=threads).load_scene(sc)
+    for pl, wh, pv in zip(sc.meta['planks'], sc.meta['wheels'], sc.meta['wheel_pivots']):
+        e.make_rigid_body(pl)
+        e.make_axis_body(wh, *pv)
+    chain, digest = [], {}
+    t0 = time.time()
+    for k in range(1, total + 1):
+        e.step(1)
+        chain.append(e.chain_hex())
+        if k % DIGEST_EVERY == 0:
+            digest[str(k)] = e.digest()
+        if k % 50 == 0:
+            print(f'construction_site: {k}/{total} substeps, {time.time() - t0:.0f} s', flush=True)
+    return {'workload': 'construction_site', 'particles': int(sc.n), 'fluid_particles': int(sc.nFluid),
+            'bodies': int(e.body_count), 'iters': 4, 'substeps': total, 'chain': chain, 'digest': digest}
 
 
 def record_3d(name: str, threads: int):
@@ -161,5 +187,7 @@ if __name__ == '__main__':
             record_batch(a.stride, a.procs)
         elif w == 'dam3d_64cubed':
             _write(w, record_3d(w, a.threads))
+        elif w == 'construction_site':
+            _write(w, record_construction(a.threads))
         else:
             _write(w, record_2d(w, a.threads))

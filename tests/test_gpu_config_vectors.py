@@ -10,7 +10,9 @@ equal chains at every recorded substep mean every digest matched:
 * the 262,144-particle 3D dam break with its 4096 lattice bonds: every substep
   of 500;
 * the 256-scene batch (stir impulses on each scene's own clock): the sampled
-  scenes' chains every 100 substeps of 1000, all 256 scenes stepped together.
+  scenes' chains every 100 substeps of 1000, all 256 scenes stepped together;
+* the 74,384-particle construction site with its 48 rigid bodies and held
+  seal rail: every substep of 500.
 
 The 2D workloads replay in each mode of the substep: the default per-phase
 graph, the tile-staged shared-memory gathers (sn_set_staged) and the
@@ -88,6 +90,29 @@ def test_dam3d_64cubed_full_length():
         assert e.chain_hex() == want, f'chain differs at substep {k}'
     assert e.fnv_hex() == vec["fnv"]
     e.close()
+
+
+@pytest.mark.parametrize('mode', MODES)
+def test_construction_site_full_length(mode):
+    from sunaengine_gb300 import scenes
+    from sunaengine_gb300.engine import Engine
+    vec = _vector('construction_site')
+    sc = scenes.construction_site()
+    assert sc.n == vec['particles'] and sc.nFluid == vec['fluid_particles']
+    # (the persistent loop serves worlds without bodies; this one steps the graph)
+    e = _mode(Engine(max_particles=sc.n, iters=vec['iters']), mode).load_scene(sc)
+    for pl, wh, pv in zip(sc.meta['planks'], sc.meta['wheels'], sc.meta['wheel_pivots']):
+        e.make_rigid_body(pl)
+        e.make_axis_body(wh, *pv)
+    assert int(e.read_bodies().shape[0]) == vec['bodies']
+    for k, want in enumerate(vec['chain'], start=1):
+        e.step(1)
+        assert e.chain_hex() == want, f'chain differs at substep {k}'
+        d = vec['digest'].get(str(k))
+        if d is not None:
+            assert e.digest().hex == d, f'digest differs at substep {k}'
+    e.check_errors()
+    e.destroy()
 
 
 @pytest.mark.parametrize('mode', MODES)
