@@ -1,6 +1,7 @@
 """The serving loop on the GPU: every job's result is the same alone and in
-the mix (bit-exact digest and chain), a scrub equals advancing straight to the
-scrub point, and device checkpoints restore scenes exactly."""
+the mix (bit-exact digest and chain), served jobs equal the oracle's straight
+runs, a scrub equals advancing straight to the scrub point, and device
+checkpoints restore scenes exactly."""
 import numpy as np
 import pytest
 
@@ -140,3 +141,36 @@ def test_engine_device_checkpoints_restore_exactly(kind):
     e.check_errors()
     pool.free(h)
     e.destroy()
+
+
+def test_served_jobs_match_the_oracle(oracle_mod):
+    """Jobs served in a mixed stream against the oracle run straight to each
+    job's final substep (target, or the scrub point): the three smallest 2D
+    jobs (stir impulses at their substep indices) and the two smallest 3D
+    jobs (stir phase per frame of 2 substeps)."""
+    import oracle
+    jobs = serving.poisson_jobs(10, rate_hz=0, seed=21, n_lo=4096, n_hi=40000, t_lo=100, t_hi=320)
+    s = serving.Server(BUDGET, quantum=25)
+    s.run(jobs, realtime=False)
+    s.close()
+    two = sorted((j for j in jobs if j.dim == 2), key=lambda j: j.n)[:3]
+    three = sorted((j for j in jobs if j.dim == 3), key=lambda j: j.n)[:2]
+    assert two and three
+    for j in two:
+        end = j.scrub_to if j.op == 'scrub' else j.target
+        sc, sched = serving.job_scene_2d(j)
+        o = oracle.OracleEngine(sc.n + 8, iters=4, threads=16).load_scene(sc)
+        at = {}
+        for (t, cx, cy, r, ix, iy) in sched:
+            at.setdefault(t, []).append((cx, cy, r, ix, iy))
+        for k in range(end):
+            for ev in at.get(k, ()):
+                o.impulse(*ev)
+            o.step(1)
+        assert (o.digest(), o.chain_hex()) == (j.digest, j.chain), f'2D job {j.jid} ({j.op}, n={sc.n})'
+    for j in three:
+        end = j.scrub_to if j.op == 'scrub' else j.target
+        sc, amp = serving.job_scene_3d(j)
+        o = oracle.Oracle3D(sc.n, iters=4, threads=16).load_scene(sc, stir_amp=amp, frame=2)
+        o.step(end)
+        assert (o.digest(), o.chain_hex()) == (j.digest, j.chain), f'3D job {j.jid} ({j.op}, n={sc.n})'
