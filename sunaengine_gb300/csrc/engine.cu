@@ -369,6 +369,11 @@ struct SceneHost {
 struct World {
   int device = 0;
   cudaStream_t st = nullptr;
+  // A side stream for work that runs beside the main chain: each colour
+  // pass's copy of the other colours forks onto it and joins before the next
+  // pass (inside the captured graph, a parallel branch).
+  cudaStream_t st2 = nullptr;
+  cudaEvent_t evFork = nullptr, evJoin = nullptr;
   bool debug = false, chainOn = true;
   uint32_t iters = 4;
   uint32_t capSlots = 0, maxCells = 0, maxScenes = 0;
@@ -428,6 +433,9 @@ struct World {
       if (p) cudaFree(p);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
+    if (evFork) cudaEventDestroy(evFork);
+    if (evJoin) cudaEventDestroy(evJoin);
+    if (st2) cudaStreamDestroy(st2);
     if (st) cudaStreamDestroy(st);
   }
 
@@ -468,8 +476,11 @@ struct World {
         return fail("mats[%u] is not seal-class but carries burstP/sealMode", m);
     }
     if (!cuda_ok(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "stream")) return false;
+    if (!cuda_ok(cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking), "stream")) return false;
     cudaEventCreate(&ev0);
     cudaEventCreate(&ev1);
+    cudaEventCreateWithFlags(&evFork, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&evJoin, cudaEventDisableTiming);
     size_t C = capSlots;
     b.state = dalloc<int32_t>(C * 8, err);
     b.stacc = dalloc<int2>(C, err);
@@ -991,7 +1002,12 @@ struct World {
     for (int c = 0; c < 4; ++c) {
       const int4* src = (c & 1) ? b.PL2 : b.PL;
       int4* dst = (c & 1) ? b.PL : b.PL2;
-      k_colour<DBG, L><<<g, 256, 0, st>>>(b, c, src, dst);
+      cudaEventRecord(evFork, st);
+      cudaStreamWaitEvent(st2, evFork, 0);
+      k_colour_copy<<<2 * numSMs, 256, 0, st2>>>(b, c, src, dst);
+      cudaEventRecord(evJoin, st2);
+      k_colour<DBG, L><<<g, 256, 0, st>>>(b, c, src, dst, 0);
+      cudaStreamWaitEvent(st, evJoin, 0);
     }
   }
   // One cooperative launch of every solver iteration (k_iters_persistent):
@@ -1101,7 +1117,7 @@ struct World {
       mark();
       SN_LANES(lc.c, (launch_colours<DBG, L_>()));
       mark();
-      Lc += 5;
+      Lc += staged ? 5 : 9;
       if (hasFriction) {
         SN_LANES(lc.c, (launch_friction<DBG, L_>()));
         k_apply_fric<DBG><<<ga, 256, 0, st>>>(b);

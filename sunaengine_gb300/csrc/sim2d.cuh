@@ -1050,16 +1050,27 @@ __device__ __forceinline__ void colour_tile(const Bufs& b, const NB& nb, ME me_o
 // into its body at the end of the iteration (src/sim.wgsl:1418-1429).
 // (No __restrict__ here: the persistent kernel reads buffers that its own
 // earlier phases wrote, which must not go through the non-coherent load path.)
-template <bool DBG, int L>
-__device__ __forceinline__ void colour_all(const Bufs& b, int colour, const int4* src, int4* dst,
-                                           const Flags<DBG>& f) {
+// Phase c's copy of colours c+1 and c-1 (the two stale in dst) from src.
+__device__ __forceinline__ void copy_other_colours(const Bufs& b, int colour, const int4* src, int4* dst) {
   const uint32_t* cb = b.world->colourBase;
-  const uint32_t lo = b.cellStart[cb[colour]], hi = b.cellStart[cb[colour + 1]];
   const int c1 = (colour + 1) & 3, c3 = (colour + 3) & 3;
   const uint32_t lo1 = b.cellStart[cb[c1]], hi1 = b.cellStart[cb[c1 + 1]];
   const uint32_t lo3 = b.cellStart[cb[c3]], hi3 = b.cellStart[cb[c3 + 1]];
+  const uint32_t n1 = hi1 - lo1, n13 = n1 + (hi3 - lo3);
+  for (uint32_t i = gtid(); i < n13; i += gstride()) {
+    const uint32_t p = i < n1 ? lo1 + i : lo3 + (i - n1);
+    *reinterpret_cast<int2*>(dst + p) = *reinterpret_cast<const int2*>(src + p);
+  }
+}
+
+template <bool DBG, int L>
+__device__ __forceinline__ void colour_all(const Bufs& b, int colour, const int4* src, int4* dst,
+                                           const Flags<DBG>& f, bool copyOthers = true) {
+  const uint32_t* cb = b.world->colourBase;
+  const uint32_t lo = b.cellStart[cb[colour]], hi = b.cellStart[cb[colour + 1]];
   // The grid covers this colour's range only (the launch is sized to the
-  // resident capacity); the copies of the neighbouring colours follow.
+  // resident capacity); the copies of the neighbouring colours follow, or
+  // run beside the pass in k_colour_copy.
   const uint32_t chunk = blockDim.x / L;
   const NbrGlobal nb{src, b.NBR, b.nbrStride};
   for (uint32_t i0 = blockIdx.x * chunk; i0 < hi - lo; i0 += gridDim.x * chunk)
@@ -1073,17 +1084,20 @@ __device__ __forceinline__ void colour_all(const Bufs& b, int colour, const int4
           *reinterpret_cast<int2*>(dst + p) = pr;
         },
         lo + i0, min(hi - lo - i0, chunk), f);
-  const uint32_t n1 = hi1 - lo1, n13 = n1 + (hi3 - lo3);
-  for (uint32_t i = gtid(); i < n13; i += gstride()) {
-    const uint32_t p = i < n1 ? lo1 + i : lo3 + (i - n1);
-    *reinterpret_cast<int2*>(dst + p) = *reinterpret_cast<const int2*>(src + p);
-  }
+  if (copyOthers) copy_other_colours(b, colour, src, dst);
 }
 template <bool DBG, int L>
 __global__ void __launch_bounds__(256, 8) k_colour(Bufs b, int colour, const int4* __restrict__ src,
-                                                int4* __restrict__ dst) {
+                                                int4* __restrict__ dst, int copyOthers) {
   Flags<DBG> f{b.dbg};
-  colour_all<DBG, L>(b, colour, src, dst, f);
+  colour_all<DBG, L>(b, colour, src, dst, f, copyOthers != 0);
+}
+// The copy of phase c, launched on a forked branch of the substep so it runs
+// in the slots the pass leaves free; it touches none of the words the pass
+// reads from dst or writes.
+__global__ void __launch_bounds__(256) k_colour_copy(Bufs b, int colour, const int4* __restrict__ src,
+                                                     int4* __restrict__ dst) {
+  copy_other_colours(b, colour, src, dst);
 }
 
 // One colour of the sweep in the tile-major layout, with staged gathers.
