@@ -1092,8 +1092,14 @@ struct World {
     radix::sort_pairs(b.keys, hw.slotEnd, bits, b.skey, b.sslot, tmpK, tmpV, hist, st);
     Lc += (uint64_t)radix::LAUNCHES_PER_PASS * ((bits + radix::RBITS - 1) / radix::RBITS);
     mark();
-    k_cellstart<<<grid_for((uint64_t)hw.K + 1), 256, 0, st>>>(b);
+    // the cell ranges (from the sorted keys) and the gather (from the sorted
+    // slots) share no word: the ranges run on the side branch
+    cudaEventRecord(evFork, st);
+    cudaStreamWaitEvent(st2, evFork, 0);
+    k_cellstart<<<grid_for((uint64_t)hw.K + 1), 256, 0, st2>>>(b);
+    cudaEventRecord(evJoin, st2);
     k_gather<<<ga, 256, 0, st>>>(b);
+    cudaStreamWaitEvent(st, evJoin, 0);
     if (staged) k_tiles<<<grid_for((uint64_t)hw.nTiles * 32), 256, 0, st>>>(b);
     if (!DBG) {
       k_cellbox<<<grid_for((uint64_t)hw.K * 32), 256, 0, st>>>(b, boxChunks);
