@@ -338,17 +338,20 @@ def workload_3d(steps: int, warmup: int, device: int, cpu_seconds: float = 6.0, 
     t0 = time.perf_counter()
     e2.load_scene(sc)
     e2.write_bonds(rows, tables3d.DAM3D_BOND_K, tables3d.DAM3D_BOND_BRK)
+    t1 = time.perf_counter()
     for _ in range(steps):
         e2.step(1)
         e2.digest()
+    t2 = time.perf_counter()
     final = e2.read_state(out=outbuf)
     wall = time.perf_counter() - t0
+    parts3 = {'load_ms': 1e3 * (t1 - t0), 'steps_ms': 1e3 * (t2 - t1), 'read_state_ms': 1e3 * (t0 + wall - t2)}
     e2.close()
     out = {'workload': WORKLOAD_3D, 'particles': sc.n, 'steps': steps, 'value': value, 'unit': UNIT,
            'ms_per_step': ms / steps, 'gpu_launches': int(launches), 'roofline': roof, 'parity': parity,
            'full_config': full,
            'e2e': {'value': sc.n * steps / wall, 'unit': UNIT, 'h2d_bytes_per_step': (sc.n * 28 + rows.nbytes) / steps,
-                   'd2h_bytes_per_step': 32 + final.nbytes / steps}}
+                   'd2h_bytes_per_step': 32 + final.nbytes / steps, 'parts': parts3}}
     if with_cpu:
         import oracle
         threads = os.cpu_count() or 1

@@ -120,6 +120,10 @@ struct Engine3 {
   uint32_t iters = 3, capSlots = 0, maxCells = 0, maxScenes = 1, matCount = 0;
   std::string err;
   cudaStream_t st = nullptr;
+  // the side branch of the substep (inside the captured graph): the cell
+  // ranges run on it beside the gather
+  cudaStream_t st2 = nullptr;
+  cudaEvent_t evFork = nullptr, evJoin = nullptr;
   Bufs3 b{};
   std::vector<int32_t> hluts;
   std::vector<int32_t> hmats;
@@ -160,6 +164,9 @@ struct Engine3 {
       if (p) cudaFree(p);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
+    if (evFork) cudaEventDestroy(evFork);
+    if (evJoin) cudaEventDestroy(evJoin);
+    if (st2) cudaStreamDestroy(st2);
     if (st) cudaStreamDestroy(st);
   }
 
@@ -190,8 +197,11 @@ struct Engine3 {
     hluts.assign(o->luts, o->luts + LUT_WORDS);
     hmats.assign(o->mats, o->mats + 4 * matCount);
     if (!cuda_ok(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "stream")) return false;
+    if (!cuda_ok(cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking), "stream")) return false;
     cudaEventCreate(&ev0);
     cudaEventCreate(&ev1);
+    cudaEventCreateWithFlags(&evFork, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&evJoin, cudaEventDisableTiming);
     size_t C = capSlots;
     b.state = dalloc3<int32_t>(C * 8, err);
     b.sceneOf = dalloc3<uint32_t>(C, err);
@@ -371,8 +381,12 @@ struct Engine3 {
     radix::sort_pairs(b.keys, hw.slotEnd, keyBits, b.skey, b.sslot, tmpK, tmpV, hist, st);
     launches += radix::LAUNCHES_PER_PASS * std::max(1, (keyBits + radix::RBITS - 1) / radix::RBITS);
     mark(nullptr);
-    k3_cellstart<<<gK, 256, 0, st>>>(b);
+    cudaEventRecord(evFork, st);
+    cudaStreamWaitEvent(st2, evFork, 0);
+    k3_cellstart<<<gK, 256, 0, st2>>>(b);
+    cudaEventRecord(evJoin, st2);
     k3_gather<<<gA, 256, 0, st>>>(b);
+    cudaStreamWaitEvent(st, evJoin, 0);
     launches += 2;
     mark(nullptr);
     switch (lanesN) {
