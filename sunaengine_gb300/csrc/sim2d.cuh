@@ -152,7 +152,8 @@ struct Bufs {
   uint32_t* work;       // [8] per-substep flags: [0] = some particle has a friction/bond row,
                         // [1] = some live fluid particle carries INFO_SEAL or INFO_CONGEAL,
                         // [2] = tiles too large to stage (entries of OVF),
-                        // [3] = chunks of crowded cells for k_cellbox_chunks;
+                        // [3] = chunks of crowded cells for k_cellbox_chunks,
+                        // [5] = some scene forms bonds this substep (formNow);
                         // and, never reset: [4] = some bond row of the world may be
                         // non-empty (set by bond formation and by every host write of
                         // bond rows)
@@ -359,6 +360,7 @@ __global__ void __launch_bounds__(256) k_predict_key(Bufs b) {
     b.work[1] = 0u;
     b.work[2] = 0u;
     b.work[3] = 0u;
+    b.work[5] = 0u;
   }
   for (uint32_t slot = gtid(); slot < slotEnd; slot += gstride()) {
     uint32_t s = b.sceneOf[slot];
@@ -423,6 +425,11 @@ __global__ void __launch_bounds__(256) k_gather(Bufs b) {
     const unsigned bfl = __ballot_sync(__activemask(), fl);
     if (fl && (threadIdx.x & 31u) == (unsigned)(__ffs(bfl) - 1) && *(volatile uint32_t*)(b.work + 1) == 0u)
       atomicOr(b.work + 1, 1u);
+    // its scene forms bonds this substep (k_predict_key set formNow): k_form1 has work
+    const bool fm = S.formNow != 0u;
+    const unsigned bfm = __ballot_sync(__activemask(), fm);
+    if (fm && (threadIdx.x & 31u) == (unsigned)(__ffs(bfm) - 1) && *(volatile uint32_t*)(b.work + 5) == 0u)
+      atomicOr(b.work + 5, 1u);
   }
 }
 
@@ -1927,6 +1934,7 @@ __global__ void k_fold(Bufs b, int doChain) {
 // markCongealNbr + bondForm1 (src/sim.wgsl:2714-2989), sorted space.
 template <bool DBG>
 __global__ void __launch_bounds__(256) k_form1(Bufs b) {
+  if (b.work[5] == 0u) return;  // no scene forms bonds this substep
   Flags<DBG> f{b.dbg};
   const uint32_t nAct = b.world->nAct, stride = b.nbrStride;
   for (uint32_t p = gtid(); p < nAct; p += gstride()) {
