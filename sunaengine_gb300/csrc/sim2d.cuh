@@ -1643,6 +1643,9 @@ __device__ int2 contain_core(const Bufs& b, Entry entry, uint32_t n, bool filter
 // last solver iteration, on the final preds in PL.
 template <bool DBG>
 __global__ void __launch_bounds__(256) k_contain(Bufs b) {
+  // a list holds a seal endpoint (NBRN_SEAL) only if some live fluid particle
+  // carries SEAL, which k_gather reports in work[1] (with CONGEAL)
+  if (b.work[1] == 0u) return;
   Flags<DBG> f{b.dbg};
   const uint32_t nAct = b.world->nAct, stride = b.nbrStride;
   for (uint32_t p = gtid(); p < nAct; p += gstride()) {
