@@ -5,13 +5,16 @@
 //
 //   k_predict_key   predict (src/sim.wgsl:958-1000) + grid key per slot
 //   radix sort      stable, atomic-free: replaces gridCount/scan/scatter/canonicalize
-//   k_cellstart     cell ranges in sorted space
+//   k_cellstart     cell ranges in sorted space (on a side branch, beside k_gather)
 //   k_gather        slot -> sorted-space working set
+//   k_cellbox       pred boxes of crowded cells (+ k_cellbox_chunks)
 //   k_nbr           neighbour lists, reference traversal order and MAXNBR cut
 //   ITERS x { k_solveA; k_colour x 4; [k_friction; k_apply_fric] }
 //                   density/lambda, then colour-classed Gauss-Seidel position
 //                   correction; solveB and applyDp are fused per colour over a
-//                   double-buffered pred (see k_colour).
+//                   double-buffered pred (see k_colour), each pass's copy of
+//                   the other colours (k_colour_copy) on a side branch beside it
+//   k_contain       containment of intruders (when a seal particle is live)
 //   k_post1         finalize + xsph + normals + conduct in one neighbour sweep
 //   k_post2         surfaceTension + thermal + formation flag clear + state hash
 //   [k_form1, k_form2, k_hash]   bond formation for worlds with bonding rows
