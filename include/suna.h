@@ -110,6 +110,10 @@ int sn_chain(sn_engine* e, uint32_t chain[8]);
 int sn_reset_chain(sn_engine* e);
 /* Engine.readState: n*8 words of the current state. */
 int sn_read_state(sn_engine* e, int32_t* out, size_t words);
+/* The positions the last loadScene loaded (2 words per particle of that load:
+ * the engine's _initialPos, src/engine.js:3947, kept on the device; spawns
+ * and edits do not change it). *words_out receives the word count. */
+int sn_read_initial_positions(sn_engine* e, int32_t* out, size_t words, size_t* words_out);
 /* The cross-substep scratch an exact keyframe needs: stAcc, n*2 words
  * (Derived.stAcc, src/sim.wgsl:200; consumed by predict at src/sim.wgsl:980). */
 int sn_read_scratch(sn_engine* e, int32_t* out, size_t words);

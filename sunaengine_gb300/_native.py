@@ -228,6 +228,7 @@ SIGNATURES = {
     'sn_batch_autotune': (ctypes.c_int, [P, u32, ctypes.POINTER(u32)]),
     'sn_set_staged': (ctypes.c_int, [P, u32]),
     'sn_set_tile_shape': (ctypes.c_int, [P, u32]),
+    'sn_read_initial_positions': (ctypes.c_int, [P, P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
     'sn_batch_set_tile_shape': (ctypes.c_int, [P, u32]),
     'sn_autotune_layout': (ctypes.c_int, [P, u32, ctypes.POINTER(u32), ctypes.POINTER(u32),
                                           ctypes.POINTER(ctypes.c_float)]),

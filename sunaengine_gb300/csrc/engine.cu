@@ -355,6 +355,7 @@ struct SceneHost {
   std::vector<uint32_t> bmat;
   uint64_t matSeen = 0;  // the material rows any particle of the scene has worn (loaded or spawned)
   uint32_t nFluid0 = 0;
+  uint32_t nInit = 0;  // particles of the last loadScene (their positions are in World::initPos)
   bool hasTemp = false, hasFuel = false;
   uint32_t weldSeq = 1;                   // _weldSeq: the loaded scene holds tag sequence 1
   uint32_t weldHold = 0, weldHoldSeq = 0;  // the gesture held open
@@ -428,7 +429,7 @@ struct World {
                     b.NBRL, b.NBRN, (void*)b.tiles, b.TR, b.OVF, b.CB,
                     (void*)b.luts, (void*)b.WG, (void*)b.CA, (void*)b.mats, (void*)b.rcp,
                     b.scenes, b.world, b.acc, b.accLast, b.chain, b.dbg, b.err, b.work, tmpK, tmpV, hist,
-                    hits, accTmp, devEv, devEp, boxChunks, upl, uplRes, barBuf, eraseBuf};
+                    hits, accTmp, devEv, devEp, boxChunks, upl, uplRes, barBuf, eraseBuf, initPos};
     for (void* p : ptrs)
       if (p) cudaFree(p);
     if (ev0) cudaEventDestroy(ev0);
@@ -796,6 +797,7 @@ struct World {
   // pos 2n, vel 2n, mat n, flags n, temp n, fuel n), checked and packed on
   // the device: a host loop over a 10^6-particle scene costs milliseconds.
   int32_t* upl = nullptr;
+  int2* initPos = nullptr;     // [cap] each scene's positions at its last load
   uint32_t* uplRes = nullptr;  // [4]: first failing index, material mask (2 words)
   bool upload_scene(const sn_scene* sc, LoadTables& T, uint64_t* seen) {
     const size_t n = sc->n;
@@ -846,6 +848,16 @@ struct World {
     }
     uint64_t seenMask = 0;
     if (!upload_scene(sc, T, &seenMask)) return false;
+    // loadScene's copy of the loaded positions (_initialPos, src/engine.js:3947),
+    // kept on the device for liveness
+    if (!initPos) {
+      initPos = dalloc<int2>(capSlots, err);
+      if (!initPos) return false;
+    }
+    if (sc->n && !cuda_ok(cudaMemcpyAsync(initPos + h.slotBase, upl, (size_t)sc->n * 8, cudaMemcpyDeviceToDevice, st),
+                          "initial positions"))
+      return false;
+    h.nInit = sc->n;
     // a scene load dissolves every body of the scene (src/engine.js:3811-3813)
     if (!drop_scene_bodies(s)) return false;
     uint32_t cs = 1u << sc->cell_shift;
@@ -2609,6 +2621,15 @@ int sn_read_state(sn_engine* e, int32_t* out, size_t words) {
   SceneHost& h = e->w.sh[0];
   if (words < (size_t)h.n * 8) { e->w.err = "output buffer too small"; return SN_E_INVALID; }
   return rc_of(e->w, e->w.read_words(e->w.b.state + (size_t)h.slotBase * 8, out, (size_t)h.n * 32));
+}
+int sn_read_initial_positions(sn_engine* e, int32_t* out, size_t words, size_t* words_out) {
+  if (!e || !out) return SN_E_INVALID;
+  SceneHost& h = e->w.sh[0];
+  if (!h.loaded) { e->w.err = "readInitialPositions before loadScene"; return SN_E_STATE; }
+  if (words < (size_t)h.nInit * 2) { e->w.err = "output buffer too small"; return SN_E_INVALID; }
+  if (words_out) *words_out = (size_t)h.nInit * 2;
+  if (h.nInit == 0) return SN_OK;
+  return rc_of(e->w, e->w.read_words(e->w.initPos + h.slotBase, out, (size_t)h.nInit * 8));
 }
 int sn_read_scratch(sn_engine* e, int32_t* out, size_t words) {
   if (!e || !out) return SN_E_INVALID;

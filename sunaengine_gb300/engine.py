@@ -140,6 +140,7 @@ class Engine:
         self._n_fluid = 0
         self._substeps = 0
         self._scene: Optional[Scene] = None
+        self._loaded_n = 0
 
     # -- plumbing ------------------------------------------------------------------
     def _check(self, rc: int, what: str):
@@ -165,7 +166,7 @@ class Engine:
         self._n, self._n_fluid = int(scene.n), int(scene.nFluid)
         self._substeps = 0
         self._scene = scene
-        self._initial_pos = np.ascontiguousarray(scene.pos, np.int32).reshape(-1).copy()
+        self._loaded_n = int(scene.n)
         return self
 
     def step(self, count: int = 1) -> int:
@@ -244,7 +245,16 @@ class Engine:
         cs = self.read_cell_start()
         sc = self._scene
         return compute_liveness(st, self.n, self.n_fluid, int(sc.domW), int(sc.domH), rho=rho, nbr_count=nbr,
-                                cell_start=cs, initial_pos=self._initial_pos, recent_pos=recent)
+                                cell_start=cs, initial_pos=self.read_initial_positions(), recent_pos=recent)
+
+    def read_initial_positions(self) -> np.ndarray:
+        """The positions the last load_scene loaded (the reference engine's
+        _initialPos, src/engine.js:3947), 2 words per particle of that load."""
+        a = np.empty(max(1, self._loaded_n) * 2, np.int32)
+        got = ctypes.c_size_t()
+        self._check(self._lib.sn_read_initial_positions(self._h, _ptr(a), a.size, ctypes.byref(got)),
+                    'readInitialPositions')
+        return a[:int(got.value)]
 
     def read_bonds(self) -> np.ndarray:
         a = np.zeros(max(1, self.n_fluid * BOND_CAP), np.uint32)

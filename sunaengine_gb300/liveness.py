@@ -56,8 +56,12 @@ def compute_liveness(state, n: int, n_fluid: int, dom_w: int, dom_h: int, rho=No
     vx_sum, vy_sum = int(fvx.sum()), int(fvy.sum())
     moved = 0
     if initial_pos is not None:
+        # a fluid slot past the loaded positions (a spawn that outgrew the
+        # load) has no initial position and counts as moved, as the
+        # reference's typed-array read of undefined compares unequal
         ip = np.asarray(initial_pos, np.int64).reshape(-1, 2)[:n_fluid]
-        moved = int(np.count_nonzero((fx != ip[:, 0]) | (fy != ip[:, 1])))
+        k = ip.shape[0]
+        moved = int(np.count_nonzero((fx[:k] != ip[:, 0]) | (fy[:k] != ip[:, 1]))) + (n_fluid - k)
     recent_moved = 0
     if recent_pos is not None:
         rp = np.asarray(recent_pos, np.int64).reshape(-1, 2)[:n_fluid]

@@ -46,3 +46,24 @@ def test_dambreak_alive_after_1000_substeps():
     # and the reference's non-vacuity controls still fail
     assert len(liveness.zero_state_liveness()[1]) >= 3
     assert all(v for _, v in liveness.degenerate_state_controls().values())
+
+
+def test_initial_positions_are_the_loaded_ones_and_spawns_outgrow_them():
+    """The engine keeps loadScene's positions on the device (_initialPos):
+    they equal the scene's, steps and spawns leave them alone, and liveness
+    after a spawn of more particles than the load held counts the slots past
+    them as moved (the reference reads undefined there)."""
+    sc = scenes.make_scene('droplet_v1')
+    e = Engine(max_particles=sc.n + 4096).load_scene(sc)
+    assert np.array_equal(e.read_initial_positions(), np.asarray(sc.pos, np.int32).reshape(-1))
+    e.step(3)
+    drop = scenes.make_droplet(64 * scenes.ONE, 36 * scenes.ONE, 14, 14)  # 615 particles: more than the load held
+    assert e.spawn_fluid([dict(p, mat=0) for p in drop]) == sc.n + len(drop)
+    assert e.n_fluid > sc.n
+    assert np.array_equal(e.read_initial_positions(), np.asarray(sc.pos, np.int32).reshape(-1))
+    e.step(2)
+    m = e.liveness()
+    assert m['movedFraction'] * e.n_fluid >= e.n_fluid - sc.n
+    e.load_scene(sc)
+    assert np.array_equal(e.read_initial_positions(), np.asarray(sc.pos, np.int32).reshape(-1))
+    e.check_errors()

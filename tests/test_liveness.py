@@ -53,3 +53,18 @@ def test_dambreak_is_alive_and_a_frozen_copy_is_not():
     now = e.read_state().reshape(-1, 8)[:sc.nFluid, :2].reshape(-1).copy()
     F = _oracle_liveness(e, sc, now)
     assert any('FROZEN' in s for s in liveness.check_liveness(F, liveness.DAMBREAK_EXPECT))
+
+
+def test_slots_past_the_loaded_positions_count_as_moved():
+    """A spawn that outgrows the load leaves fluid slots with no initial
+    position; computeLiveness reads undefined there, which compares unequal,
+    so they count as moved."""
+    from sunaengine_gb300.liveness import compute_liveness
+    n = 6
+    st = np.zeros((n, 8), np.int32)
+    st[:, 0] = np.arange(n) * 65536
+    st[:, 1] = 65536
+    init = st[:4, :2].reshape(-1).copy()  # four loaded, six fluid now
+    init[2] += 1                          # the second loaded particle moved
+    m = compute_liveness(st.reshape(-1), n, n, 10 * 65536, 10 * 65536, initial_pos=init)
+    assert m['movedFraction'] * n == 1 + 2
