@@ -298,8 +298,12 @@ struct Engine3 {
       return;
     }
     if (lanesTuned) return;
+    // Measured on 3D columns (ms per substep with 1 / 2 / 4 lanes): 32,768
+    // particles 0.162 / 0.141 / 0.119, 64,000 0.183 / 0.179 / 0.166,
+    // 85,184 0.209 / 0.211 / 0.206, 97,336 0.226 / 0.237 / 0.238, 262,144
+    // 0.387 / 0.500 / 0.531: two lanes never won.
     const uint32_t n = hw.nAct;
-    lanesD = lanesS = n < 65536 ? 4 : (n < 131072 ? 2 : 1);
+    lanesD = lanesS = n < 90112 ? 4 : 1;
     lanesN = 1;  // the ballot-split list build measured slower than one lane per particle
   }
 
